@@ -1,0 +1,326 @@
+"""Benchmark: transient GROUNDWATER_FLOW on a 128x128x64 hex mesh.
+
+Workload (the configuration the solves/s metric is quoted on): 1,081,665
+nodes, 1,048,576 linear hexes, element-wise ln K a seeded Gaussian random
+field (mean ln 1e-5, variance 1, exponential covariance, correlation length
+8 cells), Ss = 1e-4 1/m, 20 implicit-Euler steps of dt = 3600 s, heads 10 m
+/ 0 m on the x faces (symmetric Dirichlet elimination), CG + Jacobi to a
+1e-10 relative residual, FP64 throughout.  One step = one global assembly
+(27 Gauss points per hex) + Dirichlet + one CG solve: one "solve".
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`value` times K steps with every input resident on the device; `e2e` times
+the same steps through the C ABI with host buffers (conductivity, previous
+heads and the initial guess copied in, heads copied out each step).  The
+matrix (343 MB of values + indices) is larger than L2, so no L2 flush is
+needed between steps.  --impl reference times the CPU oracle (a C
+restatement of the reference's path) on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NX, NY, NZ = 128, 128, 64
+STEPS_TOTAL = 20
+DT = 3600.0
+SS = 1e-4
+TOL = 1e-10
+SEED = 2
+WORKLOAD = "transient GROUNDWATER_FLOW hex 128x128x64, lnK GRF var 1 ell 8, 20 steps dt 3600, CG+Jacobi 1e-10"
+
+
+def make_deck(nx=NX, ny=NY, nz=NZ):
+    from ogs5_gb300 import fields
+    from ogs5_gb300 import mesh as M
+    m = M.structured_hex(nx, ny, nz)
+    ek = fields.lognormal_k(m.shape, np.log(1e-5), 1.0, 8.0, seed=SEED)
+    lf, rf = m.face_nodes(0, 0), m.face_nodes(0, 1)
+    rows = np.concatenate([lf, rf]).astype(np.int64)
+    vals = np.concatenate([np.full(len(lf), 10.0), np.zeros(len(rf))])
+    h0 = np.zeros(m.n_nodes)
+    h0[lf] = 10.0
+    return m, ek, rows, vals, h0
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, dev=0):
+        self.dev = dev
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", "clocks.csv")
+
+    def __enter__(self):
+        os.makedirs(os.path.dirname(self.path), exist_ok=True)
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.dev}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+            self.f.close()
+
+    def summary(self):
+        try:
+            rows = [r.split(",") for r in open(self.path).read().strip().splitlines() if r.strip()]
+        except Exception:
+            return None
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows]
+        mx = max(float(r[2]) for r in rows)
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in rows:
+            for k, nm in enumerate(names):
+                if r[5 + k].strip() == "Active":
+                    reasons.add(nm)
+        load = [s for s in sm if s > 0.5 * mx] or sm
+        return {"sm_mhz": statistics.median(load), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(rows)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def run_steps(eqs, capi, p, ek, rows, vals, h0, k_steps, host: bool, torch, stream):
+    """k_steps implicit-Euler steps from the initial heads h0; returns
+    (elapsed ms, per-step ms list, total CG iterations, final heads)."""
+    n = len(h0)
+    if host:
+        ek_b = torch.empty(len(ek), dtype=torch.float64, pin_memory=True).numpy()
+        ek_b[:] = ek
+        u = torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
+        x = torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
+        u[:] = h0
+        rws, vls = rows, vals
+    else:
+        ek_b = torch.tensor(ek, device="cuda")
+        u = torch.tensor(h0, device="cuda")
+        x = torch.empty_like(u)
+        rws = torch.tensor(rows, device="cuda")
+        vls = torch.tensor(vals, device="cuda")
+    torch.cuda.synchronize()
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(k_steps + 1)]
+    iters = 0
+    evs[0].record(stream)
+    for k in range(k_steps):
+        eqs.Initialize()
+        eqs.GlobalAssembly(p, ek_b, u)
+        eqs.SetKnownX(rws, vls, capi.DIRICHLET_SYMMETRIC)
+        if host:
+            x[:] = u
+        else:
+            x.copy_(u)
+        iters += eqs.Solver(x)
+        if host:
+            u[:] = x
+        else:
+            u.copy_(x)
+        evs[k + 1].record(stream)
+    torch.cuda.synchronize()
+    per = [evs[k].elapsed_time(evs[k + 1]) for k in range(k_steps)]
+    heads = x.copy() if host else x.cpu().numpy()
+    return evs[0].elapsed_time(evs[-1]), per, iters, heads
+
+
+def time_spmv(eqs, torch, stream, n, reps=30):
+    x = torch.rand(n, dtype=torch.float64, device="cuda")
+    y = torch.empty_like(x)
+    for _ in range(3):
+        eqs.spmv(x, y)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ms = []
+    for _ in range(reps):
+        e0.record(stream)
+        eqs.spmv(x, y)
+        e1.record(stream)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    return statistics.median(ms)
+
+
+def cpu_baseline_sample(threads: int = 1):
+    """Oracle (C restatement) on a bounded sample of the workload: the full
+    assembly of one 16-cell x-slab plus 40 CG iterations on the full system,
+    extrapolated per element and per iteration.  Returns per-unit seconds."""
+    from oracle import oracle as O
+    m, ek, rows, vals, h0 = make_deck()
+    slab = m.conn.reshape(NZ, NY, NX, 8)[:, :, :16, :].reshape(-1, 8)
+    import copy
+    ms = copy.copy(m)
+    ms.conn = np.ascontiguousarray(slab)
+    op = O.make_params(pcs_type=0, dt=DT, storage=SS)
+    rp, col = O.build_pattern(m.n_nodes, m.conn)
+    t0 = time.perf_counter()
+    eks = ek.reshape(NZ, NY, NX)[:, :, :16].ravel().copy()
+    O.assemble(ms, rp, col, op, elem_k=eks, u0=h0)
+    t_asm = (time.perf_counter() - t0) / len(slab)
+    val, b = O.assemble(m, rp, col, op, elem_k=ek, u0=h0) if False else (None, None)
+    # CG iterations on a full-size system (values from a cheap stand-in with
+    # the same pattern: the cost per iteration does not depend on values)
+    val = np.zeros(len(col))
+    diag = np.nonzero(col == np.repeat(np.arange(m.n_nodes), np.diff(rp)))[0]
+    val[diag] = 1.0
+    val += 1e-3
+    b = np.ones(m.n_nodes)
+    t0 = time.perf_counter()
+    O.solve(rp, col, val, b, np.zeros(m.n_nodes), method=5, precond=1, max_iter=40, tol=1e-300)
+    t_it = (time.perf_counter() - t0) / 40
+    return t_asm, t_it
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=STEPS_TOTAL)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        return reference_arm(args, rank)
+
+    import torch
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    from ogs5_gb300 import build as B
+    B.build()
+    from ogs5_gb300 import capi
+
+    m, ek, rows, vals, h0 = make_deck()
+    stream = torch.cuda.Stream()
+    gm = capi.GpuMesh(m)
+    eqs = capi.LinearEQS(gm, stream=stream)
+    eqs.ConfigNumerics(capi.LS_CG, capi.PRECOND_JACOBI, 20000, TOL)
+    p = capi.make_params(capi.GROUNDWATER_FLOW, dt=DT, storage=SS)
+    k_steps = max(1, args.steps)
+    warm = max(3, args.warmup)
+
+    # warm-up (graph capture, allocator, clocks)
+    run_steps(eqs, capi, p, ek, rows, vals, h0, warm, False, torch, stream)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        dist.barrier()
+    capi.kernel_launches(reset=True)
+    with ClockSampler(local) as clk:
+        ms, per, iters, heads = run_steps(eqs, capi, p, ek, rows, vals, h0, k_steps, False, torch, stream)
+    launches = capi.kernel_launches(reset=True)
+    ms_e2e, per_e2e, iters_e2e, heads_e2e = run_steps(eqs, capi, p, ek, rows, vals, h0, k_steps, True,
+                                                      torch, stream)
+    if world > 1:
+        t = torch.tensor([ms, ms_e2e], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms, ms_e2e = float(t[0]), float(t[1])
+        dist.barrier()
+
+    t_spmv = time_spmv(eqs, torch, stream, m.n_nodes)
+    N, nnz = gm.n_rows, gm.nnz
+    spmv_bytes = nnz * 12 + N * 20
+    hbm, peak_kind = peaks()
+    achieved = spmv_bytes / (t_spmv * 1e-3) / 1e9
+    value = world * k_steps / (ms * 1e-3)
+    e2e = world * k_steps / (ms_e2e * 1e-3)
+    h2d = 8 * m.n_elements + 8 * N * 2 + 12 * len(rows)
+    d2h = 8 * N
+    out = {
+        "metric": "solves/s", "value": round(value, 4), "unit": "solves/s", "n_gpus": world,
+        "steps": k_steps, "warmup": warm, "ms_per_step": round(ms / k_steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded GRF conductivity, generated mesh)",
+        "config": {"workload": WORKLOAD, "nodes": N, "elements": m.n_elements, "nnz": nnz,
+                   "l2": "inputs larger than L2 (matrix 343 MB), no flush",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "p50_step_ms": round(float(np.percentile(per, 50)), 3),
+        "p99_step_ms": round(float(np.percentile(per, 99)), 3),
+        "cg_iterations": iters, "dof_per_s": round(value * N, 1),
+        "e2e": {"value": round(e2e, 4), "unit": "solves/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "e2e_heads_match": bool(np.abs(heads_e2e - heads).max() <= 1e-9 * np.abs(heads).max()),
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+                     "frac": round(achieved / hbm, 4), "traffic": None,
+                     "kernel": "k_cg_spmv (CSR FP64 SpMV + fused p.s)",
+                     "bytes_per_launch": spmv_bytes, "launch_ms": round(t_spmv, 4),
+                     "peak_kind": peak_kind},
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        t_asm, t_it = cpu_baseline_sample()
+        est = m.n_elements * t_asm + (iters / k_steps) * t_it
+        out["cpu_baseline"] = {"value": round(1.0 / est, 6), "unit": "solves/s", "cores": 1,
+                               "kind": "port",
+                               "sample": (f"oracle C port, 1 thread: assembly of a 16-cell x-slab "
+                                          f"({t_asm*1e6:.2f} us/element) + 40 CG iterations on the full "
+                                          f"system ({t_it*1e3:.1f} ms/iter), extrapolated to "
+                                          f"{m.n_elements} elements + {iters / k_steps:.0f} iterations/step")}
+    if rank == 0:
+        print(json.dumps(out))
+
+
+def reference_arm(args, rank):
+    """CPU implementation of the path (the oracle port; the reference's own
+    build needs its cmake-generated sources) on all host cores."""
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    cores = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        res = pool.map(_ref_worker, range(cores))
+    wall = time.perf_counter() - t0
+    t_asm = statistics.median(r[0] for r in res)
+    t_it = statistics.median(r[1] for r in res)
+    iters_per_step = 300.0
+    est = NX * NY * NZ * t_asm + iters_per_step * t_it
+    value = cores / est
+    print(json.dumps({
+        "metric": "solves/s", "value": round(value, 6), "unit": "solves/s", "n_gpus": 0,
+        "steps": args.steps, "warmup": args.warmup, "impl": "reference",
+        "higher_is_better": True, "dtype": "f64", "config": {"workload": WORKLOAD},
+        "cpu_baseline": {"value": round(value, 6), "unit": "solves/s", "cores": cores, "kind": "port",
+                         "sample": f"{cores} independent processes, each: slab assembly + 40 CG "
+                                   f"iterations, extrapolated to one step ({iters_per_step:.0f} "
+                                   f"iterations); wall {wall:.1f} s"},
+        "e2e": {"value": round(value, 6), "unit": "solves/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0}}))
+
+
+def _ref_worker(i):
+    return cpu_baseline_sample()
+
+
+if __name__ == "__main__":
+    main()

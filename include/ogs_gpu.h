@@ -1,0 +1,265 @@
+/*
+ * ogs_gpu.h -- C ABI of the GB300 flow/transport path for OpenGeoSys 5.
+ *
+ * The OGS-5 host code keeps its own process and solver surface
+ * (CRFProcess::GlobalAssembly, Linear_EQS::Solver); at the call sites listed
+ * beside each entry point it calls into this library instead of running its
+ * serial element loop and CPU Krylov solver.  All arithmetic is FP64 unless a
+ * solver configuration asks for the FP32-inner / FP64-refinement mode.
+ *
+ * Conventions
+ *   - Every entry point returns an ogs_status; nothing aborts or traps.
+ *     ogs_gpu_last_error() returns a text for the last failure on the
+ *     calling thread.
+ *   - Array arguments are plain pointers.  Host pointers are copied to the
+ *     device inside the call; device pointers (cudaMalloc'd memory of the
+ *     current device) are used in place.
+ *   - Row, column and node indices are zero based; the equation index of a
+ *     node equals its node index (linear elements, one DOF per node), as in
+ *     CFEMesh::RenumberNodesForGlobalAssembly for meshes without quadratic
+ *     nodes (MSH/msh_mesh.cpp:1308).
+ *   - One ogs_system per host thread or stream; handles are not thread safe.
+ */
+#ifndef OGS_GPU_H
+#define OGS_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum
+{
+    OGS_OK = 0,
+    OGS_NOT_CONVERGED = 1, /* max_iter reached (Linear_EQS::Message warning) */
+    OGS_BREAKDOWN = 2,     /* |rho| or |omega| < DBL_MIN in BiCGStab       */
+    OGS_NONFINITE = 3,     /* NaN/Inf in a residual norm                   */
+    OGS_OOM = 4,
+    OGS_BAD_ARG = 5,
+    OGS_CUDA_ERROR = 6,
+    OGS_SINGULAR_JACOBIAN = 7 /* |det J| < DBL_EPSILON (fem_ele.cpp:639,695) */
+} ogs_status;
+
+/* Element types on the path (MshElemType QUAD, HEXAHEDRON, TETRAHEDRON). */
+typedef enum
+{
+    OGS_ELEM_QUAD4 = 0,
+    OGS_ELEM_HEX8 = 1,
+    OGS_ELEM_TET4 = 2
+} ogs_elem_type;
+
+/* Process types on the path (FiniteElement::ProcessType). */
+typedef enum
+{
+    OGS_PCS_GROUNDWATER_FLOW = 0,
+    OGS_PCS_LIQUID_FLOW = 1,
+    OGS_PCS_MASS_TRANSPORT = 2
+} ogs_pcs_type;
+
+/* Dirichlet treatment.  ROW_ONLY is CSparseMatrix::Diagonize of the SP
+ * build (FEM/matrix_class.cpp:1663): the row is zeroed except the diagonal
+ * and b_i = a_ii * value; the column stays.  SYMMETRIC is MXRandbed of the
+ * legacy build (FEM/matrix_routines.cpp:2314): the column is lifted into the
+ * right-hand side, row and column are zeroed, the diagonal is kept. */
+typedef enum
+{
+    OGS_DIRICHLET_ROW_ONLY = 0,
+    OGS_DIRICHLET_SYMMETRIC = 1
+} ogs_dirichlet_mode;
+
+/* Linear solver codes of $LINEAR_SOLVER (FEM/equation_class.cpp:197-244). */
+enum
+{
+    OGS_LS_BICGSTAB = 2,
+    OGS_LS_CG = 5
+};
+/* Preconditioner codes of $LINEAR_SOLVER (FEM/equation_class.cpp:294-308). */
+enum
+{
+    OGS_PRECOND_NONE = 0,
+    OGS_PRECOND_JACOBI = 1,
+    OGS_PRECOND_ILU0 = 100
+};
+/* Arithmetic of the Krylov iteration. */
+enum
+{
+    OGS_PRECISION_FP64 = 0,
+    OGS_PRECISION_FP32_REFINED = 1 /* FP32 matrix + inner sweeps, FP64 IR */
+};
+
+/* Mesh description: the data CFEMesh hands to SparseTable and the element
+ * loop (node coordinates, element connectivity).  Host arrays. */
+typedef struct
+{
+    int32_t elem_type;          /* ogs_elem_type                               */
+    int32_t dim;                /* 2 for quad meshes in the x-y plane, else 3  */
+    int64_t n_nodes;
+    int64_t n_elements;
+    const double* x;            /* node coordinates, n_nodes each              */
+    const double* y;
+    const double* z;            /* may be NULL when dim == 2                   */
+    const int32_t* connectivity;/* n_elements * nodes_per_element, element-major,
+                                   OGS node order of CElem::nodes_index       */
+    int32_t gauss_points;       /* $ELE_GAUSS_POINTS for quad/hex (1..3);
+                                   tets always use the 5-point rule            */
+} ogs_mesh_desc;
+
+/* Material and time-stepping parameters of one assembly call.  Each field
+ * names the OGS-5 source of the value. */
+typedef struct
+{
+    int32_t pcs_type;          /* ogs_pcs_type                                 */
+    int32_t steady;            /* TimType::STEADY: no mass matrix
+                                  (fem_ele_std.cpp:8549); for flow the same
+                                  as storage 0                                 */
+    double dt;                 /* pcs->Tim->time_step_length                   */
+    double theta;              /* m_num->ls_theta, MT time weighting           */
+    double nls_relaxation;     /* m_num->nls_relaxation, flow LHS weight;
+                                  < DBL_MIN means 1 (fem_ele_std.cpp:7715)     */
+    double time_unit_factor;   /* CElement::time_unit_factor (1 for seconds)  */
+    double storage;            /* StorageFunction, storage_model 1             */
+    double porosity;           /* Porosity, constant model                     */
+    double drho_dp;            /* LIQUID_FLOW: FluidProp->drho_dp, rho = rho_0 */
+    double viscosity;          /* LIQUID_FLOW: FluidProp->Viscosity()          */
+    double density;            /* LIQUID_FLOW: FluidProp->Density()            */
+    double gravity;            /* gravity_constant; < DBL_EPSILON = HEAD form  */
+    int32_t gravity_on;        /* coordinate_system % 10 == 2 and
+                                  FluidProp->CheckGravityCalculation()         */
+    int32_t pad0;
+    double alpha_l;            /* MT: mass_dispersion_longitudinal             */
+    double alpha_t;            /* MT: mass_dispersion_transverse               */
+    double diffusion;          /* MT: Daq * TortuosityFunction                 */
+    double decay;              /* MT: CalcElementDecayRateNew                  */
+    double retardation;        /* MT: CalcElementRetardationFactorNew          */
+    double saturation;         /* MT: SATURATION1 of the flow process (1)      */
+} ogs_assembly_params;
+
+/* Linear_EQS::ConfigNumerics inputs (CNumerics, FEM/rf_num_new.h:34-60). */
+typedef struct
+{
+    int32_t method;            /* ls_method: OGS_LS_BICGSTAB or OGS_LS_CG      */
+    int32_t precond;           /* ls_precond: 0, 1 (Jacobi), 100 (ILU(0))      */
+    int32_t max_iter;          /* ls_max_iterations                            */
+    int32_t precision;         /* OGS_PRECISION_*                              */
+    double tol;                /* ls_error_tolerance (relative to |b|)         */
+    double inner_tol;          /* FP32 mode: relative tolerance of one inner
+                                  solve (0 selects 1e-4)                       */
+    int32_t check_norm_rhs;    /* 1: keep Linear_EQS::CheckNormRHS, i.e.
+                                  return at once when |b|/|b_prev| < tol
+                                  (equation_class.cpp:1104-1121)               */
+    int32_t pad0;
+} ogs_solver_config;
+
+typedef struct
+{
+    int32_t iterations;        /* Krylov iterations (outer+inner in FP32 mode) */
+    int32_t status;            /* ogs_status of the solve                      */
+    double rel_residual;       /* |r| / |b| at exit (Linear_EQS::error)        */
+    double b_norm;             /* |b| at entry (Linear_EQS::bNorm)             */
+    int32_t refinements;       /* FP32 mode: outer FP64 refinement steps       */
+    int32_t pad0;
+    double solve_ms;           /* device time of the solve, CUDA events        */
+} ogs_solve_stats;
+
+typedef struct ogs_mesh ogs_mesh;
+typedef struct ogs_system ogs_system;
+
+/* Text of the last error on the calling thread ("" if none). */
+const char* ogs_gpu_last_error(void);
+
+/* Library version string. */
+const char* ogs_gpu_version(void);
+
+/* Builds the CSR pattern of the node-node adjacency and the element -> CSR
+ * slot map on the device.  Replaces CFEMesh::ConnectedNodes
+ * (MSH/msh_mesh.cpp:2931), SparseTable::SparseTable in CRS storage
+ * (FEM/matrix_class.cpp:691-776) and the per-entry search of
+ * CSparseMatrix::operator() (FEM/matrix_class.cpp:1178-1237).  Called where
+ * CRFProcess::CreateEQS_LinearSolver creates the SparseTable
+ * (FEM/rf_pcs.cpp:13455-13481). */
+ogs_status ogs_gpu_mesh_create(const ogs_mesh_desc* desc, ogs_mesh** out);
+ogs_status ogs_gpu_mesh_destroy(ogs_mesh* mesh);
+/* Number of rows and stored entries of the pattern. */
+ogs_status ogs_gpu_mesh_info(const ogs_mesh* mesh, int64_t* n_rows,
+                             int64_t* nnz);
+
+/* Creates the equation system on a mesh: matrix values, b, x and Krylov
+ * buffers.  Replaces `new Linear_EQS(*sp, dof)` (FEM/equation_class.cpp:85).
+ * stream: a cudaStream_t, or NULL for the default stream. */
+ogs_status ogs_gpu_system_create(ogs_mesh* mesh, void* stream,
+                                 ogs_system** out);
+ogs_status ogs_gpu_system_destroy(ogs_system* sys);
+
+/* Linear_EQS::ConfigNumerics (FEM/equation_class.cpp:191-318). */
+ogs_status ogs_gpu_configure(ogs_system* sys, const ogs_solver_config* cfg);
+
+/* Linear_EQS::Initialize (FEM/equation_class.cpp:325-332): A = 0, b = 0. */
+ogs_status ogs_gpu_initialize(ogs_system* sys);
+
+/* One global assembly: the element loop of CRFProcess::GlobalAssembly
+ * (FEM/rf_pcs.cpp:5738-5757) calling CFiniteElementStd::Assembly
+ * (FEM/fem_ele_std.cpp:9367) for GROUNDWATER_FLOW, LIQUID_FLOW or
+ * MASS_TRANSPORT, with add2GlobalMatrixII (fem_ele_std.cpp:8272-8352) and the
+ * RHS scatter.  Adds into the current A and b (call ogs_gpu_initialize
+ * first, as CRFProcess::Execute does).
+ *   elem_k       flow: conductivity (GWF) or permeability (LIQUID) per
+ *                element, isotropic (PermeabilityTensor, rf_mmp_new.cpp:4517);
+ *                ignored for MASS_TRANSPORT (may be NULL)
+ *   u0           primary variable of the previous time level per node
+ *                (NodalVal0 / NodalVal1 of Config, fem_ele_std.cpp:9184)
+ *   gp_velocity  MASS_TRANSPORT only: Darcy flux at the Gauss points,
+ *                n_elements * n_gauss * 3, from ogs_gpu_gp_velocity. */
+ogs_status ogs_gpu_assemble(ogs_system* sys, const ogs_assembly_params* p,
+                            const double* elem_k, const double* u0,
+                            const double* gp_velocity);
+
+/* Dirichlet values on a node set: the SetKnownX_i loop of
+ * CRFProcess::IncorporateBoundaryConditions (FEM/rf_pcs.cpp:6930-6995).
+ * Also records the values so that ogs_gpu_solve starts from an x0 that
+ * carries them. */
+ogs_status ogs_gpu_set_dirichlet(ogs_system* sys, const int64_t* rows,
+                                 const double* values, int64_t n_rows,
+                                 int32_t mode);
+
+/* Linear_EQS::Solver (FEM/equation_class.cpp:857-895), CG
+ * (equation_class.cpp:1129-1187) or BiCGStab (equation_class.cpp:1287-1420)
+ * with Jacobi (CSparseMatrix::Precond_Jacobi, matrix_class.cpp:1786-1822) or
+ * ILU(0).  x_inout: initial guess in, solution out (n_rows doubles).  Called
+ * at `iter_lin = eqs_new->Solver()` (FEM/rf_pcs.cpp:4847). */
+ogs_status ogs_gpu_solve(ogs_system* sys, double* x_inout,
+                         ogs_solve_stats* stats);
+
+/* Gauss-point Darcy flux q = -mat * grad(u) (CFiniteElementStd::Cal_Velocity,
+ * FEM/fem_ele_std.cpp:6554-6870, driven by CRFProcess::
+ * CalIntegrationPointValue, FEM/rf_pcs.cpp:5915).  q_gp: n_elements * n_gauss
+ * * 3 doubles, Gauss point g of element e at [(e * n_gauss + g) * 3]. */
+ogs_status ogs_gpu_gp_velocity(ogs_system* sys, const ogs_assembly_params* p,
+                               const double* elem_k, const double* u,
+                               double* q_gp);
+
+/* Read-back for checks: the CRS arrays of Linear_EQS::Write_BIN
+ * (FEM/equation_class.cpp:409, matrix_class.cpp:1403-1460) and b, x. */
+ogs_status ogs_gpu_get_csr(const ogs_system* sys, int64_t* row_ptr,
+                           int64_t* col, double* val);
+ogs_status ogs_gpu_get_rhs(const ogs_system* sys, double* b);
+ogs_status ogs_gpu_get_x(const ogs_system* sys, double* x);
+
+/* y = A x with the current matrix (CSparseMatrix::multiVec,
+ * FEM/matrix_class.cpp:1467-1555). */
+ogs_status ogs_gpu_spmv(ogs_system* sys, const double* x, double* y);
+
+/* Number of Gauss points per element of the mesh (9/27 at the default
+ * $ELE_GAUSS_POINTS 3 for quad/hex, 5 for tets). */
+int32_t ogs_gpu_mesh_gauss_points(const ogs_mesh* mesh);
+
+/* Number of this library's kernels launched on the calling thread since the
+ * last reset (instrumentation for benchmarks). */
+int64_t ogs_gpu_kernel_launches(int32_t reset);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* OGS_GPU_H */

@@ -1,0 +1,310 @@
+"""ctypes binding of include/ogs_gpu.h and a host-side mirror of the OGS-5
+solver surface (Linear_EQS, CRFProcess::GlobalAssembly) over it.
+
+The mirror keeps the reference's names and argument meanings so that test
+code reads like the reference's own driver code:
+
+    eqs = LinearEQS(mesh)                      # Linear_EQS(SparseTable, dof)
+    eqs.ConfigNumerics(ls_method=5, ls_precond=1, ls_max_iterations=1000,
+                       ls_error_tolerance=1e-10)
+    eqs.Initialize()                           # A = 0, b = 0
+    eqs.GlobalAssembly(params, elem_k, u0)     # element loop + scatter
+    eqs.SetKnownX(rows, values)                # SetKnownX_i over a node set
+    iters = eqs.Solver(x)                      # x: initial guess in, solution out
+
+Arrays may be numpy (host) or torch CUDA tensors (device, used in place).
+Errors raise OgsError carrying the ogs_status and the library's message.
+There is no CPU fallback: without the compiled library or a GPU every call
+fails loudly.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+OK, NOT_CONVERGED, BREAKDOWN, NONFINITE, OOM, BAD_ARG, CUDA_ERROR, SINGULAR_JACOBIAN = range(8)
+STATUS_NAMES = ["OK", "NOT_CONVERGED", "BREAKDOWN", "NONFINITE", "OOM", "BAD_ARG", "CUDA_ERROR",
+                "SINGULAR_JACOBIAN"]
+QUAD4, HEX8, TET4 = 0, 1, 2
+GROUNDWATER_FLOW, LIQUID_FLOW, MASS_TRANSPORT = 0, 1, 2
+DIRICHLET_ROW_ONLY, DIRICHLET_SYMMETRIC = 0, 1
+LS_BICGSTAB, LS_CG = 2, 5
+PRECOND_NONE, PRECOND_JACOBI, PRECOND_ILU0 = 0, 1, 100
+PRECISION_FP64, PRECISION_FP32_REFINED = 0, 1
+
+# every entry point include/ogs_gpu.h declares
+EXPORTS = [
+    "ogs_gpu_last_error", "ogs_gpu_version", "ogs_gpu_mesh_create", "ogs_gpu_mesh_destroy",
+    "ogs_gpu_mesh_info", "ogs_gpu_system_create", "ogs_gpu_system_destroy", "ogs_gpu_configure",
+    "ogs_gpu_initialize", "ogs_gpu_assemble", "ogs_gpu_set_dirichlet", "ogs_gpu_solve",
+    "ogs_gpu_gp_velocity", "ogs_gpu_get_csr", "ogs_gpu_get_rhs", "ogs_gpu_get_x",
+    "ogs_gpu_spmv", "ogs_gpu_mesh_gauss_points", "ogs_gpu_kernel_launches",
+]
+
+
+class OgsError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        name = STATUS_NAMES[status] if 0 <= status < len(STATUS_NAMES) else str(status)
+        super().__init__(f"{name}: {msg}")
+        self.status = status
+
+
+class MeshDesc(C.Structure):
+    _fields_ = [("elem_type", C.c_int32), ("dim", C.c_int32), ("n_nodes", C.c_int64),
+                ("n_elements", C.c_int64), ("x", C.c_void_p), ("y", C.c_void_p),
+                ("z", C.c_void_p), ("connectivity", C.c_void_p), ("gauss_points", C.c_int32)]
+
+
+class AssemblyParams(C.Structure):
+    _fields_ = [
+        ("pcs_type", C.c_int32), ("steady", C.c_int32), ("dt", C.c_double),
+        ("theta", C.c_double), ("nls_relaxation", C.c_double),
+        ("time_unit_factor", C.c_double), ("storage", C.c_double),
+        ("porosity", C.c_double), ("drho_dp", C.c_double),
+        ("viscosity", C.c_double), ("density", C.c_double),
+        ("gravity", C.c_double), ("gravity_on", C.c_int32), ("pad0", C.c_int32),
+        ("alpha_l", C.c_double), ("alpha_t", C.c_double),
+        ("diffusion", C.c_double), ("decay", C.c_double),
+        ("retardation", C.c_double), ("saturation", C.c_double),
+    ]
+
+
+class SolverConfig(C.Structure):
+    _fields_ = [("method", C.c_int32), ("precond", C.c_int32), ("max_iter", C.c_int32),
+                ("precision", C.c_int32), ("tol", C.c_double), ("inner_tol", C.c_double),
+                ("check_norm_rhs", C.c_int32), ("pad0", C.c_int32)]
+
+
+class SolveStats(C.Structure):
+    _fields_ = [("iterations", C.c_int32), ("status", C.c_int32), ("rel_residual", C.c_double),
+                ("b_norm", C.c_double), ("refinements", C.c_int32), ("pad0", C.c_int32),
+                ("solve_ms", C.c_double)]
+
+
+def make_params(pcs_type=GROUNDWATER_FLOW, **kw) -> AssemblyParams:
+    """ogs_assembly_params with the defaults of an OGS-5 deck."""
+    p = AssemblyParams()
+    p.pcs_type = pcs_type
+    p.dt = 1.0
+    p.theta = 1.0
+    p.time_unit_factor = 1.0
+    p.viscosity = 1.0e-3
+    p.density = 1000.0
+    p.retardation = 1.0
+    p.saturation = 1.0
+    for k, v in kw.items():
+        if not hasattr(p, k):
+            raise AttributeError(k)
+        setattr(p, k, v)
+    return p
+
+
+_LIB = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def lib():
+    """Loads libogs_gpu.so (raises if it has not been built)."""
+    global _LIB
+    if _LIB is None:
+        path = library_path()
+        if not os.path.exists(path):
+            raise OSError(f"{path} is missing: run ogs5_gb300.build.build() (nvcc) first")
+        L = C.CDLL(path)
+        vp = C.c_void_p
+        st = C.c_int
+        L.ogs_gpu_last_error.restype = C.c_char_p
+        L.ogs_gpu_version.restype = C.c_char_p
+        L.ogs_gpu_mesh_create.argtypes = [C.POINTER(MeshDesc), C.POINTER(vp)]
+        L.ogs_gpu_mesh_destroy.argtypes = [vp]
+        L.ogs_gpu_mesh_info.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+        L.ogs_gpu_system_create.argtypes = [vp, vp, C.POINTER(vp)]
+        L.ogs_gpu_system_destroy.argtypes = [vp]
+        L.ogs_gpu_configure.argtypes = [vp, C.POINTER(SolverConfig)]
+        L.ogs_gpu_initialize.argtypes = [vp]
+        L.ogs_gpu_assemble.argtypes = [vp, C.POINTER(AssemblyParams), vp, vp, vp]
+        L.ogs_gpu_set_dirichlet.argtypes = [vp, vp, vp, C.c_int64, C.c_int32]
+        L.ogs_gpu_solve.argtypes = [vp, vp, C.POINTER(SolveStats)]
+        L.ogs_gpu_gp_velocity.argtypes = [vp, C.POINTER(AssemblyParams), vp, vp, vp]
+        L.ogs_gpu_get_csr.argtypes = [vp, vp, vp, vp]
+        L.ogs_gpu_get_rhs.argtypes = [vp, vp]
+        L.ogs_gpu_get_x.argtypes = [vp, vp]
+        L.ogs_gpu_spmv.argtypes = [vp, vp, vp]
+        L.ogs_gpu_mesh_gauss_points.argtypes = [vp]
+        L.ogs_gpu_mesh_gauss_points.restype = C.c_int32
+        L.ogs_gpu_kernel_launches.argtypes = [C.c_int32]
+        L.ogs_gpu_kernel_launches.restype = C.c_int64
+        for name in ("ogs_gpu_mesh_create", "ogs_gpu_mesh_destroy", "ogs_gpu_mesh_info",
+                     "ogs_gpu_system_create", "ogs_gpu_system_destroy", "ogs_gpu_configure",
+                     "ogs_gpu_initialize", "ogs_gpu_assemble", "ogs_gpu_set_dirichlet",
+                     "ogs_gpu_solve", "ogs_gpu_gp_velocity", "ogs_gpu_get_csr", "ogs_gpu_get_rhs",
+                     "ogs_gpu_get_x", "ogs_gpu_spmv"):
+            getattr(L, name).restype = st
+        _LIB = L
+    return _LIB
+
+
+def _check(status: int, allow=()):
+    if status != OK and status not in allow:
+        raise OgsError(status, lib().ogs_gpu_last_error().decode())
+    return status
+
+
+def _ptr(a):
+    """Raw pointer of a numpy array or torch tensor (None passes through)."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        if not a.flags["C_CONTIGUOUS"]:
+            raise ValueError("array must be C-contiguous")
+        return a.ctypes.data
+    if hasattr(a, "data_ptr"):
+        if not a.is_contiguous():
+            raise ValueError("tensor must be contiguous")
+        return a.data_ptr()
+    raise TypeError(f"unsupported array type {type(a)}")
+
+
+def _f64(a):
+    if a is None or hasattr(a, "data_ptr"):
+        return a
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def kernel_launches(reset: bool = False) -> int:
+    return int(lib().ogs_gpu_kernel_launches(1 if reset else 0))
+
+
+class GpuMesh:
+    """CSR pattern + slot map of a mesh on the device (SparseTable)."""
+
+    def __init__(self, mesh, gauss_points: int = 3):
+        self.mesh = mesh
+        self._keep = [np.ascontiguousarray(mesh.x, dtype=np.float64),
+                      np.ascontiguousarray(mesh.y, dtype=np.float64),
+                      np.ascontiguousarray(mesh.z, dtype=np.float64),
+                      np.ascontiguousarray(mesh.conn, dtype=np.int32)]
+        d = MeshDesc(mesh.elem_type, mesh.dim, mesh.n_nodes, mesh.n_elements,
+                     _ptr(self._keep[0]), _ptr(self._keep[1]),
+                     _ptr(self._keep[2]) if mesh.dim == 3 else None, _ptr(self._keep[3]),
+                     gauss_points)
+        h = C.c_void_p()
+        _check(lib().ogs_gpu_mesh_create(C.byref(d), C.byref(h)))
+        self.h = h
+        n, nnz = C.c_int64(), C.c_int64()
+        _check(lib().ogs_gpu_mesh_info(h, C.byref(n), C.byref(nnz)))
+        self.n_rows, self.nnz = n.value, nnz.value
+        self.n_gauss = int(lib().ogs_gpu_mesh_gauss_points(h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().ogs_gpu_mesh_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class LinearEQS:
+    """Mirror of Math_Group::Linear_EQS (FEM/equation_class.h:56) on the GPU."""
+
+    def __init__(self, gmesh: GpuMesh, stream=None):
+        self.gmesh = gmesh
+        h = C.c_void_p()
+        sptr = None if stream is None else getattr(stream, "cuda_stream", stream)
+        _check(lib().ogs_gpu_system_create(gmesh.h, sptr, C.byref(h)))
+        self.h = h
+        self.n = gmesh.n_rows
+        self.last_stats = SolveStats()
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().ogs_gpu_system_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # Linear_EQS::ConfigNumerics
+    def ConfigNumerics(self, ls_method=LS_BICGSTAB, ls_precond=PRECOND_JACOBI,
+                       ls_max_iterations=1000, ls_error_tolerance=1e-12,
+                       precision=PRECISION_FP64, inner_tol=0.0, check_norm_rhs=True):
+        c = SolverConfig(ls_method, ls_precond, ls_max_iterations, precision, ls_error_tolerance,
+                         inner_tol, 1 if check_norm_rhs else 0, 0)
+        _check(lib().ogs_gpu_configure(self.h, C.byref(c)))
+
+    # Linear_EQS::Initialize
+    def Initialize(self):
+        _check(lib().ogs_gpu_initialize(self.h))
+
+    # CRFProcess::GlobalAssembly element loop
+    def GlobalAssembly(self, params: AssemblyParams, elem_k=None, u0=None, gp_velocity=None):
+        ek, u, gv = _f64(elem_k), _f64(u0), _f64(gp_velocity)
+        _check(lib().ogs_gpu_assemble(self.h, C.byref(params), _ptr(ek), _ptr(u), _ptr(gv)))
+
+    # SetKnownX_i over a node set (IncorporateBoundaryConditions)
+    def SetKnownX(self, rows, values, mode=DIRICHLET_ROW_ONLY):
+        r = rows if hasattr(rows, "data_ptr") else np.ascontiguousarray(rows, dtype=np.int64)
+        v = _f64(values)
+        _check(lib().ogs_gpu_set_dirichlet(self.h, _ptr(r), _ptr(v), len(r), mode))
+
+    # Linear_EQS::Solver; x is updated in place; returns the iteration count
+    def Solver(self, x, allow_fail=False):
+        st = SolveStats()
+        status = lib().ogs_gpu_solve(self.h, _ptr(x), C.byref(st))
+        self.last_stats = st
+        if not allow_fail:
+            _check(status)
+        return st.iterations
+
+    def stats(self) -> dict:
+        s = self.last_stats
+        return {"iterations": s.iterations, "status": s.status, "rel_residual": s.rel_residual,
+                "b_norm": s.b_norm, "refinements": s.refinements, "solve_ms": s.solve_ms}
+
+    def gp_velocity(self, params: AssemblyParams, elem_k, u, out=None):
+        ng = self.gmesh.n_gauss
+        if out is None:
+            out = np.zeros((self.gmesh.mesh.n_elements, ng, 3))
+        _check(lib().ogs_gpu_gp_velocity(self.h, C.byref(params), _ptr(_f64(elem_k)),
+                                         _ptr(_f64(u)), _ptr(out)))
+        return out
+
+    def get_csr(self):
+        nnz = self.gmesh.nnz
+        rp = np.zeros(self.n + 1, dtype=np.int64)
+        col = np.zeros(nnz, dtype=np.int64)
+        val = np.zeros(nnz)
+        _check(lib().ogs_gpu_get_csr(self.h, _ptr(rp), _ptr(col), _ptr(val)))
+        return rp, col, val
+
+    def get_values(self, out=None):
+        if out is None:
+            out = np.zeros(self.gmesh.nnz)
+        _check(lib().ogs_gpu_get_csr(self.h, None, None, _ptr(out)))
+        return out
+
+    def get_rhs(self, out=None):
+        if out is None:
+            out = np.zeros(self.n)
+        _check(lib().ogs_gpu_get_rhs(self.h, _ptr(out)))
+        return out
+
+    def spmv(self, x, out=None):
+        if out is None:
+            out = np.zeros(self.n)
+        _check(lib().ogs_gpu_spmv(self.h, _ptr(_f64(x)), _ptr(out)))
+        return out

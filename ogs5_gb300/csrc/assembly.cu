@@ -1,0 +1,662 @@
+// assembly.cu -- element-per-thread global assembly and Gauss-point flux.
+//
+// One thread per element.  The element loop of CRFProcess::GlobalAssembly
+// (FEM/rf_pcs.cpp:5738-5757) with CFiniteElementStd::Assembly
+// (FEM/fem_ele_std.cpp:9367) becomes one launch: each thread gathers its
+// node coordinates and primary variable, forms the local matrices in
+// registers, combines them into the LHS and RHS exactly as
+// AssembleParabolicEquation (fem_ele_std.cpp:7702-8126) or
+// AssembleMixedHyperbolicParabolicEquation (:8504-8735) does, and scatters
+// with FP64 atomics through the precomputed CSR slot map (no colouring).
+//
+// Two element paths:
+//  * general -- per Gauss point Jacobian, inverse and global gradients,
+//    CElement::computeJacobian / ComputeGradShapefct (FEM/fem_ele.cpp:585,
+//    1128), then CalcMass / CalcLaplace / CalcAdvection / CalcStorage in
+//    the reference's summation order;
+//  * affine  -- elements with a constant Jacobian (every tet, parallelogram
+//    quads, parallelepiped hexes): Laplace_ij = |J| sum_ab C_ab Q_abij and
+//    Mass_ij = c |J| M0_ij with reference tensors Q, M0 summed once over
+//    the Gauss points.  Mathematically identical, ~25x fewer FP64 FMAs on
+//    hexes, which matters on a part with 1.2 TFLOP/s of FP64.
+// Tables (N, dN/dxi, weights; Q, M0) are staged in shared memory per block.
+#include <cfloat>
+#include <cstdio>
+
+#include "common.cuh"
+
+namespace ogs {
+
+template <int ET> struct ElemTraits;
+template <> struct ElemTraits<OGS_ELEM_QUAD4> { static constexpr int NN = 4, DIM = 2; };
+template <> struct ElemTraits<OGS_ELEM_HEX8> { static constexpr int NN = 8, DIM = 3; };
+template <> struct ElemTraits<OGS_ELEM_TET4> { static constexpr int NN = 4, DIM = 3; };
+
+// Jacobian (row = local direction), |det| and the inverse, as
+// CElement::computeJacobian.  Returns false on |det| < DBL_EPSILON.
+template <int NN, int DIM>
+__device__ __forceinline__ bool jacobian(const double* X, const double* Y,
+                                         const double* Z, const double* dN,
+                                         double* iJ, double& det)
+{
+    double J[DIM * DIM];
+#pragma unroll
+    for (int k = 0; k < DIM * DIM; k++) J[k] = 0.0;
+    if (DIM == 2)
+    {
+#pragma unroll
+        for (int i = 0; i < NN; i++)
+        {
+            J[0] += X[i] * dN[i];
+            J[1] += Y[i] * dN[i];
+            J[2] += X[i] * dN[NN + i];
+            J[3] += Y[i] * dN[NN + i];
+        }
+        det = J[0] * J[3] - J[1] * J[2];
+        if (fabs(det) < DBL_EPSILON) return false;
+        iJ[0] = J[3] / det;
+        iJ[1] = -J[1] / det;
+        iJ[2] = -J[2] / det;
+        iJ[3] = J[0] / det;
+    }
+    else
+    {
+#pragma unroll
+        for (int i = 0; i < NN; i++)
+        {
+            J[0] += X[i] * dN[i];
+            J[1] += Y[i] * dN[i];
+            J[2] += Z[i] * dN[i];
+            J[3] += X[i] * dN[NN + i];
+            J[4] += Y[i] * dN[NN + i];
+            J[5] += Z[i] * dN[NN + i];
+            J[6] += X[i] * dN[2 * NN + i];
+            J[7] += Y[i] * dN[2 * NN + i];
+            J[8] += Z[i] * dN[2 * NN + i];
+        }
+        det = J[0] * (J[4] * J[8] - J[7] * J[5]) + J[6] * (J[1] * J[5] - J[4] * J[2]) +
+              J[3] * (J[2] * J[7] - J[8] * J[1]);
+        if (fabs(det) < DBL_EPSILON) return false;
+        iJ[0] = (J[4] * J[8] - J[7] * J[5]) / det;
+        iJ[1] = (J[2] * J[7] - J[1] * J[8]) / det;
+        iJ[2] = (J[1] * J[5] - J[2] * J[4]) / det;
+        iJ[3] = (J[5] * J[6] - J[8] * J[3]) / det;
+        iJ[4] = (J[0] * J[8] - J[6] * J[2]) / det;
+        iJ[5] = (J[2] * J[3] - J[5] * J[0]) / det;
+        iJ[6] = (J[3] * J[7] - J[6] * J[4]) / det;
+        iJ[7] = (J[1] * J[6] - J[7] * J[0]) / det;
+        iJ[8] = (J[0] * J[4] - J[3] * J[1]) / det;
+    }
+    det = fabs(det);
+    return true;
+}
+
+// global gradients dNg[j*NN+i] = sum_k iJ[j*DIM+k] dN[k*NN+i]
+template <int NN, int DIM>
+__device__ __forceinline__ void grad_global(const double* iJ, const double* dN, double* dNg)
+{
+#pragma unroll
+    for (int i = 0; i < NN; i++)
+#pragma unroll
+        for (int j = 0; j < DIM; j++)
+        {
+            double s = 0.0;
+#pragma unroll
+            for (int k = 0; k < DIM; k++) s += iJ[j * DIM + k] * dN[k * NN + i];
+            dNg[j * NN + i] = s;
+        }
+}
+
+// MassDispersionTensorNew (FEM/rf_mmp_new.cpp:3090-3328), isotropic
+// tortuosity: D = n S Daq tau I + alpha_T |q| I + (alpha_L - alpha_T) q q^T / |q|
+template <int DIM>
+__device__ __forceinline__ void dispersion(const ogs_assembly_params& p, const double* v,
+                                           double* D)
+{
+    const double dm = p.diffusion * p.porosity * p.saturation;
+    const double vg = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+#pragma unroll
+    for (int i = 0; i < DIM * DIM; i++) D[i] = 0.0;
+    if (fabs(vg) > DBL_EPSILON)
+    {
+        const double al = p.alpha_l, at = p.alpha_t;
+#pragma unroll
+        for (int i = 0; i < DIM; i++)
+#pragma unroll
+            for (int j = 0; j < DIM; j++)
+                D[i * DIM + j] = ((al - at) * (v[i] * v[j])) / vg;
+#pragma unroll
+        for (int i = 0; i < DIM; i++)
+            D[i * DIM + i] = (at * vg) + (al - at) * (v[i] * v[i]) / vg + dm;
+    }
+    else
+    {
+#pragma unroll
+        for (int i = 0; i < DIM; i++) D[i * DIM + i] = dm;
+    }
+#pragma unroll
+    for (int i = 0; i < DIM * DIM; i++) D[i] = D[i] * 1.0 * p.time_unit_factor;
+}
+
+// flow coefficient of the Laplace term: CalCoefLaplace GWF (:2308-2384,
+// mat = K * time_unit_factor * k_rel) or LIQUID_FLOW (:2232-2306,
+// mat = time_unit_factor * k / mu, mu -> 1 in the HEAD form)
+__device__ __forceinline__ double flow_mat(const ogs_assembly_params& p, double k)
+{
+    if (p.pcs_type == OGS_PCS_LIQUID_FLOW)
+    {
+        double mat_fac = p.viscosity;
+        if (p.gravity < DBL_EPSILON) mat_fac = 1.0;
+        return p.time_unit_factor * k / mat_fac * 1.0 * 1.0;
+    }
+    return k * p.time_unit_factor * 1.0;
+}
+
+// CalCoefMass for GWF (StorageFunction) and LIQUID_FLOW (Ss + n drho/dp)
+__device__ __forceinline__ double flow_mass_coef(const ogs_assembly_params& p)
+{
+    if (p.steady) return 0.0;
+    if (p.pcs_type == OGS_PCS_LIQUID_FLOW) return p.storage + p.porosity * p.drho_dp;
+    return p.storage;
+}
+
+__device__ __forceinline__ void flag_bad(int* bad, int64_t e)
+{
+    atomicMin(bad, (int)(e + 1));
+}
+
+// stage a table block into shared memory
+__device__ __forceinline__ void stage(double* dst, const double* src, int n)
+{
+    for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
+}
+
+template <int NN>
+__device__ __forceinline__ void gather(const AsmArgs& a, int64_t e, int* nd, double* X,
+                                       double* Y, double* Z, double* U)
+{
+    const int64_t E = a.E;
+#pragma unroll
+    for (int i = 0; i < NN; i++) nd[i] = __ldg(a.conn_t + (int64_t)i * E + e);
+#pragma unroll
+    for (int i = 0; i < NN; i++)
+    {
+        X[i] = __ldg(a.x + nd[i]);
+        Y[i] = __ldg(a.y + nd[i]);
+        Z[i] = __ldg(a.z + nd[i]);
+        U[i] = a.u0 ? __ldg(a.u0 + nd[i]) : 0.0;
+    }
+}
+
+template <int NN>
+__device__ __forceinline__ void scatter(const AsmArgs& a, int64_t e, const int* nd,
+                                        const double* S, const double* r)
+{
+    const int64_t E = a.E;
+#pragma unroll
+    for (int i = 0; i < NN; i++)
+    {
+#pragma unroll
+        for (int j = 0; j < NN; j++)
+        {
+            const int32_t k = __ldg(a.slot_t + (int64_t)(i * NN + j) * E + e);
+            atomicAdd(a.val + k, S[i * NN + j]);
+        }
+        atomicAdd(a.b + nd[i], r[i]);
+    }
+}
+
+// ------------------------------------------------------------------
+// flow: GROUNDWATER_FLOW / LIQUID_FLOW
+// ------------------------------------------------------------------
+template <int NN>
+__device__ __forceinline__ void flow_combine(const AsmArgs& a, int64_t e, const int* nd,
+                                             const double* U, const double* Ml,
+                                             const double* Ll, const double* grav)
+{
+    // AssembleParabolicEquation: fac1 = 1/dt, fac2 = relax0; RHS with relax1
+    const double dt_inverse = 1.0 / a.p.dt;
+    double relax0 = a.p.nls_relaxation;
+    if (relax0 < DBL_MIN) relax0 = 1.0;
+    const double relax1 = 1.0 - relax0;
+    double S[NN * NN], r[NN];
+#pragma unroll
+    for (int i = 0; i < NN; i++) r[i] = 0.0;
+#pragma unroll
+    for (int i = 0; i < NN; i++)
+#pragma unroll
+        for (int j = 0; j < NN; j++)
+        {
+            const int l = i >= j ? i * (i + 1) / 2 + j : j * (j + 1) / 2 + i;
+            const double m = Ml[l], lp = Ll[l];
+            S[i * NN + j] = m * dt_inverse + lp * relax0;
+            r[i] += (m * dt_inverse - lp * relax1) * U[j];
+        }
+    if (a.p.pcs_type == OGS_PCS_LIQUID_FLOW && a.p.gravity_on)
+#pragma unroll
+        for (int i = 0; i < NN; i++) r[i] += grav[i];
+    scatter<NN>(a, e, nd, S, r);
+}
+
+template <int ET, int NGP>
+__global__ void __launch_bounds__(128) k_flow_general(AsmArgs a)
+{
+    constexpr int NN = ElemTraits<ET>::NN, DIM = ElemTraits<ET>::DIM;
+    __shared__ double sN[NGP * NN], sdN[NGP * NN * DIM], sw[NGP * 3];
+    stage(sN, a.tab, NGP * NN);
+    stage(sdN, a.tab + NGP * NN, NGP * NN * DIM);
+    stage(sw, a.tab + NGP * NN + NGP * NN * DIM, NGP * 3);
+    __syncthreads();
+    const double cm = flow_mass_coef(a.p);
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < a.E;
+         e += (int64_t)gridDim.x * blockDim.x)
+    {
+        int nd[NN];
+        double X[NN], Y[NN], Z[NN], U[NN];
+        gather<NN>(a, e, nd, X, Y, Z, U);
+        const double mat = flow_mat(a.p, __ldg(a.elem_k + e));
+        double Ml[NN * (NN + 1) / 2], Ll[NN * (NN + 1) / 2], grav[NN];
+#pragma unroll
+        for (int l = 0; l < NN * (NN + 1) / 2; l++) Ml[l] = Ll[l] = 0.0;
+#pragma unroll
+        for (int i = 0; i < NN; i++) grav[i] = 0.0;
+        bool ok = true;
+#pragma unroll 1
+        for (int gp = 0; gp < NGP; gp++)
+        {
+            double iJ[DIM * DIM], det, dNg[DIM * NN];
+            if (!jacobian<NN, DIM>(X, Y, Z, sdN + gp * NN * DIM, iJ, det)) { ok = false; break; }
+            grad_global<NN, DIM>(iJ, sdN + gp * NN * DIM, dNg);
+            const double* w = sw + gp * 3;
+            const double fkt = ET == OGS_ELEM_HEX8 ? det * w[0] * w[1] * w[2]
+                             : ET == OGS_ELEM_QUAD4 ? det * w[0] * w[1] : det * w[0];
+            const double* sf = sN + gp * NN;
+            const double mf = cm * fkt * 1.0;
+#pragma unroll
+            for (int i = 0; i < NN; i++)
+#pragma unroll
+                for (int j = 0; j <= i; j++)
+                {
+                    const int l = i * (i + 1) / 2 + j;
+                    Ml[l] += mf * sf[i] * sf[j];
+                    double s = Ll[l];
+#pragma unroll
+                    for (int k = 0; k < DIM; k++) s += fkt * dNg[k * NN + i] * mat * dNg[k * NN + j];
+                    Ll[l] = s;
+                }
+            if (a.p.pcs_type == OGS_PCS_LIQUID_FLOW && a.p.gravity_on)
+            {
+                const double rho = a.p.gravity < DBL_EPSILON ? 1.0 : a.p.density * a.p.gravity;
+                const double fg = fkt * rho;
+#pragma unroll
+                for (int i = 0; i < NN; i++) grav[i] -= fg * dNg[(DIM - 1) * NN + i] * mat;
+            }
+        }
+        if (!ok) { flag_bad(a.bad_elem, e); continue; }
+        flow_combine<NN>(a, e, nd, U, Ml, Ll, grav);
+    }
+}
+
+// affine flow: C = mat * iJ^T iJ (isotropic), Laplace = |J| sum_ab C_ab Q_ab
+template <int ET>
+__global__ void __launch_bounds__(128) k_flow_affine(AsmArgs a)
+{
+    constexpr int NN = ElemTraits<ET>::NN, DIM = ElemTraits<ET>::DIM;
+    constexpr int NQ = DIM * DIM * NN * NN;
+    __shared__ double sQ[NQ], sM0[NN * NN], sdNc[DIM * NN];
+    stage(sQ, a.aff, NQ);
+    stage(sM0, a.aff + NQ, NN * NN);
+    stage(sdNc, a.aff + NQ + NN * NN, DIM * NN);
+    __syncthreads();
+    const double cm = flow_mass_coef(a.p);
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < a.E;
+         e += (int64_t)gridDim.x * blockDim.x)
+    {
+        int nd[NN];
+        double X[NN], Y[NN], Z[NN], U[NN];
+        gather<NN>(a, e, nd, X, Y, Z, U);
+        const double mat = flow_mat(a.p, __ldg(a.elem_k + e));
+        double iJ[DIM * DIM], det;
+        if (!jacobian<NN, DIM>(X, Y, Z, sdNc, iJ, det)) { flag_bad(a.bad_elem, e); continue; }
+        double C[DIM * DIM];
+#pragma unroll
+        for (int p = 0; p < DIM; p++)
+#pragma unroll
+            for (int q = 0; q < DIM; q++)
+            {
+                double s = 0.0;
+#pragma unroll
+                for (int k = 0; k < DIM; k++) s += iJ[k * DIM + p] * iJ[k * DIM + q];
+                C[p * DIM + q] = det * mat * s;
+            }
+        double Ml[NN * (NN + 1) / 2], Ll[NN * (NN + 1) / 2], grav[NN];
+        const double md = cm * det;
+#pragma unroll
+        for (int i = 0; i < NN; i++)
+#pragma unroll
+            for (int j = 0; j <= i; j++)
+            {
+                const int l = i * (i + 1) / 2 + j;
+                double s = 0.0;
+#pragma unroll
+                for (int pq = 0; pq < DIM * DIM; pq++) s += C[pq] * sQ[(pq * NN + i) * NN + j];
+                Ll[l] = s;
+                Ml[l] = md * sM0[i * NN + j];
+            }
+#pragma unroll
+        for (int i = 0; i < NN; i++) grav[i] = 0.0;
+        if (a.p.pcs_type == OGS_PCS_LIQUID_FLOW && a.p.gravity_on)
+        {
+            // -rho g |J| sum_gp w dNg_last,i = -rho g |J| sum_k iJ[last][k] sum_gp w dN_k,i;
+            // sum_gp w dN_k,i is Q-independent: recompute from the centre
+            // gradient (constant for affine tets) via the weight sum
+            const double rho = a.p.gravity < DBL_EPSILON ? 1.0 : a.p.density * a.p.gravity;
+            // sum_gp w_gp dN(gp) for affine maps equals vol_ref * dN(centre)
+            const double vol_ref = ET == OGS_ELEM_HEX8 ? 8.0 : ET == OGS_ELEM_QUAD4 ? 4.0 : 1.0 / 6.0;
+#pragma unroll
+            for (int i = 0; i < NN; i++)
+            {
+                double g = 0.0;
+#pragma unroll
+                for (int k = 0; k < DIM; k++) g += iJ[(DIM - 1) * DIM + k] * sdNc[k * NN + i];
+                grav[i] = -(det * rho * vol_ref) * g * mat;
+            }
+        }
+        flow_combine<NN>(a, e, nd, U, Ml, Ll, grav);
+    }
+}
+
+// ------------------------------------------------------------------
+// MASS_TRANSPORT
+// ------------------------------------------------------------------
+template <int NN>
+__device__ __forceinline__ void mt_combine(const AsmArgs& a, int64_t e, const int* nd,
+                                           const double* U, const double* Ml,
+                                           const double* L, const double* A,
+                                           const double* St)
+{
+    // AssembleMixedHyperbolicParabolicEquation (fem_ele_std.cpp:8592-8692)
+    const double dt_inverse = 1.0 / a.p.dt;
+    const double th = a.p.theta;
+    double S[NN * NN], r[NN];
+#pragma unroll
+    for (int i = 0; i < NN; i++) r[i] = 0.0;
+#pragma unroll
+    for (int i = 0; i < NN; i++)
+#pragma unroll
+        for (int j = 0; j < NN; j++)
+        {
+            const int l = i >= j ? i * (i + 1) / 2 + j : j * (j + 1) / 2 + i;
+            const int k = i * NN + j;
+            double s = Ml[l] * dt_inverse;
+            s += L[k] * th;
+            s += A[k] * th;
+            s += St[l] * th;
+            S[k] = s;
+            double q = Ml[l] * dt_inverse;
+            q += L[k] * (-(1.0 - th));
+            q += A[k] * (-(1.0 - th));
+            q += St[l] * (-(1.0 - th));
+            r[i] += q * U[j];
+        }
+    scatter<NN>(a, e, nd, S, r);
+}
+
+template <int ET, int NGP>
+__global__ void __launch_bounds__(128) k_mt_general(AsmArgs a)
+{
+    constexpr int NN = ElemTraits<ET>::NN, DIM = ElemTraits<ET>::DIM;
+    __shared__ double sN[NGP * NN], sdN[NGP * NN * DIM], sw[NGP * 3];
+    stage(sN, a.tab, NGP * NN);
+    stage(sdN, a.tab + NGP * NN, NGP * NN * DIM);
+    stage(sw, a.tab + NGP * NN + NGP * NN * DIM, NGP * 3);
+    __syncthreads();
+    const ogs_assembly_params& p = a.p;
+    const double cm = p.steady ? 0.0 : p.porosity * p.saturation * p.retardation;
+    const double cs = p.porosity * p.saturation * p.decay * p.retardation;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < a.E;
+         e += (int64_t)gridDim.x * blockDim.x)
+    {
+        int nd[NN];
+        double X[NN], Y[NN], Z[NN], U[NN];
+        gather<NN>(a, e, nd, X, Y, Z, U);
+        double Ml[NN * (NN + 1) / 2], St[NN * (NN + 1) / 2], L[NN * NN], A[NN * NN];
+#pragma unroll
+        for (int l = 0; l < NN * (NN + 1) / 2; l++) Ml[l] = St[l] = 0.0;
+#pragma unroll
+        for (int k = 0; k < NN * NN; k++) L[k] = A[k] = 0.0;
+        bool ok = true;
+        const double* ve = a.gpv + e * NGP * 3;
+#pragma unroll 1
+        for (int gp = 0; gp < NGP; gp++)
+        {
+            double iJ[DIM * DIM], det, dNg[DIM * NN];
+            if (!jacobian<NN, DIM>(X, Y, Z, sdN + gp * NN * DIM, iJ, det)) { ok = false; break; }
+            grad_global<NN, DIM>(iJ, sdN + gp * NN * DIM, dNg);
+            const double* w = sw + gp * 3;
+            const double fkt = ET == OGS_ELEM_HEX8 ? det * w[0] * w[1] * w[2]
+                             : ET == OGS_ELEM_QUAD4 ? det * w[0] * w[1] : det * w[0];
+            const double* sf = sN + gp * NN;
+            const double v[3] = {__ldg(ve + gp * 3), __ldg(ve + gp * 3 + 1), __ldg(ve + gp * 3 + 2)};
+            double D[DIM * DIM];
+            dispersion<DIM>(p, v, D);
+            const double mf = cm * fkt * 1.0;
+            const double fs = fkt * cs;
+            const double vt[3] = {1.0 * p.time_unit_factor * v[0], 1.0 * p.time_unit_factor * v[1],
+                                  1.0 * p.time_unit_factor * v[2]};
+#pragma unroll
+            for (int i = 0; i < NN; i++)
+            {
+#pragma unroll
+                for (int j = 0; j <= i; j++)
+                {
+                    const int l = i * (i + 1) / 2 + j;
+                    Ml[l] += mf * sf[i] * sf[j];
+                    St[l] += fs * sf[i] * sf[j];
+                }
+#pragma unroll
+                for (int j = 0; j < NN; j++)
+                {
+                    double s = L[i * NN + j], t = A[i * NN + j];
+#pragma unroll
+                    for (int k = 0; k < DIM; k++)
+                    {
+#pragma unroll
+                        for (int l2 = 0; l2 < DIM; l2++)
+                            s += fkt * dNg[k * NN + i] * D[DIM * k + l2] * dNg[l2 * NN + j];
+                        t += fkt * sf[i] * vt[k] * dNg[k * NN + j];
+                    }
+                    L[i * NN + j] = s;
+                    A[i * NN + j] = t;
+                }
+            }
+        }
+        if (!ok) { flag_bad(a.bad_elem, e); continue; }
+        mt_combine<NN>(a, e, nd, U, Ml, L, A, St);
+    }
+}
+
+// affine MASS_TRANSPORT on tets: gradients are constant, so
+// Laplace = |J| dNg^T (sum_gp w D(gp)) dNg and
+// Advection_ij = |J| sum_gp w N_i(gp) (v(gp) . dNg_j)
+__global__ void __launch_bounds__(128) k_mt_tet_affine(AsmArgs a)
+{
+    constexpr int NN = 4, DIM = 3, NGP = 5;
+    __shared__ double sN[NGP * NN], sw[NGP * 3], sM0[NN * NN], sdNc[DIM * NN];
+    stage(sN, a.tab, NGP * NN);
+    stage(sw, a.tab + NGP * NN + NGP * NN * DIM, NGP * 3);
+    stage(sM0, a.aff + DIM * DIM * NN * NN, NN * NN);
+    stage(sdNc, a.aff + DIM * DIM * NN * NN + NN * NN, DIM * NN);
+    __syncthreads();
+    const ogs_assembly_params& p = a.p;
+    const double cm = p.steady ? 0.0 : p.porosity * p.saturation * p.retardation;
+    const double cs = p.porosity * p.saturation * p.decay * p.retardation;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < a.E;
+         e += (int64_t)gridDim.x * blockDim.x)
+    {
+        int nd[NN];
+        double X[NN], Y[NN], Z[NN], U[NN];
+        gather<NN>(a, e, nd, X, Y, Z, U);
+        double iJ[DIM * DIM], det, dNg[DIM * NN];
+        if (!jacobian<NN, DIM>(X, Y, Z, sdNc, iJ, det)) { flag_bad(a.bad_elem, e); continue; }
+        grad_global<NN, DIM>(iJ, sdNc, dNg);
+        const double* ve = a.gpv + e * NGP * 3;
+        double Ds[DIM * DIM], A[NN * NN];
+#pragma unroll
+        for (int k = 0; k < DIM * DIM; k++) Ds[k] = 0.0;
+#pragma unroll
+        for (int k = 0; k < NN * NN; k++) A[k] = 0.0;
+#pragma unroll
+        for (int gp = 0; gp < NGP; gp++)
+        {
+            const double w = sw[gp * 3];
+            const double v[3] = {__ldg(ve + gp * 3), __ldg(ve + gp * 3 + 1), __ldg(ve + gp * 3 + 2)};
+            double D[DIM * DIM];
+            dispersion<DIM>(p, v, D);
+#pragma unroll
+            for (int k = 0; k < DIM * DIM; k++) Ds[k] += w * D[k];
+            const double tf = 1.0 * p.time_unit_factor;
+            double vd[NN];
+#pragma unroll
+            for (int j = 0; j < NN; j++)
+                vd[j] = tf * v[0] * dNg[j] + tf * v[1] * dNg[NN + j] + tf * v[2] * dNg[2 * NN + j];
+            const double wd = det * w;
+#pragma unroll
+            for (int i = 0; i < NN; i++)
+#pragma unroll
+                for (int j = 0; j < NN; j++) A[i * NN + j] += wd * sN[gp * NN + i] * vd[j];
+        }
+        double L[NN * NN], Ml[NN * (NN + 1) / 2], St[NN * (NN + 1) / 2];
+#pragma unroll
+        for (int i = 0; i < NN; i++)
+#pragma unroll
+            for (int j = 0; j < NN; j++)
+            {
+                double s = 0.0;
+#pragma unroll
+                for (int k = 0; k < DIM; k++)
+#pragma unroll
+                    for (int l = 0; l < DIM; l++) s += dNg[k * NN + i] * Ds[k * DIM + l] * dNg[l * NN + j];
+                L[i * NN + j] = det * s;
+            }
+#pragma unroll
+        for (int i = 0; i < NN; i++)
+#pragma unroll
+            for (int j = 0; j <= i; j++)
+            {
+                const int l = i * (i + 1) / 2 + j;
+                Ml[l] = cm * det * sM0[i * NN + j];
+                St[l] = cs * det * sM0[i * NN + j];
+            }
+        mt_combine<NN>(a, e, nd, U, Ml, L, A, St);
+    }
+}
+
+// ------------------------------------------------------------------
+// Gauss-point Darcy flux (Cal_Velocity scalar branch, fem_ele_std.cpp:6627-6870)
+// ------------------------------------------------------------------
+template <int ET, int NGP>
+__global__ void __launch_bounds__(128) k_gp_velocity(AsmArgs a)
+{
+    constexpr int NN = ElemTraits<ET>::NN, DIM = ElemTraits<ET>::DIM;
+    __shared__ double sdN[NGP * NN * DIM];
+    stage(sdN, a.tab + NGP * NN, NGP * NN * DIM);
+    __syncthreads();
+    const ogs_assembly_params& p = a.p;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < a.E;
+         e += (int64_t)gridDim.x * blockDim.x)
+    {
+        int nd[NN];
+        double X[NN], Y[NN], Z[NN], U[NN];
+        gather<NN>(a, e, nd, X, Y, Z, U);
+        const double mat = flow_mat(p, __ldg(a.elem_k + e));
+        double* qo = a.q_out + e * NGP * 3;
+#pragma unroll 1
+        for (int gp = 0; gp < NGP; gp++)
+        {
+            double iJ[DIM * DIM], det, dNg[DIM * NN];
+            if (!jacobian<NN, DIM>(X, Y, Z, sdN + gp * NN * DIM, iJ, det)) { flag_bad(a.bad_elem, e); break; }
+            grad_global<NN, DIM>(iJ, sdN + gp * NN * DIM, dNg);
+            double vel[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+            for (int i = 0; i < DIM; i++)
+            {
+                double s = 0.0;
+#pragma unroll
+                for (int j = 0; j < NN; j++) s += U[j] * dNg[i * NN + j];
+                vel[i] = s;
+            }
+            if (p.pcs_type == OGS_PCS_LIQUID_FLOW && p.gravity_on && p.gravity >= DBL_EPSILON)
+                vel[DIM - 1] += p.gravity * p.density;
+            double q[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+            for (int i = 0; i < DIM; i++) q[i] -= mat * vel[i] / p.time_unit_factor;
+            qo[gp * 3 + 0] = q[0];
+            qo[gp * 3 + 1] = q[1];
+            qo[gp * 3 + 2] = q[2];
+        }
+    }
+}
+
+static int grid_for(int64_t E, int threads)
+{
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t need = (E + threads - 1) / threads;
+    const int64_t cap = (int64_t)sms * 16;
+    return (int)std::max<int64_t>(1, std::min(need, cap));
+}
+
+template <int ET, int NGP>
+static void launch_flow(const AsmArgs& a, bool affine, cudaStream_t s)
+{
+    const int g = grid_for(a.E, 128);
+    if (affine)
+        k_flow_affine<ET><<<g, 128, 0, s>>>(a);
+    else
+        k_flow_general<ET, NGP><<<g, 128, 0, s>>>(a);
+}
+
+template <int ET, int NGP>
+static void launch_mt(const AsmArgs& a, bool affine, cudaStream_t s)
+{
+    const int g = grid_for(a.E, 128);
+    if (ET == OGS_ELEM_TET4 && affine)
+        k_mt_tet_affine<<<g, 128, 0, s>>>(a);
+    else
+        k_mt_general<ET, NGP><<<g, 128, 0, s>>>(a);
+}
+
+template <int ET, int NGP>
+static void launch_vel(const AsmArgs& a, cudaStream_t s)
+{
+    k_gp_velocity<ET, NGP><<<grid_for(a.E, 128), 128, 0, s>>>(a);
+}
+
+// dispatch on (element type, Gauss points); returns false for an
+// unsupported combination
+bool launch_assembly(const ogs_mesh* m, const AsmArgs& a, bool affine, int kind,
+                     cudaStream_t s)
+{
+    const int et = m->elem_type, ngp = m->ngp;
+#define OGS_DISPATCH(ET_, NGP_)                                      \
+    if (et == ET_ && ngp == NGP_)                                    \
+    {                                                                \
+        if (kind == 0) launch_flow<ET_, NGP_>(a, affine, s);         \
+        else if (kind == 1) launch_mt<ET_, NGP_>(a, affine, s);      \
+        else launch_vel<ET_, NGP_>(a, s);                            \
+        return true;                                                 \
+    }
+    OGS_DISPATCH(OGS_ELEM_QUAD4, 1)
+    OGS_DISPATCH(OGS_ELEM_QUAD4, 4)
+    OGS_DISPATCH(OGS_ELEM_QUAD4, 9)
+    OGS_DISPATCH(OGS_ELEM_HEX8, 1)
+    OGS_DISPATCH(OGS_ELEM_HEX8, 8)
+    OGS_DISPATCH(OGS_ELEM_HEX8, 27)
+    OGS_DISPATCH(OGS_ELEM_TET4, 5)
+#undef OGS_DISPATCH
+    return false;
+}
+
+}  // namespace ogs

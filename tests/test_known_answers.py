@@ -1,0 +1,82 @@
+"""Closed-form known answers for the oracle's element matrices."""
+import numpy as np
+import pytest
+
+from ogs5_gb300 import mesh as M
+
+
+def unit_elem(et):
+    if et == 1:
+        m = M.structured_hex(1, 1, 1)
+    elif et == 0:
+        m = M.structured_quad(1, 1)
+    else:
+        m = M.structured_tet(1, 1, 1)
+        m.conn = m.conn[:1]
+    return np.stack([m.x[m.conn[0]], m.y[m.conn[0]], m.z[m.conn[0]]], axis=1)
+
+
+def test_unit_cube_hex_laplace(oracle):
+    c = unit_elem(1)
+    m = oracle.element_matrices(1, c, oracle.make_params(pcs_type=0, storage=1.0), k_e=1.0)
+    L, Ms = m["laplace"], m["mass"]
+    assert np.allclose(np.diag(L), 1 / 3, rtol=1e-13)
+    assert np.allclose(L.sum(axis=1), 0.0, atol=1e-14)
+    # nodes 0 and 6 are opposite corners: -1/12; face diagonal 0-2: -1/12; edge 0-1: 0
+    assert abs(L[0, 6] + 1 / 12) < 1e-14 and abs(L[0, 2] + 1 / 12) < 1e-14 and abs(L[0, 1]) < 1e-14
+    # consistent mass of the unit cube: diag 1/27, total 1
+    assert abs(Ms[0, 0] - 1 / 27) < 1e-14 and abs(Ms.sum() - 1.0) < 1e-13
+
+
+def test_unit_square_quad(oracle):
+    c = unit_elem(0)
+    m = oracle.element_matrices(0, c, oracle.make_params(pcs_type=0, storage=1.0), k_e=1.0)
+    L, Ms = m["laplace"], m["mass"]
+    assert np.allclose(np.diag(L), 2 / 3, rtol=1e-13)
+    assert abs(L[0, 2] + 1 / 3) < 1e-14 and abs(L[0, 1] + 1 / 6) < 1e-14
+    assert abs(Ms[0, 0] - 1 / 9) < 1e-14 and abs(Ms.sum() - 1.0) < 1e-13
+
+
+def test_reference_tet(oracle):
+    c = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]], dtype=float)
+    m = oracle.element_matrices(2, c, oracle.make_params(pcs_type=0, storage=1.0), k_e=1.0)
+    L, Ms = m["laplace"], m["mass"]
+    vol = 1 / 6
+    g = np.array([[-1, -1, -1], [1, 0, 0], [0, 1, 0], [0, 0, 1]], dtype=float)
+    assert np.allclose(L, vol * g @ g.T, rtol=1e-12, atol=1e-15)
+    # the 5-point rule (negative centre weight) integrates N_i N_j exactly
+    want = vol / 20 * (np.ones((4, 4)) + np.eye(4))
+    assert np.allclose(Ms, want, rtol=1e-12)
+
+
+def test_linear_profile_exact(oracle):
+    """Config-1 deck: h = 1 - x/100 is reproduced to rounding."""
+    m = M.structured_quad(100, 100)
+    rp, col = oracle.build_pattern(m.n_nodes, m.conn)
+    assert len(col) == 301 * 301  # 90,601 stored entries
+    p = oracle.make_params(pcs_type=0, steady=1)
+    val, b = oracle.assemble(m, rp, col, p, elem_k=np.full(m.n_elements, 1e-4), u0=np.zeros(m.n_nodes))
+    lf, rf = m.face_nodes(0, 0), m.face_nodes(0, 1)
+    rows = np.concatenate([lf, rf])
+    vals = np.concatenate([np.ones(len(lf)), np.zeros(len(rf))])
+    oracle.dirichlet(rp, col, val, b, rows, vals)
+    x0 = np.full(m.n_nodes, 0.5)
+    x0[lf], x0[rf] = 1.0, 0.0
+    x, info = oracle.solve(rp, col, val, b, x0, method=2, precond=1, tol=1e-10)
+    assert info["rel_residual"] < 1e-10
+    assert np.abs(x - (1 - m.x / 100)).max() < 1e-8  # residual 1e-10 x conditioning
+
+
+def test_advection_dispersion_known_answer(oracle):
+    """Tet, uniform flux q along x: advection row sums vanish (sum_j dN_j = 0)
+    and the dispersion tensor is alpha_L|q| along x, alpha_T|q| across."""
+    c = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]], dtype=float)
+    q = 2e-5
+    vel = np.zeros((5, 3))
+    vel[:, 0] = q
+    p = oracle.make_params(pcs_type=2, porosity=0.3, alpha_l=1.0, alpha_t=0.1, diffusion=0.0)
+    m = oracle.element_matrices(2, c, p, vel=vel)
+    assert np.allclose(m["advection"].sum(axis=1), 0.0, atol=1e-20)
+    g = np.array([[-1, -1, -1], [1, 0, 0], [0, 1, 0], [0, 0, 1]], dtype=float)
+    D = np.diag([1.0 * q, 0.1 * q, 0.1 * q])
+    assert np.allclose(m["laplace"], (1 / 6) * g @ D @ g.T, rtol=1e-11, atol=1e-22)

@@ -1,0 +1,315 @@
+"""Parity of the CUDA path (through the C ABI) against the CPU oracle.
+
+Assembly: every entry of A and b within 1e-12 relative (floor 1e-14 x row
+max), for quad/hex/tet x GROUNDWATER_FLOW/LIQUID_FLOW/MASS_TRANSPORT, on
+affine meshes (affine kernels) and distorted meshes (per-Gauss-point
+kernels).  Solves: converged heads within 1e-10 relative of the oracle's
+Linear_EQS iteration on the same system and initial guess.
+"""
+import numpy as np
+import pytest
+
+from ogs5_gb300 import fields
+from ogs5_gb300 import mesh as M
+from tests.helpers import (SOLUTION_RTOL, assert_matrix_close, assert_vector_close, distort,
+                           rel_max_err)
+
+pytestmark = pytest.mark.gpu
+
+
+def small_mesh(kind):
+    if kind == "quad":
+        return M.structured_quad(12, 9, 1.0, 0.5)
+    if kind == "hex":
+        return M.structured_hex(6, 5, 4, 1.0, 2.0, 0.5)
+    return M.structured_tet(4, 3, 3, 1.0, 1.5, 0.75)
+
+
+def k_field(m, seed=1):
+    rng = np.random.default_rng(seed)
+    return np.exp(np.log(1e-5) + rng.standard_normal(m.n_elements))
+
+
+def oracle_params(O, gp, **over):
+    """oracle AssemblyParams with the same values as a capi AssemblyParams"""
+    names = [f[0] for f in gp._fields_]
+    return O.make_params(**{n: getattr(gp, n) for n in names if n != "pad0"})
+
+
+def run_assembly(gpu, oracle, m, params, ek=None, u0=None, gpv=None, ngauss=3):
+    gm = gpu.GpuMesh(m, gauss_points=ngauss)
+    eqs = gpu.LinearEQS(gm)
+    eqs.Initialize()
+    eqs.GlobalAssembly(params, ek, u0, gpv)
+    rp, col, val = eqs.get_csr()
+    b = eqs.get_rhs()
+    orp, ocol = oracle.build_pattern(m.n_nodes, m.conn)
+    assert np.array_equal(rp, orp) and np.array_equal(col, ocol), "CSR pattern differs"
+    oval, ob = oracle.assemble(m, orp, ocol, oracle_params(oracle, params), elem_k=ek, u0=u0,
+                               gp_vel=gpv, ngauss=ngauss)
+    return eqs, gm, (rp, col, val, b), (oval, ob)
+
+
+@pytest.mark.parametrize("kind", ["quad", "hex", "tet"])
+@pytest.mark.parametrize("distorted", [False, True])
+@pytest.mark.parametrize("ngauss", [2, 3])
+def test_assembly_groundwater_flow(gpu, oracle, kind, distorted, ngauss):
+    if kind == "tet" and ngauss == 2:
+        pytest.skip("tets always use the 5-point rule")
+    m = small_mesh(kind)
+    if distorted:
+        m = distort(m, 0.2, seed=3)
+    ek = k_field(m)
+    rng = np.random.default_rng(7)
+    u0 = rng.uniform(0, 10, m.n_nodes)
+    p = gpu.make_params(gpu.GROUNDWATER_FLOW, dt=3600.0, storage=1e-4)
+    eqs, gm, (rp, col, val, b), (oval, ob) = run_assembly(gpu, oracle, m, p, ek, u0, ngauss=ngauss)
+    assert_matrix_close(rp, val, oval)
+    assert_vector_close(b, ob)
+
+
+@pytest.mark.parametrize("kind", ["quad", "hex", "tet"])
+def test_assembly_groundwater_relaxation_and_steady(gpu, oracle, kind):
+    m = small_mesh(kind)
+    ek = k_field(m, 2)
+    u0 = np.random.default_rng(1).uniform(0, 1, m.n_nodes)
+    for kw in ({"nls_relaxation": 0.6, "storage": 2e-4, "dt": 10.0},
+               {"steady": 1, "storage": 1e-4, "dt": 1.0}):
+        p = gpu.make_params(gpu.GROUNDWATER_FLOW, **kw)
+        _, _, (rp, col, val, b), (oval, ob) = run_assembly(gpu, oracle, m, p, ek, u0)
+        assert_matrix_close(rp, val, oval)
+        assert_vector_close(b, ob)
+
+
+@pytest.mark.parametrize("kind", ["quad", "hex", "tet"])
+@pytest.mark.parametrize("distorted", [False, True])
+def test_assembly_liquid_flow_gravity(gpu, oracle, kind, distorted):
+    m = small_mesh(kind)
+    if distorted:
+        m = distort(m, 0.15, seed=5)
+    ek = k_field(m, 3) * 1e-7  # permeability
+    u0 = np.random.default_rng(2).uniform(1e5, 2e5, m.n_nodes)
+    p = gpu.make_params(gpu.LIQUID_FLOW, dt=100.0, storage=1e-9, porosity=0.3, drho_dp=4.5e-10,
+                        viscosity=1e-3, density=1000.0, gravity=9.81, gravity_on=1)
+    _, _, (rp, col, val, b), (oval, ob) = run_assembly(gpu, oracle, m, p, ek, u0)
+    assert_matrix_close(rp, val, oval)
+    assert_vector_close(b, ob)
+
+
+@pytest.mark.parametrize("kind", ["quad", "hex", "tet"])
+@pytest.mark.parametrize("distorted", [False, True])
+def test_assembly_mass_transport(gpu, oracle, kind, distorted):
+    m = small_mesh(kind)
+    if distorted:
+        m = distort(m, 0.15, seed=9)
+    ngp = {"quad": 9, "hex": 27, "tet": 5}[kind]
+    rng = np.random.default_rng(11)
+    gpv = rng.normal(0, 1e-5, (m.n_elements, ngp, 3))
+    if m.dim == 2:
+        gpv[:, :, 2] = 0.0
+    gpv[0, :, :] = 0.0  # zero-velocity branch of the dispersion tensor
+    c0 = rng.uniform(0, 1, m.n_nodes)
+    p = gpu.make_params(gpu.MASS_TRANSPORT, dt=3600.0, theta=0.6, porosity=0.3,
+                        alpha_l=1.0, alpha_t=0.1, diffusion=1e-9, decay=1e-7, retardation=1.5)
+    _, _, (rp, col, val, b), (oval, ob) = run_assembly(gpu, oracle, m, p, None, c0, gpv)
+    assert_matrix_close(rp, val, oval)
+    assert_vector_close(b, ob)
+
+
+@pytest.mark.parametrize("kind", ["quad", "hex", "tet"])
+@pytest.mark.parametrize("distorted", [False, True])
+def test_gp_velocity(gpu, oracle, kind, distorted):
+    m = small_mesh(kind)
+    if distorted:
+        m = distort(m, 0.2, seed=4)
+    ek = k_field(m, 4)
+    h = np.random.default_rng(3).uniform(0, 10, m.n_nodes)
+    for pcs, kw in ((gpu.GROUNDWATER_FLOW, {}),
+                    (gpu.LIQUID_FLOW, {"gravity": 9.81, "gravity_on": 1, "viscosity": 1e-3})):
+        p = gpu.make_params(pcs, **kw)
+        gm = gpu.GpuMesh(m)
+        eqs = gpu.LinearEQS(gm)
+        q = eqs.gp_velocity(p, ek, h)
+        qo = oracle.gp_velocity(m, oracle_params(oracle, p), ek, h)
+        assert_vector_close(q.ravel(), qo.ravel())
+
+
+@pytest.mark.parametrize("symmetric", [False, True])
+def test_dirichlet(gpu, oracle, symmetric):
+    m = M.structured_hex(7, 5, 4)
+    ek = k_field(m, 5)
+    p = gpu.make_params(gpu.GROUNDWATER_FLOW, dt=3600.0, storage=1e-4)
+    u0 = np.zeros(m.n_nodes)
+    eqs, gm, (rp, col, val, b), (oval, ob) = run_assembly(gpu, oracle, m, p, ek, u0)
+    rows = np.concatenate([m.face_nodes(0, 0), m.face_nodes(0, 1), m.face_nodes(2, 0)[:7]])
+    rows = np.concatenate([rows, rows[:3]])  # duplicates, as repeated SetKnownX_i calls
+    vals = np.concatenate([np.full(len(m.face_nodes(0, 0)), 10.0),
+                           np.zeros(len(m.face_nodes(0, 1))), np.linspace(1, 2, 7)])
+    vals = np.concatenate([vals, vals[:3]])
+    eqs.SetKnownX(rows, vals, gpu.DIRICHLET_SYMMETRIC if symmetric else gpu.DIRICHLET_ROW_ONLY)
+    val2 = eqs.get_values()
+    b2 = eqs.get_rhs()
+    oracle.dirichlet(rp, col, oval, ob, rows, vals, symmetric=symmetric)
+    assert_matrix_close(rp, val2, oval)
+    assert_vector_close(b2, ob)
+
+
+def test_spmv(gpu, oracle):
+    m = M.structured_tet(5, 4, 3)
+    ek = k_field(m, 6)
+    p = gpu.make_params(gpu.GROUNDWATER_FLOW, dt=1.0, storage=1e-3)
+    eqs, gm, (rp, col, val, b), (oval, ob) = run_assembly(gpu, oracle, m, p, ek, np.zeros(m.n_nodes))
+    x = np.random.default_rng(0).standard_normal(m.n_nodes)
+    y = eqs.spmv(x)
+    yo = oracle.spmv(rp, col, val, x)
+    assert_vector_close(y, yo, rtol=1e-12, scale=np.abs(val).max() * np.abs(x).max())
+
+
+def _flow_system(gpu, oracle, m, ek, symmetric, dt=None, storage=0.0, left=1.0, right=0.0):
+    p = gpu.make_params(gpu.GROUNDWATER_FLOW, dt=dt or 1.0, storage=storage, steady=0 if dt else 1)
+    gm = gpu.GpuMesh(m)
+    eqs = gpu.LinearEQS(gm)
+    eqs.Initialize()
+    u0 = np.zeros(m.n_nodes)
+    eqs.GlobalAssembly(p, ek, u0)
+    lf, rf = m.face_nodes(0, 0), m.face_nodes(0, 1)
+    rows = np.concatenate([lf, rf])
+    vals = np.concatenate([np.full(len(lf), left), np.full(len(rf), right)])
+    eqs.SetKnownX(rows, vals, gpu.DIRICHLET_SYMMETRIC if symmetric else gpu.DIRICHLET_ROW_ONLY)
+    rp, col, val = eqs.get_csr()
+    b = eqs.get_rhs()
+    x0 = np.full(m.n_nodes, 0.5 * (left + right))
+    x0[lf] = left
+    x0[rf] = right
+    return eqs, (rp, col, val, b), x0
+
+
+def test_config1_bicgstab_jacobi_linear_profile(gpu, oracle):
+    """Config-1 deck: 100x100 quads, K=1e-4, h=1|0 on the x faces, BiCGStab+Jacobi 1e-10."""
+    m = M.structured_quad(100, 100)
+    ek = np.full(m.n_elements, 1e-4)
+    eqs, (rp, col, val, b), x0 = _flow_system(gpu, oracle, m, ek, symmetric=False)
+    eqs.ConfigNumerics(gpu.LS_BICGSTAB, gpu.PRECOND_JACOBI, 1000, 1e-10)
+    x = x0.copy()
+    it = eqs.Solver(x)
+    xo, info = oracle.solve(rp, col, val, b, x0, method=2, precond=1, max_iter=1000, tol=1e-10)
+    assert abs(it - info["iterations"]) <= 2
+    assert eqs.stats()["rel_residual"] < 1e-10
+    assert rel_max_err(x, xo) < SOLUTION_RTOL
+    assert np.abs(x - (1.0 - m.x / 100.0)).max() < 1e-8  # exact bilinear solution
+
+
+@pytest.mark.parametrize("kind", ["hex", "tet"])
+def test_cg_jacobi_heterogeneous(gpu, oracle, kind):
+    m = M.structured_hex(16, 12, 8) if kind == "hex" else M.structured_tet(10, 8, 6)
+    nh = (m.shape[0] * m.shape[1] * m.shape[2])
+    kh = fields.lognormal_k(m.shape, np.log(1e-5), 1.0, 3.0, seed=2)
+    ek = kh if kind == "hex" else np.repeat(kh, 6)
+    assert len(ek) == m.n_elements and nh > 0
+    eqs, (rp, col, val, b), x0 = _flow_system(gpu, oracle, m, ek, symmetric=True, dt=3600.0,
+                                              storage=1e-4, left=10.0, right=0.0)
+    eqs.ConfigNumerics(gpu.LS_CG, gpu.PRECOND_JACOBI, 5000, 1e-13)
+    x = x0.copy()
+    it = eqs.Solver(x)
+    xo, info = oracle.solve(rp, col, val, b, x0, method=5, precond=1, max_iter=5000, tol=1e-13)
+    assert abs(it - info["iterations"]) <= max(2, info["iterations"] // 50)
+    assert rel_max_err(x, xo) < SOLUTION_RTOL
+
+
+@pytest.mark.parametrize("precond", [0, 1])
+def test_bicgstab_matches_oracle_iterates(gpu, oracle, precond):
+    m = M.structured_hex(10, 8, 6)
+    ek = k_field(m, 8)
+    eqs, (rp, col, val, b), x0 = _flow_system(gpu, oracle, m, ek, symmetric=False, dt=100.0,
+                                              storage=1e-3, left=3.0, right=1.0)
+    eqs.ConfigNumerics(gpu.LS_BICGSTAB, precond, 2000, 1e-12)
+    x = x0.copy()
+    it = eqs.Solver(x)
+    xo, info = oracle.solve(rp, col, val, b, x0, method=2, precond=precond, max_iter=2000, tol=1e-12)
+    assert abs(it - info["iterations"]) <= 2
+    assert rel_max_err(x, xo) < SOLUTION_RTOL
+
+
+def test_check_norm_rhs_and_max_iter_status(gpu, oracle):
+    """CheckNormRHS: a second solve whose |b| dropped below tol*|b_prev| returns
+    at once; max_iter=1 reports NOT_CONVERGED (host-side fault injection)."""
+    m = M.structured_quad(20, 20)
+    ek = np.full(m.n_elements, 1e-4)
+    eqs, (rp, col, val, b), x0 = _flow_system(gpu, oracle, m, ek, symmetric=False)
+    eqs.ConfigNumerics(gpu.LS_BICGSTAB, gpu.PRECOND_JACOBI, 1, 1e-10)
+    x = x0.copy()
+    eqs.Solver(x, allow_fail=True)
+    assert eqs.stats()["status"] == gpu.NOT_CONVERGED
+    # second solve, b scaled by 1e-12: |b|/|b_prev| < tol -> immediate return
+    eqs.ConfigNumerics(gpu.LS_BICGSTAB, gpu.PRECOND_JACOBI, 1000, 1e-10)
+    eqs.Initialize()
+    eqs.GlobalAssembly(gpu.make_params(gpu.GROUNDWATER_FLOW, steady=1), ek * 1e-12, np.zeros(m.n_nodes))
+    lf = m.face_nodes(0, 0)
+    eqs.SetKnownX(lf, np.full(len(lf), 1.0))
+    x2 = np.zeros(m.n_nodes)
+    it = eqs.Solver(x2)
+    assert it == 0 and eqs.stats()["status"] == gpu.OK
+
+
+def test_error_statuses(gpu):
+    m = M.structured_hex(3, 3, 3)
+    # degenerate element -> SINGULAR_JACOBIAN, not a trap
+    bad = M.structured_hex(3, 3, 3)
+    bad.x = bad.x.copy()
+    e0 = bad.conn[0]
+    bad.x[e0] = bad.x[e0[0]]
+    bad.y = bad.y.copy()
+    bad.y[e0] = bad.y[e0[0]]
+    bad.z = bad.z.copy()
+    bad.z[e0] = bad.z[e0[0]]
+    gm = gpu.GpuMesh(bad)
+    eqs = gpu.LinearEQS(gm)
+    with pytest.raises(gpu.OgsError) as ei:
+        eqs.GlobalAssembly(gpu.make_params(), np.ones(bad.n_elements), np.zeros(bad.n_nodes))
+    assert ei.value.status == gpu.SINGULAR_JACOBIAN
+    # NaN conductivity -> NONFINITE from the solver
+    gm = gpu.GpuMesh(m)
+    eqs = gpu.LinearEQS(gm)
+    ek = np.ones(m.n_elements)
+    ek[5] = np.nan
+    eqs.GlobalAssembly(gpu.make_params(steady=1), ek, np.zeros(m.n_nodes))
+    eqs.SetKnownX(m.face_nodes(0, 0), np.ones(len(m.face_nodes(0, 0))))
+    x = np.zeros(m.n_nodes)
+    eqs.Solver(x, allow_fail=True)
+    assert eqs.stats()["status"] == gpu.NONFINITE
+    # bad arguments
+    with pytest.raises(gpu.OgsError) as ei:
+        eqs.SetKnownX([m.n_nodes + 5], [1.0])
+    assert ei.value.status == gpu.BAD_ARG
+    with pytest.raises(gpu.OgsError):
+        eqs.ConfigNumerics(ls_method=13)
+    with pytest.raises(gpu.OgsError):
+        eqs.GlobalAssembly(gpu.make_params(dt=0.0), np.ones(m.n_elements), np.zeros(m.n_nodes))
+
+
+def test_device_pointers(gpu, oracle):
+    """torch CUDA tensors are used in place (no host staging)."""
+    import torch
+    m = M.structured_hex(8, 6, 5)
+    ek = k_field(m, 9)
+    p = gpu.make_params(gpu.GROUNDWATER_FLOW, dt=3600.0, storage=1e-4)
+    gm = gpu.GpuMesh(m)
+    eqs = gpu.LinearEQS(gm)
+    eqs.Initialize()
+    ek_d = torch.tensor(ek, device="cuda")
+    u_d = torch.zeros(m.n_nodes, dtype=torch.float64, device="cuda")
+    eqs.GlobalAssembly(p, ek_d, u_d)
+    torch.cuda.synchronize()
+    rp, col, val = eqs.get_csr()
+    oval, ob = oracle.assemble(m, rp, col, oracle_params(oracle, p), elem_k=ek, u0=np.zeros(m.n_nodes))
+    assert_matrix_close(rp, val, oval)
+    # steady system with one Dirichlet face: the solution is that value everywhere
+    eqs.Initialize()
+    eqs.GlobalAssembly(gpu.make_params(gpu.GROUNDWATER_FLOW, steady=1), ek_d, u_d)
+    lf = torch.tensor(m.face_nodes(0, 0), device="cuda")
+    eqs.SetKnownX(lf, torch.full((len(lf),), 2.0, dtype=torch.float64, device="cuda"),
+                  gpu.DIRICHLET_SYMMETRIC)
+    eqs.ConfigNumerics(gpu.LS_CG, gpu.PRECOND_JACOBI, 2000, 1e-12)
+    x = torch.zeros(m.n_nodes, dtype=torch.float64, device="cuda")
+    eqs.Solver(x)
+    assert torch.allclose(x, torch.full_like(x, 2.0), rtol=0, atol=1e-9)
