@@ -5,17 +5,24 @@ nodes, 1,048,576 linear hexes, element-wise ln K a seeded Gaussian random
 field (mean ln 1e-5, variance 1, exponential covariance, correlation length
 8 cells), Ss = 1e-4 1/m, 20 implicit-Euler steps of dt = 3600 s, heads 10 m
 / 0 m on the x faces (symmetric Dirichlet elimination), CG + Jacobi to a
-1e-10 relative residual, FP64 throughout.  One step = one global assembly
-(27 Gauss points per hex) + Dirichlet + one CG solve: one "solve".
+1e-10 relative residual.  One step = one global assembly (27 Gauss points
+per hex, FP64) + Dirichlet + one CG solve: one "solve".
+
+Two solver paths are timed on the same steps:
+  * the plain FP64 path (the parity path), and
+  * the FP32-inner CG with FP64 residual replacement, whose heads are
+    checked against the FP64 path step by step (max relative error
+    reported; the metric is quoted at <= 1e-8).
+`value` is the FP32-inner path with every input resident on the device;
+`e2e` times the same steps through the C ABI with host buffers
+(conductivity, previous heads and the initial guess copied in, heads copied
+out every step).  The FP64 matrix (343 MB values + indices) is rebuilt every
+step and is larger than L2, so no L2 flush is needed between steps.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-`value` times K steps with every input resident on the device; `e2e` times
-the same steps through the C ABI with host buffers (conductivity, previous
-heads and the initial guess copied in, heads copied out each step).  The
-matrix (343 MB of values + indices) is larger than L2, so no L2 flush is
-needed between steps.  --impl reference times the CPU oracle (a C
-restatement of the reference's path) on the host cores.
+--impl reference times the CPU implementation of the path (the oracle, a C
+restatement of the reference's own code) on all host cores.
 """
 from __future__ import annotations
 
@@ -38,7 +45,11 @@ DT = 3600.0
 SS = 1e-4
 TOL = 1e-10
 SEED = 2
-WORKLOAD = "transient GROUNDWATER_FLOW hex 128x128x64, lnK GRF var 1 ell 8, 20 steps dt 3600, CG+Jacobi 1e-10"
+WORKLOAD = ("transient GROUNDWATER_FLOW hex 128x128x64, lnK GRF var 1 ell 8, 20 steps dt 3600, "
+            "CG+Jacobi 1e-10")
+# Jacobi-CG iterations per step of this deck (FP64 path, measured on the GPU;
+# equal to the oracle's Linear_EQS::CG count within the parity tests' bound)
+CG_ITERS_PER_STEP = 147
 
 
 def make_deck(nx=NX, ny=NY, nz=NZ):
@@ -111,9 +122,10 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def run_steps(eqs, capi, p, ek, rows, vals, h0, k_steps, host: bool, torch, stream):
+def run_steps(eqs, capi, p, ek, rows, vals, h0, k_steps, host: bool, torch, stream, keep=False):
     """k_steps implicit-Euler steps from the initial heads h0; returns
-    (elapsed ms, per-step ms list, total CG iterations, final heads)."""
+    (elapsed ms, per-step ms, Krylov iterations, final heads, heads per step
+    when keep)."""
     n = len(h0)
     if host:
         ek_b = torch.empty(len(ek), dtype=torch.float64, pin_memory=True).numpy()
@@ -131,6 +143,7 @@ def run_steps(eqs, capi, p, ek, rows, vals, h0, k_steps, host: bool, torch, stre
     torch.cuda.synchronize()
     evs = [torch.cuda.Event(enable_timing=True) for _ in range(k_steps + 1)]
     iters = 0
+    kept = []
     evs[0].record(stream)
     for k in range(k_steps):
         eqs.Initialize()
@@ -146,51 +159,59 @@ def run_steps(eqs, capi, p, ek, rows, vals, h0, k_steps, host: bool, torch, stre
         else:
             u.copy_(x)
         evs[k + 1].record(stream)
+        if keep:
+            kept.append(x.copy() if host else x.clone())
     torch.cuda.synchronize()
     per = [evs[k].elapsed_time(evs[k + 1]) for k in range(k_steps)]
     heads = x.copy() if host else x.cpu().numpy()
-    return evs[0].elapsed_time(evs[-1]), per, iters, heads
+    return evs[0].elapsed_time(evs[-1]), per, iters, heads, kept
 
 
-def time_spmv(eqs, torch, stream, n, reps=30):
-    x = torch.rand(n, dtype=torch.float64, device="cuda")
-    y = torch.empty_like(x)
-    for _ in range(3):
-        eqs.spmv(x, y)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    ms = []
-    for _ in range(reps):
-        e0.record(stream)
-        eqs.spmv(x, y)
-        e1.record(stream)
-        e1.synchronize()
-        ms.append(e0.elapsed_time(e1))
-    return statistics.median(ms)
+def configure(eqs, capi, mixed: bool):
+    if mixed:
+        eqs.ConfigNumerics(capi.LS_CG, capi.PRECOND_JACOBI, 20000, TOL,
+                           precision=capi.PRECISION_FP32_REFINED)
+    else:
+        eqs.ConfigNumerics(capi.LS_CG, capi.PRECOND_JACOBI, 20000, TOL)
 
 
-def cpu_baseline_sample(threads: int = 1):
+def time_path(eqs, capi, p, deck, k_steps, warm, torch, stream, mixed, keep=False):
+    """Warm-up steps, then the timed K steps with in-graph SpMV timing on."""
+    m, ek, rows, vals, h0 = deck
+    configure(eqs, capi, mixed)
+    run_steps(eqs, capi, p, ek, rows, vals, h0, warm, False, torch, stream)
+    eqs.profile(True)
+    capi.kernel_launches(reset=True)
+    ms, per, iters, heads, kept = run_steps(eqs, capi, p, ek, rows, vals, h0, k_steps, False, torch,
+                                            stream, keep)
+    launches = capi.kernel_launches(reset=True)
+    prof = eqs.profile(False)
+    return {"ms": ms, "per": per, "iters": iters, "heads": heads, "kept": kept,
+            "launches": launches, "prof": prof}
+
+
+def cpu_baseline_sample():
     """Oracle (C restatement) on a bounded sample of the workload: the full
-    assembly of one 16-cell x-slab plus 40 CG iterations on the full system,
-    extrapolated per element and per iteration.  Returns per-unit seconds."""
+    assembly of one 16-cell x-slab plus 40 CG iterations on a system with the
+    full pattern.  Returns (seconds per element, seconds per CG iteration)."""
+    import copy
+
     from oracle import oracle as O
+    O.build("/nonexistent")
     m, ek, rows, vals, h0 = make_deck()
     slab = m.conn.reshape(NZ, NY, NX, 8)[:, :, :16, :].reshape(-1, 8)
-    import copy
     ms = copy.copy(m)
     ms.conn = np.ascontiguousarray(slab)
     op = O.make_params(pcs_type=0, dt=DT, storage=SS)
     rp, col = O.build_pattern(m.n_nodes, m.conn)
-    t0 = time.perf_counter()
     eks = ek.reshape(NZ, NY, NX)[:, :, :16].ravel().copy()
+    t0 = time.perf_counter()
     O.assemble(ms, rp, col, op, elem_k=eks, u0=h0)
     t_asm = (time.perf_counter() - t0) / len(slab)
-    val, b = O.assemble(m, rp, col, op, elem_k=ek, u0=h0) if False else (None, None)
-    # CG iterations on a full-size system (values from a cheap stand-in with
-    # the same pattern: the cost per iteration does not depend on values)
-    val = np.zeros(len(col))
+    # the cost of a CG iteration depends on the pattern, not on the values
+    val = np.full(len(col), 1e-3)
     diag = np.nonzero(col == np.repeat(np.arange(m.n_nodes), np.diff(rp)))[0]
     val[diag] = 1.0
-    val += 1e-3
     b = np.ones(m.n_nodes)
     t0 = time.perf_counter()
     O.solve(rp, col, val, b, np.zeros(m.n_nodes), method=5, precond=1, max_iter=40, tol=1e-300)
@@ -218,80 +239,101 @@ def main():
     B.build()
     from ogs5_gb300 import capi
 
-    m, ek, rows, vals, h0 = make_deck()
+    deck = make_deck()
+    m, ek, rows, vals, h0 = deck
     stream = torch.cuda.Stream()
     gm = capi.GpuMesh(m)
     eqs = capi.LinearEQS(gm, stream=stream)
-    eqs.ConfigNumerics(capi.LS_CG, capi.PRECOND_JACOBI, 20000, TOL)
     p = capi.make_params(capi.GROUNDWATER_FLOW, dt=DT, storage=SS)
     k_steps = max(1, args.steps)
     warm = max(3, args.warmup)
-
-    # warm-up (graph capture, allocator, clocks)
-    run_steps(eqs, capi, p, ek, rows, vals, h0, warm, False, torch, stream)
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("gloo")
         dist.barrier()
-    capi.kernel_launches(reset=True)
+
+    # plain FP64 path (the parity path), then the FP32-inner / FP64 path
+    f64 = time_path(eqs, capi, p, deck, k_steps, warm, torch, stream, mixed=False, keep=True)
     with ClockSampler(local) as clk:
-        ms, per, iters, heads = run_steps(eqs, capi, p, ek, rows, vals, h0, k_steps, False, torch, stream)
-    launches = capi.kernel_launches(reset=True)
-    ms_e2e, per_e2e, iters_e2e, heads_e2e = run_steps(eqs, capi, p, ek, rows, vals, h0, k_steps, True,
+        mix = time_path(eqs, capi, p, deck, k_steps, warm, torch, stream, mixed=True, keep=True)
+    err = max(float((a - b).abs().max() / b.abs().max()) for a, b in zip(mix["kept"], f64["kept"]))
+    f64["kept"] = mix["kept"] = None
+    torch.cuda.empty_cache()
+    # end to end through the C ABI with host buffers (FP32-inner path)
+    configure(eqs, capi, True)
+    ms_e2e, per_e2e, it_e2e, heads_e2e, _ = run_steps(eqs, capi, p, ek, rows, vals, h0, k_steps, True,
                                                       torch, stream)
+    ms = mix["ms"]
     if world > 1:
-        t = torch.tensor([ms, ms_e2e], dtype=torch.float64)
+        t = torch.tensor([ms, ms_e2e, f64["ms"]], dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms, ms_e2e = float(t[0]), float(t[1])
+        ms, ms_e2e, f64["ms"] = float(t[0]), float(t[1]), float(t[2])
         dist.barrier()
 
-    t_spmv = time_spmv(eqs, torch, stream, m.n_nodes)
     N, nnz = gm.n_rows, gm.nnz
-    spmv_bytes = nnz * 12 + N * 20
     hbm, peak_kind = peaks()
+    pr = mix["prof"]
+    t_spmv = pr["spmv_ms"] / max(1, pr["spmv_launches"])
+    n_up = 14  # column offsets >= 0 of the 27-point hex pattern, diagonal included
+    spmv_bytes = (4 * n_up + 8) * N
     achieved = spmv_bytes / (t_spmv * 1e-3) / 1e9
+    pr64 = f64["prof"]
+    t64 = pr64["spmv_ms"] / max(1, pr64["spmv_launches"])
+    b64 = nnz * 12 + N * 20
     value = world * k_steps / (ms * 1e-3)
+    value64 = world * k_steps / (f64["ms"] * 1e-3)
     e2e = world * k_steps / (ms_e2e * 1e-3)
     h2d = 8 * m.n_elements + 8 * N * 2 + 12 * len(rows)
     d2h = 8 * N
     out = {
         "metric": "solves/s", "value": round(value, 4), "unit": "solves/s", "n_gpus": world,
         "steps": k_steps, "warmup": warm, "ms_per_step": round(ms / k_steps, 3),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 inner CG, f64 residual/solution/convergence",
         "data": "synthetic (seeded GRF conductivity, generated mesh)",
         "config": {"workload": WORKLOAD, "nodes": N, "elements": m.n_elements, "nnz": nnz,
-                   "l2": "inputs larger than L2 (matrix 343 MB), no flush",
+                   "l2": "inputs larger than L2 (FP64 matrix 343 MB re-assembled every step), no flush",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
-        "p50_step_ms": round(float(np.percentile(per, 50)), 3),
-        "p99_step_ms": round(float(np.percentile(per, 99)), 3),
-        "cg_iterations": iters, "dof_per_s": round(value * N, 1),
+        "p50_step_ms": round(float(np.percentile(mix["per"], 50)), 3),
+        "p99_step_ms": round(float(np.percentile(mix["per"], 99)), 3),
+        "max_rel_err_vs_fp64": err,
+        "krylov_iterations": mix["iters"], "dof_per_s": round(value * N, 1),
+        "fp64_path": {"value": round(value64, 4), "unit": "solves/s",
+                      "ms_per_step": round(f64["ms"] / k_steps, 3), "cg_iterations": f64["iters"],
+                      "spmv": {"kernel": "k_cg_spmv (SELL-32 FP64 + fused p.s)",
+                               "launch_ms": round(t64, 4), "bytes_per_launch": b64,
+                               "achieved_gbs": round(b64 / (t64 * 1e-3) / 1e9, 1)}},
+        "speedup_vs_fp64_path": round(value / value64, 3),
         "e2e": {"value": round(e2e, 4), "unit": "solves/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
-        "e2e_heads_match": bool(np.abs(heads_e2e - heads).max() <= 1e-9 * np.abs(heads).max()),
-        "gpu_launches": int(launches),
+        "e2e_heads_match": bool(np.abs(heads_e2e - mix["heads"]).max()
+                                <= 1e-8 * np.abs(mix["heads"]).max()),
+        "gpu_launches": int(mix["launches"]),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                      "frac": round(achieved / hbm, 4), "traffic": None,
-                     "kernel": "k_cg_spmv (CSR FP64 SpMV + fused p.s)",
-                     "bytes_per_launch": spmv_bytes, "launch_ms": round(t_spmv, 4),
-                     "peak_kind": peak_kind},
+                     "kernel": "k_mp_spmv (FP32 upper-diagonal-offset SpMV + fused p.s)",
+                     "bytes_per_launch": spmv_bytes, "launch_ms": round(t_spmv, 5),
+                     "launches": pr["spmv_launches"], "peak_kind": peak_kind},
         "clocks": clk.summary(),
     }
     if rank == 0 and not args.no_cpu_baseline:
         t_asm, t_it = cpu_baseline_sample()
-        est = m.n_elements * t_asm + (iters / k_steps) * t_it
+        est = m.n_elements * t_asm + (f64["iters"] / k_steps) * t_it
         out["cpu_baseline"] = {"value": round(1.0 / est, 6), "unit": "solves/s", "cores": 1,
                                "kind": "port",
                                "sample": (f"oracle C port, 1 thread: assembly of a 16-cell x-slab "
                                           f"({t_asm*1e6:.2f} us/element) + 40 CG iterations on the full "
-                                          f"system ({t_it*1e3:.1f} ms/iter), extrapolated to "
-                                          f"{m.n_elements} elements + {iters / k_steps:.0f} iterations/step")}
+                                          f"pattern ({t_it*1e3:.1f} ms/iter), extrapolated to "
+                                          f"{m.n_elements} elements + {f64['iters'] / k_steps:.0f} "
+                                          f"iterations/step")}
     if rank == 0:
         print(json.dumps(out))
 
 
 def reference_arm(args, rank):
-    """CPU implementation of the path (the oracle port; the reference's own
-    build needs its cmake-generated sources) on all host cores."""
+    """CPU implementation of the path (the oracle; the reference's own build
+    needs its cmake-generated sources) on all host cores: one process per
+    core, each timing a bounded sample of one step."""
     if rank != 0:
         return
     import multiprocessing as mp
@@ -303,17 +345,16 @@ def reference_arm(args, rank):
     wall = time.perf_counter() - t0
     t_asm = statistics.median(r[0] for r in res)
     t_it = statistics.median(r[1] for r in res)
-    iters_per_step = 300.0
-    est = NX * NY * NZ * t_asm + iters_per_step * t_it
+    est = NX * NY * NZ * t_asm + CG_ITERS_PER_STEP * t_it
     value = cores / est
     print(json.dumps({
         "metric": "solves/s", "value": round(value, 6), "unit": "solves/s", "n_gpus": 0,
         "steps": args.steps, "warmup": args.warmup, "impl": "reference",
         "higher_is_better": True, "dtype": "f64", "config": {"workload": WORKLOAD},
         "cpu_baseline": {"value": round(value, 6), "unit": "solves/s", "cores": cores, "kind": "port",
-                         "sample": f"{cores} independent processes, each: slab assembly + 40 CG "
-                                   f"iterations, extrapolated to one step ({iters_per_step:.0f} "
-                                   f"iterations); wall {wall:.1f} s"},
+                         "sample": (f"{cores} concurrent processes, each: assembly of a 16-cell x-slab "
+                                    f"+ 40 CG iterations on the full pattern, extrapolated to one step "
+                                    f"({CG_ITERS_PER_STEP} CG iterations); wall {wall:.1f} s")},
         "e2e": {"value": round(value, 6), "unit": "solves/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0}}))
 

@@ -144,8 +144,9 @@ typedef struct
     int32_t max_iter;          /* ls_max_iterations                            */
     int32_t precision;         /* OGS_PRECISION_*                              */
     double tol;                /* ls_error_tolerance (relative to |b|)         */
-    double inner_tol;          /* FP32 mode: relative tolerance of one inner
-                                  solve (0 selects 1e-4)                       */
+    double inner_tol;          /* FP32 mode: the FP64 residual is recomputed
+                                  when the FP32 residual fell by this factor
+                                  since the last replacement (0 selects 1e-2) */
     int32_t check_norm_rhs;    /* 1: keep Linear_EQS::CheckNormRHS, i.e.
                                   return at once when |b|/|b_prev| < tol
                                   (equation_class.cpp:1104-1121)               */
@@ -154,11 +155,11 @@ typedef struct
 
 typedef struct
 {
-    int32_t iterations;        /* Krylov iterations (outer+inner in FP32 mode) */
+    int32_t iterations;        /* Krylov iterations (FP32 iterations in FP32 mode) */
     int32_t status;            /* ogs_status of the solve                      */
     double rel_residual;       /* |r| / |b| at exit (Linear_EQS::error)        */
     double b_norm;             /* |b| at entry (Linear_EQS::bNorm)             */
-    int32_t refinements;       /* FP32 mode: outer FP64 refinement steps       */
+    int32_t refinements;       /* FP32 mode: FP64 residual replacements        */
     int32_t pad0;
     double solve_ms;           /* device time of the solve, CUDA events        */
 } ogs_solve_stats;
@@ -257,6 +258,22 @@ int32_t ogs_gpu_mesh_gauss_points(const ogs_mesh* mesh);
 /* Number of this library's kernels launched on the calling thread since the
  * last reset (instrumentation for benchmarks). */
 int64_t ogs_gpu_kernel_launches(int32_t reset);
+
+/* Device time of the SpMV kernel of every Krylov iteration, measured with
+ * CUDA events recorded around it inside the captured iteration graphs
+ * (instrumentation, no counterpart in the reference). */
+typedef struct
+{
+    double spmv_ms;            /* summed SpMV kernel time                     */
+    int64_t spmv_launches;     /* SpMV launches that did work                 */
+    double solve_ms;           /* summed device time of the solves            */
+    int64_t solves;
+} ogs_profile;
+
+/* enable != 0 turns the timing on (graphs are re-captured with the events);
+ * out (may be NULL) receives the totals since the previous call, which are
+ * then reset. */
+ogs_status ogs_gpu_profile(ogs_system* sys, int32_t enable, ogs_profile* out);
 
 #ifdef __cplusplus
 }

@@ -42,7 +42,7 @@ EXPORTS = [
     "ogs_gpu_mesh_info", "ogs_gpu_system_create", "ogs_gpu_system_destroy", "ogs_gpu_configure",
     "ogs_gpu_initialize", "ogs_gpu_assemble", "ogs_gpu_set_dirichlet", "ogs_gpu_solve",
     "ogs_gpu_gp_velocity", "ogs_gpu_get_csr", "ogs_gpu_get_rhs", "ogs_gpu_get_x",
-    "ogs_gpu_spmv", "ogs_gpu_mesh_gauss_points", "ogs_gpu_kernel_launches",
+    "ogs_gpu_spmv", "ogs_gpu_mesh_gauss_points", "ogs_gpu_kernel_launches", "ogs_gpu_profile",
 ]
 
 
@@ -77,6 +77,11 @@ class SolverConfig(C.Structure):
     _fields_ = [("method", C.c_int32), ("precond", C.c_int32), ("max_iter", C.c_int32),
                 ("precision", C.c_int32), ("tol", C.c_double), ("inner_tol", C.c_double),
                 ("check_norm_rhs", C.c_int32), ("pad0", C.c_int32)]
+
+
+class Profile(C.Structure):
+    _fields_ = [("spmv_ms", C.c_double), ("spmv_launches", C.c_int64), ("solve_ms", C.c_double),
+                ("solves", C.c_int64)]
 
 
 class SolveStats(C.Structure):
@@ -139,6 +144,8 @@ def lib():
         L.ogs_gpu_spmv.argtypes = [vp, vp, vp]
         L.ogs_gpu_mesh_gauss_points.argtypes = [vp]
         L.ogs_gpu_mesh_gauss_points.restype = C.c_int32
+        L.ogs_gpu_profile.argtypes = [vp, C.c_int32, C.POINTER(Profile)]
+        L.ogs_gpu_profile.restype = st
         L.ogs_gpu_kernel_launches.argtypes = [C.c_int32]
         L.ogs_gpu_kernel_launches.restype = C.c_int64
         for name in ("ogs_gpu_mesh_create", "ogs_gpu_mesh_destroy", "ogs_gpu_mesh_info",
@@ -282,6 +289,13 @@ class LinearEQS:
         _check(lib().ogs_gpu_gp_velocity(self.h, C.byref(params), _ptr(_f64(elem_k)),
                                          _ptr(_f64(u)), _ptr(out)))
         return out
+
+    def profile(self, enable: bool) -> dict:
+        """Turns SpMV timing on/off; returns (and resets) the totals so far."""
+        p = Profile()
+        _check(lib().ogs_gpu_profile(self.h, 1 if enable else 0, C.byref(p)))
+        return {"spmv_ms": p.spmv_ms, "spmv_launches": p.spmv_launches, "solve_ms": p.solve_ms,
+                "solves": p.solves}
 
     def get_csr(self):
         nnz = self.gmesh.nnz

@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <cfloat>
 #include <cstddef>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -11,22 +12,35 @@
 namespace ogs {
 
 bool launch_assembly(const ogs_mesh* m, const AsmArgs& a, bool affine, int kind, cudaStream_t s);
-void launch_spmv(const CsrView<double>& A, const double* x, double* y, int G, cudaStream_t s);
+void launch_spmv(const SellView<double>& A, const double* x, double* y, cudaStream_t s);
 void launch_dinv(const double* val, const int32_t* diag_pos, double* dinv, int n, cudaStream_t s);
-void launch_krylov_init(const SolveArgs& a, int kind, int G, cudaStream_t s);
-void launch_krylov_iteration(const SolveArgs& a, int kind, int G, cudaStream_t s);
+void launch_krylov_init(const SolveArgs& a, int kind, cudaStream_t s);
+void launch_krylov_iteration(const SolveArgs& a, int kind, cudaStream_t s, cudaEvent_t eb, cudaEvent_t ee);
 void launch_bicgstab_finish(const SolveArgs& a, cudaStream_t s);
+void launch_norm_b(const SolveArgs& a, cudaStream_t s);
+void launch_mp_convert(const MixedArgs& a, const int32_t* row_len, const int8_t* slot_up, float* U,
+                       float* val32, const double* dinv64, float* d32, cudaStream_t s);
+void launch_mp_replace(const MixedArgs& a, cudaStream_t s);
+void launch_mp_iteration(const MixedArgs& a, cudaStream_t s, cudaEvent_t eb, cudaEvent_t ee);
 int kernels_per_iteration(int kind);
-int row_group(double avg_nnz);
 int vec_grid(int n);
 
 // ------------------------------------------------------------------
 // small kernels
 // ------------------------------------------------------------------
-__global__ void k_dirichlet_row_only(const int32_t* __restrict__ rp, const int32_t* __restrict__ col,
-                                     const int32_t* __restrict__ diag_pos, double* val, double* b,
-                                     const int32_t* __restrict__ rows, const double* __restrict__ vals,
-                                     int nbc)
+// stored entries of row r in SELL-32 order: slot(j) = slice_ptr[r/32] + 32 j + r%32
+struct SellRow
+{
+    int beg, len;
+    __device__ __forceinline__ SellRow(const int32_t* slice_ptr, const int32_t* row_len, int r)
+        : beg(slice_ptr[r >> 5] + (r & 31)), len(row_len[r]) {}
+    __device__ __forceinline__ int slot(int j) const { return beg + (j << 5); }
+};
+
+__global__ void k_dirichlet_row_only(const int32_t* __restrict__ slice_ptr, const int32_t* __restrict__ row_len,
+                                     const int32_t* __restrict__ col, const int32_t* __restrict__ diag_pos,
+                                     double* val, double* b, const int32_t* __restrict__ rows,
+                                     const double* __restrict__ vals, int nbc)
 {
     // CSparseMatrix::Diagonize, CRS, column kept (matrix_class.cpp:1663-1700,1783)
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nbc; q += gridDim.x * blockDim.x)
@@ -34,19 +48,24 @@ __global__ void k_dirichlet_row_only(const int32_t* __restrict__ rp, const int32
         const int id = rows[q];
         const int dp = diag_pos[id];
         const double vdiag = dp >= 0 ? val[dp] : 0.0;
-        for (int k = rp[id]; k < rp[id + 1]; k++)
-            if (col[k] != id) val[k] = 0.0;
+        const SellRow R(slice_ptr, row_len, id);
+        for (int j = 0; j < R.len; j++)
+            if (col[R.slot(j)] != id) val[R.slot(j)] = 0.0;
         b[id] = vdiag * vals[q];
     }
 }
 
-__global__ void k_dirichlet_symmetric(const int32_t* __restrict__ rp, const int32_t* __restrict__ col,
+__global__ void k_dirichlet_symmetric(const int32_t* __restrict__ slice_ptr,
+                                      const int32_t* __restrict__ row_len, const int32_t* __restrict__ col,
                                       const int32_t* __restrict__ diag_pos, double* val, double* b,
                                       const unsigned char* __restrict__ flag,
-                                      const double* __restrict__ valn, int n)
+                                      const double* __restrict__ valn, const double* __restrict__ valf, int n)
 {
     // MXRandbed (matrix_routines.cpp:2314-2520): lift column into b, zero
-    // row and column, keep the diagonal (a zero diagonal -> DBL_EPSILON)
+    // row and column, keep the diagonal (a zero diagonal -> DBL_EPSILON).
+    // A row given twice is lifted with its first value (the column is zero
+    // afterwards) and keeps its last value on the diagonal, as the
+    // sequential SetKnownX loop leaves it.
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     {
         if (flag[i])
@@ -54,19 +73,22 @@ __global__ void k_dirichlet_symmetric(const int32_t* __restrict__ rp, const int3
             const int dp = diag_pos[i];
             double d = dp >= 0 ? val[dp] : 0.0;
             if (fabs(d) < DBL_MIN) d = DBL_EPSILON;
-            for (int k = rp[i]; k < rp[i + 1]; k++) val[k] = 0.0;
+            const SellRow R(slice_ptr, row_len, i);
+            for (int j = 0; j < R.len; j++) val[R.slot(j)] = 0.0;
             if (dp >= 0) val[dp] = d;
             b[i] = valn[i] * d;
         }
         else
         {
             double bi = b[i];
-            for (int k = rp[i]; k < rp[i + 1]; k++)
+            const SellRow R(slice_ptr, row_len, i);
+            for (int j = 0; j < R.len; j++)
             {
+                const int k = R.slot(j);
                 const int c = col[k];
                 if (flag[c])
                 {
-                    bi -= val[k] * valn[c];
+                    bi -= val[k] * valf[c];
                     val[k] = 0.0;
                 }
             }
@@ -82,20 +104,22 @@ __global__ void k_scatter_rows(double* x, const int32_t* __restrict__ rows, cons
         x[rows[q]] = vals[q];
 }
 
-__global__ void k_mark_rows(unsigned char* flag, double* valn, const int32_t* __restrict__ rows,
-                            const double* __restrict__ vals, int nbc)
+__global__ void k_mark_rows(unsigned char* flag, double* valn, double* valf, const int32_t* __restrict__ rows,
+                            const double* __restrict__ vals, const double* __restrict__ vfirst, int nbc)
 {
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nbc; q += gridDim.x * blockDim.x)
     {
         flag[rows[q]] = 1;
         valn[rows[q]] = vals[q];
+        valf[rows[q]] = vfirst[q];
     }
 }
 
-__global__ void k_i32_to_i64(const int32_t* __restrict__ a, int64_t* __restrict__ b, int64_t n)
+__global__ void k_sell_to_csr(const double* __restrict__ sell, const int32_t* __restrict__ csr2sell,
+                              double* __restrict__ out, int64_t nnz)
 {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        b[i] = a[i];
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nnz; k += (int64_t)gridDim.x * blockDim.x)
+        out[k] = sell[csr2sell[k]];
 }
 
 static bool is_device_ptr(const void* p)
@@ -139,16 +163,91 @@ struct ogs_system
     int bc_cap = 0;
     unsigned char* bc_flag = nullptr;
     double* bc_valn = nullptr;
+    double* bc_valf = nullptr;
+    double* bc_vfirst = nullptr;
     // iteration chunks captured as graphs, per solver kind
     cudaGraphExec_t chunk[2] = {nullptr, nullptr};
     int chunk_iters[2] = {0, 0};
-    int G = 1;
+    void* vec_block = nullptr;
+    size_t vec_stride = 0;
+    // FP32-inner / FP64-refinement buffers (allocated on first use)
+    void* f32_block = nullptr;
+    size_t f32_bytes = 0;
+    float *x32 = nullptr, *r32 = nullptr, *p32 = nullptr, *s32 = nullptr, *d32 = nullptr, *U = nullptr,
+          *val32 = nullptr;
+    int fmt = -1;
+    cudaGraphExec_t mp_chunk = nullptr, mp_replace = nullptr;
+    // SpMV timing inside the chunk graphs (ogs_gpu_profile)
+    static constexpr int kChunk = 16;
+    bool prof_on = false;
+    cudaEvent_t prof_b[kChunk] = {}, prof_e[kChunk] = {};
+    double prof_spmv_ms = 0.0, prof_solve_ms = 0.0;
+    int64_t prof_spmv_n = 0, prof_solves = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
 
 namespace {
 
 constexpr size_t kStateHeader = offsetof(KState, ticket);
+
+// Keeps the Krylov vectors L2-resident (GB300: 126 MB L2) while the SELL
+// matrix streams through with evict-first loads.  The set-aside is a limit
+// of this process's context; OGS_GPU_L2_PERSIST=0 turns it off.
+void set_l2_window_region(ogs_system* s, void* base, size_t bytes)
+{
+    const char* env = getenv("OGS_GPU_L2_PERSIST");
+    if (env && env[0] == '0') return;
+    int dev = 0, max_win = 0, max_persist = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&max_win, cudaDevAttrMaxAccessPolicyWindowSize, dev);
+    cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, dev);
+    if (max_win <= 0 || max_persist <= 0) return;
+    const size_t want = std::min<size_t>((size_t)max_win, bytes);
+    size_t cur = 0;
+    cudaDeviceGetLimit(&cur, cudaLimitPersistingL2CacheSize);
+    const size_t setaside = std::min<size_t>((size_t)max_persist, std::max(cur, want));
+    if (setaside > cur && cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, setaside) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return;
+    }
+    cudaStreamAttrValue v{};
+    v.accessPolicyWindow.base_ptr = base;
+    v.accessPolicyWindow.num_bytes = want;
+    v.accessPolicyWindow.hitRatio = (float)std::min(1.0, (double)setaside / (double)want);
+    v.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+    v.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+    if (cudaStreamSetAttribute(s->stream, cudaStreamAttributeAccessPolicyWindow, &v) != cudaSuccess)
+        cudaGetLastError();
+}
+
+void set_l2_window(ogs_system* s)
+{
+    const char* env = getenv("OGS_GPU_L2_PERSIST");
+    if (env && env[0] == '0') return;
+    int dev = 0, max_win = 0, max_persist = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&max_win, cudaDevAttrMaxAccessPolicyWindowSize, dev);
+    cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, dev);
+    if (max_win <= 0 || max_persist <= 0) return;
+    const size_t want = std::min<size_t>((size_t)max_win, s->vec_stride * 5);  // p r s x dinv
+    size_t cur = 0;
+    cudaDeviceGetLimit(&cur, cudaLimitPersistingL2CacheSize);
+    const size_t setaside = std::min<size_t>((size_t)max_persist, std::max(cur, want));
+    if (setaside > cur && cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, setaside) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return;
+    }
+    cudaStreamAttrValue v{};
+    v.accessPolicyWindow.base_ptr = s->vec_block;
+    v.accessPolicyWindow.num_bytes = want;
+    v.accessPolicyWindow.hitRatio = (float)std::min(1.0, (double)setaside / (double)want);
+    v.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+    v.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+    if (cudaStreamSetAttribute(s->stream, cudaStreamAttributeAccessPolicyWindow, &v) != cudaSuccess)
+        cudaGetLastError();
+}
 
 ogs_status stage_in(ogs_system* s, const double* src, size_t n, double** scratch, const double** out)
 {
@@ -163,8 +262,8 @@ ogs_status stage_in(ogs_system* s, const double* src, size_t n, double** scratch
 SolveArgs make_solve_args(ogs_system* s)
 {
     SolveArgs a;
-    a.A.row_ptr = s->m->row_ptr;
-    a.A.col = s->m->col;
+    a.A.slice_ptr = s->m->slice_ptr;
+    a.A.col = s->m->sell_col;
     a.A.val = s->val;
     a.A.n = s->n;
     std::memset(&a.v, 0, sizeof a.v);
@@ -179,16 +278,49 @@ void drop_graphs(ogs_system* s)
 {
     for (int k = 0; k < 2; k++)
         if (s->chunk[k]) { cudaGraphExecDestroy(s->chunk[k]); s->chunk[k] = nullptr; }
+    if (s->mp_chunk) { cudaGraphExecDestroy(s->mp_chunk); s->mp_chunk = nullptr; }
+    if (s->mp_replace) { cudaGraphExecDestroy(s->mp_replace); s->mp_replace = nullptr; }
+}
+
+void accumulate_prof(ogs_system* s, int executed)
+{
+    for (int i = 0; i < executed; i++)
+    {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, s->prof_b[i], s->prof_e[i]) == cudaSuccess)
+        {
+            s->prof_spmv_ms += ms;
+            s->prof_spmv_n += 1;
+        }
+        else
+            cudaGetLastError();
+    }
+}
+
+template <class F>
+ogs_status capture(ogs_system* s, cudaGraphExec_t* out, F body)
+{
+    cudaGraph_t g;
+    OGS_CUDA_TRY(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+    body();
+    cudaError_t e = cudaStreamEndCapture(s->stream, &g);
+    if (e != cudaSuccess) { set_error("graph capture: %s", cudaGetErrorString(e)); return OGS_CUDA_ERROR; }
+    e = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) { set_error("graph instantiate: %s", cudaGetErrorString(e)); return OGS_CUDA_ERROR; }
+    return OGS_OK;
 }
 
 ogs_status get_chunk(ogs_system* s, int kind, const SolveArgs& a, cudaGraphExec_t* out, int* iters)
 {
     if (!s->chunk[kind])
     {
-        const int C = kind == SK_CG ? 16 : 8;
+        const int C = ogs_system::kChunk;
         cudaGraph_t g;
         OGS_CUDA_TRY(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
-        for (int i = 0; i < C; i++) launch_krylov_iteration(a, kind, s->G, s->stream);
+        for (int i = 0; i < C; i++)
+            launch_krylov_iteration(a, kind, s->stream, s->prof_on ? s->prof_b[i] : nullptr,
+                                    s->prof_on ? s->prof_e[i] : nullptr);
         cudaError_t e = cudaStreamEndCapture(s->stream, &g);
         if (e != cudaSuccess) { set_error("graph capture: %s", cudaGetErrorString(e)); return OGS_CUDA_ERROR; }
         e = cudaGraphInstantiate(&s->chunk[kind], g, 0);
@@ -207,15 +339,28 @@ extern "C" ogs_status ogs_gpu_system_destroy(ogs_system* s)
 {
     if (!s) return OGS_OK;
     drop_graphs(s);
-    double* bufs[] = {s->val, s->b, s->x, s->r, s->r0, s->p, s->ph, s->s, s->sh, s->t, s->v, s->dinv,
-                      s->ek, s->u0, s->gpv, s->qbuf, s->vec_in, s->vec_out, s->bc_vals, s->bc_valn};
+    if (s->vec_block)
+    {
+        cudaStreamSynchronize(s->stream);
+        cudaCtxResetPersistingL2Cache();  // hand the persisting lines back
+        cudaGetLastError();
+    }
+    double* bufs[] = {s->val,     s->ek,      s->u0,      s->gpv,     s->qbuf,     s->vec_in,
+                      s->vec_out, s->bc_vals, s->bc_valn, s->bc_valf, s->bc_vfirst};
     for (double* p : bufs) cudaFree(p);
+    cudaFree(s->vec_block);
+    cudaFree(s->f32_block);
     cudaFree(s->st);
     cudaFree(s->d_bad);
     cudaFree(s->bc_rows);
     cudaFree(s->bc_flag);
     if (s->h_st) cudaFreeHost(s->h_st);
     if (s->h_bad) cudaFreeHost(s->h_bad);
+    for (int i = 0; i < ogs_system::kChunk; i++)
+    {
+        if (s->prof_b[i]) cudaEventDestroy(s->prof_b[i]);
+        if (s->prof_e[i]) cudaEventDestroy(s->prof_e[i]);
+    }
     if (s->ev0) cudaEventDestroy(s->ev0);
     if (s->ev1) cudaEventDestroy(s->ev1);
     if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
@@ -243,10 +388,16 @@ extern "C" ogs_status ogs_gpu_system_create(ogs_mesh* m, void* stream, ogs_syste
         s->own_stream = true;
     }
     const size_t nb = (size_t)s->n * sizeof(double);
-    double** vecs[] = {&s->b, &s->x, &s->r, &s->r0, &s->p, &s->ph, &s->s, &s->sh, &s->t, &s->v, &s->dinv};
-    cudaError_t e = cudaMalloc(&s->val, std::max<int64_t>(1, m->nnz) * sizeof(double));
-    for (double** p : vecs)
-        if (e == cudaSuccess) e = cudaMalloc(p, nb);
+    double** vecs[] = {&s->p, &s->r, &s->s, &s->x, &s->dinv, &s->ph, &s->sh, &s->r0, &s->v, &s->t, &s->b};
+    cudaError_t e = cudaMalloc(&s->val, std::max<int64_t>(1, m->sell_nnz) * sizeof(double));
+    // Krylov vectors in one block, most-reused first, so that one L2
+    // access-policy window can keep them resident while the matrix streams
+    const size_t nvec = sizeof(vecs) / sizeof(vecs[0]);
+    const size_t stride = (nb + 255) & ~size_t(255);
+    if (e == cudaSuccess) e = cudaMalloc(&s->vec_block, stride * nvec);
+    for (size_t k = 0; k < nvec && e == cudaSuccess; k++)
+        *vecs[k] = (double*)((char*)s->vec_block + k * stride);
+    s->vec_stride = stride;
     if (e == cudaSuccess) e = cudaMalloc(&s->st, sizeof(KState));
     if (e == cudaSuccess) e = cudaMemset(s->st, 0, sizeof(KState));
     if (e == cudaSuccess) e = cudaMalloc(&s->d_bad, sizeof(int));
@@ -254,7 +405,8 @@ extern "C" ogs_status ogs_gpu_system_create(ogs_mesh* m, void* stream, ogs_syste
     if (e == cudaSuccess) e = cudaMallocHost(&s->h_bad, sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc(&s->bc_flag, std::max(1, s->n));
     if (e == cudaSuccess) e = cudaMalloc(&s->bc_valn, nb);
-    if (e == cudaSuccess) e = cudaMemset(s->val, 0, m->nnz * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&s->bc_valf, nb);
+    if (e == cudaSuccess) e = cudaMemset(s->val, 0, m->sell_nnz * sizeof(double));
     if (e == cudaSuccess) e = cudaMemset(s->b, 0, nb);
     if (e == cudaSuccess) e = cudaMemset(s->x, 0, nb);
     if (e == cudaSuccess) e = cudaEventCreate(&s->ev0);
@@ -265,7 +417,7 @@ extern "C" ogs_status ogs_gpu_system_create(ogs_mesh* m, void* stream, ogs_syste
         ogs_gpu_system_destroy(s);
         return e == cudaErrorMemoryAllocation ? OGS_OOM : OGS_CUDA_ERROR;
     }
-    s->G = row_group((double)m->nnz / std::max<int64_t>(1, m->n_nodes));
+    set_l2_window(s);
     // CNumerics defaults (rf_num_new.cpp:77-165): BiCGStab, Jacobi, 1000, 1e-12
     s->cfg.method = OGS_LS_BICGSTAB;
     s->cfg.precond = OGS_PRECOND_JACOBI;
@@ -304,7 +456,7 @@ extern "C" ogs_status ogs_gpu_configure(ogs_system* s, const ogs_solver_config* 
 extern "C" ogs_status ogs_gpu_initialize(ogs_system* s)
 {
     if (!s) { set_error("initialize: NULL system"); return OGS_BAD_ARG; }
-    OGS_CUDA_TRY(cudaMemsetAsync(s->val, 0, s->m->nnz * sizeof(double), s->stream));
+    OGS_CUDA_TRY(cudaMemsetAsync(s->val, 0, s->m->sell_nnz * sizeof(double), s->stream));
     OGS_CUDA_TRY(cudaMemsetAsync(s->b, 0, (size_t)s->n * sizeof(double), s->stream));
     return OGS_OK;
 }
@@ -417,40 +569,163 @@ extern "C" ogs_status ogs_gpu_set_dirichlet(ogs_system* s, const int64_t* rows, 
         if (rsrc[q] < 0 || rsrc[q] >= s->n) { set_error("set_dirichlet: row %lld out of range", (long long)rsrc[q]); return OGS_BAD_ARG; }
         r32[q] = (int32_t)rsrc[q];
     }
+    // SetKnownX_i is applied row by row in list order, so a row listed twice
+    // keeps its last value: keep the last occurrence of every row
+    std::vector<double> vsrc(n_rows), vfirst;
+    if (n_rows) OGS_CUDA_TRY(cudaMemcpy(vsrc.data(), values, n_rows * sizeof(double),
+                                        vdev ? cudaMemcpyDeviceToHost : cudaMemcpyHostToHost));
+    {
+        std::vector<int64_t> order(n_rows);
+        for (int64_t q = 0; q < n_rows; q++) order[q] = q;
+        std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return r32[a] < r32[b]; });
+        std::vector<int32_t> ru;
+        std::vector<double> vu;
+        ru.reserve(n_rows);
+        vu.reserve(n_rows);
+        vfirst.reserve(n_rows);
+        double first = 0.0;
+        for (int64_t k = 0; k < n_rows; k++)
+        {
+            const int64_t q = order[k];
+            if (k == 0 || r32[order[k - 1]] != r32[q]) first = vsrc[q];
+            if (k + 1 < n_rows && r32[order[k + 1]] == r32[q]) continue;  // a later duplicate follows
+            ru.push_back(r32[q]);
+            vu.push_back(vsrc[q]);
+            vfirst.push_back(first);
+        }
+        r32.swap(ru);
+        vh.swap(vu);
+        n_rows = (int64_t)r32.size();
+    }
     if (n_rows > s->bc_cap)
     {
         cudaFree(s->bc_rows);
         cudaFree(s->bc_vals);
+        cudaFree(s->bc_vfirst);
         s->bc_rows = nullptr;
         s->bc_vals = nullptr;
+        s->bc_vfirst = nullptr;
         OGS_CUDA_TRY(cudaMalloc(&s->bc_rows, n_rows * sizeof(int32_t)));
         OGS_CUDA_TRY(cudaMalloc(&s->bc_vals, n_rows * sizeof(double)));
+        OGS_CUDA_TRY(cudaMalloc(&s->bc_vfirst, n_rows * sizeof(double)));
         s->bc_cap = (int)n_rows;
     }
     s->nbc = (int)n_rows;
     if (!n_rows) return OGS_OK;
     OGS_CUDA_TRY(cudaMemcpyAsync(s->bc_rows, r32.data(), n_rows * sizeof(int32_t), cudaMemcpyHostToDevice, s->stream));
-    OGS_CUDA_TRY(cudaMemcpyAsync(s->bc_vals, values, n_rows * sizeof(double),
-                                 vdev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s->stream));
+    OGS_CUDA_TRY(cudaMemcpyAsync(s->bc_vals, vh.data(), n_rows * sizeof(double), cudaMemcpyHostToDevice,
+                                 s->stream));
+    OGS_CUDA_TRY(cudaMemcpyAsync(s->bc_vfirst, vfirst.data(), n_rows * sizeof(double),
+                                 cudaMemcpyHostToDevice, s->stream));
     ogs_mesh* m = s->m;
     const int g = std::max(1, std::min(1024, (int)((n_rows + 255) / 256)));
     if (mode == OGS_DIRICHLET_ROW_ONLY)
     {
-        k_dirichlet_row_only<<<g, 256, 0, s->stream>>>(m->row_ptr, m->col, m->diag_pos, s->val, s->b,
-                                                       s->bc_rows, s->bc_vals, s->nbc);
+        k_dirichlet_row_only<<<g, 256, 0, s->stream>>>(m->slice_ptr, m->row_len, m->sell_col, m->diag_pos,
+                                                       s->val, s->b, s->bc_rows, s->bc_vals, s->nbc);
         OGS_LAUNCH_CHECK();
     }
     else
     {
         OGS_CUDA_TRY(cudaMemsetAsync(s->bc_flag, 0, s->n, s->stream));
-        k_mark_rows<<<g, 256, 0, s->stream>>>(s->bc_flag, s->bc_valn, s->bc_rows, s->bc_vals, s->nbc);
+        k_mark_rows<<<g, 256, 0, s->stream>>>(s->bc_flag, s->bc_valn, s->bc_valf, s->bc_rows, s->bc_vals,
+                                              s->bc_vfirst, s->nbc);
         OGS_LAUNCH_CHECK();
-        k_dirichlet_symmetric<<<vec_grid(s->n), 256, 0, s->stream>>>(m->row_ptr, m->col, m->diag_pos, s->val,
-                                                                      s->b, s->bc_flag, s->bc_valn, s->n);
+        k_dirichlet_symmetric<<<vec_grid(s->n), 256, 0, s->stream>>>(m->slice_ptr, m->row_len, m->sell_col,
+                                                                      m->diag_pos, s->val, s->b, s->bc_flag,
+                                                                      s->bc_valn, s->bc_valf, s->n);
         OGS_LAUNCH_CHECK();
     }
-    // values must stay valid until the copies above ran
-    if (!vdev) OGS_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    // the host staging vectors must outlive the copies above
+    OGS_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    return OGS_OK;
+}
+
+// FP32 inner CG with FP64 residual replacement (mixed.cu); x64 already holds
+// the initial guess with the Dirichlet values, dinv the FP64 Jacobi inverse.
+static ogs_status solve_fp32_refined(ogs_system* s, KState* h)
+{
+    ogs_mesh* m = s->m;
+    const ogs_solver_config& c = s->cfg;
+    const int n = s->n;
+    if (s->fmt < 0)
+    {
+        // diagonal-offset kernels exist for the hex (14), Kuhn-tet (8) and
+        // quad (5) patterns; anything else runs SELL-32 with FP32 values
+        s->fmt = (m->n_up == 14 || m->n_up == 8 || m->n_up == 5) ? 0 : 1;
+        const size_t v4 = ((size_t)n * sizeof(float) + 255) & ~size_t(255);
+        const size_t op = s->fmt == 0 ? (size_t)m->n_up * n * sizeof(float)
+                                      : (size_t)m->sell_nnz * sizeof(float);
+        s->f32_bytes = 5 * v4 + op;
+        OGS_CUDA_TRY(cudaMalloc(&s->f32_block, s->f32_bytes));
+        OGS_CUDA_TRY(cudaMemset(s->f32_block, 0, s->f32_bytes));
+        char* p = (char*)s->f32_block;
+        s->p32 = (float*)p; s->r32 = (float*)(p + v4); s->x32 = (float*)(p + 2 * v4);
+        s->s32 = (float*)(p + 3 * v4); s->d32 = (float*)(p + 4 * v4);
+        float* opb = (float*)(p + 5 * v4);
+        if (s->fmt == 0) s->U = opb; else s->val32 = opb;
+    }
+    MixedArgs a;
+    std::memset(&a, 0, sizeof a);
+    a.A.slice_ptr = m->slice_ptr; a.A.col = m->sell_col; a.A.val = s->val; a.A.n = n;
+    a.fmt = s->fmt; a.U = s->U; a.up_off = m->up_off; a.n_up = m->n_up; a.val32 = s->val32;
+    for (int d = 0; d < 16 && d < (int)m->host_up_off.size(); d++) a.off[d] = m->host_up_off[d];
+    a.d32 = s->d32; a.x = s->x; a.b = s->b; a.r64 = s->r;
+    a.x32 = s->x32; a.r32 = s->r32; a.p32 = s->p32; a.s32 = s->s32; a.st = s->st; a.n = n;
+    set_l2_window_region(s, s->f32_block, s->f32_bytes);
+    launch_mp_convert(a, m->row_len, m->slot_up, s->U, s->val32, s->dinv, s->d32, s->stream);
+    OGS_LAUNCH_CHECK();
+    OGS_CUDA_TRY(cudaMemsetAsync(s->x32, 0, (size_t)n * sizeof(float), s->stream));
+    h->scale = 1.0;
+    h->ratio = 1.0;
+    h->first = 1;
+    h->delta = c.inner_tol > 0.0 ? c.inner_tol : 1e-2;
+    OGS_CUDA_TRY(cudaMemcpyAsync(s->st, h, kStateHeader, cudaMemcpyHostToDevice, s->stream));
+    SolveArgs sa = make_solve_args(s);
+    launch_norm_b(sa, s->stream);
+    OGS_LAUNCH_CHECK();
+    if (!s->mp_replace)
+    {
+        ogs_status st = capture(s, &s->mp_replace, [&]() { launch_mp_replace(a, s->stream); });
+        if (st) return st;
+    }
+    if (!s->mp_chunk)
+    {
+        ogs_status st = capture(s, &s->mp_chunk, [&]() {
+            for (int i = 0; i < ogs_system::kChunk; i++)
+                launch_mp_iteration(a, s->stream, s->prof_on ? s->prof_b[i] : nullptr,
+                                    s->prof_on ? s->prof_e[i] : nullptr);
+        });
+        if (st) return st;
+    }
+    OGS_CUDA_TRY(cudaGraphLaunch(s->mp_replace, s->stream));
+    count_launches(4);
+    int rounds = 0;
+    int chunk_before = -1;  // iteration count when the pending chunk was launched
+    for (;;)
+    {
+        OGS_CUDA_TRY(cudaMemcpyAsync(h, s->st, kStateHeader, cudaMemcpyDeviceToHost, s->stream));
+        OGS_CUDA_TRY(cudaStreamSynchronize(s->stream));
+        if (chunk_before >= 0)
+        {
+            if (s->prof_on) accumulate_prof(s, std::min(ogs_system::kChunk, h->iter - chunk_before));
+            chunk_before = -1;
+        }
+        if (h->done) break;
+        if (++rounds > 4 * c.max_iter + 64) { set_error("solve: mixed-precision state did not finish"); return OGS_CUDA_ERROR; }
+        if (h->replace)
+        {
+            OGS_CUDA_TRY(cudaGraphLaunch(s->mp_replace, s->stream));
+            count_launches(4);
+        }
+        else
+        {
+            chunk_before = h->iter;
+            OGS_CUDA_TRY(cudaGraphLaunch(s->mp_chunk, s->stream));
+            count_launches(3 * ogs_system::kChunk);
+        }
+    }
+    // the events of the last chunk are read at the next header read
     return OGS_OK;
 }
 
@@ -458,9 +733,14 @@ extern "C" ogs_status ogs_gpu_solve(ogs_system* s, double* x_inout, ogs_solve_st
 {
     if (!s || !x_inout) { set_error("solve: NULL argument"); return OGS_BAD_ARG; }
     const ogs_solver_config& c = s->cfg;
-    if (c.precond == OGS_PRECOND_ILU0 || c.precision != OGS_PRECISION_FP64)
+    if (c.precond == OGS_PRECOND_ILU0)
     {
-        set_error("solve: ILU(0) / FP32 refinement not available in this build");
+        set_error("solve: ILU(0) not available in this build");
+        return OGS_BAD_ARG;
+    }
+    if (c.precision == OGS_PRECISION_FP32_REFINED && c.method != OGS_LS_CG)
+    {
+        set_error("solve: the FP32-inner / FP64-refinement mode runs CG (ls_method 5)");
         return OGS_BAD_ARG;
     }
     const int kind = c.method == OGS_LS_CG ? SK_CG : SK_BICGSTAB;
@@ -476,10 +756,18 @@ extern "C" ogs_status ogs_gpu_solve(ogs_system* s, double* x_inout, ogs_solve_st
         OGS_LAUNCH_CHECK();
     }
     SolveArgs a = make_solve_args(s);
+    const bool mixed = c.precision == OGS_PRECISION_FP32_REFINED;
     if (a.precond == OGS_PRECOND_JACOBI)
     {
         launch_dinv(s->val, s->m->diag_pos, s->dinv, s->n, s->stream);
         OGS_LAUNCH_CHECK();
+    }
+    else if (mixed)
+    {
+        // no preconditioner: M^-1 = I
+        std::vector<double> ones(s->n, 1.0);
+        OGS_CUDA_TRY(cudaMemcpyAsync(s->dinv, ones.data(), nb, cudaMemcpyHostToDevice, s->stream));
+        OGS_CUDA_TRY(cudaStreamSynchronize(s->stream));
     }
     KState* h = s->h_st;
     std::memset(h, 0, kStateHeader);
@@ -488,32 +776,45 @@ extern "C" ogs_status ogs_gpu_solve(ogs_system* s, double* x_inout, ogs_solve_st
     h->error = 1.0e10;
     h->max_iter = c.max_iter;
     h->alpha = h->omega = h->rho0 = 1.0;
-    OGS_CUDA_TRY(cudaMemcpyAsync(s->st, h, kStateHeader, cudaMemcpyHostToDevice, s->stream));
-    launch_krylov_init(a, kind, s->G, s->stream);
-    OGS_LAUNCH_CHECK();
-    cudaGraphExec_t ge;
-    int per = 0;
-    ogs_status st = get_chunk(s, kind, a, &ge, &per);
-    if (st) return st;
-    int launched = 0;
-    for (;;)
+    if (mixed)
     {
-        OGS_CUDA_TRY(cudaMemcpyAsync(h, s->st, kStateHeader, cudaMemcpyDeviceToHost, s->stream));
-        OGS_CUDA_TRY(cudaStreamSynchronize(s->stream));
-        if (h->done || launched > c.max_iter + per) break;
-        OGS_CUDA_TRY(cudaGraphLaunch(ge, s->stream));
-        count_launches((int64_t)per * kernels_per_iteration(kind));
-        launched += per;
+        ogs_status st = solve_fp32_refined(s, h);
+        if (st) return st;
     }
-    if (!h->done)
+    else
     {
-        set_error("solve: solver state did not finish");
-        return OGS_CUDA_ERROR;
-    }
-    if (h->finish_s)
-    {
-        launch_bicgstab_finish(a, s->stream);
+        OGS_CUDA_TRY(cudaMemcpyAsync(s->st, h, kStateHeader, cudaMemcpyHostToDevice, s->stream));
+        launch_krylov_init(a, kind, s->stream);
         OGS_LAUNCH_CHECK();
+        cudaGraphExec_t ge;
+        int per = 0;
+        ogs_status st = get_chunk(s, kind, a, &ge, &per);
+        if (st) return st;
+        int launched = 0;
+        int chunk_before = -1;
+        for (;;)
+        {
+            OGS_CUDA_TRY(cudaMemcpyAsync(h, s->st, kStateHeader, cudaMemcpyDeviceToHost, s->stream));
+            OGS_CUDA_TRY(cudaStreamSynchronize(s->stream));
+            if (chunk_before >= 0 && s->prof_on)  // the iteration that converged ran its SpMV
+                accumulate_prof(s, std::min(per, h->iter - chunk_before + (h->done ? 1 : 0)));
+            chunk_before = -1;
+            if (h->done || launched > c.max_iter + per) break;
+            chunk_before = h->iter;
+            OGS_CUDA_TRY(cudaGraphLaunch(ge, s->stream));
+            count_launches((int64_t)per * kernels_per_iteration(kind));
+            launched += per;
+        }
+        if (!h->done)
+        {
+            set_error("solve: solver state did not finish");
+            return OGS_CUDA_ERROR;
+        }
+        if (h->finish_s)
+        {
+            launch_bicgstab_finish(a, s->stream);
+            OGS_LAUNCH_CHECK();
+        }
     }
     OGS_CUDA_TRY(cudaMemcpyAsync(x_inout, s->x, nb, xdev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
                                  s->stream));
@@ -522,6 +823,11 @@ extern "C" ogs_status ogs_gpu_solve(ogs_system* s, double* x_inout, ogs_solve_st
     float ms = 0.f;
     cudaEventElapsedTime(&ms, s->ev0, s->ev1);
     s->bnorm_prev = h->bnorm;
+    if (s->prof_on)
+    {
+        s->prof_solve_ms += ms;
+        s->prof_solves += 1;
+    }
     if (stats)
     {
         std::memset(stats, 0, sizeof *stats);
@@ -529,6 +835,7 @@ extern "C" ogs_status ogs_gpu_solve(ogs_system* s, double* x_inout, ogs_solve_st
         stats->status = h->status;
         stats->rel_residual = h->error;
         stats->b_norm = h->bnorm;
+        stats->refinements = h->replacements;
         stats->solve_ms = ms;
     }
     return h->status == OGS_OK ? OGS_OK : (ogs_status)h->status;
@@ -552,8 +859,8 @@ extern "C" ogs_status ogs_gpu_spmv(ogs_system* s, const double* x, double* y)
         if (!s->vec_out) OGS_CUDA_TRY(cudaMalloc(&s->vec_out, nb));
         yd = s->vec_out;
     }
-    CsrView<double> A{s->m->row_ptr, s->m->col, s->val, s->n};
-    launch_spmv(A, xd, yd, s->G, s->stream);
+    SellView<double> A{s->m->slice_ptr, s->m->sell_col, s->val, s->n};
+    launch_spmv(A, xd, yd, s->stream);
     OGS_LAUNCH_CHECK();
     if (!ydev) OGS_CUDA_TRY(cudaMemcpyAsync(y, yd, nb, cudaMemcpyDeviceToHost, s->stream));
     OGS_CUDA_TRY(cudaStreamSynchronize(s->stream));
@@ -574,9 +881,18 @@ extern "C" ogs_status ogs_gpu_get_csr(const ogs_system* s, int64_t* row_ptr, int
     }
     if (val)
     {
-        OGS_CUDA_TRY(cudaStreamSynchronize(s->stream));
-        OGS_CUDA_TRY(cudaMemcpy(val, s->val, m->nnz * sizeof(double),
-                                is_device_ptr(val) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost));
+        // gather the SELL-32 slots back into CSR order
+        double* tmp = nullptr;
+        OGS_CUDA_TRY(cudaMalloc(&tmp, std::max<int64_t>(1, m->nnz) * sizeof(double)));
+        k_sell_to_csr<<<vec_grid((int)std::min<int64_t>(m->nnz, 1 << 30)), 256, 0, s->stream>>>(
+            s->val, m->csr2sell, tmp, m->nnz);
+        cudaError_t e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpy(val, tmp, m->nnz * sizeof(double),
+                           is_device_ptr(val) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost);
+        cudaFree(tmp);
+        if (e != cudaSuccess) { set_error("get_csr: %s", cudaGetErrorString(e)); return OGS_CUDA_ERROR; }
     }
     return OGS_OK;
 }
@@ -596,5 +912,32 @@ extern "C" ogs_status ogs_gpu_get_x(const ogs_system* s, double* x)
     OGS_CUDA_TRY(cudaStreamSynchronize(s->stream));
     OGS_CUDA_TRY(cudaMemcpy(x, s->x, (size_t)s->n * sizeof(double),
                             is_device_ptr(x) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost));
+    return OGS_OK;
+}
+
+extern "C" ogs_status ogs_gpu_profile(ogs_system* s, int32_t enable, ogs_profile* out)
+{
+    if (!s) { set_error("profile: NULL system"); return OGS_BAD_ARG; }
+    if (out)
+    {
+        out->spmv_ms = s->prof_spmv_ms;
+        out->spmv_launches = s->prof_spmv_n;
+        out->solve_ms = s->prof_solve_ms;
+        out->solves = s->prof_solves;
+    }
+    s->prof_spmv_ms = s->prof_solve_ms = 0.0;
+    s->prof_spmv_n = s->prof_solves = 0;
+    const bool on = enable != 0;
+    if (on && !s->prof_b[0])
+        for (int i = 0; i < ogs_system::kChunk; i++)
+        {
+            OGS_CUDA_TRY(cudaEventCreate(&s->prof_b[i]));
+            OGS_CUDA_TRY(cudaEventCreate(&s->prof_e[i]));
+        }
+    if (on != s->prof_on)
+    {
+        s->prof_on = on;
+        drop_graphs(s);  // re-capture with / without the events
+    }
     return OGS_OK;
 }

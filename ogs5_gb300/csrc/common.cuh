@@ -113,25 +113,43 @@ struct AsmArgs
 
 }  // namespace ogs
 
+// Matrix values live in SELL-32 order on the device: rows are grouped in
+// slices of 32 consecutive rows; inside a slice, entry j of every row is
+// stored contiguously (j-major), so one warp -- one thread per row -- reads
+// 32 consecutive values per step.  Rows shorter than the slice width are
+// padded with (own column, 0.0).  The CSR pattern of SparseTable is kept for
+// read-back; csr2sell maps a CSR position to its SELL slot.
+constexpr int kSlice = 32;
+
 struct ogs_mesh
 {
     int elem_type = 0, dim = 3, nn = 8, ngauss = 3, ngp = 27;
     int64_t n_nodes = 0, n_elem = 0;
-    int64_t nnz = 0;
+    int64_t nnz = 0;          // CSR entries (SparseTable size_entry_column)
+    int64_t sell_nnz = 0;     // SELL-32 slots including padding
+    int n_slices = 0;
     bool affine = false;      // every element has a constant Jacobian
     int device = 0;
     // device arrays
     double *x = nullptr, *y = nullptr, *z = nullptr;
-    int32_t* conn_t = nullptr;   // [nn][n_elem]
-    int32_t* row_ptr = nullptr;  // [n_nodes+1]
-    int32_t* col = nullptr;      // [nnz]
-    int32_t* diag_pos = nullptr; // [n_nodes]
-    int32_t* slot_t = nullptr;   // [nn*nn][n_elem]
-    double* tab = nullptr;       // shape table block (N, dN, w3)
-    double* aff = nullptr;       // affine table block (Q, M0, dNc)
+    int32_t* conn_t = nullptr;     // [nn][n_elem]
+    int32_t* row_ptr = nullptr;    // CSR [n_nodes+1]
+    int32_t* col = nullptr;        // CSR [nnz]
+    int32_t* csr2sell = nullptr;   // [nnz] SELL slot of each CSR entry
+    int32_t* slice_ptr = nullptr;  // [n_slices+1] first SELL slot of a slice
+    int32_t* sell_col = nullptr;   // [sell_nnz]
+    int32_t* row_len = nullptr;    // [n_nodes] stored entries per row
+    int32_t* diag_pos = nullptr;   // [n_nodes] SELL slot of the diagonal
+    int32_t* slot_t = nullptr;     // [nn*nn][n_elem] SELL slot of (i, j)
+    // diagonal-offset form of the pattern (structured grids): the distinct
+    // column offsets (col - row), sorted, and per SELL slot the index of
+    // its offset (-1 for padding); n_off == 0 when there are too many
+    int n_off = 0;
+    int n_up = 0;                  // offsets >= 0 (the first is the diagonal)
+    int32_t* up_off = nullptr;     // [n_up] offsets >= 0, ascending
+    int8_t* slot_up = nullptr;     // [sell_nnz] index into up_off, -1 if col < row or padding
+    std::vector<int32_t> host_up_off;
+    double* tab = nullptr;         // shape table block (N, dN, w3)
+    double* aff = nullptr;         // affine table block (Q, M0, dNc)
     ogs::ShapeTable host_tab;
-    // structured 27/9-point form (hex/quad box meshes): diagonal offsets
-    int n_diag = 0;
-    int32_t* dia_off = nullptr;  // [n_diag] column offset of each diagonal
-    int32_t* dia_slot = nullptr; // [n_diag][n_nodes] CSR slot or -1
 };

@@ -1,4 +1,4 @@
-// krylov.cu -- CSR SpMV, fused vector updates and the device-resident
+// krylov.cu -- SELL-32 SpMV, fused vector updates and the device-resident
 // CG / BiCGStab iterations of Linear_EQS (FEM/equation_class.cpp).
 //
 // Each iteration is a short fixed sequence of kernels.  Every kernel that
@@ -9,6 +9,13 @@
 // iteration counter.  After `done` is set every later kernel returns at
 // once, so the host can replay a captured chunk of iterations (CUDA graph)
 // and poll a single flag between chunks: no host round trip per iteration.
+//
+// GB300 issues about two FP64 FMAs per clock per SM, so the SpMV is written
+// to spend exactly one DFMA per stored entry: one thread per row, SELL-32
+// slices read warp-coalesced with streaming (evict-first) loads, the row
+// sum accumulated in ascending column order like CSparseMatrix::multiVec,
+// no shuffle reductions.  Vector kernels load four elements per thread
+// before computing to keep enough bytes in flight.
 #include <algorithm>
 #include <cfloat>
 
@@ -19,87 +26,38 @@ namespace ogs {
 // ------------------------------------------------------------------
 // reductions
 // ------------------------------------------------------------------
-template <int NV>
-__device__ __forceinline__ void warp_sum(double* v)
-{
-#pragma unroll
-    for (int k = 0; k < NV; k++)
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
-}
-
-// Block-reduces v[NV]; thread 0 stores the block partials; returns true in
-// every thread of the last block to arrive, with the grid totals in v.
+// grid_reduce: FP64 grid sum (krylov.cuh grid_sum) with the totals
+// broadcast back into v for the calling thread 0
 template <int NV>
 __device__ __forceinline__ bool grid_reduce(double* v, double* part, unsigned int* ticket)
 {
-    __shared__ double sm[NV][kThreads / 32];
-    __shared__ bool last;
-    warp_sum<NV>(v);
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (lane == 0)
-#pragma unroll
-        for (int k = 0; k < NV; k++) sm[k][wid] = v[k];
-    __syncthreads();
+    double out[NV];
+    if (!grid_sum<NV, double>(v, out, part, ticket)) return false;
     if (threadIdx.x == 0)
-    {
-        const int nw = blockDim.x >> 5;
 #pragma unroll
-        for (int k = 0; k < NV; k++)
-        {
-            double s = 0.0;
-            for (int w = 0; w < nw; w++) s += sm[k][w];
-            part[k * kMaxBlocks + blockIdx.x] = s;
-        }
-        __threadfence();
-        const unsigned int t = atomicAdd(ticket, 1u);
-        last = (t == gridDim.x - 1);
-    }
-    __syncthreads();
-    if (!last) return false;
-    __threadfence();
-#pragma unroll
-    for (int k = 0; k < NV; k++)
-    {
-        double s = 0.0;
-        for (int bidx = threadIdx.x; bidx < (int)gridDim.x; bidx += blockDim.x)
-            s += *((volatile double*)&part[k * kMaxBlocks + bidx]);
-        v[k] = s;
-    }
-    warp_sum<NV>(v);
-    __syncthreads();
-    if (lane == 0)
-#pragma unroll
-        for (int k = 0; k < NV; k++) sm[k][wid] = v[k];
-    __syncthreads();
-    const int nw = blockDim.x >> 5;
-#pragma unroll
-    for (int k = 0; k < NV; k++)
-    {
-        double s = 0.0;
-        for (int w = 0; w < nw; w++) s += sm[k][w];
-        v[k] = s;
-    }
-    if (threadIdx.x == 0) *ticket = 0u;
+        for (int k = 0; k < NV; k++) v[k] = out[k];
     return true;
 }
 
 // ------------------------------------------------------------------
-// SpMV: G lanes per row, lane-strided partial sums, shuffle within the group
+// SELL-32 row product: entries of row r sit at slice_ptr[r/32] + 32 j + r%32
 // ------------------------------------------------------------------
-template <int G>
-__device__ __forceinline__ double row_dot(const int32_t* __restrict__ rp,
-                                          const int32_t* __restrict__ col,
-                                          const double* __restrict__ val,
-                                          const double* __restrict__ x, int row, int lane,
-                                          bool valid)
+template <typename T>
+__device__ __forceinline__ double sell_row(const SellView<T>& A, const double* __restrict__ x,
+                                           int row)
 {
-    const int beg = valid ? __ldg(rp + row) : 0, end = valid ? __ldg(rp + row + 1) : 0;
-    double s = 0.0;
-    for (int k = beg + lane; k < end; k += G) s += __ldcs(val + k) * __ldg(x + __ldcs(col + k));
-#pragma unroll
-    for (int o = G / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, G);
-    return s;
+    const int s = row >> 5;
+    const int b0 = __ldg(A.slice_ptr + s), b1 = __ldg(A.slice_ptr + s + 1);
+    const int w = (b1 - b0) >> 5;
+    const int beg = b0 + (row & 31);
+    double acc = 0.0;
+#pragma unroll 3
+    for (int j = 0; j < w; j++)
+    {
+        const int k = beg + (j << 5);
+        acc += (double)__ldcs(A.val + k) * __ldg(x + __ldcs(A.col + k));
+    }
+    return acc;
 }
 
 __device__ __forceinline__ double apply_jacobi(const SolveArgs& a, int i, double r)
@@ -121,22 +79,11 @@ __global__ void k_dinv(const double* __restrict__ val, const int32_t* __restrict
 }
 
 // y = A x (ogs_gpu_spmv, CSparseMatrix::multiVec)
-template <int G>
-__global__ void __launch_bounds__(kThreads) k_spmv(CsrView<double> A, const double* __restrict__ x,
+__global__ void __launch_bounds__(kThreads) k_spmv(SellView<double> A, const double* __restrict__ x,
                                                    double* __restrict__ y)
 {
-    const int lane = threadIdx.x & (G - 1);
-    const int rows_per_block = blockDim.x / G;
-    const int sub = (threadIdx.x & 31) / G;              // row slot within the warp
-    const int wrow = (threadIdx.x >> 5) * (32 / G);      // warp's first row in the block
-    for (int base = blockIdx.x * rows_per_block + wrow; base < A.n;
-         base += gridDim.x * rows_per_block)
-    {
-        const int row = base + sub;
-        const bool valid = row < A.n;
-        const double s = row_dot<G>(A.row_ptr, A.col, A.val, x, row, lane, valid);
-        if (valid && lane == 0) y[row] = s;
-    }
+    for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < A.n; row += gridDim.x * blockDim.x)
+        y[row] = sell_row(A, x, row);
 }
 
 // |b| and Linear_EQS::CheckNormRHS (equation_class.cpp:1104-1121)
@@ -165,40 +112,28 @@ __global__ void __launch_bounds__(kThreads) k_norm_b(SolveArgs a)
 
 // r = b - A x; CG: z = M^-1 r, p = z, dots r.r, r.z;  BiCGStab: r0 = r,
 // v = p = 0, dots r.r
-template <int G>
 __global__ void __launch_bounds__(kThreads) k_init_residual(SolveArgs a, int kind)
 {
     KState* st = a.st;
     if (st->done) return;
-    const int lane = threadIdx.x & (G - 1);
-    const int rows_per_block = blockDim.x / G;
-    const int sub = (threadIdx.x & 31) / G;              // row slot within the warp
-    const int wrow = (threadIdx.x >> 5) * (32 / G);      // warp's first row in the block
     double v[2] = {0.0, 0.0};
-    for (int base = blockIdx.x * rows_per_block + wrow; base < a.A.n;
-         base += gridDim.x * rows_per_block)
+    for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < a.A.n; row += gridDim.x * blockDim.x)
     {
-        const int row = base + sub;
-        const bool valid = row < a.A.n;
-        const double ax = row_dot<G>(a.A.row_ptr, a.A.col, a.A.val, a.v.x, row, lane, valid);
-        if (valid && lane == 0)
+        const double r = a.v.b[row] - sell_row(a.A, a.v.x, row);
+        a.v.r[row] = r;
+        if (kind == SK_CG)
         {
-            const double r = a.v.b[row] - ax;
-            a.v.r[row] = r;
-            if (kind == SK_CG)
-            {
-                const double z = apply_jacobi(a, row, r);
-                a.v.p[row] = z;
-                v[1] += r * z;
-            }
-            else
-            {
-                a.v.r0[row] = r;
-                a.v.v[row] = 0.0;
-                a.v.p[row] = 0.0;
-            }
-            v[0] += r * r;
+            const double z = apply_jacobi(a, row, r);
+            a.v.p[row] = z;
+            v[1] += r * z;
         }
+        else
+        {
+            a.v.r0[row] = r;
+            a.v.v[row] = 0.0;
+            a.v.p[row] = 0.0;
+        }
+        v[0] += r * r;
     }
     if (grid_reduce<2>(v, st->part[1], &st->ticket[1]) && threadIdx.x == 0)
     {
@@ -222,47 +157,62 @@ __global__ void __launch_bounds__(kThreads) k_init_residual(SolveArgs a, int kin
 // CG (Linear_EQS::CG, equation_class.cpp:1129-1187)
 // ------------------------------------------------------------------
 // s = A p ; alpha = rr / (p . s)
-template <int G>
 __global__ void __launch_bounds__(kThreads) k_cg_spmv(SolveArgs a)
 {
     KState* st = a.st;
     if (st->done) return;
-    const int lane = threadIdx.x & (G - 1);
-    const int rows_per_block = blockDim.x / G;
-    const int sub = (threadIdx.x & 31) / G;              // row slot within the warp
-    const int wrow = (threadIdx.x >> 5) * (32 / G);      // warp's first row in the block
     double v[1] = {0.0};
-    for (int base = blockIdx.x * rows_per_block + wrow; base < a.A.n;
-         base += gridDim.x * rows_per_block)
+    for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < a.A.n; row += gridDim.x * blockDim.x)
     {
-        const int row = base + sub;
-        const bool valid = row < a.A.n;
-        const double s = row_dot<G>(a.A.row_ptr, a.A.col, a.A.val, a.v.p, row, lane, valid);
-        if (valid && lane == 0)
-        {
-            a.v.s[row] = s;
-            v[0] += a.v.p[row] * s;
-        }
+        const double s = sell_row(a.A, a.v.p, row);
+        a.v.s[row] = s;
+        v[0] += a.v.p[row] * s;
     }
     if (grid_reduce<1>(v, st->part[2], &st->ticket[2]) && threadIdx.x == 0)
         st->alpha = st->rr / v[0];
 }
 
+constexpr int kU = 4;  // elements per thread per step in the vector kernels
+
 // x += alpha p ; r -= alpha s ; convergence test ; z = M^-1 r ; beta
+template <bool JAC>
 __global__ void __launch_bounds__(kThreads) k_cg_update(SolveArgs a)
 {
     KState* st = a.st;
     if (st->done) return;
     const double alpha = st->alpha;
+    const int n = a.A.n;
     double v[2] = {0.0, 0.0};
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.A.n; i += gridDim.x * blockDim.x)
+    const int stride = gridDim.x * blockDim.x;
+    for (int base = blockIdx.x * blockDim.x + threadIdx.x; base < n; base += kU * stride)
     {
-        a.v.x[i] += alpha * a.v.p[i];
-        const double r = a.v.r[i] - alpha * a.v.s[i];
-        a.v.r[i] = r;
-        const double z = apply_jacobi(a, i, r);
-        v[0] += r * r;
-        v[1] += z * r;
+        double xv[kU], pv[kU], rv[kU], sv[kU], dv[kU];
+#pragma unroll
+        for (int u = 0; u < kU; u++)
+        {
+            const int i = base + u * stride;
+            if (i < n)
+            {
+                xv[u] = a.v.x[i];
+                pv[u] = a.v.p[i];
+                rv[u] = a.v.r[i];
+                sv[u] = a.v.s[i];
+                dv[u] = JAC ? a.v.dinv[i] : 1.0;
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kU; u++)
+        {
+            const int i = base + u * stride;
+            if (i < n)
+            {
+                a.v.x[i] = xv[u] + alpha * pv[u];
+                const double r = rv[u] - alpha * sv[u];
+                a.v.r[i] = r;
+                v[0] += r * r;
+                v[1] += JAC ? (r * dv[u]) * r : r * r;
+            }
+        }
     }
     if (grid_reduce<2>(v, st->part[3], &st->ticket[3]) && threadIdx.x == 0)
     {
@@ -278,13 +228,35 @@ __global__ void __launch_bounds__(kThreads) k_cg_update(SolveArgs a)
 }
 
 // p = z + beta p
+template <bool JAC>
 __global__ void __launch_bounds__(kThreads) k_cg_p(SolveArgs a)
 {
     KState* st = a.st;
     if (st->done) return;
     const double beta = st->beta;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.A.n; i += gridDim.x * blockDim.x)
-        a.v.p[i] = apply_jacobi(a, i, a.v.r[i]) + beta * a.v.p[i];
+    const int n = a.A.n;
+    const int stride = gridDim.x * blockDim.x;
+    for (int base = blockIdx.x * blockDim.x + threadIdx.x; base < n; base += kU * stride)
+    {
+        double rv[kU], dv[kU], pv[kU];
+#pragma unroll
+        for (int u = 0; u < kU; u++)
+        {
+            const int i = base + u * stride;
+            if (i < n)
+            {
+                rv[u] = a.v.r[i];
+                dv[u] = JAC ? a.v.dinv[i] : 1.0;
+                pv[u] = a.v.p[i];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kU; u++)
+        {
+            const int i = base + u * stride;
+            if (i < n) a.v.p[i] = (JAC ? rv[u] * dv[u] : rv[u]) + beta * pv[u];
+        }
+    }
 }
 
 // ------------------------------------------------------------------
@@ -306,27 +278,16 @@ __global__ void __launch_bounds__(kThreads) k_bi_p(SolveArgs a)
 }
 
 // v = A p_h ; alpha = rho1 / (r0 . v)
-template <int G>
 __global__ void __launch_bounds__(kThreads) k_bi_v(SolveArgs a)
 {
     KState* st = a.st;
     if (st->done) return;
-    const int lane = threadIdx.x & (G - 1);
-    const int rows_per_block = blockDim.x / G;
-    const int sub = (threadIdx.x & 31) / G;              // row slot within the warp
-    const int wrow = (threadIdx.x >> 5) * (32 / G);      // warp's first row in the block
     double v[1] = {0.0};
-    for (int base = blockIdx.x * rows_per_block + wrow; base < a.A.n;
-         base += gridDim.x * rows_per_block)
+    for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < a.A.n; row += gridDim.x * blockDim.x)
     {
-        const int row = base + sub;
-        const bool valid = row < a.A.n;
-        const double s = row_dot<G>(a.A.row_ptr, a.A.col, a.A.val, a.v.ph, row, lane, valid);
-        if (valid && lane == 0)
-        {
-            a.v.v[row] = s;
-            v[0] += a.v.r0[row] * s;
-        }
+        const double s = sell_row(a.A, a.v.ph, row);
+        a.v.v[row] = s;
+        v[0] += a.v.r0[row] * s;
     }
     if (grid_reduce<1>(v, st->part[4], &st->ticket[4]) && threadIdx.x == 0)
         st->alpha = st->rho1 / v[0];
@@ -355,28 +316,17 @@ __global__ void __launch_bounds__(kThreads) k_bi_s(SolveArgs a)
 }
 
 // t = A s_h ; omega = (t . s) / (t . t), or 1 when t . t <= DBL_MIN
-template <int G>
 __global__ void __launch_bounds__(kThreads) k_bi_t(SolveArgs a)
 {
     KState* st = a.st;
     if (st->done) return;
-    const int lane = threadIdx.x & (G - 1);
-    const int rows_per_block = blockDim.x / G;
-    const int sub = (threadIdx.x & 31) / G;              // row slot within the warp
-    const int wrow = (threadIdx.x >> 5) * (32 / G);      // warp's first row in the block
     double v[2] = {0.0, 0.0};
-    for (int base = blockIdx.x * rows_per_block + wrow; base < a.A.n;
-         base += gridDim.x * rows_per_block)
+    for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < a.A.n; row += gridDim.x * blockDim.x)
     {
-        const int row = base + sub;
-        const bool valid = row < a.A.n;
-        const double t = row_dot<G>(a.A.row_ptr, a.A.col, a.A.val, a.v.sh, row, lane, valid);
-        if (valid && lane == 0)
-        {
-            a.v.t[row] = t;
-            v[0] += t * t;
-            v[1] += t * a.v.s[row];
-        }
+        const double t = sell_row(a.A, a.v.sh, row);
+        a.v.t[row] = t;
+        v[0] += t * t;
+        v[1] += t * a.v.s[row];
     }
     if (grid_reduce<2>(v, st->part[6], &st->ticket[6]) && threadIdx.x == 0)
         st->omega = v[0] > DBL_MIN ? v[1] / v[0] : 1.0;
@@ -423,44 +373,37 @@ __global__ void k_bi_finish(SolveArgs a)
 // ------------------------------------------------------------------
 // host side launchers
 // ------------------------------------------------------------------
+static int sm_count()
+{
+    static int sms = 0;
+    if (!sms)
+    {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 152;
+    }
+    return sms;
+}
+
 int vec_grid(int n)
 {
-    int dev = 0, sms = 152;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int need = (n + kThreads - 1) / kThreads;
-    return std::max(1, std::min(need, std::min(sms * 8, kMaxBlocks)));
+    return std::max(1, std::min(need, std::min(sm_count() * 8, kMaxBlocks)));
 }
 
-int row_group(double avg_nnz)
+// Grid of the reducing vector kernels: two blocks per SM, so each thread
+// handles a dozen or more elements and the FP64 adds of the block
+// reduction stay a small fraction of the FP64 work.
+static int red_grid(int n)
 {
-    if (avg_nnz >= 20.0) return 4;
-    if (avg_nnz >= 6.0) return 2;
-    return 1;
+    const int need = (n + kThreads - 1) / kThreads;
+    return std::max(1, std::min(need, std::min(sm_count() * 2, kMaxBlocks)));
 }
 
-static int spmv_grid(int n, int G)
+void launch_spmv(const SellView<double>& A, const double* x, double* y, cudaStream_t s)
 {
-    int dev = 0, sms = 152;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int rows_per_block = kThreads / G;
-    const int need = (n + rows_per_block - 1) / rows_per_block;
-    return std::max(1, std::min(need, std::min(sms * 8, kMaxBlocks)));
-}
-
-#define OGS_G_DISPATCH(G, KERNEL, GRID, ...)                                               \
-    do                                                                                     \
-    {                                                                                      \
-        if (G == 4) KERNEL<4><<<GRID, kThreads, 0, s>>>(__VA_ARGS__);                      \
-        else if (G == 2) KERNEL<2><<<GRID, kThreads, 0, s>>>(__VA_ARGS__);                 \
-        else if (G == 8) KERNEL<8><<<GRID, kThreads, 0, s>>>(__VA_ARGS__);                 \
-        else KERNEL<1><<<GRID, kThreads, 0, s>>>(__VA_ARGS__);                             \
-    } while (0)
-
-void launch_spmv(const CsrView<double>& A, const double* x, double* y, int G, cudaStream_t s)
-{
-    OGS_G_DISPATCH(G, k_spmv, spmv_grid(A.n, G), A, x, y);
+    k_spmv<<<vec_grid(A.n), kThreads, 0, s>>>(A, x, y);
 }
 
 void launch_dinv(const double* val, const int32_t* diag_pos, double* dinv, int n, cudaStream_t s)
@@ -468,31 +411,50 @@ void launch_dinv(const double* val, const int32_t* diag_pos, double* dinv, int n
     k_dinv<<<vec_grid(n), kThreads, 0, s>>>(val, diag_pos, dinv, n);
 }
 
-// start of a solve: |b| check and initial residual
-void launch_krylov_init(const SolveArgs& a, int kind, int G, cudaStream_t s)
+void launch_norm_b(const SolveArgs& a, cudaStream_t s)
 {
-    const int vg = vec_grid(a.A.n), sg = spmv_grid(a.A.n, G);
-    k_norm_b<<<vg, kThreads, 0, s>>>(a);
-    OGS_G_DISPATCH(G, k_init_residual, sg, a, kind);
+    k_norm_b<<<vec_grid(a.A.n), kThreads, 0, s>>>(a);
 }
 
-// one iteration's kernels (captured into the chunk graph)
-void launch_krylov_iteration(const SolveArgs& a, int kind, int G, cudaStream_t s)
+// start of a solve: |b| check and initial residual
+void launch_krylov_init(const SolveArgs& a, int kind, cudaStream_t s)
 {
-    const int vg = vec_grid(a.A.n), sg = spmv_grid(a.A.n, G);
+    const int vg = vec_grid(a.A.n);
+    k_norm_b<<<vg, kThreads, 0, s>>>(a);
+    k_init_residual<<<vg, kThreads, 0, s>>>(a, kind);
+}
+
+// one iteration's kernels (captured into the chunk graph); eb/ee, when
+// given, are recorded around the iteration's first SpMV
+void launch_krylov_iteration(const SolveArgs& a, int kind, cudaStream_t s, cudaEvent_t eb, cudaEvent_t ee)
+{
+    const int vg = vec_grid(a.A.n), rg = red_grid(a.A.n);
+    const bool jac = a.precond == OGS_PRECOND_JACOBI;
     if (kind == SK_CG)
     {
-        OGS_G_DISPATCH(G, k_cg_spmv, sg, a);
-        k_cg_update<<<vg, kThreads, 0, s>>>(a);
-        k_cg_p<<<vg, kThreads, 0, s>>>(a);
+        if (eb) cudaEventRecordWithFlags(eb, s, cudaEventRecordExternal);
+        k_cg_spmv<<<vg, kThreads, 0, s>>>(a);
+        if (ee) cudaEventRecordWithFlags(ee, s, cudaEventRecordExternal);
+        if (jac)
+        {
+            k_cg_update<true><<<rg, kThreads, 0, s>>>(a);
+            k_cg_p<true><<<vg, kThreads, 0, s>>>(a);
+        }
+        else
+        {
+            k_cg_update<false><<<rg, kThreads, 0, s>>>(a);
+            k_cg_p<false><<<vg, kThreads, 0, s>>>(a);
+        }
     }
     else
     {
         k_bi_p<<<vg, kThreads, 0, s>>>(a);
-        OGS_G_DISPATCH(G, k_bi_v, sg, a);
-        k_bi_s<<<vg, kThreads, 0, s>>>(a);
-        OGS_G_DISPATCH(G, k_bi_t, sg, a);
-        k_bi_x<<<vg, kThreads, 0, s>>>(a);
+        if (eb) cudaEventRecordWithFlags(eb, s, cudaEventRecordExternal);
+        k_bi_v<<<vg, kThreads, 0, s>>>(a);
+        if (ee) cudaEventRecordWithFlags(ee, s, cudaEventRecordExternal);
+        k_bi_s<<<rg, kThreads, 0, s>>>(a);
+        k_bi_t<<<vg, kThreads, 0, s>>>(a);
+        k_bi_x<<<rg, kThreads, 0, s>>>(a);
     }
 }
 

@@ -17,6 +17,15 @@ struct KState
     int iter, max_iter, done, status;
     int finish_s;                // BiCGStab left at the s-test (x += alpha p_h pending)
     int pad;
+    // FP32 inner CG with FP64 residual replacement
+    double scale;                // r32 = scale * r64 (scale = 1 / |r64| at the last replacement)
+    double ratio;                // scale_new / scale_old at a replacement
+    double rmax;                 // |r32| right after the last replacement
+    double delta;                // replace when |r32| < delta * rmax
+    int replace;                 // 1: the FP64 residual replacement is due
+    int replacements;
+    int first;                   // first restart of a solve (p = z)
+    int pad2;
     unsigned int ticket[8];
     double part[8][2 * kMaxBlocks];
 };
@@ -27,11 +36,11 @@ enum SolveKind
     SK_BICGSTAB = 1
 };
 
-// Views of the matrix in the precision of the sweep.
+// SELL-32 view of the matrix in the precision of the sweep.
 template <typename T>
-struct CsrView
+struct SellView
 {
-    const int32_t* row_ptr;
+    const int32_t* slice_ptr;
     const int32_t* col;
     const T* val;
     int32_t n;
@@ -54,10 +63,106 @@ struct KrylovVecs
 
 struct SolveArgs
 {
-    CsrView<double> A;
+    SellView<double> A;
     KrylovVecs v;
     KState* st;
     int precond;  // 0 none, 1 Jacobi
+};
+
+// ------------------------------------------------------------------
+// Grid-wide sums.  Each block reduces its threads' values and stores one
+// partial per value; the last block to take a ticket adds the partials of
+// all blocks with all of its threads (block order fixed by the strided
+// loop and the tree, so the result is deterministic for a launch shape)
+// and resets the ticket.  FP32 inputs are reduced in FP32 inside a warp
+// (cheap FADDs) and in FP64 from the warp sums on.
+// ------------------------------------------------------------------
+template <int NV, typename T>
+__device__ __forceinline__ void warp_allsum(T* v)
+{
+#pragma unroll
+    for (int k = 0; k < NV; k++)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+}
+
+// returns true in every thread of the last block; out[] valid in thread 0
+template <int NV, typename T>
+__device__ __forceinline__ bool grid_sum(const T* vin, double* out, double* part, unsigned int* ticket)
+{
+    __shared__ double sm[NV][kThreads / 32];
+    __shared__ bool last;
+    T w[NV];
+#pragma unroll
+    for (int k = 0; k < NV; k++) w[k] = vin[k];
+    warp_allsum<NV, T>(w);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int nw = blockDim.x >> 5;
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < NV; k++) sm[k][wid] = (double)w[k];
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+#pragma unroll
+        for (int k = 0; k < NV; k++)
+        {
+            double s = 0.0;
+            for (int q = 0; q < nw; q++) s += sm[k][q];
+            part[k * kMaxBlocks + blockIdx.x] = s;
+        }
+        __threadfence();
+        last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    double v[NV];
+#pragma unroll
+    for (int k = 0; k < NV; k++)
+    {
+        double s = 0.0;
+        for (int q = threadIdx.x; q < (int)gridDim.x; q += blockDim.x)
+            s += *((volatile double*)&part[k * kMaxBlocks + q]);
+        v[k] = s;
+    }
+    warp_allsum<NV, double>(v);
+    __syncthreads();
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < NV; k++) sm[k][wid] = v[k];
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+#pragma unroll
+        for (int k = 0; k < NV; k++)
+        {
+            double s = 0.0;
+            for (int q = 0; q < nw; q++) s += sm[k][q];
+            out[k] = s;
+        }
+        *ticket = 0u;
+    }
+    return true;
+}
+
+// Arguments of the FP32-inner / FP64-refinement kernels (mixed.cu).
+struct MixedArgs
+{
+    SellView<double> A;       // FP64 matrix
+    int fmt;                  // 0: diagonal-offset upper half, 1: SELL-32 FP32
+    const float* U;           // [n_up][n]
+    const int32_t* up_off;    // [n_up]
+    int n_up;
+    int off[16];              // up_off by value (diagonal-offset kernels)
+    const float* val32;       // SELL-32 FP32 values
+    const float* d32;         // Jacobi inverse, FP32
+    double* x;                // FP64 solution
+    const double* b;
+    double* r64;
+    float *x32, *r32, *p32, *s32;
+    KState* st;
+    int n;
 };
 
 }  // namespace ogs

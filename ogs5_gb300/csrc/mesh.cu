@@ -278,8 +278,12 @@ extern "C" ogs_status ogs_gpu_mesh_destroy(ogs_mesh* m)
     cudaFree(m->slot_t);
     cudaFree(m->tab);
     cudaFree(m->aff);
-    cudaFree(m->dia_off);
-    cudaFree(m->dia_slot);
+    cudaFree(m->csr2sell);
+    cudaFree(m->slice_ptr);
+    cudaFree(m->sell_col);
+    cudaFree(m->row_len);
+    cudaFree(m->up_off);
+    cudaFree(m->slot_up);
     delete m;
     return OGS_OK;
 }
@@ -363,7 +367,89 @@ extern "C" ogs_status ogs_gpu_mesh_create(const ogs_mesh_desc* d, ogs_mesh** out
             }
         }
     });
-    // slot map, transposed [i*nn+j][e] for coalesced loads
+    // SELL-32 layout of the pattern
+    const int n_slices = (int)((N + kSlice - 1) / kSlice);
+    std::vector<int32_t> slice_ptr(n_slices + 1, 0);
+    int64_t sell_nnz = 0;
+    for (int s = 0; s < n_slices; s++)
+    {
+        int w = 0;
+        for (int64_t r = (int64_t)s * kSlice; r < std::min<int64_t>(N, (int64_t)(s + 1) * kSlice); r++)
+            w = std::max(w, deg[r]);
+        slice_ptr[s] = (int32_t)sell_nnz;
+        sell_nnz += (int64_t)w * kSlice;
+        if (sell_nnz >= (int64_t(1) << 31)) { delete m; set_error("mesh_create: padded nnz exceeds 2^31"); return OGS_BAD_ARG; }
+    }
+    slice_ptr[n_slices] = (int32_t)sell_nnz;
+    m->sell_nnz = sell_nnz;
+    m->n_slices = n_slices;
+    std::vector<int32_t> csr2sell(nnz), sell_col(sell_nnz);
+    parallel_for(N, [&](int64_t lo, int64_t hi) {
+        for (int64_t r = lo; r < hi; r++)
+        {
+            const int64_t s = r / kSlice, l = r % kSlice;
+            const int w = (slice_ptr[s + 1] - slice_ptr[s]) / kSlice;
+            for (int j = 0; j < w; j++)
+            {
+                const int64_t slot = slice_ptr[s] + (int64_t)j * kSlice + l;
+                if (j < deg[r])
+                {
+                    csr2sell[row_ptr[r] + j] = (int32_t)slot;
+                    sell_col[slot] = col[row_ptr[r] + j];
+                }
+                else
+                    sell_col[slot] = (int32_t)r;  // padding: own column, value 0
+            }
+            if (diag[r] >= 0) diag[r] = csr2sell[diag[r]];
+        }
+    });
+    // pad rows of the last, partial slice
+    for (int64_t r = N; r < (int64_t)n_slices * kSlice; r++)
+    {
+        const int64_t s = r / kSlice, l = r % kSlice;
+        const int w = (slice_ptr[s + 1] - slice_ptr[s]) / kSlice;
+        for (int j = 0; j < w; j++) sell_col[slice_ptr[s] + (int64_t)j * kSlice + l] = 0;
+    }
+    // distinct column offsets: a structured grid has a handful (27 for
+    // hexes, 15 for Kuhn tets, 9 for quads)
+    std::vector<int32_t> up_off;
+    std::vector<int8_t> slot_up;
+    {
+        std::vector<int32_t> offs;
+        bool few = true;
+        for (int64_t r = 0; r < N && few; r++)
+            for (int64_t k = row_ptr[r]; k < row_ptr[r + 1]; k++)
+            {
+                const int32_t o = col[k] - (int32_t)r;
+                auto it = std::lower_bound(offs.begin(), offs.end(), o);
+                if (it == offs.end() || *it != o)
+                {
+                    offs.insert(it, o);
+                    if (offs.size() > 64) { few = false; break; }
+                }
+            }
+        if (few)
+        {
+            for (int32_t o : offs)
+                if (o >= 0) up_off.push_back(o);
+            std::sort(up_off.begin(), up_off.end());
+            m->n_off = (int)offs.size();
+            m->n_up = (int)up_off.size();
+            m->host_up_off = up_off;
+            slot_up.assign(sell_nnz, (int8_t)-1);
+            parallel_for(N, [&](int64_t lo, int64_t hi) {
+                for (int64_t r = lo; r < hi; r++)
+                    for (int64_t k = row_ptr[r]; k < row_ptr[r + 1]; k++)
+                    {
+                        const int32_t o = col[k] - (int32_t)r;
+                        if (o < 0) continue;
+                        const int d = (int)(std::lower_bound(up_off.begin(), up_off.end(), o) - up_off.begin());
+                        slot_up[csr2sell[k]] = (int8_t)d;
+                    }
+            });
+        }
+    }
+    // slot map (SELL slots), transposed [i*nn+j][e] for coalesced loads
     std::vector<int32_t> slot_t((size_t)nn * nn * E);
     std::vector<int32_t> conn_t((size_t)nn * E);
     std::vector<char> aff(E, 1);
@@ -383,7 +469,7 @@ extern "C" ogs_status ogs_gpu_mesh_create(const ogs_mesh_desc* d, ogs_mesh** out
                 for (int j = 0; j < nn; j++)
                 {
                     const int32_t* p = std::lower_bound(cb, ce, en[j]);
-                    slot_t[(size_t)(i * nn + j) * E + e] = (int32_t)(p - col.data());
+                    slot_t[(size_t)(i * nn + j) * E + e] = csr2sell[p - col.data()];
                 }
             }
             double ex[8], ey[8], ez[8];
@@ -419,6 +505,12 @@ extern "C" ogs_status ogs_gpu_mesh_create(const ogs_mesh_desc* d, ogs_mesh** out
         (st = upload(&m->row_ptr, row_ptr.data(), row_ptr.size())) ||
         (st = upload(&m->col, col.data(), col.size())) ||
         (st = upload(&m->diag_pos, diag.data(), diag.size())) ||
+        (st = upload(&m->csr2sell, csr2sell.data(), csr2sell.size())) ||
+        (st = upload(&m->slice_ptr, slice_ptr.data(), slice_ptr.size())) ||
+        (st = upload(&m->sell_col, sell_col.data(), sell_col.size())) ||
+        (st = upload(&m->row_len, deg.data(), deg.size())) ||
+        (m->n_up && (st = upload(&m->up_off, up_off.data(), up_off.size()))) ||
+        (m->n_up && (st = upload(&m->slot_up, slot_up.data(), slot_up.size()))) ||
         (st = upload(&m->slot_t, slot_t.data(), slot_t.size())) ||
         (st = upload(&m->tab, tab.data(), tab.size())) ||
         (st = upload(&m->aff, affb.data(), affb.size())))

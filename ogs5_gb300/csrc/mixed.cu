@@ -1,0 +1,345 @@
+// mixed.cu -- FP32 inner CG inside FP64 iterative refinement.
+//
+// The precision extension of Linear_EQS::CG: the matrix and every inner
+// sweep (SpMV, vector updates) run in FP32, which halves the bytes moved and
+// uses FP32 FMAs (GB300: ~60x the FP64 rate).  The solution x, the true
+// residual r = b - A x and the convergence test |r|/|b| < tol stay FP64:
+//
+//   r64 = b - A64 x64 ; r32 = r64 / |r64| ; p32 = M^-1 r32
+//   repeat  (FP32 CG on A32 d = r32, Jacobi preconditioned)
+//     s32 = A32 p32 ; alpha ; x32 += alpha p32 ; r32 -= alpha s32 ; beta
+//     when |r32| fell by `delta` since the last replacement, or the FP32
+//     recurrence claims convergence:  x64 += |r64| x32 ; x32 = 0 ;
+//     r64 = b - A64 x64 (FP64) ; replace r32 by r64 / |r64| and rescale p32
+//   until |r64| / |b| < tol
+//
+// The FP64 residual replacement (a reliable-update form of iterative
+// refinement) keeps the FP32 Krylov space instead of restarting it, so the
+// iteration count stays close to FP64 CG.  Convergence is only ever
+// declared on the FP64 residual.  Dot products accumulate FP32 per thread
+// and FP64 across threads and blocks.
+//
+// FP32 operator storage: for patterns with at most 64 distinct column
+// offsets (structured grids) the symmetric matrix is stored as the upper
+// half of its diagonal-offset form, U[d][i] = A[i][i + off_d] for off_d >= 0
+// (14 rows of 4 bytes per node for hexes: the config-2 matrix is 61 MB and
+// stays in L2 with the FP32 vectors); y_i = sum_d U[d][i] x_{i+off_d} +
+// sum_{d>0} U[d][i-off_d] x_{i-off_d}.  Other patterns use SELL-32 with
+// FP32 values.
+#include <algorithm>
+#include <cfloat>
+
+#include "krylov.cuh"
+
+namespace ogs {
+
+
+// ------------------------------------------------------------------
+// FP32 operator
+// ------------------------------------------------------------------
+// Diagonal-offset row with the number of stored offsets known at compile
+// time.  All 2*NU-1 (value, x) pairs of the row are loaded into registers
+// before any FMA, so a warp keeps ~50 independent loads in flight (the
+// kernel is latency-bound otherwise); out-of-range neighbours are
+// predicated off.  Summation order: diagonal, then per offset the upper and
+// the mirrored lower entry.
+template <int NU>
+__device__ __forceinline__ float dia_row(const MixedArgs& a, const float* __restrict__ x, int i)
+{
+    constexpr int K = 2 * NU - 1;
+    const int n = a.n;
+    float uv[K], xv[K];
+    uv[0] = __ldg(a.U + i);
+    xv[0] = __ldg(x + i);
+#pragma unroll
+    for (int d = 1; d < NU; d++)
+    {
+        const int o = a.off[d];
+        const float* Ud = a.U + (size_t)d * n;
+        const bool up = i + o < n, lo = i - o >= 0;
+        uv[2 * d - 1] = up ? __ldg(Ud + i) : 0.f;
+        xv[2 * d - 1] = up ? __ldg(x + i + o) : 0.f;
+        uv[2 * d] = lo ? __ldg(Ud + i - o) : 0.f;
+        xv[2 * d] = lo ? __ldg(x + i - o) : 0.f;
+    }
+    float acc = 0.f;
+#pragma unroll
+    for (int k = 0; k < K; k++) acc += uv[k] * xv[k];
+    return acc;
+}
+
+__device__ __forceinline__ float sell32_row(const MixedArgs& a, const float* __restrict__ x, int row)
+{
+    const int s = row >> 5;
+    const int b0 = __ldg(a.A.slice_ptr + s), b1 = __ldg(a.A.slice_ptr + s + 1);
+    const int w = (b1 - b0) >> 5;
+    const int beg = b0 + (row & 31);
+    float acc = 0.f;
+#pragma unroll 3
+    for (int j = 0; j < w; j++)
+    {
+        const int k = beg + (j << 5);
+        acc += __ldg(a.val32 + k) * __ldg(x + __ldg(a.A.col + k));
+    }
+    return acc;
+}
+
+// NU > 0: diagonal-offset operator with NU stored offsets; NU == 0: SELL-32
+template <int NU>
+__device__ __forceinline__ float op_row(const MixedArgs& a, const float* __restrict__ x, int i)
+{
+    if constexpr (NU > 0)
+        return dia_row<NU>(a, x, i);
+    else
+        return sell32_row(a, x, i);
+}
+
+// U[d][i] = (float) A[i][i + off_d]; d32 = (float) (1 / a_ii)
+__global__ void k_mp_convert(MixedArgs a, const int32_t* __restrict__ row_len,
+                             const int8_t* __restrict__ slot_up, float* U, float* val32,
+                             const double* __restrict__ dinv64, float* d32)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x)
+    {
+        d32[i] = (float)dinv64[i];
+        const int beg = a.A.slice_ptr[i >> 5] + (i & 31);
+        const int len = row_len[i];
+        for (int j = 0; j < len; j++)
+        {
+            const int k = beg + (j << 5);
+            if (a.fmt == 0)
+            {
+                const int d = slot_up[k];
+                if (d >= 0) U[(size_t)d * a.n + i] = (float)a.A.val[k];
+            }
+            else
+                val32[k] = (float)a.A.val[k];
+        }
+    }
+}
+
+// ------------------------------------------------------------------
+// FP64 residual replacement
+// ------------------------------------------------------------------
+// x64 += x32 / scale ; x32 = 0
+__global__ void __launch_bounds__(kThreads) k_mp_accumulate(MixedArgs a)
+{
+    KState* st = a.st;
+    if (st->done) return;
+    const double inv = 1.0 / st->scale;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x)
+    {
+        a.x[i] += (double)a.x32[i] * inv;
+        a.x32[i] = 0.f;
+    }
+}
+
+// r64 = b - A64 x64 ; |r64| ; convergence on the FP64 residual ; new scale
+__global__ void __launch_bounds__(kThreads) k_mp_residual(MixedArgs a)
+{
+    KState* st = a.st;
+    if (st->done) return;
+    double v[1] = {0.0};
+    for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < a.n; row += gridDim.x * blockDim.x)
+    {
+        const int s = row >> 5;
+        const int b0 = __ldg(a.A.slice_ptr + s), b1 = __ldg(a.A.slice_ptr + s + 1);
+        const int w = (b1 - b0) >> 5;
+        const int beg = b0 + (row & 31);
+        double acc = 0.0;
+        for (int j = 0; j < w; j++)
+        {
+            const int k = beg + (j << 5);
+            acc += __ldcs(a.A.val + k) * __ldg(a.x + __ldcs(a.A.col + k));
+        }
+        const double r = a.b[row] - acc;
+        a.r64[row] = r;
+        v[0] += r * r;
+    }
+    double out[1];
+    if (grid_sum<1, double>(v, out, st->part[0], &st->ticket[0]) && threadIdx.x == 0)
+    {
+        const double rn = sqrt(out[0]);
+        st->error = rn / st->bnorm;
+        st->replacements += 1;
+        if (!isfinite(st->error)) { st->status = OGS_NONFINITE; st->done = 1; return; }
+        if (st->error < st->tol) { st->status = OGS_OK; st->done = 1; return; }
+        if (st->iter >= st->max_iter) { st->status = OGS_NOT_CONVERGED; st->done = 1; return; }
+        const double ns = rn > DBL_MIN ? 1.0 / rn : 1.0;
+        st->ratio = st->first ? 1.0 : ns / st->scale;
+        st->scale = ns;
+    }
+}
+
+// r32 = scale r64 ; z = M^-1 r32 ; p32 rescaled (or zeroed first) ; rz ; beta
+__global__ void __launch_bounds__(kThreads) k_mp_restart(MixedArgs a)
+{
+    KState* st = a.st;
+    if (st->done) return;
+    const double sc = st->scale;
+    const float ratio = (float)st->ratio;
+    const bool first = st->first != 0;
+    float v[2] = {0.f, 0.f};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x)
+    {
+        const float r = (float)(a.r64[i] * sc);
+        a.r32[i] = r;
+        a.p32[i] = first ? 0.f : a.p32[i] * ratio;
+        const float z = r * a.d32[i];
+        v[0] += r * r;
+        v[1] += z * r;
+    }
+    double out[2];
+    if (grid_sum<2, float>(v, out, st->part[1], &st->ticket[1]) && threadIdx.x == 0)
+    {
+        const double rz_old = st->rr * st->ratio * st->ratio;
+        st->beta = first ? 0.0 : out[1] / rz_old;
+        st->rr = out[1];
+        st->rmax = sqrt(out[0]);
+        st->first = 0;
+        st->replace = 0;
+    }
+}
+
+// ------------------------------------------------------------------
+// FP32 CG iteration
+// ------------------------------------------------------------------
+// s32 = A32 p32 ; alpha = rz / (p . s)
+template <int NU>
+__global__ void __launch_bounds__(kThreads, 3) k_mp_spmv(MixedArgs a)
+{
+    KState* st = a.st;
+    if (st->done || st->replace) return;
+    float v[1] = {0.f};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x)
+    {
+        const float s = op_row<NU>(a, a.p32, i);
+        a.s32[i] = s;
+        v[0] += a.p32[i] * s;
+    }
+    double out[1];
+    if (grid_sum<1, float>(v, out, st->part[2], &st->ticket[2]) && threadIdx.x == 0)
+        st->alpha = st->rr / out[0];
+}
+
+constexpr int kU32 = 4;  // elements per thread per step, loaded before use
+
+// x32 += alpha p ; r32 -= alpha s ; rr, rz ; replacement / beta
+__global__ void __launch_bounds__(kThreads) k_mp_update(MixedArgs a)
+{
+    KState* st = a.st;
+    if (st->done || st->replace) return;
+    const float alpha = (float)st->alpha;
+    const int n = a.n, stride = gridDim.x * blockDim.x;
+    float v[2] = {0.f, 0.f};
+    for (int base = blockIdx.x * blockDim.x + threadIdx.x; base < n; base += kU32 * stride)
+    {
+        float xv[kU32], pv[kU32], rv[kU32], sv[kU32], dv[kU32];
+#pragma unroll
+        for (int u = 0; u < kU32; u++)
+        {
+            const int i = base + u * stride;
+            const bool in = i < n;
+            xv[u] = in ? a.x32[i] : 0.f;
+            pv[u] = in ? a.p32[i] : 0.f;
+            rv[u] = in ? a.r32[i] : 0.f;
+            sv[u] = in ? a.s32[i] : 0.f;
+            dv[u] = in ? a.d32[i] : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < kU32; u++)
+        {
+            const int i = base + u * stride;
+            if (i < n)
+            {
+                a.x32[i] = xv[u] + alpha * pv[u];
+                const float r = rv[u] - alpha * sv[u];
+                a.r32[i] = r;
+                v[0] += r * r;
+                v[1] += (r * dv[u]) * r;
+            }
+        }
+    }
+    double out[2];
+    if (grid_sum<2, float>(v, out, st->part[3], &st->ticket[3]) && threadIdx.x == 0)
+    {
+        st->iter += 1;
+        const double rn = sqrt(out[0]);
+        if (!isfinite(rn)) { st->status = OGS_NONFINITE; st->done = 1; return; }
+        const double est = rn / st->scale / st->bnorm;  // estimate of |r64| / |b|
+        if (est < st->tol || rn < st->delta * st->rmax || st->iter >= st->max_iter)
+        {
+            st->replace = 1;
+            return;
+        }
+        st->beta = out[1] / st->rr;
+        st->rr = out[1];
+    }
+}
+
+// p32 = z + beta p32
+__global__ void __launch_bounds__(kThreads) k_mp_p(MixedArgs a)
+{
+    KState* st = a.st;
+    if (st->done || st->replace) return;
+    const float beta = (float)st->beta;
+    const int n = a.n, stride = gridDim.x * blockDim.x;
+    for (int base = blockIdx.x * blockDim.x + threadIdx.x; base < n; base += kU32 * stride)
+    {
+        float rv[kU32], dv[kU32], pv[kU32];
+#pragma unroll
+        for (int u = 0; u < kU32; u++)
+        {
+            const int i = base + u * stride;
+            const bool in = i < n;
+            rv[u] = in ? a.r32[i] : 0.f;
+            dv[u] = in ? a.d32[i] : 0.f;
+            pv[u] = in ? a.p32[i] : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < kU32; u++)
+        {
+            const int i = base + u * stride;
+            if (i < n) a.p32[i] = rv[u] * dv[u] + beta * pv[u];
+        }
+    }
+}
+
+// ------------------------------------------------------------------
+// launchers
+// ------------------------------------------------------------------
+int vec_grid(int n);
+
+void launch_mp_convert(const MixedArgs& a, const int32_t* row_len, const int8_t* slot_up, float* U,
+                       float* val32, const double* dinv64, float* d32, cudaStream_t s)
+{
+    k_mp_convert<<<vec_grid(a.n), kThreads, 0, s>>>(a, row_len, slot_up, U, val32, dinv64, d32);
+}
+
+// FP64 residual replacement: accumulate, residual, restart, first p update
+void launch_mp_replace(const MixedArgs& a, cudaStream_t s)
+{
+    const int g = vec_grid(a.n);
+    k_mp_accumulate<<<g, kThreads, 0, s>>>(a);
+    k_mp_residual<<<g, kThreads, 0, s>>>(a);
+    k_mp_restart<<<g, kThreads, 0, s>>>(a);
+    k_mp_p<<<g, kThreads, 0, s>>>(a);
+}
+
+void launch_mp_iteration(const MixedArgs& a, cudaStream_t s, cudaEvent_t eb, cudaEvent_t ee)
+{
+    const int g = vec_grid(a.n);
+    if (eb) cudaEventRecordWithFlags(eb, s, cudaEventRecordExternal);
+    switch (a.fmt == 0 ? a.n_up : 0)
+    {
+        case 14: k_mp_spmv<14><<<g, kThreads, 0, s>>>(a); break;  // hex, 27-point
+        case 8: k_mp_spmv<8><<<g, kThreads, 0, s>>>(a); break;    // Kuhn tets, 15-point
+        case 5: k_mp_spmv<5><<<g, kThreads, 0, s>>>(a); break;    // quads, 9-point
+        default: k_mp_spmv<0><<<g, kThreads, 0, s>>>(a); break;   // SELL-32 FP32
+    }
+    if (ee) cudaEventRecordWithFlags(ee, s, cudaEventRecordExternal);
+    k_mp_update<<<g, kThreads, 0, s>>>(a);
+    k_mp_p<<<g, kThreads, 0, s>>>(a);
+}
+
+}  // namespace ogs

@@ -53,3 +53,16 @@ def distort(mesh, amount, seed):
     out = copy.copy(m)
     out.x, out.y, out.z = coords
     return out
+
+
+def renumber(mesh, seed):
+    """Random node renumbering (scatters the CSR pattern: no diagonal form)."""
+    import copy
+    rng = np.random.default_rng(seed)
+    perm = rng.permutation(mesh.n_nodes)          # new id of old node i
+    inv = np.empty_like(perm)
+    inv[perm] = np.arange(mesh.n_nodes)
+    out = copy.copy(mesh)
+    out.x, out.y, out.z = mesh.x[inv], mesh.y[inv], mesh.z[inv]
+    out.conn = perm[mesh.conn].astype(np.int32)
+    return out, perm

@@ -1,0 +1,94 @@
+"""FP32-inner CG with FP64 residual replacement against the plain FP64 path:
+heads within 1e-8 relative (the precision extension's accuracy bar), FP64
+relative residual below the tolerance, on the diagonal-offset FP32 operator
+(structured hex and tet patterns) and on the SELL-32 FP32 fallback."""
+import numpy as np
+import pytest
+
+from ogs5_gb300 import fields
+from ogs5_gb300 import mesh as M
+from tests.helpers import rel_max_err, renumber
+
+pytestmark = pytest.mark.gpu
+
+MIXED_RTOL = 1e-8
+
+
+def _deck(gpu, m, ek, left=10.0, right=0.0, steady=False):
+    p = gpu.make_params(gpu.GROUNDWATER_FLOW, dt=3600.0, storage=1e-4, steady=1 if steady else 0)
+    gm = gpu.GpuMesh(m)
+    eqs = gpu.LinearEQS(gm)
+    eqs.Initialize()
+    eqs.GlobalAssembly(p, ek, np.zeros(m.n_nodes))
+    lf, rf = m.face_nodes(0, 0), m.face_nodes(0, 1)
+    rows = np.concatenate([lf, rf])
+    vals = np.concatenate([np.full(len(lf), left), np.full(len(rf), right)])
+    eqs.SetKnownX(rows, vals, gpu.DIRICHLET_SYMMETRIC)
+    x0 = np.zeros(m.n_nodes)
+    x0[lf] = left
+    return eqs, x0
+
+
+def _both(gpu, eqs, x0, tol=1e-10):
+    eqs.ConfigNumerics(gpu.LS_CG, gpu.PRECOND_JACOBI, 20000, tol, check_norm_rhs=False)
+    x64 = x0.copy()
+    it64 = eqs.Solver(x64)
+    eqs.ConfigNumerics(gpu.LS_CG, gpu.PRECOND_JACOBI, 20000, tol, precision=gpu.PRECISION_FP32_REFINED,
+                       check_norm_rhs=False)
+    x32 = x0.copy()
+    it32 = eqs.Solver(x32)
+    return x64, it64, x32, it32, eqs.stats()
+
+
+@pytest.mark.parametrize("kind", ["hex", "tet", "hex_renumbered"])
+def test_fp32_refined_matches_fp64(gpu, kind):
+    if kind == "tet":
+        m = M.structured_tet(14, 10, 8)
+        ek = np.repeat(fields.lognormal_k((14, 10, 8), np.log(1e-5), 1.0, 4.0, seed=3), 6)
+    else:
+        m = M.structured_hex(24, 20, 12)
+        ek = fields.lognormal_k(m.shape, np.log(1e-5), 1.0, 4.0, seed=3)
+    if kind == "hex_renumbered":
+        m, _ = renumber(m, 5)
+    eqs, x0 = _deck(gpu, m, ek)
+    x64, it64, x32, it32, st = _both(gpu, eqs, x0)
+    assert st["status"] == gpu.OK and st["rel_residual"] < 1e-10
+    assert st["refinements"] >= 2
+    assert rel_max_err(x32, x64) < MIXED_RTOL
+    # residual replacement keeps the Krylov space: iterations near the FP64 count
+    assert it32 <= 1.6 * it64 + 20
+
+
+def test_fp32_refined_config1_quads(gpu):
+    """Precision form of config 1 (100x100 quads, K=1e-4) to 1e-10."""
+    m = M.structured_quad(100, 100)
+    ek = np.full(m.n_elements, 1e-4)
+    eqs, x0 = _deck(gpu, m, ek, 1.0, 0.0, steady=True)
+    x64, it64, x32, it32, st = _both(gpu, eqs, x0)
+    assert rel_max_err(x32, x64) < MIXED_RTOL
+    assert np.abs(x32 - (1 - m.x / 100)).max() < 1e-8
+
+
+def test_fp32_refined_rejects_bicgstab(gpu):
+    m = M.structured_hex(4, 4, 4)
+    eqs, x0 = _deck(gpu, m, np.ones(m.n_elements))
+    eqs.ConfigNumerics(gpu.LS_BICGSTAB, gpu.PRECOND_JACOBI, 100, 1e-10, precision=gpu.PRECISION_FP32_REFINED)
+    with pytest.raises(gpu.OgsError) as ei:
+        eqs.Solver(x0.copy())
+    assert ei.value.status == gpu.BAD_ARG
+
+
+@pytest.mark.parametrize("mixed", [False, True])
+def test_profile_counts_spmv_launches(gpu, mixed):
+    """ogs_gpu_profile times one SpMV per executed Krylov iteration."""
+    m = M.structured_hex(16, 12, 8)
+    ek = fields.lognormal_k(m.shape, np.log(1e-5), 1.0, 4.0, seed=1)
+    eqs, x0 = _deck(gpu, m, ek)
+    eqs.ConfigNumerics(gpu.LS_CG, gpu.PRECOND_JACOBI, 5000, 1e-10,
+                       precision=gpu.PRECISION_FP32_REFINED if mixed else gpu.PRECISION_FP64)
+    eqs.profile(True)
+    x = x0.copy()
+    it = eqs.Solver(x)
+    pr = eqs.profile(False)
+    assert pr["solves"] == 1 and pr["spmv_ms"] > 0
+    assert abs(pr["spmv_launches"] - it) <= 1

@@ -185,7 +185,12 @@ def _flow_system(gpu, oracle, m, ek, symmetric, dt=None, storage=0.0, left=1.0, 
 
 
 def test_config1_bicgstab_jacobi_linear_profile(gpu, oracle):
-    """Config-1 deck: 100x100 quads, K=1e-4, h=1|0 on the x faces, BiCGStab+Jacobi 1e-10."""
+    """Config-1 deck: 100x100 quads, K=1e-4, h=1|0 on the x faces, BiCGStab+Jacobi.
+
+    At the deck's tolerance 1e-10 both codes stop on |r|/|b| < 1e-10 within
+    two iterations of each other; their heads then differ by up to
+    cond(A) x 1e-10 (about 3e-9 here), so head parity is checked on the same
+    system solved to 1e-13, where both iterations have converged."""
     m = M.structured_quad(100, 100)
     ek = np.full(m.n_elements, 1e-4)
     eqs, (rp, col, val, b), x0 = _flow_system(gpu, oracle, m, ek, symmetric=False)
@@ -195,8 +200,12 @@ def test_config1_bicgstab_jacobi_linear_profile(gpu, oracle):
     xo, info = oracle.solve(rp, col, val, b, x0, method=2, precond=1, max_iter=1000, tol=1e-10)
     assert abs(it - info["iterations"]) <= 2
     assert eqs.stats()["rel_residual"] < 1e-10
-    assert rel_max_err(x, xo) < SOLUTION_RTOL
     assert np.abs(x - (1.0 - m.x / 100.0)).max() < 1e-8  # exact bilinear solution
+    eqs.ConfigNumerics(gpu.LS_BICGSTAB, gpu.PRECOND_JACOBI, 2000, 1e-13, check_norm_rhs=False)
+    x = x0.copy()
+    eqs.Solver(x)
+    xo, info = oracle.solve(rp, col, val, b, x0, method=2, precond=1, max_iter=2000, tol=1e-13)
+    assert rel_max_err(x, xo) < SOLUTION_RTOL
 
 
 @pytest.mark.parametrize("kind", ["hex", "tet"])
