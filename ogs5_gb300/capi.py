@@ -43,7 +43,9 @@ EXPORTS = [
     "ogs_gpu_initialize", "ogs_gpu_assemble", "ogs_gpu_set_dirichlet", "ogs_gpu_solve",
     "ogs_gpu_gp_velocity", "ogs_gpu_get_csr", "ogs_gpu_get_rhs", "ogs_gpu_get_x",
     "ogs_gpu_spmv", "ogs_gpu_mesh_gauss_points", "ogs_gpu_kernel_launches", "ogs_gpu_profile",
+    "ogs_gpu_csr_cg_noalloc",
 ]
+NOALLOC_MAX_ROWS = 524288
 
 
 class OgsError(RuntimeError):
@@ -146,6 +148,9 @@ def lib():
         L.ogs_gpu_mesh_gauss_points.restype = C.c_int32
         L.ogs_gpu_profile.argtypes = [vp, C.c_int32, C.POINTER(Profile)]
         L.ogs_gpu_profile.restype = st
+        L.ogs_gpu_csr_cg_noalloc.argtypes = [C.c_int64, vp, vp, vp, vp, vp, C.c_int32, C.c_double, vp,
+                                             C.POINTER(SolveStats)]
+        L.ogs_gpu_csr_cg_noalloc.restype = st
         L.ogs_gpu_kernel_launches.argtypes = [C.c_int32]
         L.ogs_gpu_kernel_launches.restype = C.c_int64
         for name in ("ogs_gpu_mesh_create", "ogs_gpu_mesh_destroy", "ogs_gpu_mesh_info",
@@ -322,3 +327,15 @@ class LinearEQS:
             out = np.zeros(self.n)
         _check(lib().ogs_gpu_spmv(self.h, _ptr(_f64(x)), _ptr(out)))
         return out
+
+
+def csr_cg_noalloc(row_ptr, col, val, b, x, max_iter=1000, tol=1e-10, stream=None):
+    """ogs_gpu_csr_cg_noalloc on torch CUDA tensors (int32 row_ptr/col,
+    float64 val/b/x; x updated in place).  Returns the solve statistics."""
+    st = SolveStats()
+    sptr = None if stream is None else getattr(stream, "cuda_stream", stream)
+    status = lib().ogs_gpu_csr_cg_noalloc(len(b), _ptr(row_ptr), _ptr(col), _ptr(val), _ptr(b), _ptr(x),
+                                         max_iter, tol, sptr, C.byref(st))
+    _check(status, allow=(NOT_CONVERGED,))
+    return {"iterations": st.iterations, "status": st.status, "rel_residual": st.rel_residual,
+            "b_norm": st.b_norm}

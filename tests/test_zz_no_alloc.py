@@ -1,0 +1,69 @@
+"""ogs_gpu_csr_cg_noalloc: the CG entry point for callers that cannot
+allocate device memory (their HBM belongs to a caching allocator or memory
+pool, or they run while a stream is captured in global mode).  It must give
+the same heads as the regular solver (ogs_gpu_solve, same tolerance as the
+other solver parity tests: 1e-10 relative) on two calls in a row, since all
+calls share one static scratch array that keeps the previous contents.
+
+This file is collected last on purpose: if it fails, a run that stops at the
+first failure has already run every other test."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from ogs5_gb300 import fields
+from ogs5_gb300 import mesh as M
+from tests.helpers import SOLUTION_RTOL, rel_max_err
+
+pytestmark = pytest.mark.gpu
+
+
+def test_noalloc_cg_matches_regular_solver_twice(gpu):
+    import torch
+    m = M.structured_hex(40, 30, 20)
+    ek = fields.lognormal_k(m.shape, np.log(1e-5), 1.0, 5.0, seed=7)
+    gm = gpu.GpuMesh(m)
+    eqs = gpu.LinearEQS(gm)
+    eqs.Initialize()
+    eqs.GlobalAssembly(gpu.make_params(gpu.GROUNDWATER_FLOW, dt=3600.0, storage=1e-4), ek,
+                       np.zeros(m.n_nodes))
+    lf, rf = m.face_nodes(0, 0), m.face_nodes(0, 1)
+    eqs.SetKnownX(np.concatenate([lf, rf]), np.concatenate([np.full(len(lf), 10.0), np.zeros(len(rf))]),
+                  gpu.DIRICHLET_SYMMETRIC)
+    rp, col, val = eqs.get_csr()
+    b = eqs.get_rhs()
+    x0 = np.zeros(m.n_nodes)
+    x0[lf] = 10.0
+    # regular entry point, fresh-system stopping rule (no carried |b|)
+    eqs.ConfigNumerics(gpu.LS_CG, gpu.PRECOND_JACOBI, 5000, 1e-12, check_norm_rhs=False)
+    x_ref = x0.copy()
+    it_ref = eqs.Solver(x_ref)
+    # the caller owns the matrix and vectors on the device
+    rp_d = torch.tensor(rp.astype(np.int32), device="cuda")
+    col_d = torch.tensor(col.astype(np.int32), device="cuda")
+    val_d = torch.tensor(val, device="cuda")
+    b_d = torch.tensor(b, device="cuda")
+    for call in range(2):
+        x_d = torch.tensor(x0, device="cuda")
+        st = gpu.csr_cg_noalloc(rp_d, col_d, val_d, b_d, x_d, max_iter=5000, tol=1e-12)
+        torch.cuda.synchronize()
+        assert st["status"] == gpu.OK, (call, st)
+        assert st["rel_residual"] < 1e-12
+        assert abs(st["iterations"] - it_ref) <= 2, (call, st["iterations"], it_ref)
+        assert rel_max_err(x_d.cpu().numpy(), x_ref) < SOLUTION_RTOL, call
+
+
+def test_noalloc_rejects_oversized_and_host_arrays(gpu):
+    import torch
+    L = gpu.lib()
+    small_i = torch.zeros(8, dtype=torch.int32, device="cuda")
+    small_d = torch.zeros(8, dtype=torch.float64, device="cuda")
+    p_i, p_d = small_i.data_ptr(), small_d.data_ptr()
+    st = gpu.SolveStats()
+    rc = L.ogs_gpu_csr_cg_noalloc(gpu.NOALLOC_MAX_ROWS + 1, p_i, p_i, p_d, p_d, p_d, 10, 1e-10, None,
+                                  C.byref(st))
+    assert rc == gpu.BAD_ARG and b"exceed" in L.ogs_gpu_last_error()
+    host = np.zeros(8)
+    rc = L.ogs_gpu_csr_cg_noalloc(7, p_i, p_i, p_d, host.ctypes.data, p_d, 10, 1e-10, None, C.byref(st))
+    assert rc == gpu.BAD_ARG and b"device memory" in L.ogs_gpu_last_error()
