@@ -322,3 +322,26 @@ def test_device_pointers(gpu, oracle):
     x = torch.zeros(m.n_nodes, dtype=torch.float64, device="cuda")
     eqs.Solver(x)
     assert torch.allclose(x, torch.full_like(x, 2.0), rtol=0, atol=1e-9)
+
+
+def test_golden_system_on_gpu(gpu):
+    """The GPU path on the golden deck: matrix within 1e-12 of the fixture,
+    CG heads within 1e-10 of the reference's own Linear_EQS::CG solution."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_linear_eqs.npz"))
+    m = M.structured_hex(*[int(v) for v in g["shape"]])
+    gm = gpu.GpuMesh(m)
+    eqs = gpu.LinearEQS(gm)
+    eqs.Initialize()
+    eqs.GlobalAssembly(gpu.make_params(gpu.GROUNDWATER_FLOW, dt=3600.0, storage=1e-4), g["elem_k"], g["u0"])
+    rp, col, val = eqs.get_csr()
+    assert np.array_equal(rp, g["row_ptr"]) and np.array_equal(col, g["col"])
+    assert_matrix_close(rp, val, g["val"])
+    assert_vector_close(eqs.get_rhs(), g["b"])
+    eqs.SetKnownX(g["bc_rows"], g["bc_vals"], gpu.DIRICHLET_SYMMETRIC)
+    assert_matrix_close(rp, eqs.get_values(), g["val_sym"])
+    eqs.ConfigNumerics(gpu.LS_CG, gpu.PRECOND_JACOBI, 2000, 1e-12)
+    x = g["x0"].copy()
+    it = eqs.Solver(x)
+    assert abs(it - int(g["iter_cg"])) <= 1
+    assert rel_max_err(x, g["x_cg"]) < SOLUTION_RTOL
