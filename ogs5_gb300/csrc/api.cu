@@ -24,6 +24,8 @@ void launch_mp_replace(const MixedArgs& a, cudaStream_t s);
 void launch_mp_iteration(const MixedArgs& a, cudaStream_t s, cudaEvent_t eb, cudaEvent_t ee);
 int kernels_per_iteration(int kind);
 int vec_grid(int n);
+int red_grid(int n);
+int mp_spmv_grid(int n);
 
 // ------------------------------------------------------------------
 // small kernels
@@ -174,7 +176,7 @@ struct ogs_system
     void* f32_block = nullptr;
     size_t f32_bytes = 0;
     float *x32 = nullptr, *r32 = nullptr, *p32 = nullptr, *s32 = nullptr, *d32 = nullptr, *U = nullptr,
-          *val32 = nullptr;
+          *val32 = nullptr, *u32 = nullptr, *w32 = nullptr;
     int fmt = -1;
     cudaGraphExec_t mp_chunk = nullptr, mp_replace = nullptr;
     // SpMV timing inside the chunk graphs (ogs_gpu_profile)
@@ -282,9 +284,14 @@ void drop_graphs(ogs_system* s)
     if (s->mp_replace) { cudaGraphExecDestroy(s->mp_replace); s->mp_replace = nullptr; }
 }
 
+// Event pairs bracket the SpMV of every kProfEvery-th iteration of a chunk
+// (one pair per iteration slowed the chunk by ~10%); the sampled launches
+// give the average SpMV duration.
+constexpr int kProfEvery = 4;
+
 void accumulate_prof(ogs_system* s, int executed)
 {
-    for (int i = 0; i < executed; i++)
+    for (int i = 0; i < executed; i += kProfEvery)
     {
         float ms = 0.f;
         if (cudaEventElapsedTime(&ms, s->prof_b[i], s->prof_e[i]) == cudaSuccess)
@@ -319,8 +326,10 @@ ogs_status get_chunk(ogs_system* s, int kind, const SolveArgs& a, cudaGraphExec_
         cudaGraph_t g;
         OGS_CUDA_TRY(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
         for (int i = 0; i < C; i++)
-            launch_krylov_iteration(a, kind, s->stream, s->prof_on ? s->prof_b[i] : nullptr,
-                                    s->prof_on ? s->prof_e[i] : nullptr);
+        {
+            const bool ev = s->prof_on && i % kProfEvery == 0;  // timing sample
+            launch_krylov_iteration(a, kind, s->stream, ev ? s->prof_b[i] : nullptr, ev ? s->prof_e[i] : nullptr);
+        }
         cudaError_t e = cudaStreamEndCapture(s->stream, &g);
         if (e != cudaSuccess) { set_error("graph capture: %s", cudaGetErrorString(e)); return OGS_CUDA_ERROR; }
         e = cudaGraphInstantiate(&s->chunk[kind], g, 0);
@@ -656,13 +665,14 @@ static ogs_status solve_fp32_refined(ogs_system* s, KState* h)
         const size_t v4 = ((size_t)n * sizeof(float) + 255) & ~size_t(255);
         const size_t op = s->fmt == 0 ? (size_t)m->n_up * n * sizeof(float)
                                       : (size_t)m->sell_nnz * sizeof(float);
-        s->f32_bytes = 5 * v4 + op;
+        s->f32_bytes = 7 * v4 + op;
         OGS_CUDA_TRY(cudaMalloc(&s->f32_block, s->f32_bytes));
         OGS_CUDA_TRY(cudaMemset(s->f32_block, 0, s->f32_bytes));
         char* p = (char*)s->f32_block;
         s->p32 = (float*)p; s->r32 = (float*)(p + v4); s->x32 = (float*)(p + 2 * v4);
         s->s32 = (float*)(p + 3 * v4); s->d32 = (float*)(p + 4 * v4);
-        float* opb = (float*)(p + 5 * v4);
+        s->u32 = (float*)(p + 5 * v4); s->w32 = (float*)(p + 6 * v4);
+        float* opb = (float*)(p + 7 * v4);
         if (s->fmt == 0) s->U = opb; else s->val32 = opb;
     }
     MixedArgs a;
@@ -671,7 +681,8 @@ static ogs_status solve_fp32_refined(ogs_system* s, KState* h)
     a.fmt = s->fmt; a.U = s->U; a.up_off = m->up_off; a.n_up = m->n_up; a.val32 = s->val32;
     for (int d = 0; d < 16 && d < (int)m->host_up_off.size(); d++) a.off[d] = m->host_up_off[d];
     a.d32 = s->d32; a.x = s->x; a.b = s->b; a.r64 = s->r;
-    a.x32 = s->x32; a.r32 = s->r32; a.p32 = s->p32; a.s32 = s->s32; a.st = s->st; a.n = n;
+    a.x32 = s->x32; a.r32 = s->r32; a.p32 = s->p32; a.s32 = s->s32; a.u32 = s->u32; a.w32 = s->w32;
+    a.st = s->st; a.n = n;
     set_l2_window_region(s, s->f32_block, s->f32_bytes);
     launch_mp_convert(a, m->row_len, m->slot_up, s->U, s->val32, s->dinv, s->d32, s->stream);
     OGS_LAUNCH_CHECK();
@@ -679,6 +690,8 @@ static ogs_status solve_fp32_refined(ogs_system* s, KState* h)
     h->scale = 1.0;
     h->ratio = 1.0;
     h->first = 1;
+    h->nb_spmv = mp_spmv_grid(n);
+    h->nb_upd = red_grid(n);
     h->delta = c.inner_tol > 0.0 ? c.inner_tol : 1e-2;
     OGS_CUDA_TRY(cudaMemcpyAsync(s->st, h, kStateHeader, cudaMemcpyHostToDevice, s->stream));
     SolveArgs sa = make_solve_args(s);
@@ -693,14 +706,16 @@ static ogs_status solve_fp32_refined(ogs_system* s, KState* h)
     {
         ogs_status st = capture(s, &s->mp_chunk, [&]() {
             for (int i = 0; i < ogs_system::kChunk; i++)
-                launch_mp_iteration(a, s->stream, s->prof_on ? s->prof_b[i] : nullptr,
-                                    s->prof_on ? s->prof_e[i] : nullptr);
+            {
+                const bool ev = s->prof_on && i % kProfEvery == 0;  // timing sample
+                launch_mp_iteration(a, s->stream, ev ? s->prof_b[i] : nullptr, ev ? s->prof_e[i] : nullptr);
+            }
         });
         if (st) return st;
     }
     OGS_CUDA_TRY(cudaGraphLaunch(s->mp_replace, s->stream));
     count_launches(4);
-    int rounds = 0;
+    int rounds = 0;  // replacement graphs count 4 launches
     int chunk_before = -1;  // iteration count when the pending chunk was launched
     for (;;)
     {
@@ -783,6 +798,8 @@ extern "C" ogs_status ogs_gpu_solve(ogs_system* s, double* x_inout, ogs_solve_st
     }
     else
     {
+        h->nb_spmv = vec_grid(s->n);
+        h->nb_upd = red_grid(s->n);
         OGS_CUDA_TRY(cudaMemcpyAsync(s->st, h, kStateHeader, cudaMemcpyHostToDevice, s->stream));
         launch_krylov_init(a, kind, s->stream);
         OGS_LAUNCH_CHECK();
@@ -796,8 +813,8 @@ extern "C" ogs_status ogs_gpu_solve(ogs_system* s, double* x_inout, ogs_solve_st
         {
             OGS_CUDA_TRY(cudaMemcpyAsync(h, s->st, kStateHeader, cudaMemcpyDeviceToHost, s->stream));
             OGS_CUDA_TRY(cudaStreamSynchronize(s->stream));
-            if (chunk_before >= 0 && s->prof_on)  // the iteration that converged ran its SpMV
-                accumulate_prof(s, std::min(per, h->iter - chunk_before + (h->done ? 1 : 0)));
+            if (chunk_before >= 0 && s->prof_on)
+                accumulate_prof(s, std::min(per, h->iter - chunk_before + (kind == SK_BICGSTAB && h->done ? 1 : 0)));
             chunk_before = -1;
             if (h->done || launched > c.max_iter + per) break;
             chunk_before = h->iter;

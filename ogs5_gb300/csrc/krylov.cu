@@ -142,11 +142,15 @@ __global__ void __launch_bounds__(kThreads) k_init_residual(SolveArgs a, int kin
         if (!isfinite(st->error)) { st->status = OGS_NONFINITE; st->done = 1; return; }
         if (st->error < st->tol) { st->status = OGS_OK; st->done = 1; return; }
         if (st->max_iter < 1) { st->status = OGS_NOT_CONVERGED; st->done = 1; return; }
-        st->iter = 1;
         if (kind == SK_CG)
-            st->rr = v[1];
+        {
+            // CG: the SpMV kernel advances iter; r.z of iteration 0
+            st->rz_base = v[1];
+            st->base_iter = 0;
+        }
         else
         {
+            st->iter = 1;
             st->rho1 = v[0];  // r0 . r with r0 = r
             if (fabs(st->rho1) < DBL_MIN) { st->status = OGS_BREAKDOWN; st->done = 1; }
         }
@@ -154,13 +158,25 @@ __global__ void __launch_bounds__(kThreads) k_init_residual(SolveArgs a, int kin
 }
 
 // ------------------------------------------------------------------
-// CG (Linear_EQS::CG, equation_class.cpp:1129-1187)
+// CG (Linear_EQS::CG, equation_class.cpp:1129-1187), ticket-free:
+//   k_cg_spmv   iter += 1 (block 0) ; s = A p ; partials of p . s
+//   k_cg_update alpha = rz_prev / (p . s) ; x += alpha p ; r -= alpha s ;
+//               partials of r . r and r . M^-1 r (parity buffer iter & 1)
+//   k_cg_p      |r| / |b| test, max_iter ; beta = rz / rz_prev ; p = z + beta p
 // ------------------------------------------------------------------
-// s = A p ; alpha = rr / (p . s)
+// r . z of the previous iteration: the base value right after a (re)start,
+// else the other parity buffer
+__device__ __forceinline__ double cg_rz_prev(const KState* st, int it)
+{
+    return it == st->base_iter + 1 ? st->rz_base : st->rz_hist[(it - 1) & 1];
+}
+
+// s = A p ; partials of p . s
 __global__ void __launch_bounds__(kThreads) k_cg_spmv(SolveArgs a)
 {
     KState* st = a.st;
     if (st->done) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) st->iter += 1;  // no block of this kernel reads iter
     double v[1] = {0.0};
     for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < a.A.n; row += gridDim.x * blockDim.x)
     {
@@ -168,19 +184,21 @@ __global__ void __launch_bounds__(kThreads) k_cg_spmv(SolveArgs a)
         a.v.s[row] = s;
         v[0] += a.v.p[row] * s;
     }
-    if (grid_reduce<1>(v, st->part[2], &st->ticket[2]) && threadIdx.x == 0)
-        st->alpha = st->rr / v[0];
+    write_partials<1, double>(v, st->cg_ps);
 }
 
 constexpr int kU = 4;  // elements per thread per step in the vector kernels
 
-// x += alpha p ; r -= alpha s ; convergence test ; z = M^-1 r ; beta
+// x += alpha p ; r -= alpha s ; partials of r . r and z . r
 template <bool JAC>
 __global__ void __launch_bounds__(kThreads) k_cg_update(SolveArgs a)
 {
     KState* st = a.st;
     if (st->done) return;
-    const double alpha = st->alpha;
+    const int it = st->iter;
+    double ps[1];
+    reduce_partials<1>(st->cg_ps, st->nb_spmv, ps);
+    const double alpha = cg_rz_prev(st, it) / ps[0];
     const int n = a.A.n;
     double v[2] = {0.0, 0.0};
     const int stride = gridDim.x * blockDim.x;
@@ -214,26 +232,32 @@ __global__ void __launch_bounds__(kThreads) k_cg_update(SolveArgs a)
             }
         }
     }
-    if (grid_reduce<2>(v, st->part[3], &st->ticket[3]) && threadIdx.x == 0)
-    {
-        st->error = sqrt(v[0]) / st->bnorm;
-        if (!isfinite(st->error)) { st->status = OGS_NONFINITE; st->done = 1; return; }
-        if (st->error < st->tol) { st->status = OGS_OK; st->done = 1; return; }
-        if (st->iter >= st->max_iter) { st->status = OGS_NOT_CONVERGED; st->done = 1; return; }
-        const double rrM1 = st->rr;
-        st->rr = v[1];
-        st->beta = st->rr / rrM1;
-        st->iter += 1;
-    }
+    write_partials<2, double>(v, st->cg_upd[it & 1]);
 }
 
-// p = z + beta p
+// convergence test ; beta ; p = z + beta p
 template <bool JAC>
 __global__ void __launch_bounds__(kThreads) k_cg_p(SolveArgs a)
 {
     KState* st = a.st;
     if (st->done) return;
-    const double beta = st->beta;
+    const int it = st->iter;
+    double rr_rz[2];
+    reduce_partials<2>(st->cg_upd[it & 1], st->nb_upd, rr_rz);
+    const double rz_prev = cg_rz_prev(st, it);
+    const double error = sqrt(rr_rz[0]) / st->bnorm;
+    int stop = -1;
+    if (!isfinite(error)) stop = OGS_NONFINITE;
+    else if (error < st->tol) stop = OGS_OK;
+    else if (it >= st->max_iter) stop = OGS_NOT_CONVERGED;
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+    {
+        st->error = error;              // read by the host only
+        st->rz_hist[it & 1] = rr_rz[1];  // read from iteration it + 1 on
+        if (stop >= 0) { st->status = stop; st->done = 1; }
+    }
+    if (stop >= 0) return;
+    const double beta = rr_rz[1] / rz_prev;
     const int n = a.A.n;
     const int stride = gridDim.x * blockDim.x;
     for (int base = blockIdx.x * blockDim.x + threadIdx.x; base < n; base += kU * stride)
@@ -395,7 +419,7 @@ int vec_grid(int n)
 // Grid of the reducing vector kernels: two blocks per SM, so each thread
 // handles a dozen or more elements and the FP64 adds of the block
 // reduction stay a small fraction of the FP64 work.
-static int red_grid(int n)
+int red_grid(int n)
 {
     const int need = (n + kThreads - 1) / kThreads;
     return std::max(1, std::min(need, std::min(sm_count() * 2, kMaxBlocks)));
@@ -438,12 +462,12 @@ void launch_krylov_iteration(const SolveArgs& a, int kind, cudaStream_t s, cudaE
         if (jac)
         {
             k_cg_update<true><<<rg, kThreads, 0, s>>>(a);
-            k_cg_p<true><<<vg, kThreads, 0, s>>>(a);
+            k_cg_p<true><<<rg, kThreads, 0, s>>>(a);
         }
         else
         {
             k_cg_update<false><<<rg, kThreads, 0, s>>>(a);
-            k_cg_p<false><<<vg, kThreads, 0, s>>>(a);
+            k_cg_p<false><<<rg, kThreads, 0, s>>>(a);
         }
     }
     else

@@ -26,8 +26,19 @@ struct KState
     int replacements;
     int first;                   // first restart of a solve (p = z)
     int pad2;
+    // ticket-free CG: r.z of the iteration after `base_iter` comes from
+    // rz_base (initial residual or the last replacement), later ones from
+    // the parity-buffered partials of the update kernel
+    double rz_base;
+    double rz_hist[2];           // r.z of iteration k at [k & 1], written by block 0 of the p kernel
+    double gam_hist[2], eta_hist[2];  // FP32 CG (Chronopoulos-Gear): gamma, eta of iteration k at [k & 1]
+    int base_iter;
+    int nb_spmv, nb_upd;         // producer grid sizes (partials to add)
+    int pad3;
     unsigned int ticket[8];
     double part[8][2 * kMaxBlocks];
+    double cg_ps[3 * kMaxBlocks];        // per SpMV block: p . s (FP64 CG); r.u, w.u, r.r (FP32 CG)
+    double cg_upd[2][2 * kMaxBlocks];    // r . r and r . z per update block, by parity
 };
 
 enum SolveKind
@@ -146,6 +157,66 @@ __device__ __forceinline__ bool grid_sum(const T* vin, double* out, double* part
     return true;
 }
 
+// ------------------------------------------------------------------
+// Ticket-free grid sums for the CG kernels.  A producer kernel only writes
+// one partial per block and value (write_partials); every block of the
+// consumer kernel adds the partials itself, in the same fixed order
+// (reduce_partials), so all blocks hold bitwise the same total without a
+// last-block step or atomics.  Partial buffers are double-buffered by
+// iteration parity where a kernel reads last iteration's sums.
+// ------------------------------------------------------------------
+template <int NV, typename T>
+__device__ __forceinline__ void write_partials(const T* vin, double* part)
+{
+    __shared__ double sm[NV][kThreads / 32];
+    T w[NV];
+#pragma unroll
+    for (int k = 0; k < NV; k++) w[k] = vin[k];
+    warp_allsum<NV, T>(w);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < NV; k++) sm[k][wid] = (double)w[k];
+    __syncthreads();
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int k = 0; k < NV; k++)
+        {
+            double s = 0.0;
+            for (int q = 0; q < (int)(blockDim.x >> 5); q++) s += sm[k][q];
+            part[k * kMaxBlocks + blockIdx.x] = s;
+        }
+}
+
+// out[k] = sum of part[k * kMaxBlocks + 0 .. nb-1], identical in every thread
+template <int NV>
+__device__ __forceinline__ void reduce_partials(const double* part, int nb, double* out)
+{
+    __shared__ double sm[NV][kThreads / 32];
+    double v[NV];
+#pragma unroll
+    for (int k = 0; k < NV; k++)
+    {
+        double s = 0.0;
+        for (int q = threadIdx.x; q < nb; q += blockDim.x) s += __ldcg(part + k * kMaxBlocks + q);
+        v[k] = s;
+    }
+    warp_allsum<NV, double>(v);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < NV; k++) sm[k][wid] = v[k];
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < NV; k++)
+    {
+        double s = 0.0;
+        for (int q = 0; q < (int)(blockDim.x >> 5); q++) s += sm[k][q];
+        out[k] = s;
+    }
+    __syncthreads();
+}
+
 // Arguments of the FP32-inner / FP64-refinement kernels (mixed.cu).
 struct MixedArgs
 {
@@ -160,7 +231,7 @@ struct MixedArgs
     double* x;                // FP64 solution
     const double* b;
     double* r64;
-    float *x32, *r32, *p32, *s32;
+    float *x32, *r32, *p32, *s32, *u32, *w32;
     KState* st;
     int n;
 };

@@ -5,12 +5,17 @@
 // uses FP32 FMAs (GB300: ~60x the FP64 rate).  The solution x, the true
 // residual r = b - A x and the convergence test |r|/|b| < tol stay FP64:
 //
-//   r64 = b - A64 x64 ; r32 = r64 / |r64| ; p32 = M^-1 r32
-//   repeat  (FP32 CG on A32 d = r32, Jacobi preconditioned)
-//     s32 = A32 p32 ; alpha ; x32 += alpha p32 ; r32 -= alpha s32 ; beta
+//   r64 = b - A64 x64 ; r32 = r64 / |r64| ; u = M^-1 r32
+//   repeat  (FP32 CG on A32 d = r32, Jacobi preconditioned, in the
+//            Chronopoulos-Gear form: one SpMV and one grid reduction per
+//            iteration)
+//     S: w = A32 u ; gamma = r.u, delta = w.u, rho = r.r
+//     V: beta = gamma / gamma_prev ; eta = delta - beta^2 eta_prev ;
+//        alpha = gamma / eta ; p = u + beta p ; s = w + beta s ;
+//        x32 += alpha p ; r32 -= alpha s ; u = M^-1 r32
 //     when |r32| fell by `delta` since the last replacement, or the FP32
 //     recurrence claims convergence:  x64 += |r64| x32 ; x32 = 0 ;
-//     r64 = b - A64 x64 (FP64) ; replace r32 by r64 / |r64| and rescale p32
+//     r64 = b - A64 x64 (FP64) ; replace r32 by r64 / |r64|, rescale p, s
 //   until |r64| / |b| < tol
 //
 // The FP64 residual replacement (a reliable-update form of iterative
@@ -94,6 +99,7 @@ __device__ __forceinline__ float op_row(const MixedArgs& a, const float* __restr
         return sell32_row(a, x, i);
 }
 
+
 // U[d][i] = (float) A[i][i + off_d]; d32 = (float) (1 / a_ii)
 __global__ void k_mp_convert(MixedArgs a, const int32_t* __restrict__ row_len,
                              const int8_t* __restrict__ slot_up, float* U, float* val32,
@@ -171,7 +177,8 @@ __global__ void __launch_bounds__(kThreads) k_mp_residual(MixedArgs a)
     }
 }
 
-// r32 = scale r64 ; z = M^-1 r32 ; p32 rescaled (or zeroed first) ; rz ; beta
+// r32 = scale r64 ; u = M^-1 r32 ; p32, s32 rescaled (zero at the first
+// restart) ; the last iteration's gamma and eta rescaled to the new units
 __global__ void __launch_bounds__(kThreads) k_mp_restart(MixedArgs a)
 {
     KState* st = a.st;
@@ -179,128 +186,121 @@ __global__ void __launch_bounds__(kThreads) k_mp_restart(MixedArgs a)
     const double sc = st->scale;
     const float ratio = (float)st->ratio;
     const bool first = st->first != 0;
-    float v[2] = {0.f, 0.f};
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x)
     {
         const float r = (float)(a.r64[i] * sc);
         a.r32[i] = r;
+        a.u32[i] = r * a.d32[i];
         a.p32[i] = first ? 0.f : a.p32[i] * ratio;
-        const float z = r * a.d32[i];
-        v[0] += r * r;
-        v[1] += z * r;
+        a.s32[i] = first ? 0.f : a.s32[i] * ratio;
     }
-    double out[2];
-    if (grid_sum<2, float>(v, out, st->part[1], &st->ticket[1]) && threadIdx.x == 0)
+    if (blockIdx.x == 0 && threadIdx.x == 0)
     {
-        const double rz_old = st->rr * st->ratio * st->ratio;
-        st->beta = first ? 0.0 : out[1] / rz_old;
-        st->rr = out[1];
-        st->rmax = sqrt(out[0]);
-        st->first = 0;
+        // The iteration that asked for the replacement stopped before forming
+        // its search direction: it is redone with the replaced residual, so
+        // the counter steps back and the scalars of the iteration before it
+        // are carried into the new units.
+        int it = st->iter;
+        if (!first) it -= 1;
+        st->iter = it;
+        const double r2 = st->ratio * st->ratio;
+        st->gam_hist[it & 1] *= r2;
+        st->eta_hist[it & 1] *= r2;
+        st->base_iter = it;
+        st->rmax = -1.0;  // set from the first rho after the restart
         st->replace = 0;
     }
 }
 
 // ------------------------------------------------------------------
-// FP32 CG iteration
+// FP32 CG iteration (Chronopoulos-Gear, ticket-free, see krylov.cuh)
 // ------------------------------------------------------------------
-// s32 = A32 p32 ; alpha = rz / (p . s)
+// S: iter += 1 ; w32 = A32 u32 ; partials of r.u, w.u, r.r
 template <int NU>
 __global__ void __launch_bounds__(kThreads, 3) k_mp_spmv(MixedArgs a)
 {
     KState* st = a.st;
     if (st->done || st->replace) return;
-    float v[1] = {0.f};
+    if (blockIdx.x == 0 && threadIdx.x == 0) st->iter += 1;  // no block of this kernel reads iter
+    float v[3] = {0.f, 0.f, 0.f};
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x)
     {
-        const float s = op_row<NU>(a, a.p32, i);
-        a.s32[i] = s;
-        v[0] += a.p32[i] * s;
+        const float w = op_row<NU>(a, a.u32, i);
+        a.w32[i] = w;
+        const float u = a.u32[i], r = a.r32[i];
+        v[0] += r * u;
+        v[1] += w * u;
+        v[2] += r * r;
     }
-    double out[1];
-    if (grid_sum<1, float>(v, out, st->part[2], &st->ticket[2]) && threadIdx.x == 0)
-        st->alpha = st->rr / out[0];
+    write_partials<3, float>(v, st->cg_ps);
 }
 
 constexpr int kU32 = 4;  // elements per thread per step, loaded before use
 
-// x32 += alpha p ; r32 -= alpha s ; rr, rz ; replacement / beta
+// V: scalars from the S partials ; replacement test ; p, s, x32, r32, u32
 __global__ void __launch_bounds__(kThreads) k_mp_update(MixedArgs a)
 {
     KState* st = a.st;
     if (st->done || st->replace) return;
-    const float alpha = (float)st->alpha;
+    const int it = st->iter;
+    double g[3];
+    reduce_partials<3>(st->cg_ps, st->nb_spmv, g);
+    const double gamma = g[0], delta = g[1], rn = sqrt(g[2]);
+    const bool first = it == 1;                  // no search direction yet: beta = 0
+    const bool fresh = it == st->base_iter + 1;  // first iteration after a (re)start
+    const double rmax = fresh ? rn : st->rmax;
+    const double beta = first ? 0.0 : gamma / st->gam_hist[(it - 1) & 1];
+    const double eta = first ? delta : delta - beta * beta * st->eta_hist[(it - 1) & 1];
+    const double alpha = gamma / eta;
+    const double est = rn / st->scale / st->bnorm;  // estimate of |r64| / |b|
+    const bool nonfinite = !isfinite(rn) || !isfinite(alpha);
+    // right after a replacement r32 is the true residual (checked in FP64 by
+    // k_mp_residual), so a fresh iteration never asks for another one
+    const bool repl = !nonfinite && !fresh &&
+                      (est < st->tol || rn < st->delta * rmax || it > st->max_iter);
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+    {
+        if (fresh) st->rmax = rn;
+        st->gam_hist[it & 1] = gamma;
+        st->eta_hist[it & 1] = eta;
+        st->first = 0;  // read by the replacement kernels only
+        if (nonfinite) { st->status = OGS_NONFINITE; st->done = 1; }
+        else if (repl) st->replace = 1;
+    }
+    if (nonfinite || repl) return;
+    const float fb = (float)beta, fa = (float)alpha;
     const int n = a.n, stride = gridDim.x * blockDim.x;
-    float v[2] = {0.f, 0.f};
     for (int base = blockIdx.x * blockDim.x + threadIdx.x; base < n; base += kU32 * stride)
     {
-        float xv[kU32], pv[kU32], rv[kU32], sv[kU32], dv[kU32];
+        float uv[kU32], wv[kU32], pv[kU32], sv[kU32], xv[kU32], rv[kU32], dv[kU32];
 #pragma unroll
-        for (int u = 0; u < kU32; u++)
+        for (int k = 0; k < kU32; k++)
         {
-            const int i = base + u * stride;
+            const int i = base + k * stride;
             const bool in = i < n;
-            xv[u] = in ? a.x32[i] : 0.f;
-            pv[u] = in ? a.p32[i] : 0.f;
-            rv[u] = in ? a.r32[i] : 0.f;
-            sv[u] = in ? a.s32[i] : 0.f;
-            dv[u] = in ? a.d32[i] : 0.f;
+            uv[k] = in ? a.u32[i] : 0.f;
+            wv[k] = in ? a.w32[i] : 0.f;
+            pv[k] = in ? a.p32[i] : 0.f;
+            sv[k] = in ? a.s32[i] : 0.f;
+            xv[k] = in ? a.x32[i] : 0.f;
+            rv[k] = in ? a.r32[i] : 0.f;
+            dv[k] = in ? a.d32[i] : 0.f;
         }
 #pragma unroll
-        for (int u = 0; u < kU32; u++)
+        for (int k = 0; k < kU32; k++)
         {
-            const int i = base + u * stride;
+            const int i = base + k * stride;
             if (i < n)
             {
-                a.x32[i] = xv[u] + alpha * pv[u];
-                const float r = rv[u] - alpha * sv[u];
+                const float p = uv[k] + fb * pv[k];
+                const float s = wv[k] + fb * sv[k];
+                const float r = rv[k] - fa * s;
+                a.p32[i] = p;
+                a.s32[i] = s;
+                a.x32[i] = xv[k] + fa * p;
                 a.r32[i] = r;
-                v[0] += r * r;
-                v[1] += (r * dv[u]) * r;
+                a.u32[i] = r * dv[k];
             }
-        }
-    }
-    double out[2];
-    if (grid_sum<2, float>(v, out, st->part[3], &st->ticket[3]) && threadIdx.x == 0)
-    {
-        st->iter += 1;
-        const double rn = sqrt(out[0]);
-        if (!isfinite(rn)) { st->status = OGS_NONFINITE; st->done = 1; return; }
-        const double est = rn / st->scale / st->bnorm;  // estimate of |r64| / |b|
-        if (est < st->tol || rn < st->delta * st->rmax || st->iter >= st->max_iter)
-        {
-            st->replace = 1;
-            return;
-        }
-        st->beta = out[1] / st->rr;
-        st->rr = out[1];
-    }
-}
-
-// p32 = z + beta p32
-__global__ void __launch_bounds__(kThreads) k_mp_p(MixedArgs a)
-{
-    KState* st = a.st;
-    if (st->done || st->replace) return;
-    const float beta = (float)st->beta;
-    const int n = a.n, stride = gridDim.x * blockDim.x;
-    for (int base = blockIdx.x * blockDim.x + threadIdx.x; base < n; base += kU32 * stride)
-    {
-        float rv[kU32], dv[kU32], pv[kU32];
-#pragma unroll
-        for (int u = 0; u < kU32; u++)
-        {
-            const int i = base + u * stride;
-            const bool in = i < n;
-            rv[u] = in ? a.r32[i] : 0.f;
-            dv[u] = in ? a.d32[i] : 0.f;
-            pv[u] = in ? a.p32[i] : 0.f;
-        }
-#pragma unroll
-        for (int u = 0; u < kU32; u++)
-        {
-            const int i = base + u * stride;
-            if (i < n) a.p32[i] = rv[u] * dv[u] + beta * pv[u];
         }
     }
 }
@@ -316,30 +316,41 @@ void launch_mp_convert(const MixedArgs& a, const int32_t* row_len, const int8_t*
     k_mp_convert<<<vec_grid(a.n), kThreads, 0, s>>>(a, row_len, slot_up, U, val32, dinv64, d32);
 }
 
-// FP64 residual replacement: accumulate, residual, restart, first p update
+int red_grid(int n);
+
+// grids of the FP32 CG kernels (the update/p kernels add this many SpMV
+// partials, the p kernel this many update partials)
+int mp_spmv_grid(int n)
+{
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    // three blocks of the register-heavy diagonal kernel are resident per SM
+    return std::max(1, std::min((n + kThreads - 1) / kThreads, std::min(sms * 3, kMaxBlocks)));
+}
+
+// FP64 residual replacement: accumulate, residual, restart
 void launch_mp_replace(const MixedArgs& a, cudaStream_t s)
 {
     const int g = vec_grid(a.n);
     k_mp_accumulate<<<g, kThreads, 0, s>>>(a);
     k_mp_residual<<<g, kThreads, 0, s>>>(a);
     k_mp_restart<<<g, kThreads, 0, s>>>(a);
-    k_mp_p<<<g, kThreads, 0, s>>>(a);
 }
 
 void launch_mp_iteration(const MixedArgs& a, cudaStream_t s, cudaEvent_t eb, cudaEvent_t ee)
 {
-    const int g = vec_grid(a.n);
+    const int gs = mp_spmv_grid(a.n), gr = red_grid(a.n);
     if (eb) cudaEventRecordWithFlags(eb, s, cudaEventRecordExternal);
     switch (a.fmt == 0 ? a.n_up : 0)
     {
-        case 14: k_mp_spmv<14><<<g, kThreads, 0, s>>>(a); break;  // hex, 27-point
-        case 8: k_mp_spmv<8><<<g, kThreads, 0, s>>>(a); break;    // Kuhn tets, 15-point
-        case 5: k_mp_spmv<5><<<g, kThreads, 0, s>>>(a); break;    // quads, 9-point
-        default: k_mp_spmv<0><<<g, kThreads, 0, s>>>(a); break;   // SELL-32 FP32
+        case 14: k_mp_spmv<14><<<gs, kThreads, 0, s>>>(a); break;  // hex, 27-point
+        case 8: k_mp_spmv<8><<<gs, kThreads, 0, s>>>(a); break;    // Kuhn tets, 15-point
+        case 5: k_mp_spmv<5><<<gs, kThreads, 0, s>>>(a); break;    // quads, 9-point
+        default: k_mp_spmv<0><<<gs, kThreads, 0, s>>>(a); break;   // SELL-32 FP32
     }
     if (ee) cudaEventRecordWithFlags(ee, s, cudaEventRecordExternal);
-    k_mp_update<<<g, kThreads, 0, s>>>(a);
-    k_mp_p<<<g, kThreads, 0, s>>>(a);
+    k_mp_update<<<gr, kThreads, 0, s>>>(a);
 }
 
 }  // namespace ogs

@@ -91,4 +91,5 @@ def test_profile_counts_spmv_launches(gpu, mixed):
     it = eqs.Solver(x)
     pr = eqs.profile(False)
     assert pr["solves"] == 1 and pr["spmv_ms"] > 0
-    assert abs(pr["spmv_launches"] - it) <= 1
+    # the SpMV of every fourth iteration of a chunk is timed
+    assert abs(pr["spmv_launches"] - it / 4) <= it / 16 + 3
