@@ -47,9 +47,10 @@ TOL = 1e-10
 SEED = 2
 WORKLOAD = ("transient GROUNDWATER_FLOW hex 128x128x64, lnK GRF var 1 ell 8, 20 steps dt 3600, "
             "CG+Jacobi 1e-10")
-# Jacobi-CG iterations per step of this deck (FP64 path, measured on the GPU;
-# equal to the oracle's Linear_EQS::CG count within the parity tests' bound)
-CG_ITERS_PER_STEP = 147
+# Jacobi-CG iterations per step of this deck (FP64 path over the 20 steps:
+# 6295 iterations, measured on the GPU; the parity tests hold the GPU count
+# within two iterations of the oracle's Linear_EQS::CG)
+CG_ITERS_PER_STEP = 315
 
 
 def make_deck(nx=NX, ny=NY, nz=NZ):
@@ -111,6 +112,17 @@ class ClockSampler:
         load = [s for s in sm if s > 0.5 * mx] or sm
         return {"sm_mhz": statistics.median(load), "sm_max_mhz": mx, "reasons": sorted(reasons),
                 "samples": len(rows)}
+
+
+def measured_traffic(name: str):
+    """DRAM bytes per launch from the committed ncu summary profiles/<name>."""
+    try:
+        for line in open(os.path.join(ROOT, "profiles", name)):
+            if line.startswith("dram_bytes_per_launch:"):
+                return int(line.split(":")[1])
+    except OSError:
+        pass
+    return None
 
 
 def peaks():
@@ -226,6 +238,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--path", default="both", choices=["both", "fp64", "mixed"],
+                    help="fp64 / mixed: time one solver path only (profiling driver)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -251,6 +265,15 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("gloo")
         dist.barrier()
+
+    if args.path != "both":
+        # one path only: warm-up steps, then the timed steps (ncu driver)
+        r = time_path(eqs, capi, p, deck, k_steps, warm, torch, stream, mixed=args.path == "mixed")
+        pr = r["prof"]
+        print(json.dumps({"path": args.path, "solves_per_s": round(k_steps / (r["ms"] * 1e-3), 4),
+                          "ms_per_step": round(r["ms"] / k_steps, 3), "iterations": r["iters"],
+                          "spmv_ms": round(pr["spmv_ms"] / max(1, pr["spmv_launches"]), 5)}))
+        return
 
     # plain FP64 path (the parity path), then the FP32-inner / FP64 path
     f64 = time_path(eqs, capi, p, deck, k_steps, warm, torch, stream, mixed=False, keep=True)
@@ -310,8 +333,9 @@ def main():
                                 <= 1e-8 * np.abs(mix["heads"]).max()),
         "gpu_launches": int(mix["launches"]),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
-                     "frac": round(achieved / hbm, 4), "traffic": None,
-                     "kernel": "k_mp_spmv (FP32 upper-diagonal-offset SpMV + fused p.s)",
+                     "frac": round(achieved / hbm, 4),
+                     "traffic": measured_traffic("k_mp_spmv_fp32_diagonal_hex128x128x64.md"),
+                     "kernel": "k_mp_spmv (FP32 upper-diagonal-offset SpMV + fused dots)",
                      "bytes_per_launch": spmv_bytes, "launch_ms": round(t_spmv, 5),
                      "launches": pr["spmv_launches"], "peak_kind": peak_kind},
         "clocks": clk.summary(),
