@@ -247,6 +247,14 @@ ogs_status ogs_gpu_get_csr(const ogs_system* sys, int64_t* row_ptr,
 ogs_status ogs_gpu_get_rhs(const ogs_system* sys, double* b);
 ogs_status ogs_gpu_get_x(const ogs_system* sys, double* x);
 
+/* ILU(0) factors of the last solve with ls_precond 100, on the CSR pattern
+ * of ogs_gpu_get_csr (nnz doubles): unit lower L below the diagonal, U on
+ * and above it.  The SP build substitutes Jacobi for precond 100
+ * (FEM/equation_class.cpp:294-308); the legacy build factors an incomplete
+ * LDU (M34Vorkond, FEM/matrix_routines.cpp:3271-3427).  Read-back for
+ * checks. */
+ogs_status ogs_gpu_get_ilu0(const ogs_system* sys, double* lu);
+
 /* y = A x with the current matrix (CSparseMatrix::multiVec,
  * FEM/matrix_class.cpp:1467-1555). */
 ogs_status ogs_gpu_spmv(ogs_system* sys, const double* x, double* y);

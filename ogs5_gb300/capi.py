@@ -43,7 +43,7 @@ EXPORTS = [
     "ogs_gpu_initialize", "ogs_gpu_assemble", "ogs_gpu_set_dirichlet", "ogs_gpu_solve",
     "ogs_gpu_gp_velocity", "ogs_gpu_get_csr", "ogs_gpu_get_rhs", "ogs_gpu_get_x",
     "ogs_gpu_spmv", "ogs_gpu_mesh_gauss_points", "ogs_gpu_kernel_launches", "ogs_gpu_profile",
-    "ogs_gpu_csr_cg_noalloc",
+    "ogs_gpu_csr_cg_noalloc", "ogs_gpu_get_ilu0",
 ]
 NOALLOC_MAX_ROWS = 524288
 
@@ -143,6 +143,7 @@ def lib():
         L.ogs_gpu_get_csr.argtypes = [vp, vp, vp, vp]
         L.ogs_gpu_get_rhs.argtypes = [vp, vp]
         L.ogs_gpu_get_x.argtypes = [vp, vp]
+        L.ogs_gpu_get_ilu0.argtypes = [vp, vp]
         L.ogs_gpu_spmv.argtypes = [vp, vp, vp]
         L.ogs_gpu_mesh_gauss_points.argtypes = [vp]
         L.ogs_gpu_mesh_gauss_points.restype = C.c_int32
@@ -157,7 +158,7 @@ def lib():
                      "ogs_gpu_system_create", "ogs_gpu_system_destroy", "ogs_gpu_configure",
                      "ogs_gpu_initialize", "ogs_gpu_assemble", "ogs_gpu_set_dirichlet",
                      "ogs_gpu_solve", "ogs_gpu_gp_velocity", "ogs_gpu_get_csr", "ogs_gpu_get_rhs",
-                     "ogs_gpu_get_x", "ogs_gpu_spmv"):
+                     "ogs_gpu_get_x", "ogs_gpu_spmv", "ogs_gpu_get_ilu0"):
             getattr(L, name).restype = st
         _LIB = L
     return _LIB
@@ -314,6 +315,12 @@ class LinearEQS:
         if out is None:
             out = np.zeros(self.gmesh.nnz)
         _check(lib().ogs_gpu_get_csr(self.h, None, None, _ptr(out)))
+        return out
+
+    def get_ilu0(self):
+        """ILU(0) factors of the last ls_precond 100 solve on the CSR pattern."""
+        out = np.zeros(self.gmesh.nnz)
+        _check(lib().ogs_gpu_get_ilu0(self.h, _ptr(out)))
         return out
 
     def get_rhs(self, out=None):

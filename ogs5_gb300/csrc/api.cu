@@ -22,7 +22,11 @@ void launch_mp_convert(const MixedArgs& a, const int32_t* row_len, const int8_t*
                        float* val32, const double* dinv64, float* d32, cudaStream_t s);
 void launch_mp_replace(const MixedArgs& a, cudaStream_t s);
 void launch_mp_iteration(const MixedArgs& a, cudaStream_t s, cudaEvent_t eb, cudaEvent_t ee);
-int kernels_per_iteration(int kind);
+int kernels_per_iteration(int kind, int precond);
+int krylov_init_launches(int kind, int precond);
+bool ilu_cluster_ok();
+void launch_ilu_factor(const IluView& f, const double* val, const int32_t* csr2sell, int64_t nnz,
+                       const KState* st, cudaStream_t s);
 int vec_grid(int n);
 int red_grid(int n);
 int mp_spmv_grid(int n);
@@ -149,6 +153,8 @@ struct ogs_system
     double *val = nullptr, *b = nullptr, *x = nullptr;
     double *r = nullptr, *r0 = nullptr, *p = nullptr, *ph = nullptr, *s = nullptr, *sh = nullptr,
            *t = nullptr, *v = nullptr, *dinv = nullptr;
+    double* lu = nullptr;     // ILU(0) factors on the CSR pattern (allocated on first use)
+    int* d_ilu_bad = nullptr;
     double *ek = nullptr, *u0 = nullptr, *gpv = nullptr, *qbuf = nullptr, *vec_in = nullptr,
            *vec_out = nullptr;
     KState* st = nullptr;
@@ -272,7 +278,19 @@ SolveArgs make_solve_args(ogs_system* s)
     a.v.x = s->x; a.v.b = s->b; a.v.r = s->r; a.v.r0 = s->r0; a.v.p = s->p; a.v.ph = s->ph;
     a.v.s = s->s; a.v.sh = s->sh; a.v.t = s->t; a.v.v = s->v; a.v.dinv = s->dinv;
     a.st = s->st;
-    a.precond = s->cfg.precond == OGS_PRECOND_JACOBI ? OGS_PRECOND_JACOBI : 0;
+    a.precond = s->cfg.precond;
+    ogs_mesh* m = s->m;
+    a.ilu.row_ptr = m->row_ptr;
+    a.ilu.col = m->col;
+    a.ilu.diag = m->csr_diag;
+    a.ilu.lu = s->lu;
+    a.ilu.lrows = m->lvl_rows;
+    a.ilu.lptr = m->lvl_ptr;
+    a.ilu.urows = m->ulvl_rows;
+    a.ilu.uptr = m->ulvl_ptr;
+    a.ilu.n_lev = m->n_lvl;
+    a.ilu.n_ulev = m->n_ulvl;
+    a.ilu.bad = s->d_ilu_bad;
     return a;
 }
 
@@ -359,6 +377,8 @@ extern "C" ogs_status ogs_gpu_system_destroy(ogs_system* s)
     for (double* p : bufs) cudaFree(p);
     cudaFree(s->vec_block);
     cudaFree(s->f32_block);
+    cudaFree(s->lu);
+    cudaFree(s->d_ilu_bad);
     cudaFree(s->st);
     cudaFree(s->d_bad);
     cudaFree(s->bc_rows);
@@ -744,19 +764,57 @@ static ogs_status solve_fp32_refined(ogs_system* s, KState* h)
     return OGS_OK;
 }
 
+// ILU(0) of the current matrix (every solve: assembly and Dirichlet
+// conditions change the values); a zero pivot ends the solve with
+// OGS_BREAKDOWN before any iteration.
+static ogs_status ilu_factor(ogs_system* s)
+{
+    ogs_mesh* m = s->m;
+    if (!ilu_cluster_ok())
+    {
+        set_error("solve: ILU(0) needs an 8-CTA thread-block cluster of 1024 threads, not available on this device");
+        return OGS_CUDA_ERROR;
+    }
+    if (!s->lu)
+    {
+        OGS_CUDA_TRY(cudaMalloc(&s->lu, std::max<int64_t>(1, m->nnz) * sizeof(double)));
+        OGS_CUDA_TRY(cudaMalloc(&s->d_ilu_bad, sizeof(int)));
+        drop_graphs(s);  // captured sweeps hold the factor pointer
+    }
+    const int big = 0x7fffffff;
+    OGS_CUDA_TRY(cudaMemcpyAsync(s->d_ilu_bad, &big, sizeof(int), cudaMemcpyHostToDevice, s->stream));
+    SolveArgs a = make_solve_args(s);
+    launch_ilu_factor(a.ilu, s->val, m->csr2sell, m->nnz, s->st, s->stream);
+    OGS_LAUNCH_CHECK();
+    count_launches(1);
+    OGS_CUDA_TRY(cudaMemcpyAsync(s->h_bad, s->d_ilu_bad, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    OGS_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    if (*s->h_bad != big)
+    {
+        set_error("solve: ILU(0) zero pivot in row %d", *s->h_bad);
+        return OGS_BREAKDOWN;
+    }
+    return OGS_OK;
+}
+
 extern "C" ogs_status ogs_gpu_solve(ogs_system* s, double* x_inout, ogs_solve_stats* stats)
 {
     if (!s || !x_inout) { set_error("solve: NULL argument"); return OGS_BAD_ARG; }
     const ogs_solver_config& c = s->cfg;
-    if (c.precond == OGS_PRECOND_ILU0)
-    {
-        set_error("solve: ILU(0) not available in this build");
-        return OGS_BAD_ARG;
-    }
     if (c.precision == OGS_PRECISION_FP32_REFINED && c.method != OGS_LS_CG)
     {
         set_error("solve: the FP32-inner / FP64-refinement mode runs CG (ls_method 5)");
         return OGS_BAD_ARG;
+    }
+    if (c.precision == OGS_PRECISION_FP32_REFINED && c.precond == OGS_PRECOND_ILU0)
+    {
+        set_error("solve: the FP32-inner / FP64-refinement mode takes Jacobi or no preconditioner");
+        return OGS_BAD_ARG;
+    }
+    if (c.precond == OGS_PRECOND_ILU0)
+    {
+        ogs_status st = ilu_factor(s);
+        if (st) return st;
     }
     const int kind = c.method == OGS_LS_CG ? SK_CG : SK_BICGSTAB;
     const size_t nb = (size_t)s->n * sizeof(double);
@@ -803,6 +861,7 @@ extern "C" ogs_status ogs_gpu_solve(ogs_system* s, double* x_inout, ogs_solve_st
         OGS_CUDA_TRY(cudaMemcpyAsync(s->st, h, kStateHeader, cudaMemcpyHostToDevice, s->stream));
         launch_krylov_init(a, kind, s->stream);
         OGS_LAUNCH_CHECK();
+        count_launches(krylov_init_launches(kind, a.precond) - 1);
         cudaGraphExec_t ge;
         int per = 0;
         ogs_status st = get_chunk(s, kind, a, &ge, &per);
@@ -819,7 +878,7 @@ extern "C" ogs_status ogs_gpu_solve(ogs_system* s, double* x_inout, ogs_solve_st
             if (h->done || launched > c.max_iter + per) break;
             chunk_before = h->iter;
             OGS_CUDA_TRY(cudaGraphLaunch(ge, s->stream));
-            count_launches((int64_t)per * kernels_per_iteration(kind));
+            count_launches((int64_t)per * kernels_per_iteration(kind, a.precond));
             launched += per;
         }
         if (!h->done)
@@ -929,6 +988,16 @@ extern "C" ogs_status ogs_gpu_get_x(const ogs_system* s, double* x)
     OGS_CUDA_TRY(cudaStreamSynchronize(s->stream));
     OGS_CUDA_TRY(cudaMemcpy(x, s->x, (size_t)s->n * sizeof(double),
                             is_device_ptr(x) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost));
+    return OGS_OK;
+}
+
+extern "C" ogs_status ogs_gpu_get_ilu0(const ogs_system* s, double* lu)
+{
+    if (!s || !lu) { set_error("get_ilu0: NULL argument"); return OGS_BAD_ARG; }
+    if (!s->lu) { set_error("get_ilu0: no ILU(0) factorisation yet (solve with ls_precond 100 first)"); return OGS_BAD_ARG; }
+    OGS_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    OGS_CUDA_TRY(cudaMemcpy(lu, s->lu, (size_t)s->m->nnz * sizeof(double),
+                            is_device_ptr(lu) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost));
     return OGS_OK;
 }
 

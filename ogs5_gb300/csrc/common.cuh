@@ -141,6 +141,14 @@ struct ogs_mesh
     int32_t* row_len = nullptr;    // [n_nodes] stored entries per row
     int32_t* diag_pos = nullptr;   // [n_nodes] SELL slot of the diagonal
     int32_t* slot_t = nullptr;     // [nn*nn][n_elem] SELL slot of (i, j)
+    // ILU(0): CSR diagonal positions and the dependency levels of the
+    // forward (lower) and backward (upper) sweeps in natural row order
+    int32_t* csr_diag = nullptr;   // [n_nodes]
+    int32_t* lvl_rows = nullptr;   // [n_nodes] rows by forward level
+    int32_t* lvl_ptr = nullptr;    // [n_lvl + 1]
+    int32_t* ulvl_rows = nullptr;  // [n_nodes] rows by backward level
+    int32_t* ulvl_ptr = nullptr;   // [n_ulvl + 1]
+    int n_lvl = 0, n_ulvl = 0;
     // diagonal-offset form of the pattern (structured grids): the distinct
     // column offsets (col - row), sorted, and per SELL slot the index of
     // its offset (-1 for padding); n_off == 0 when there are too many

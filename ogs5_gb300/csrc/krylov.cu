@@ -189,8 +189,9 @@ __global__ void __launch_bounds__(kThreads) k_cg_spmv(SolveArgs a)
 
 constexpr int kU = 4;  // elements per thread per step in the vector kernels
 
-// x += alpha p ; r -= alpha s ; partials of r . r and z . r
-template <bool JAC>
+// x += alpha p ; r -= alpha s ; partials of r . r and z . r (PC: 0 none,
+// 1 Jacobi, 2 ILU(0) -- z comes from the sweeps, k_cg_dots_z writes the partials)
+template <int PC>
 __global__ void __launch_bounds__(kThreads) k_cg_update(SolveArgs a)
 {
     KState* st = a.st;
@@ -215,7 +216,7 @@ __global__ void __launch_bounds__(kThreads) k_cg_update(SolveArgs a)
                 pv[u] = a.v.p[i];
                 rv[u] = a.v.r[i];
                 sv[u] = a.v.s[i];
-                dv[u] = JAC ? a.v.dinv[i] : 1.0;
+                dv[u] = PC == 1 ? a.v.dinv[i] : 1.0;
             }
         }
 #pragma unroll
@@ -228,15 +229,16 @@ __global__ void __launch_bounds__(kThreads) k_cg_update(SolveArgs a)
                 const double r = rv[u] - alpha * sv[u];
                 a.v.r[i] = r;
                 v[0] += r * r;
-                v[1] += JAC ? (r * dv[u]) * r : r * r;
+                v[1] += PC == 1 ? (r * dv[u]) * r : r * r;
             }
         }
     }
-    write_partials<2, double>(v, st->cg_upd[it & 1]);
+    if (PC != 2) write_partials<2, double>(v, st->cg_upd[it & 1]);
 }
 
-// convergence test ; beta ; p = z + beta p
-template <bool JAC>
+// convergence test ; beta ; p = z + beta p (z = dinv r, r, or the ILU(0)
+// sweep result in ph)
+template <int PC>
 __global__ void __launch_bounds__(kThreads) k_cg_p(SolveArgs a)
 {
     KState* st = a.st;
@@ -269,8 +271,8 @@ __global__ void __launch_bounds__(kThreads) k_cg_p(SolveArgs a)
             const int i = base + u * stride;
             if (i < n)
             {
-                rv[u] = a.v.r[i];
-                dv[u] = JAC ? a.v.dinv[i] : 1.0;
+                rv[u] = PC == 2 ? a.v.ph[i] : a.v.r[i];
+                dv[u] = PC == 1 ? a.v.dinv[i] : 1.0;
                 pv[u] = a.v.p[i];
             }
         }
@@ -278,7 +280,7 @@ __global__ void __launch_bounds__(kThreads) k_cg_p(SolveArgs a)
         for (int u = 0; u < kU; u++)
         {
             const int i = base + u * stride;
-            if (i < n) a.v.p[i] = (JAC ? rv[u] * dv[u] : rv[u]) + beta * pv[u];
+            if (i < n) a.v.p[i] = (PC == 1 ? rv[u] * dv[u] : rv[u]) + beta * pv[u];
         }
     }
 }
@@ -440,12 +442,27 @@ void launch_norm_b(const SolveArgs& a, cudaStream_t s)
     k_norm_b<<<vec_grid(a.A.n), kThreads, 0, s>>>(a);
 }
 
-// start of a solve: |b| check and initial residual
+void launch_ilu_apply(const IluView& f, const double* in, double* out, const KState* st, cudaStream_t s);
+void launch_cg_dots_z(const SolveArgs& a, int grid, cudaStream_t s);
+void launch_cg_init_z(const SolveArgs& a, int grid, cudaStream_t s);
+
+// start of a solve: |b| check and initial residual (ILU(0) CG: then
+// z = M^-1 r, p = z, r . z)
 void launch_krylov_init(const SolveArgs& a, int kind, cudaStream_t s)
 {
     const int vg = vec_grid(a.A.n);
     k_norm_b<<<vg, kThreads, 0, s>>>(a);
     k_init_residual<<<vg, kThreads, 0, s>>>(a, kind);
+    if (kind == SK_CG && a.precond == OGS_PRECOND_ILU0)
+    {
+        launch_ilu_apply(a.ilu, a.v.r, a.v.ph, a.st, s);
+        launch_cg_init_z(a, vg, s);
+    }
+}
+
+int krylov_init_launches(int kind, int precond)
+{
+    return kind == SK_CG && precond == OGS_PRECOND_ILU0 ? 5 : 2;
 }
 
 // one iteration's kernels (captured into the chunk graph); eb/ee, when
@@ -453,36 +470,49 @@ void launch_krylov_init(const SolveArgs& a, int kind, cudaStream_t s)
 void launch_krylov_iteration(const SolveArgs& a, int kind, cudaStream_t s, cudaEvent_t eb, cudaEvent_t ee)
 {
     const int vg = vec_grid(a.A.n), rg = red_grid(a.A.n);
-    const bool jac = a.precond == OGS_PRECOND_JACOBI;
+    const bool ilu = a.precond == OGS_PRECOND_ILU0;
     if (kind == SK_CG)
     {
         if (eb) cudaEventRecordWithFlags(eb, s, cudaEventRecordExternal);
         k_cg_spmv<<<vg, kThreads, 0, s>>>(a);
         if (ee) cudaEventRecordWithFlags(ee, s, cudaEventRecordExternal);
-        if (jac)
+        if (a.precond == OGS_PRECOND_JACOBI)
         {
-            k_cg_update<true><<<rg, kThreads, 0, s>>>(a);
-            k_cg_p<true><<<rg, kThreads, 0, s>>>(a);
+            k_cg_update<1><<<rg, kThreads, 0, s>>>(a);
+            k_cg_p<1><<<rg, kThreads, 0, s>>>(a);
+        }
+        else if (ilu)
+        {
+            k_cg_update<2><<<rg, kThreads, 0, s>>>(a);
+            launch_ilu_apply(a.ilu, a.v.r, a.v.ph, a.st, s);
+            launch_cg_dots_z(a, rg, s);  // same grid as the update: k_cg_p adds nb_upd partials
+            k_cg_p<2><<<rg, kThreads, 0, s>>>(a);
         }
         else
         {
-            k_cg_update<false><<<rg, kThreads, 0, s>>>(a);
-            k_cg_p<false><<<rg, kThreads, 0, s>>>(a);
+            k_cg_update<0><<<rg, kThreads, 0, s>>>(a);
+            k_cg_p<0><<<rg, kThreads, 0, s>>>(a);
         }
     }
     else
     {
         k_bi_p<<<vg, kThreads, 0, s>>>(a);
+        if (ilu) launch_ilu_apply(a.ilu, a.v.p, a.v.ph, a.st, s);
         if (eb) cudaEventRecordWithFlags(eb, s, cudaEventRecordExternal);
         k_bi_v<<<vg, kThreads, 0, s>>>(a);
         if (ee) cudaEventRecordWithFlags(ee, s, cudaEventRecordExternal);
         k_bi_s<<<rg, kThreads, 0, s>>>(a);
+        if (ilu) launch_ilu_apply(a.ilu, a.v.s, a.v.sh, a.st, s);
         k_bi_t<<<vg, kThreads, 0, s>>>(a);
         k_bi_x<<<rg, kThreads, 0, s>>>(a);
     }
 }
 
-int kernels_per_iteration(int kind) { return kind == SK_CG ? 3 : 5; }
+int kernels_per_iteration(int kind, int precond)
+{
+    const bool ilu = precond == OGS_PRECOND_ILU0;
+    return kind == SK_CG ? (ilu ? 6 : 3) : (ilu ? 9 : 5);
+}
 
 void launch_bicgstab_finish(const SolveArgs& a, cudaStream_t s)
 {

@@ -60,24 +60,32 @@ struct SellView
 struct KrylovVecs
 {
     double *x, *b, *r, *r0, *p, *ph, *s, *sh, *t, *v, *dinv;
-    // ILU(0)
-    const double* lu;           // factors on the CSR pattern
-    const int32_t* diag_pos;
-    const int32_t* lvl_rows;    // rows ordered by level (lower solve)
-    const int32_t* lvl_ptr;     // level boundaries
-    int n_levels;
-    const int32_t* ulvl_rows;   // rows ordered by level (upper solve)
-    const int32_t* ulvl_ptr;
-    int n_ulevels;
 };
 
+// ILU(0) factors on the CSR pattern (unit lower L below the diagonal, U on
+// and above it, in place) and the dependency levels of the two sweeps: the
+// rows of a level depend only on rows of earlier levels.
+struct IluView
+{
+    const int32_t* row_ptr;
+    const int32_t* col;
+    const int32_t* diag;      // CSR position of the diagonal
+    double* lu;
+    const int32_t* lrows;     // rows ordered by forward level
+    const int32_t* lptr;      // [n_lev + 1]
+    const int32_t* urows;     // rows ordered by backward level
+    const int32_t* uptr;      // [n_ulev + 1]
+    int n_lev, n_ulev;
+    int* bad;                 // smallest row with a zero pivot (factorisation)
+};
 
 struct SolveArgs
 {
     SellView<double> A;
     KrylovVecs v;
     KState* st;
-    int precond;  // 0 none, 1 Jacobi
+    int precond;  // OGS_PRECOND_NONE / JACOBI / ILU0
+    IluView ilu;
 };
 
 // ------------------------------------------------------------------

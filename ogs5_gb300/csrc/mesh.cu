@@ -265,6 +265,36 @@ extern "C" const char* ogs_gpu_last_error(void) { return ogs::last_error(); }
 extern "C" const char* ogs_gpu_version(void) { return "ogs5_gb300 0.1 (sm_103a)"; }
 extern "C" int64_t ogs_gpu_kernel_launches(int32_t reset) { return ogs::launches(reset); }
 
+// Dependency levels of a triangular sweep over the CSR pattern (natural row
+// order): a row's level is one more than the deepest row it reads -- the
+// columns below the diagonal for the forward sweep, above it for the
+// backward sweep.  Rows are returned grouped by level, ascending inside a
+// level; ptr holds the level boundaries.
+static void sweep_levels(int64_t N, const std::vector<int32_t>& row_ptr, const std::vector<int32_t>& col,
+                         bool forward, std::vector<int32_t>& rows, std::vector<int32_t>& ptr)
+{
+    std::vector<int32_t> lev(N, 0);
+    int32_t nl = N ? 1 : 0;
+    for (int64_t q = 0; q < N; q++)
+    {
+        const int64_t r = forward ? q : N - 1 - q;
+        int32_t l = 0;
+        for (int32_t k = row_ptr[r]; k < row_ptr[r + 1]; k++)
+        {
+            const int32_t c = col[k];
+            if (forward ? c < r : c > r) l = std::max(l, lev[c] + 1);
+        }
+        lev[r] = l;
+        nl = std::max(nl, l + 1);
+    }
+    ptr.assign((size_t)nl + 1, 0);
+    for (int64_t r = 0; r < N; r++) ptr[lev[r] + 1]++;
+    for (int32_t l = 0; l < nl; l++) ptr[l + 1] += ptr[l];
+    std::vector<int32_t> fill(ptr.begin(), ptr.end() - 1);
+    rows.resize(N);
+    for (int64_t r = 0; r < N; r++) rows[fill[lev[r]]++] = (int32_t)r;
+}
+
 extern "C" ogs_status ogs_gpu_mesh_destroy(ogs_mesh* m)
 {
     if (!m) return OGS_OK;
@@ -284,6 +314,11 @@ extern "C" ogs_status ogs_gpu_mesh_destroy(ogs_mesh* m)
     cudaFree(m->row_len);
     cudaFree(m->up_off);
     cudaFree(m->slot_up);
+    cudaFree(m->csr_diag);
+    cudaFree(m->lvl_rows);
+    cudaFree(m->lvl_ptr);
+    cudaFree(m->ulvl_rows);
+    cudaFree(m->ulvl_ptr);
     delete m;
     return OGS_OK;
 }
@@ -367,6 +402,12 @@ extern "C" ogs_status ogs_gpu_mesh_create(const ogs_mesh_desc* d, ogs_mesh** out
             }
         }
     });
+    // ILU(0) sweep orders (CSR diagonal positions before they become SELL slots)
+    std::vector<int32_t> csr_diag(diag), lvl_rows, lvl_ptr, ulvl_rows, ulvl_ptr;
+    sweep_levels(N, row_ptr, col, true, lvl_rows, lvl_ptr);
+    sweep_levels(N, row_ptr, col, false, ulvl_rows, ulvl_ptr);
+    m->n_lvl = (int)lvl_ptr.size() - 1;
+    m->n_ulvl = (int)ulvl_ptr.size() - 1;
     // SELL-32 layout of the pattern
     const int n_slices = (int)((N + kSlice - 1) / kSlice);
     std::vector<int32_t> slice_ptr(n_slices + 1, 0);
@@ -512,6 +553,11 @@ extern "C" ogs_status ogs_gpu_mesh_create(const ogs_mesh_desc* d, ogs_mesh** out
         (m->n_up && (st = upload(&m->up_off, up_off.data(), up_off.size()))) ||
         (m->n_up && (st = upload(&m->slot_up, slot_up.data(), slot_up.size()))) ||
         (st = upload(&m->slot_t, slot_t.data(), slot_t.size())) ||
+        (st = upload(&m->csr_diag, csr_diag.data(), csr_diag.size())) ||
+        (st = upload(&m->lvl_rows, lvl_rows.data(), lvl_rows.size())) ||
+        (st = upload(&m->lvl_ptr, lvl_ptr.data(), lvl_ptr.size())) ||
+        (st = upload(&m->ulvl_rows, ulvl_rows.data(), ulvl_rows.size())) ||
+        (st = upload(&m->ulvl_ptr, ulvl_ptr.data(), ulvl_ptr.size())) ||
         (st = upload(&m->tab, tab.data(), tab.size())) ||
         (st = upload(&m->aff, affb.data(), affb.size())))
     {

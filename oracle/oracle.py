@@ -207,6 +207,19 @@ def dirichlet(row_ptr, col, val, b, rows, vals, symmetric=False):
         lib().orc_dirichlet_row_only(row_ptr, col, val, b, len(rows), rows, vals)
 
 
+def ilu0_factor(row_ptr, col, val):
+    """orc_ilu0_factor: ILU(0) (IKJ) on the CSR pattern; returns the in-place
+    factors (unit lower L below the diagonal, U on and above it)."""
+    rp = np.ascontiguousarray(row_ptr, dtype=np.int64)
+    cl = np.ascontiguousarray(col, dtype=np.int64)
+    lu = np.zeros(len(cl))
+    dpos = np.zeros(len(rp) - 1, dtype=np.int64)
+    rc = lib().orc_ilu0_factor(len(rp) - 1, rp, cl, np.ascontiguousarray(val, dtype=np.float64), lu, dpos)
+    if rc:
+        raise ValueError("ILU(0): zero pivot")
+    return lu
+
+
 def spmv(row_ptr, col, val, x):
     y = np.zeros(len(row_ptr) - 1)
     lib().orc_spmv(len(y), row_ptr, col, val, np.ascontiguousarray(x, dtype=np.float64), y)

@@ -80,3 +80,54 @@ def test_advection_dispersion_known_answer(oracle):
     g = np.array([[-1, -1, -1], [1, 0, 0], [0, 1, 0], [0, 0, 1]], dtype=float)
     D = np.diag([1.0 * q, 0.1 * q, 0.1 * q])
     assert np.allclose(m["laplace"], (1 / 6) * g @ D @ g.T, rtol=1e-11, atol=1e-22)
+
+
+def test_ilu0_reproduces_matrix_on_pattern(oracle):
+    """ILU(0) property: (L U)_ij = a_ij for every (i, j) of the pattern, and
+    for a tridiagonal matrix ILU(0) is the exact LU factorisation."""
+    from ogs5_gb300 import mesh as M
+    m = M.structured_quad(7, 5)
+    rp, col = oracle.build_pattern(m.n_nodes, m.conn)
+    p = oracle.make_params(pcs_type=0, dt=10.0, storage=1e-3, time_unit_factor=1.0, theta=1.0)
+    val, _ = oracle.assemble(m, rp, col, p, elem_k=np.full(m.n_elements, 1e-4),
+                             u0=np.zeros(m.n_nodes))
+    lu = oracle.ilu0_factor(rp, col, val)
+    n = m.n_nodes
+    A = np.zeros((n, n))
+    L = np.eye(n)
+    U = np.zeros((n, n))
+    for i in range(n):
+        for k in range(rp[i], rp[i + 1]):
+            j = col[k]
+            A[i, j] = val[k]
+            if j < i:
+                L[i, j] = lu[k]
+            else:
+                U[i, j] = lu[k]
+    P = L @ U
+    mask = A != 0
+    assert np.allclose(P[mask], A[mask], rtol=1e-12, atol=1e-14 * np.abs(A).max())
+    # tridiagonal: exact
+    t = 9
+    trp = np.concatenate([[0], np.cumsum([2] + [3] * (t - 2) + [2])]).astype(np.int64)
+    tcol = []
+    for i in range(t):
+        tcol += [j for j in (i - 1, i, i + 1) if 0 <= j < t]
+    tcol = np.array(tcol, dtype=np.int64)
+    rng = np.random.default_rng(0)
+    tval = rng.uniform(-1, 0, len(tcol))
+    T = np.zeros((t, t))
+    for i in range(t):
+        for k in range(trp[i], trp[i + 1]):
+            T[i, tcol[k]] = tval[k]
+        T[i, i] = 4.0
+    for i in range(t):
+        for k in range(trp[i], trp[i + 1]):
+            tval[k] = T[i, tcol[k]]
+    tlu = oracle.ilu0_factor(trp, tcol, tval)
+    L = np.eye(t)
+    U = np.zeros((t, t))
+    for i in range(t):
+        for k in range(trp[i], trp[i + 1]):
+            (L if tcol[k] < i else U)[i, tcol[k]] = tlu[k]
+    assert np.allclose(L @ U, T, rtol=1e-13, atol=1e-14)
