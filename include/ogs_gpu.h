@@ -305,6 +305,85 @@ ogs_status ogs_gpu_csr_cg_noalloc(int64_t n, const int32_t* row_ptr,
                                   int32_t max_iter, double tol, void* stream,
                                   ogs_solve_stats* stats);
 
+/* ------------------------------------------------------------------------
+ * Monte-Carlo batch (extension; no single counterpart in the reference,
+ * which runs one realisation per ogs process: CRFProcess::GlobalAssembly,
+ * IncorporateBoundaryConditions and Linear_EQS::Solver once per deck).
+ *
+ * Many steady GROUNDWATER_FLOW realisations on structured hex boxes of
+ * different sizes, each with its own element conductivity field, Dirichlet
+ * heads on the two x faces (symmetric elimination, as
+ * OGS_DIRICHLET_SYMMETRIC) and no-flow elsewhere, are assembled and solved
+ * by ONE cooperative persistent kernel launch (captured in a CUDA graph):
+ * row-centric assembly straight into the upper diagonal-offset form (no
+ * slot map, no atomics), then Jacobi-preconditioned CG with FP32 matrix
+ * and sweeps and FP64 residual replacement (as OGS_PRECISION_FP32_REFINED)
+ * for all realisations at once; converged realisations drop out of the
+ * work list.  Node (ix, iy, iz) of a box has index ix + nx (iy + ny iz);
+ * element (ex, ey, ez) has index ex + (nx-1) (ey + (ny-1) ez).
+ * ---------------------------------------------------------------------- */
+typedef struct ogs_batch ogs_batch;
+
+typedef struct
+{
+    int32_t nx, ny, nz;         /* nodes per axis (>= 2 each)                  */
+    int32_t pad0;
+    const double* elem_k;       /* (nx-1)(ny-1)(nz-1) conductivities, host    */
+    double h_left, h_right;     /* heads on the x = 0 and x = max faces       */
+} ogs_batch_realisation;
+
+typedef struct
+{
+    double hx, hy, hz;          /* cell sizes, all realisations                */
+    double time_unit_factor;    /* CalCoefLaplace factor (1 for seconds)       */
+    double tol;                 /* |b - A x| / |b| < tol                       */
+    double inner_tol;           /* FP32 residual drop per replacement (0: 1e-2) */
+    int32_t max_iter;           /* FP32 iterations per realisation             */
+    int32_t pad0;
+} ogs_batch_config;
+
+/* Launch shape of the persistent kernel (chosen by ogs_gpu_batch_autotune
+ * or set by the caller): rows per work tile, threads per block, resident
+ * blocks per SM (the grid is blocks_per_sm x SM count). */
+typedef struct
+{
+    int32_t tile_rows;
+    int32_t block_threads;      /* 256 or 512                                  */
+    int32_t blocks_per_sm;
+    int32_t graph;              /* out: 1 if the launch runs as a CUDA graph   */
+    double ms_per_step;         /* out (autotune): measured time per CG step   */
+} ogs_batch_tuning;
+
+typedef struct
+{
+    int32_t iterations;         /* FP32 inner iterations                       */
+    int32_t status;             /* ogs_status                                  */
+    int32_t refinements;        /* FP64 residual replacements                  */
+    int32_t pad0;
+    double rel_residual;        /* final FP64 |b - A x| / |b|                  */
+} ogs_batch_stats;
+
+/* Copies the realisations' fields to the device and lays out the batch. */
+ogs_status ogs_gpu_batch_create(const ogs_batch_config* cfg,
+                                const ogs_batch_realisation* reals,
+                                int32_t n_real, void* stream, ogs_batch** out);
+ogs_status ogs_gpu_batch_destroy(ogs_batch* b);
+/* Replaces the conductivity field of every realisation (host or device
+ * array of all elements, realisations in order). */
+ogs_status ogs_gpu_batch_set_k(ogs_batch* b, const double* elem_k_all);
+/* Times every candidate launch shape on this batch (a bounded number of CG
+ * steps each) and keeps the fastest; *chosen receives it (may be NULL). */
+ogs_status ogs_gpu_batch_autotune(ogs_batch* b, ogs_batch_tuning* chosen);
+ogs_status ogs_gpu_batch_set_tuning(ogs_batch* b, const ogs_batch_tuning* t);
+/* Assembly and solve of every realisation in one launch.  stats: n_real
+ * entries (may be NULL).  Returns OGS_OK when every realisation converged,
+ * else the first failing status. */
+ogs_status ogs_gpu_batch_solve(ogs_batch* b, ogs_batch_stats* stats);
+/* Heads of all realisations, concatenated (host or device array). */
+ogs_status ogs_gpu_batch_get_heads(const ogs_batch* b, double* heads);
+/* Total rows (sum of nx ny nz) and elements of the batch. */
+ogs_status ogs_gpu_batch_info(const ogs_batch* b, int64_t* rows, int64_t* elements);
+
 #ifdef __cplusplus
 }
 #endif

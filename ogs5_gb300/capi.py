@@ -44,6 +44,8 @@ EXPORTS = [
     "ogs_gpu_gp_velocity", "ogs_gpu_get_csr", "ogs_gpu_get_rhs", "ogs_gpu_get_x",
     "ogs_gpu_spmv", "ogs_gpu_mesh_gauss_points", "ogs_gpu_kernel_launches", "ogs_gpu_profile",
     "ogs_gpu_csr_cg_noalloc", "ogs_gpu_get_ilu0",
+    "ogs_gpu_batch_create", "ogs_gpu_batch_destroy", "ogs_gpu_batch_set_k", "ogs_gpu_batch_autotune",
+    "ogs_gpu_batch_set_tuning", "ogs_gpu_batch_solve", "ogs_gpu_batch_get_heads", "ogs_gpu_batch_info",
 ]
 NOALLOC_MAX_ROWS = 524288
 
@@ -90,6 +92,27 @@ class SolveStats(C.Structure):
     _fields_ = [("iterations", C.c_int32), ("status", C.c_int32), ("rel_residual", C.c_double),
                 ("b_norm", C.c_double), ("refinements", C.c_int32), ("pad0", C.c_int32),
                 ("solve_ms", C.c_double)]
+
+
+class BatchRealisation(C.Structure):
+    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32), ("pad0", C.c_int32),
+                ("elem_k", C.c_void_p), ("h_left", C.c_double), ("h_right", C.c_double)]
+
+
+class BatchConfig(C.Structure):
+    _fields_ = [("hx", C.c_double), ("hy", C.c_double), ("hz", C.c_double),
+                ("time_unit_factor", C.c_double), ("tol", C.c_double), ("inner_tol", C.c_double),
+                ("max_iter", C.c_int32), ("pad0", C.c_int32)]
+
+
+class BatchTuning(C.Structure):
+    _fields_ = [("tile_rows", C.c_int32), ("block_threads", C.c_int32), ("blocks_per_sm", C.c_int32),
+                ("graph", C.c_int32), ("ms_per_step", C.c_double)]
+
+
+class BatchStats(C.Structure):
+    _fields_ = [("iterations", C.c_int32), ("status", C.c_int32), ("refinements", C.c_int32),
+                ("pad0", C.c_int32), ("rel_residual", C.c_double)]
 
 
 def make_params(pcs_type=GROUNDWATER_FLOW, **kw) -> AssemblyParams:
@@ -152,6 +175,19 @@ def lib():
         L.ogs_gpu_csr_cg_noalloc.argtypes = [C.c_int64, vp, vp, vp, vp, vp, C.c_int32, C.c_double, vp,
                                              C.POINTER(SolveStats)]
         L.ogs_gpu_csr_cg_noalloc.restype = st
+        L.ogs_gpu_batch_create.argtypes = [C.POINTER(BatchConfig), C.POINTER(BatchRealisation), C.c_int32,
+                                           vp, C.POINTER(vp)]
+        L.ogs_gpu_batch_destroy.argtypes = [vp]
+        L.ogs_gpu_batch_set_k.argtypes = [vp, vp]
+        L.ogs_gpu_batch_autotune.argtypes = [vp, C.POINTER(BatchTuning)]
+        L.ogs_gpu_batch_set_tuning.argtypes = [vp, C.POINTER(BatchTuning)]
+        L.ogs_gpu_batch_solve.argtypes = [vp, C.POINTER(BatchStats)]
+        L.ogs_gpu_batch_get_heads.argtypes = [vp, vp]
+        L.ogs_gpu_batch_info.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+        for name in ("ogs_gpu_batch_create", "ogs_gpu_batch_destroy", "ogs_gpu_batch_set_k",
+                     "ogs_gpu_batch_autotune", "ogs_gpu_batch_set_tuning", "ogs_gpu_batch_solve",
+                     "ogs_gpu_batch_get_heads", "ogs_gpu_batch_info"):
+            getattr(L, name).restype = st
         L.ogs_gpu_kernel_launches.argtypes = [C.c_int32]
         L.ogs_gpu_kernel_launches.restype = C.c_int64
         for name in ("ogs_gpu_mesh_create", "ogs_gpu_mesh_destroy", "ogs_gpu_mesh_info",
@@ -346,3 +382,86 @@ def csr_cg_noalloc(row_ptr, col, val, b, x, max_iter=1000, tol=1e-10, stream=Non
     _check(status, allow=(NOT_CONVERGED,))
     return {"iterations": st.iterations, "status": st.status, "rel_residual": st.rel_residual,
             "b_norm": st.b_norm}
+
+
+class Batch:
+    """Monte-Carlo batch of steady GROUNDWATER_FLOW realisations on
+    structured hex boxes (ogs_gpu_batch_*): one persistent launch assembles
+    and solves them all.
+
+        b = Batch([(nx, ny, nz, elem_k, h_left, h_right), ...], tol=1e-10)
+        b.autotune()
+        stats = b.solve()          # list of dicts, one per realisation
+        heads = b.heads()          # list of arrays (nx*ny*nz each)
+    """
+
+    def __init__(self, reals, hx=1.0, hy=1.0, hz=1.0, tol=1e-10, max_iter=5000, inner_tol=0.0,
+                 time_unit_factor=1.0, stream=None):
+        self.h = None
+        cfg = BatchConfig(hx, hy, hz, time_unit_factor, tol, inner_tol, max_iter, 0)
+        arr = (BatchRealisation * len(reals))()
+        self._keep = []
+        self.sizes = []
+        for i, (nx, ny, nz, ek, hl, hr) in enumerate(reals):
+            ek = np.ascontiguousarray(ek, dtype=np.float64)
+            if ek.size != (nx - 1) * (ny - 1) * (nz - 1):
+                raise ValueError(f"realisation {i}: {ek.size} conductivities for {nx}x{ny}x{nz} nodes")
+            self._keep.append(ek)
+            arr[i] = BatchRealisation(nx, ny, nz, 0, ek.ctypes.data, hl, hr)
+            self.sizes.append(nx * ny * nz)
+        h = C.c_void_p()
+        s = None if stream is None else C.c_void_p(stream)
+        _check(lib().ogs_gpu_batch_create(C.byref(cfg), arr, len(reals), s, C.byref(h)))
+        self.h = h
+        self._keep = None
+        rows, elems = C.c_int64(), C.c_int64()
+        _check(lib().ogs_gpu_batch_info(self.h, C.byref(rows), C.byref(elems)))
+        self.rows, self.elements = rows.value, elems.value
+        self.n = len(reals)
+
+    def close(self):
+        if self.h is not None and _LIB is not None:
+            lib().ogs_gpu_batch_destroy(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def _tuning_dict(t):
+        return {"tile_rows": t.tile_rows, "block_threads": t.block_threads,
+                "blocks_per_sm": t.blocks_per_sm, "graph": t.graph, "ms_per_step": t.ms_per_step}
+
+    def autotune(self) -> dict:
+        t = BatchTuning()
+        _check(lib().ogs_gpu_batch_autotune(self.h, C.byref(t)))
+        return self._tuning_dict(t)
+
+    def set_tuning(self, tile_rows, block_threads, blocks_per_sm):
+        t = BatchTuning(tile_rows, block_threads, blocks_per_sm, 0, 0.0)
+        _check(lib().ogs_gpu_batch_set_tuning(self.h, C.byref(t)))
+
+    def set_k(self, elem_k_all):
+        k = elem_k_all if hasattr(elem_k_all, "data_ptr") else _f64(elem_k_all)
+        _check(lib().ogs_gpu_batch_set_k(self.h, _ptr(k)))
+
+    def solve(self, allow_fail=False) -> list:
+        st = (BatchStats * self.n)()
+        status = lib().ogs_gpu_batch_solve(self.h, st)
+        if not allow_fail:
+            _check(status)
+        return [{"iterations": s.iterations, "status": s.status, "refinements": s.refinements,
+                 "rel_residual": s.rel_residual} for s in st]
+
+    def heads_flat(self, out=None):
+        if out is None:
+            out = np.zeros(self.rows)
+        _check(lib().ogs_gpu_batch_get_heads(self.h, _ptr(out)))
+        return out
+
+    def heads(self) -> list:
+        flat = self.heads_flat()
+        return np.split(flat, np.cumsum(self.sizes)[:-1])
