@@ -361,6 +361,8 @@ typedef struct
     int32_t refinements;        /* FP64 residual replacements                  */
     int32_t pad0;
     double rel_residual;        /* final FP64 |b - A x| / |b|                  */
+    double finish_ms;           /* device time from the start of the launch to
+                                   this realisation's convergence              */
 } ogs_batch_stats;
 
 /* Copies the realisations' fields to the device and lays out the batch. */

@@ -112,7 +112,7 @@ class BatchTuning(C.Structure):
 
 class BatchStats(C.Structure):
     _fields_ = [("iterations", C.c_int32), ("status", C.c_int32), ("refinements", C.c_int32),
-                ("pad0", C.c_int32), ("rel_residual", C.c_double)]
+                ("pad0", C.c_int32), ("rel_residual", C.c_double), ("finish_ms", C.c_double)]
 
 
 def make_params(pcs_type=GROUNDWATER_FLOW, **kw) -> AssemblyParams:
@@ -403,11 +403,13 @@ class Batch:
         self._keep = []
         self.sizes = []
         for i, (nx, ny, nz, ek, hl, hr) in enumerate(reals):
-            ek = np.ascontiguousarray(ek, dtype=np.float64)
-            if ek.size != (nx - 1) * (ny - 1) * (nz - 1):
-                raise ValueError(f"realisation {i}: {ek.size} conductivities for {nx}x{ny}x{nz} nodes")
+            if not hasattr(ek, "data_ptr"):  # numpy / sequence (host); tensors are used in place
+                ek = np.ascontiguousarray(ek, dtype=np.float64)
+            size = ek.numel() if hasattr(ek, "numel") else ek.size
+            if size != (nx - 1) * (ny - 1) * (nz - 1):
+                raise ValueError(f"realisation {i}: {size} conductivities for {nx}x{ny}x{nz} nodes")
             self._keep.append(ek)
-            arr[i] = BatchRealisation(nx, ny, nz, 0, ek.ctypes.data, hl, hr)
+            arr[i] = BatchRealisation(nx, ny, nz, 0, _ptr(ek), hl, hr)
             self.sizes.append(nx * ny * nz)
         h = C.c_void_p()
         s = None if stream is None else C.c_void_p(stream)
@@ -454,7 +456,7 @@ class Batch:
         if not allow_fail:
             _check(status)
         return [{"iterations": s.iterations, "status": s.status, "refinements": s.refinements,
-                 "rel_residual": s.rel_residual} for s in st]
+                 "rel_residual": s.rel_residual, "finish_ms": s.finish_ms} for s in st]
 
     def heads_flat(self, out=None):
         if out is None:

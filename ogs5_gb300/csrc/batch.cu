@@ -46,10 +46,13 @@
 namespace ogs {
 
 // upper stencil offsets (dx, dy, dz): linear offset dx + nx dy + nx ny dz
-// >= 0, ascending for nx, ny >= 3
-__constant__ int8_t c_up[14][3] = {{0, 0, 0},  {1, 0, 0},  {-1, 1, 0}, {0, 1, 0},  {1, 1, 0},
-                                   {-1, -1, 1}, {0, -1, 1}, {1, -1, 1}, {-1, 0, 1}, {0, 0, 1},
-                                   {1, 0, 1},  {-1, 1, 1}, {0, 1, 1},  {1, 1, 1}};
+// >= 0, ascending for nx, ny >= 3 (compile-time table: unrolled loops fold
+// each offset into one integer multiply-add)
+__host__ __device__ constexpr int kUpX(int d) { return d == 0 ? 0 : d == 1 ? 1 : (d - 2) % 3 - 1; }
+__host__ __device__ constexpr int kUpY(int d) { return d < 2 ? 0 : d < 5 ? 1 : (d - 5) / 3 - 1; }
+__host__ __device__ constexpr int kUpZ(int d) { return d < 5 ? 0 : 1; }
+
+__device__ __forceinline__ int up_offset(int d, int nx, int nxy) { return kUpX(d) + nx * kUpY(d) + nxy * kUpZ(d); }
 
 struct BReal
 {
@@ -81,7 +84,7 @@ struct BCtl
     int done_count, seen_done;
     int step, max_steps;
     int n_act, n_act_tiles;
-    int pad[2];
+    unsigned long long t0;  // %globaltimer at the start of the launch (ns)
 };
 
 struct BatchArgs
@@ -101,7 +104,7 @@ struct BatchArgs
     ogs_batch_stats* out;
     double tol, delta;
     int max_iter;
-    double kloc[64];   // local Laplace of a cell, corner-bit order, times time_unit_factor
+    const double* kloc;  // [64] local Laplace of a cell, corner-bit order, times time_unit_factor
 };
 
 // ------------------------------------------------------------------
@@ -122,6 +125,13 @@ __device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v)
 }
 
 __device__ __forceinline__ int ld_volatile(const int* p) { return *(const volatile int*)p; }
+
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
 
 // Returns false in every thread of the block when the batch must stop
 // (timeout anywhere, or ctl->exit set by the last arriver).  on_last runs
@@ -226,15 +236,28 @@ __device__ __forceinline__ void realisation_sum(const double* part, int tile0, i
     __syncthreads();
 }
 
-// tile state written by another block in an earlier step: L2 loads
+// tile state written by another block in an earlier step: L2 loads, field
+// by field (keeps the copy in registers)
 __device__ __forceinline__ TState load_state(const TState* p)
 {
-    static_assert(sizeof(TState) % 8 == 0, "TState is read as 8-byte words");
     TState s;
-    const unsigned long long* src = reinterpret_cast<const unsigned long long*>(p);
-    unsigned long long* dst = reinterpret_cast<unsigned long long*>(&s);
-#pragma unroll
-    for (int k = 0; k < (int)(sizeof(TState) / 8); k++) dst[k] = __ldcg(src + k);
+    s.bnorm = __ldcg(&p->bnorm);
+    s.scale = __ldcg(&p->scale);
+    s.ratio = __ldcg(&p->ratio);
+    s.rmax = __ldcg(&p->rmax);
+    s.gam[0] = __ldcg(&p->gam[0]);
+    s.gam[1] = __ldcg(&p->gam[1]);
+    s.eta[0] = __ldcg(&p->eta[0]);
+    s.eta[1] = __ldcg(&p->eta[1]);
+    s.error = __ldcg(&p->error);
+    s.iter = __ldcg(&p->iter);
+    s.base_iter = __ldcg(&p->base_iter);
+    s.mode = __ldcg(&p->mode);
+    s.status = __ldcg(&p->status);
+    s.first = __ldcg(&p->first);
+    s.replacements = __ldcg(&p->replacements);
+    s.done = __ldcg(&p->done);
+    s.pad = 0;
     return s;
 }
 
@@ -255,16 +278,11 @@ __device__ __forceinline__ double stencil_entry(const BatchArgs& a, const BReal&
                 const int ca = (ix - ex) + 2 * (iy - ey) + 4 * (iz - ez);
                 const int cb = (jx - ex) + 2 * (jy - ey) + 4 * (jz - ez);
                 const double k = __ldg(ek + ex + (R.nx - 1) * (ey + (R.ny - 1) * ez));
-                acc += k * a.kloc[ca * 8 + cb];
+                acc += k * __ldg(a.kloc + ca * 8 + cb);
             }
     return acc;
 }
 
-__device__ __forceinline__ void tile_offsets(const BReal& R, int* off)
-{
-#pragma unroll
-    for (int d = 0; d < 14; d++) off[d] = c_up[d][0] + R.nx * (c_up[d][1] + R.ny * c_up[d][2]);
-}
 
 // ------------------------------------------------------------------
 // phases
@@ -306,12 +324,13 @@ __device__ void assemble_tile(const BatchArgs& a, const BTile& T)
         }
         U64[i] = diag;
         U32[i] = (float)diag;
+#pragma unroll
         for (int d = 1; d < 14; d++)
         {
-            const int jx = ix + c_up[d][0];
+            const int jx = ix + kUpX(d);
             double v = 0.0;
             if (!bc && jx != 0 && jx != R.nx - 1)
-                v = stencil_entry(a, R, ek, ix, iy, iz, c_up[d][0], c_up[d][1], c_up[d][2]);
+                v = stencil_entry(a, R, ek, ix, iy, iz, kUpX(d), kUpY(d), kUpZ(d));
             U64[(size_t)d * R.n + i] = v;
             U32[(size_t)d * R.n + i] = (float)v;
         }
@@ -327,14 +346,14 @@ __device__ void assemble_tile(const BatchArgs& a, const BTile& T)
 }
 
 // FP64 row of the half diagonal-offset operator applied to x64 + x32 / scale
-__device__ __forceinline__ double row64(const double* __restrict__ U, const int* off, int n, int i,
+__device__ __forceinline__ double row64(const double* __restrict__ U, int nx, int nxy, int n, int i,
                                         const double* x64, const float* x32, double inv)
 {
     double acc = U[i] * (x64[i] + (double)x32[i] * inv);
 #pragma unroll
     for (int d = 1; d < 14; d++)
     {
-        const int o = off[d];
+        const int o = up_offset(d, nx, nxy);
         const double* Ud = U + (size_t)d * n;
         if (i + o < n) acc += Ud[i] * (x64[i + o] + (double)x32[i + o] * inv);
         if (i - o >= 0) acc += Ud[i - o] * (x64[i - o] + (double)x32[i - o] * inv);
@@ -343,7 +362,7 @@ __device__ __forceinline__ double row64(const double* __restrict__ U, const int*
 }
 
 // FP32 row, all pairs loaded before the FMAs (27 independent loads per thread)
-__device__ __forceinline__ float row32(const float* __restrict__ U, const int* off, int n, int i,
+__device__ __forceinline__ float row32(const float* __restrict__ U, int nx, int nxy, int n, int i,
                                        const float* x)
 {
     float uv[27], xv[27];
@@ -352,7 +371,7 @@ __device__ __forceinline__ float row32(const float* __restrict__ U, const int* o
 #pragma unroll
     for (int d = 1; d < 14; d++)
     {
-        const int o = off[d];
+        const int o = up_offset(d, nx, nxy);
         const float* Ud = U + (size_t)d * n;
         const bool up = i + o < n, lo = i - o >= 0;
         uv[2 * d - 1] = up ? Ud[i] : 0.f;
@@ -372,8 +391,7 @@ __device__ void phase_a(const BatchArgs& a, int g)
     const BTile T = a.tiles[g];
     const BReal R = a.real[T.r];
     const TState S = load_state(a.ts + g);
-    int off[14];
-    tile_offsets(R, off);
+    const int nxy = R.nx * R.ny;
     const int64_t r0 = R.row0;
     if (S.mode == kModeReplace)
     {
@@ -383,7 +401,7 @@ __device__ void phase_a(const BatchArgs& a, int g)
         for (int i = T.i0 + threadIdx.x; i < T.i1; i += NT)
         {
             const double bi = a.b[r0 + i];
-            const double r = bi - row64(U, off, R.n, i, a.x64 + r0, a.x32 + r0, inv);
+            const double r = bi - row64(U, R.nx, nxy, R.n, i, a.x64 + r0, a.x32 + r0, inv);
             a.r64[r0 + i] = r;
             v[0] += r * r;
             v[1] += bi * bi;
@@ -397,7 +415,7 @@ __device__ void phase_a(const BatchArgs& a, int g)
         float v[3] = {0.f, 0.f, 0.f};
         for (int i = T.i0 + threadIdx.x; i < T.i1; i += NT)
         {
-            const float w = row32(U, off, R.n, i, u);
+            const float w = row32(U, R.nx, nxy, R.n, i, u);
             a.w32[r0 + i] = w;
             const float ui = u[i], ri = a.r32[r0 + i];
             v[0] += ri * ui;
@@ -419,9 +437,60 @@ __device__ void finish_realisation(const BatchArgs& a, const BTile& T, int g, co
         o.refinements = S.replacements;
         o.pad0 = 0;
         o.rel_residual = S.error;
+        o.finish_ms = (double)(global_ns() - *(volatile unsigned long long*)&a.ctl->t0) * 1e-6;
         a.out[T.r] = o;
         a.real_done[T.r] = 1;
         atomicAdd(&a.ctl->done_count, 1);
+    }
+}
+
+// p = u + beta p ; s = w + beta s ; x += alpha p ; r -= alpha s ; u = d r
+// over rows [q0, q0 + len): four rows per thread per pass, all loads first,
+// so each thread keeps 28 loads in flight
+constexpr int kVU = 4;
+
+template <int NT>
+__device__ __forceinline__ void cg_update(const BatchArgs& a, int64_t q0, int len, float fb, float fa)
+{
+    float* __restrict__ u32 = a.u32 + q0;
+    const float* __restrict__ w32 = a.w32 + q0;
+    const float* __restrict__ d32 = a.d32 + q0;
+    float* __restrict__ p32 = a.p32 + q0;
+    float* __restrict__ s32 = a.s32 + q0;
+    float* __restrict__ x32 = a.x32 + q0;
+    float* __restrict__ r32 = a.r32 + q0;
+    for (int base = threadIdx.x; base < len; base += kVU * NT)
+    {
+        float uv[kVU], wv[kVU], pv[kVU], sv[kVU], xv[kVU], rv[kVU], dv[kVU];
+#pragma unroll
+        for (int k = 0; k < kVU; k++)
+        {
+            const int i = base + k * NT;
+            const bool in = i < len;
+            uv[k] = in ? u32[i] : 0.f;
+            wv[k] = in ? w32[i] : 0.f;
+            pv[k] = in ? p32[i] : 0.f;
+            sv[k] = in ? s32[i] : 0.f;
+            xv[k] = in ? x32[i] : 0.f;
+            rv[k] = in ? r32[i] : 0.f;
+            dv[k] = in ? d32[i] : 0.f;
+        }
+#pragma unroll
+        for (int k = 0; k < kVU; k++)
+        {
+            const int i = base + k * NT;
+            if (i < len)
+            {
+                const float p = uv[k] + fb * pv[k];
+                const float s = wv[k] + fb * sv[k];
+                const float r = rv[k] - fa * s;
+                p32[i] = p;
+                s32[i] = s;
+                x32[i] = xv[k] + fa * p;
+                r32[i] = r;
+                u32[i] = r * dv[k];
+            }
+        }
     }
 }
 
@@ -476,8 +545,9 @@ __device__ void phase_b(const BatchArgs& a, int g)
                 int it = S.iter;
                 if (!first) it -= 1;
                 S.iter = it;
-                S.gam[it & 1] *= ratio * ratio;
-                S.eta[it & 1] *= ratio * ratio;
+                const double r2 = ratio * ratio;
+                if (it & 1) { S.gam[1] *= r2; S.eta[1] *= r2; }
+                else { S.gam[0] *= r2; S.eta[0] *= r2; }
                 S.base_iter = it;
                 S.rmax = -1.0;
                 S.mode = kModeIter;
@@ -507,15 +577,19 @@ __device__ void phase_b(const BatchArgs& a, int g)
         const bool first = it == 1;
         const bool fresh = it == S.base_iter + 1;
         const double rmax = fresh ? rn : S.rmax;
-        const double beta = first ? 0.0 : gamma / S.gam[(it - 1) & 1];
-        const double eta = first ? delta : delta - beta * beta * S.eta[(it - 1) & 1];
+        // scalars of the previous iteration (parity slots, selected without
+        // dynamic indexing so the state stays in registers)
+        const double gam_prev = (it - 1) & 1 ? S.gam[1] : S.gam[0];
+        const double eta_prev = (it - 1) & 1 ? S.eta[1] : S.eta[0];
+        const double beta = first ? 0.0 : gamma / gam_prev;
+        const double eta = first ? delta : delta - beta * beta * eta_prev;
         const double alpha = gamma / eta;
         const double est = rn / S.scale / S.bnorm;
         const bool nonfinite = !isfinite(rn) || !isfinite(alpha);
         const bool repl = !nonfinite && !fresh && (est < a.tol || rn < a.delta * rmax || it > a.max_iter);
         if (fresh) S.rmax = rn;
-        S.gam[it & 1] = gamma;
-        S.eta[it & 1] = eta;
+        if (it & 1) { S.gam[1] = gamma; S.eta[1] = eta; }
+        else { S.gam[0] = gamma; S.eta[0] = eta; }
         S.iter = it;
         if (nonfinite)
         {
@@ -527,21 +601,7 @@ __device__ void phase_b(const BatchArgs& a, int g)
         else if (repl)
             S.mode = kModeReplace;
         else
-        {
-            const float fb = (float)beta, fa = (float)alpha;
-            for (int i = T.i0 + threadIdx.x; i < T.i1; i += NT)
-            {
-                const int64_t q = r0 + i;
-                const float p = a.u32[q] + fb * a.p32[q];
-                const float s = a.w32[q] + fb * a.s32[q];
-                const float r = a.r32[q] - fa * s;
-                a.p32[q] = p;
-                a.s32[q] = s;
-                a.x32[q] += fa * p;
-                a.r32[q] = r;
-                a.u32[q] = r * a.d32[q];
-            }
-        }
+            cg_update<NT>(a, r0 + T.i0, T.i1 - T.i0, (float)beta, (float)alpha);
     }
     __syncthreads();
     if (threadIdx.x == 0) a.ts[g] = S;
@@ -585,10 +645,12 @@ __device__ void end_of_step(const BatchArgs& a)
     if (c->n_act == 0 || c->step >= c->max_steps) c->exit = 1;
 }
 
+// 256 threads: three blocks per SM (<= 85 registers); 512: one (<= 128)
 template <int NT>
-__global__ void __launch_bounds__(NT) k_batch(BatchArgs a)
+__global__ void __launch_bounds__(NT, NT == 256 ? 3 : 1) k_batch(BatchArgs a)
 {
     BCtl* c = a.ctl;
+    if (blockIdx.x == 0 && threadIdx.x == 0) c->t0 = global_ns();
     for (int t = blockIdx.x; t < a.n_tiles; t += gridDim.x) assemble_tile<NT>(a, a.tiles[t]);
     if (!grid_barrier(c, [] {})) return;
     for (;;)
@@ -642,6 +704,7 @@ struct ogs_batch
     cudaGraphExec_t graph = nullptr;
     int graph_steps = -1;      // max_steps captured in the graph
     double kloc[64];
+    double* d_kloc = nullptr;
 };
 
 namespace {
@@ -771,7 +834,7 @@ BatchArgs make_args(ogs_batch* B)
     a.tol = B->cfg.tol;
     a.delta = B->cfg.inner_tol > 0.0 ? B->cfg.inner_tol : 1e-2;
     a.max_iter = B->cfg.max_iter;
-    std::memcpy(a.kloc, B->kloc, sizeof a.kloc);
+    a.kloc = B->d_kloc;
     return a;
 }
 
@@ -893,6 +956,7 @@ extern "C" ogs_status ogs_gpu_batch_destroy(ogs_batch* B)
     cudaFree(B->act_pref);
     cudaFree(B->real_done);
     cudaFree(B->out);
+    cudaFree(B->d_kloc);
     if (B->h_init) cudaFreeHost(B->h_init);
     if (B->h_res) cudaFreeHost(B->h_res);
     if (B->own_stream && B->stream) cudaStreamDestroy(B->stream);
@@ -969,6 +1033,8 @@ extern "C" ogs_status ogs_gpu_batch_create(const ogs_batch_config* cfg, const og
     if (e == cudaSuccess) e = cudaMalloc(&B->real_done, n_real * sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc(&B->out, n_real * sizeof(ogs_batch_stats));
     if (e == cudaSuccess) e = cudaMallocHost(&B->h_res, sizeof(BCtl));
+    if (e == cudaSuccess) e = cudaMalloc(&B->d_kloc, sizeof B->kloc);
+    if (e == cudaSuccess) e = cudaMemcpy(B->d_kloc, B->kloc, sizeof B->kloc, cudaMemcpyHostToDevice);
     if (e != cudaSuccess)
     {
         set_error("batch_create: %s (%lld rows)", cudaGetErrorString(e), (long long)rows);

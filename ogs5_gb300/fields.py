@@ -34,3 +34,28 @@ def lognormal_k(shape, mean_ln: float, var: float, ell: float, seed: int) -> np.
     """Element-wise K = exp(mean_ln + GRF), flattened x-fastest like the meshes."""
     g = gaussian_random_field(shape[::-1], var, ell, seed)  # (nz, ny, nx) order
     return np.exp(mean_ln + g).ravel().astype(np.float64)
+
+
+def lognormal_k_device(shape, mean_ln: float, var: float, ell: float, seed: int, device="cuda"):
+    """lognormal_k computed with torch on a device (same construction, torch's
+    random stream: the values differ from the numpy version, the
+    distribution does not).  Returns a flattened float64 tensor."""
+    import torch
+
+    sh = tuple(int(s) for s in shape[::-1])  # (nz, ny, nx)
+    ext = tuple(2 * s for s in sh)
+    axes = [torch.minimum(torch.arange(m, device=device), m - torch.arange(m, device=device)).double()
+            for m in ext]
+    grids = torch.meshgrid(*axes, indexing="ij")
+    r = torch.sqrt(sum(g * g for g in grids))
+    lam = torch.fft.fftn(var * torch.exp(-r / ell)).real.clamp_min(0.0)
+    gen = torch.Generator(device=device)
+    gen.manual_seed(int(seed))
+    n = 1
+    for m in ext:
+        n *= m
+    noise = torch.complex(torch.randn(ext, generator=gen, device=device, dtype=torch.float64),
+                          torch.randn(ext, generator=gen, device=device, dtype=torch.float64))
+    f = torch.fft.ifftn(torch.sqrt(lam / n) * noise * n).real
+    f = f[: sh[0], : sh[1], : sh[2]]
+    return torch.exp(mean_ln + f).reshape(-1).contiguous()
