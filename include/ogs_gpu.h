@@ -232,6 +232,20 @@ ogs_status ogs_gpu_set_dirichlet(ogs_system* sys, const int64_t* rows,
 ogs_status ogs_gpu_solve(ogs_system* sys, double* x_inout,
                          ogs_solve_stats* stats);
 
+/* The same solve split so that one host thread can keep the solves of many
+ * systems in flight (no counterpart in the reference): _begin enqueues the
+ * start of the solve on the system's stream and returns; _poll checks
+ * without blocking whether the GPU has reached the next decision point and,
+ * if so, enqueues the next chunk of iterations (finished = 1 once x_inout
+ * holds the solution); _end waits for the rest and returns what
+ * ogs_gpu_solve returns.  The kernels, launch shapes and order are those of
+ * ogs_gpu_solve, so results are bitwise the same.  x_inout must stay valid
+ * until _end; for a host array use pinned memory to keep _poll
+ * non-blocking. */
+ogs_status ogs_gpu_solve_begin(ogs_system* sys, double* x_inout);
+ogs_status ogs_gpu_solve_poll(ogs_system* sys, int32_t* finished);
+ogs_status ogs_gpu_solve_end(ogs_system* sys, ogs_solve_stats* stats);
+
 /* Gauss-point Darcy flux q = -mat * grad(u) (CFiniteElementStd::Cal_Velocity,
  * FEM/fem_ele_std.cpp:6554-6870, driven by CRFProcess::
  * CalIntegrationPointValue, FEM/rf_pcs.cpp:5915).  q_gp: n_elements * n_gauss
@@ -385,6 +399,74 @@ ogs_status ogs_gpu_batch_solve(ogs_batch* b, ogs_batch_stats* stats);
 ogs_status ogs_gpu_batch_get_heads(const ogs_batch* b, double* heads);
 /* Total rows (sum of nx ny nz) and elements of the batch. */
 ogs_status ogs_gpu_batch_info(const ogs_batch* b, int64_t* rows, int64_t* elements);
+
+/* ------------------------------------------------------------------------
+ * Request server with continuous batching (serving extension; no
+ * counterpart in the reference).  Requests of registered classes (mesh,
+ * kind, Dirichlet set, solver configuration) arrive at any time with their
+ * own conductivity field and tolerance; admitted requests run concurrently,
+ * one CUDA stream and one device-resident equation system ("slot") each,
+ * and join or leave between chunks of Krylov iterations.  Slots are reused
+ * per class and created while their device bytes fit the HBM budget.  Each
+ * request is a fresh Linear_EQS (CheckNormRHS against bNorm = 1.0).
+ * ---------------------------------------------------------------------- */
+typedef struct ogs_server ogs_server;
+
+enum
+{
+    OGS_REQUEST_FLOW = 0,      /* steady or transient flow solve              */
+    OGS_REQUEST_TRANSPORT = 1  /* MASS_TRANSPORT step; the Darcy flux comes from
+                                  the class's head field and the request's K */
+};
+
+typedef struct
+{
+    ogs_mesh* mesh;             /* kept alive by the caller                    */
+    int32_t kind;               /* OGS_REQUEST_*                               */
+    int32_t bc_mode;            /* ogs_dirichlet_mode                          */
+    ogs_assembly_params params; /* assembly of the solved equation             */
+    ogs_assembly_params flow_params; /* transport: flux parameters (flow)     */
+    int64_t n_elements;         /* transport: elements of the mesh             */
+    const double* flow_head;    /* transport: head field (n_nodes), copied     */
+    const int64_t* bc_rows;     /* Dirichlet rows and values (host), copied    */
+    const double* bc_values;
+    int64_t n_bc;
+    ogs_solver_config solver;   /* tol is replaced by each request's tol       */
+} ogs_server_class;
+
+typedef struct
+{
+    int32_t state;              /* 0 queued, 1 running, 2 done                 */
+    int32_t status;             /* ogs_status (state 2)                        */
+    int32_t iterations;
+    int32_t refinements;
+    double rel_residual;
+    double latency_ms;          /* submit -> completion seen by the server     */
+    double queue_ms;            /* submit -> admission                         */
+    double solve_ms;            /* device time of the solve                    */
+} ogs_server_result;
+
+typedef struct
+{
+    int32_t slots, running, queued, pad0;
+    int64_t completed;
+    int64_t bytes_used, bytes_budget;
+} ogs_server_info;
+
+/* hbm_budget_bytes <= 0: 80% of the free device memory at creation. */
+ogs_status ogs_gpu_server_create(int64_t hbm_budget_bytes, int32_t max_active, ogs_server** out);
+ogs_status ogs_gpu_server_destroy(ogs_server* srv);
+ogs_status ogs_gpu_server_add_class(ogs_server* srv, const ogs_server_class* cls, int32_t* class_id);
+/* Queues a request.  elem_k: device array (n_elements) that stays valid
+ * until the request is done; out: n_nodes doubles (device or pinned host),
+ * written when the request is done. */
+ogs_status ogs_gpu_server_submit(ogs_server* srv, int32_t class_id, const double* elem_k, double tol,
+                                 double* out, int64_t* request_id);
+/* One scheduling round (never blocks on the GPU): polls running requests,
+ * retires finished ones, admits queued ones. */
+ogs_status ogs_gpu_server_progress(ogs_server* srv, int32_t* n_running, int32_t* n_queued);
+ogs_status ogs_gpu_server_result(const ogs_server* srv, int64_t request_id, ogs_server_result* r);
+ogs_status ogs_gpu_server_info(const ogs_server* srv, ogs_server_info* info);
 
 #ifdef __cplusplus
 }

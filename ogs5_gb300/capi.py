@@ -46,7 +46,11 @@ EXPORTS = [
     "ogs_gpu_csr_cg_noalloc", "ogs_gpu_get_ilu0",
     "ogs_gpu_batch_create", "ogs_gpu_batch_destroy", "ogs_gpu_batch_set_k", "ogs_gpu_batch_autotune",
     "ogs_gpu_batch_set_tuning", "ogs_gpu_batch_solve", "ogs_gpu_batch_get_heads", "ogs_gpu_batch_info",
+    "ogs_gpu_solve_begin", "ogs_gpu_solve_poll", "ogs_gpu_solve_end",
+    "ogs_gpu_server_create", "ogs_gpu_server_destroy", "ogs_gpu_server_add_class", "ogs_gpu_server_submit",
+    "ogs_gpu_server_progress", "ogs_gpu_server_result", "ogs_gpu_server_info",
 ]
+REQUEST_FLOW, REQUEST_TRANSPORT = 0, 1
 NOALLOC_MAX_ROWS = 524288
 
 
@@ -113,6 +117,24 @@ class BatchTuning(C.Structure):
 class BatchStats(C.Structure):
     _fields_ = [("iterations", C.c_int32), ("status", C.c_int32), ("refinements", C.c_int32),
                 ("pad0", C.c_int32), ("rel_residual", C.c_double), ("finish_ms", C.c_double)]
+
+
+class ServerClass(C.Structure):
+    _fields_ = [("mesh", C.c_void_p), ("kind", C.c_int32), ("bc_mode", C.c_int32),
+                ("params", AssemblyParams), ("flow_params", AssemblyParams), ("n_elements", C.c_int64),
+                ("flow_head", C.c_void_p), ("bc_rows", C.c_void_p), ("bc_values", C.c_void_p),
+                ("n_bc", C.c_int64), ("solver", SolverConfig)]
+
+
+class ServerResult(C.Structure):
+    _fields_ = [("state", C.c_int32), ("status", C.c_int32), ("iterations", C.c_int32),
+                ("refinements", C.c_int32), ("rel_residual", C.c_double), ("latency_ms", C.c_double),
+                ("queue_ms", C.c_double), ("solve_ms", C.c_double)]
+
+
+class ServerInfo(C.Structure):
+    _fields_ = [("slots", C.c_int32), ("running", C.c_int32), ("queued", C.c_int32), ("pad0", C.c_int32),
+                ("completed", C.c_int64), ("bytes_used", C.c_int64), ("bytes_budget", C.c_int64)]
 
 
 def make_params(pcs_type=GROUNDWATER_FLOW, **kw) -> AssemblyParams:
@@ -187,6 +209,20 @@ def lib():
         for name in ("ogs_gpu_batch_create", "ogs_gpu_batch_destroy", "ogs_gpu_batch_set_k",
                      "ogs_gpu_batch_autotune", "ogs_gpu_batch_set_tuning", "ogs_gpu_batch_solve",
                      "ogs_gpu_batch_get_heads", "ogs_gpu_batch_info"):
+            getattr(L, name).restype = st
+        L.ogs_gpu_solve_begin.argtypes = [vp, vp]
+        L.ogs_gpu_solve_poll.argtypes = [vp, C.POINTER(C.c_int32)]
+        L.ogs_gpu_solve_end.argtypes = [vp, C.POINTER(SolveStats)]
+        L.ogs_gpu_server_create.argtypes = [C.c_int64, C.c_int32, C.POINTER(vp)]
+        L.ogs_gpu_server_destroy.argtypes = [vp]
+        L.ogs_gpu_server_add_class.argtypes = [vp, C.POINTER(ServerClass), C.POINTER(C.c_int32)]
+        L.ogs_gpu_server_submit.argtypes = [vp, C.c_int32, vp, C.c_double, vp, C.POINTER(C.c_int64)]
+        L.ogs_gpu_server_progress.argtypes = [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+        L.ogs_gpu_server_result.argtypes = [vp, C.c_int64, C.POINTER(ServerResult)]
+        L.ogs_gpu_server_info.argtypes = [vp, C.POINTER(ServerInfo)]
+        for name in ("ogs_gpu_solve_begin", "ogs_gpu_solve_poll", "ogs_gpu_solve_end", "ogs_gpu_server_create",
+                     "ogs_gpu_server_destroy", "ogs_gpu_server_add_class", "ogs_gpu_server_submit",
+                     "ogs_gpu_server_progress", "ogs_gpu_server_result", "ogs_gpu_server_info"):
             getattr(L, name).restype = st
         L.ogs_gpu_kernel_launches.argtypes = [C.c_int32]
         L.ogs_gpu_kernel_launches.restype = C.c_int64
@@ -467,3 +503,90 @@ class Batch:
     def heads(self) -> list:
         flat = self.heads_flat()
         return np.split(flat, np.cumsum(self.sizes)[:-1])
+
+
+def solver_config(method=LS_CG, precond=PRECOND_JACOBI, max_iter=20000, tol=1e-10,
+                  precision=PRECISION_FP64, inner_tol=0.0, check_norm_rhs=True) -> SolverConfig:
+    return SolverConfig(method, precond, max_iter, precision, tol, inner_tol, 1 if check_norm_rhs else 0, 0)
+
+
+class Server:
+    """Request server with continuous batching (ogs_gpu_server_*).
+
+        srv = Server(budget_bytes=0, max_active=64)
+        c = srv.add_class(gmesh, REQUEST_FLOW, params, bc_rows, bc_values, DIRICHLET_SYMMETRIC,
+                          solver_config(precision=PRECISION_FP32_REFINED))
+        rid = srv.submit(c, k_device_tensor, 1e-10, out_tensor)
+        while srv.progress() != (0, 0): ...
+        srv.result(rid)
+    """
+
+    def __init__(self, budget_bytes=0, max_active=64):
+        self.h = None
+        h = C.c_void_p()
+        _check(lib().ogs_gpu_server_create(int(budget_bytes), int(max_active), C.byref(h)))
+        self.h = h
+        self._refs = {}
+
+    def close(self):
+        if self.h is not None and _LIB is not None:
+            lib().ogs_gpu_server_destroy(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_class(self, gmesh, kind, params, bc_rows, bc_values, bc_mode, solver, flow_params=None,
+                  flow_head=None) -> int:
+        rows = np.ascontiguousarray(bc_rows, dtype=np.int64)
+        vals = np.ascontiguousarray(bc_values, dtype=np.float64)
+        head = None if flow_head is None else _f64(flow_head)
+        c = ServerClass()
+        c.mesh = gmesh.h
+        c.kind = kind
+        c.bc_mode = bc_mode
+        c.params = params
+        if flow_params is not None:
+            c.flow_params = flow_params
+        c.n_elements = gmesh.mesh.n_elements
+        c.flow_head = _ptr(head)
+        c.bc_rows = rows.ctypes.data
+        c.bc_values = vals.ctypes.data
+        c.n_bc = len(rows)
+        c.solver = solver
+        cid = C.c_int32()
+        _check(lib().ogs_gpu_server_add_class(self.h, C.byref(c), C.byref(cid)))
+        return cid.value
+
+    def submit(self, class_id, elem_k, tol, out) -> int:
+        rid = C.c_int64()
+        _check(lib().ogs_gpu_server_submit(self.h, class_id, _ptr(elem_k), tol, _ptr(out), C.byref(rid)))
+        self._refs[rid.value] = (elem_k, out)  # inputs stay alive until the request is done
+        return rid.value
+
+    def progress(self):
+        r, q = C.c_int32(), C.c_int32()
+        _check(lib().ogs_gpu_server_progress(self.h, C.byref(r), C.byref(q)))
+        return r.value, q.value
+
+    def drain(self):
+        while self.progress() != (0, 0):
+            pass
+
+    def result(self, rid) -> dict:
+        r = ServerResult()
+        _check(lib().ogs_gpu_server_result(self.h, rid, C.byref(r)))
+        if r.state == 2:
+            self._refs.pop(rid, None)
+        return {"state": r.state, "status": r.status, "iterations": r.iterations,
+                "refinements": r.refinements, "rel_residual": r.rel_residual, "latency_ms": r.latency_ms,
+                "queue_ms": r.queue_ms, "solve_ms": r.solve_ms}
+
+    def info(self) -> dict:
+        i = ServerInfo()
+        _check(lib().ogs_gpu_server_info(self.h, C.byref(i)))
+        return {"slots": i.slots, "running": i.running, "queued": i.queued, "completed": i.completed,
+                "bytes_used": i.bytes_used, "bytes_budget": i.bytes_budget}

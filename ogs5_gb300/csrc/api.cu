@@ -144,6 +144,20 @@ static bool is_device_ptr(const void* p)
 
 using namespace ogs;
 
+// state of a solve in flight (see solve_begin / solve_advance)
+struct SolveTask
+{
+    cudaEvent_t ev = nullptr;   // marks the pending header (or x) copy
+    int phase = 0;              // 0 idle, 1 iterating, 2 copying x out, 3 finished
+    bool mixed = false, xdev = false;
+    int kind = 0;
+    cudaGraphExec_t ge = nullptr;
+    int per = 0, launched = 0, rounds = 0, chunk_before = -1;
+    double* x_out = nullptr;
+    ogs_status status = OGS_OK;
+    float ms = 0.f;
+};
+
 struct ogs_system
 {
     ogs_mesh* m = nullptr;
@@ -166,6 +180,7 @@ struct ogs_system
     double bnorm_prev = 1.0;  // Linear_EQS ctor: bNorm = 1.0
     // Dirichlet
     int nbc = 0;
+    int bc_mode = OGS_DIRICHLET_ROW_ONLY;
     int32_t* bc_rows = nullptr;
     double* bc_vals = nullptr;
     int bc_cap = 0;
@@ -192,6 +207,7 @@ struct ogs_system
     double prof_spmv_ms = 0.0, prof_solve_ms = 0.0;
     int64_t prof_spmv_n = 0, prof_solves = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    SolveTask task;
 };
 
 namespace {
@@ -390,6 +406,7 @@ extern "C" ogs_status ogs_gpu_system_destroy(ogs_system* s)
         if (s->prof_b[i]) cudaEventDestroy(s->prof_b[i]);
         if (s->prof_e[i]) cudaEventDestroy(s->prof_e[i]);
     }
+    if (s->task.ev) cudaEventDestroy(s->task.ev);
     if (s->ev0) cudaEventDestroy(s->ev0);
     if (s->ev1) cudaEventDestroy(s->ev1);
     if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
@@ -499,8 +516,15 @@ static ogs_status check_params(const ogs_assembly_params* p)
     return OGS_OK;
 }
 
-static ogs_status run_element_kernel(ogs_system* s, const ogs_assembly_params* p, const double* elem_k,
-                                     const double* u0, const double* gpv, int kind, double* q_out)
+__global__ void k_set_int(int* p, int v) { *p = v; }
+
+constexpr int kNoBadElement = 0x7fffffff;
+
+// Enqueues an element kernel (kind 0 flow, 1 transport assembly, 2 Gauss-
+// point flux); the singular-Jacobian flag lands in s->h_bad (pinned) once
+// the stream has passed this point.
+static ogs_status enqueue_element_kernel(ogs_system* s, const ogs_assembly_params* p, const double* elem_k,
+                                         const double* u0, const double* gpv, int kind, double* q_out)
 {
     ogs_mesh* m = s->m;
     AsmArgs a;
@@ -520,8 +544,8 @@ static ogs_status run_element_kernel(ogs_system* s, const ogs_assembly_params* p
     if ((st = stage_in(s, elem_k, m->n_elem, &s->ek, &a.elem_k))) return st;
     if ((st = stage_in(s, u0, m->n_nodes, &s->u0, &a.u0))) return st;
     if ((st = stage_in(s, gpv, (size_t)m->n_elem * m->ngp * 3, &s->gpv, &a.gpv))) return st;
-    const int big = 0x7fffffff;
-    OGS_CUDA_TRY(cudaMemcpyAsync(s->d_bad, &big, sizeof(int), cudaMemcpyHostToDevice, s->stream));
+    k_set_int<<<1, 1, 0, s->stream>>>(s->d_bad, kNoBadElement);
+    OGS_LAUNCH_CHECK();
     if (!launch_assembly(m, a, m->affine, kind, s->stream))
     {
         set_error("no kernel for element type %d with %d Gauss points", m->elem_type, m->ngp);
@@ -529,13 +553,26 @@ static ogs_status run_element_kernel(ogs_system* s, const ogs_assembly_params* p
     }
     OGS_LAUNCH_CHECK();
     OGS_CUDA_TRY(cudaMemcpyAsync(s->h_bad, s->d_bad, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
-    OGS_CUDA_TRY(cudaStreamSynchronize(s->stream));
-    if (*s->h_bad != big)
+    return OGS_OK;
+}
+
+static ogs_status element_flag_status(const ogs_system* s)
+{
+    if (*s->h_bad != kNoBadElement)
     {
         set_error("singular Jacobian (|det J| < DBL_EPSILON) in element %d", *s->h_bad - 1);
         return OGS_SINGULAR_JACOBIAN;
     }
     return OGS_OK;
+}
+
+static ogs_status run_element_kernel(ogs_system* s, const ogs_assembly_params* p, const double* elem_k,
+                                     const double* u0, const double* gpv, int kind, double* q_out)
+{
+    ogs_status st = enqueue_element_kernel(s, p, elem_k, u0, gpv, kind, q_out);
+    if (st) return st;
+    OGS_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    return element_flag_status(s);
 }
 
 extern "C" ogs_status ogs_gpu_assemble(ogs_system* s, const ogs_assembly_params* p, const double* elem_k,
@@ -576,8 +613,11 @@ extern "C" ogs_status ogs_gpu_gp_velocity(ogs_system* s, const ogs_assembly_para
     return OGS_OK;
 }
 
-extern "C" ogs_status ogs_gpu_set_dirichlet(ogs_system* s, const int64_t* rows, const double* values,
-                                            int64_t n_rows, int32_t mode)
+// Dirichlet set of the system: host checks and de-duplication, device
+// arrays (rows, values; for SYMMETRIC the row flags and the diagonal / lift
+// values per row).  Waits for its copies.
+static ogs_status dirichlet_upload(ogs_system* s, const int64_t* rows, const double* values, int64_t n_rows,
+                                   int32_t mode)
 {
     if (!s || (n_rows > 0 && (!rows || !values)) || n_rows < 0) { set_error("set_dirichlet: bad arguments"); return OGS_BAD_ARG; }
     if (mode != OGS_DIRICHLET_ROW_ONLY && mode != OGS_DIRICHLET_SYMMETRIC) { set_error("set_dirichlet: bad mode %d", mode); return OGS_BAD_ARG; }
@@ -640,29 +680,19 @@ extern "C" ogs_status ogs_gpu_set_dirichlet(ogs_system* s, const int64_t* rows, 
         s->bc_cap = (int)n_rows;
     }
     s->nbc = (int)n_rows;
+    s->bc_mode = mode;
     if (!n_rows) return OGS_OK;
     OGS_CUDA_TRY(cudaMemcpyAsync(s->bc_rows, r32.data(), n_rows * sizeof(int32_t), cudaMemcpyHostToDevice, s->stream));
     OGS_CUDA_TRY(cudaMemcpyAsync(s->bc_vals, vh.data(), n_rows * sizeof(double), cudaMemcpyHostToDevice,
                                  s->stream));
     OGS_CUDA_TRY(cudaMemcpyAsync(s->bc_vfirst, vfirst.data(), n_rows * sizeof(double),
                                  cudaMemcpyHostToDevice, s->stream));
-    ogs_mesh* m = s->m;
-    const int g = std::max(1, std::min(1024, (int)((n_rows + 255) / 256)));
-    if (mode == OGS_DIRICHLET_ROW_ONLY)
+    if (mode == OGS_DIRICHLET_SYMMETRIC)
     {
-        k_dirichlet_row_only<<<g, 256, 0, s->stream>>>(m->slice_ptr, m->row_len, m->sell_col, m->diag_pos,
-                                                       s->val, s->b, s->bc_rows, s->bc_vals, s->nbc);
-        OGS_LAUNCH_CHECK();
-    }
-    else
-    {
+        const int g = std::max(1, std::min(1024, (int)((n_rows + 255) / 256)));
         OGS_CUDA_TRY(cudaMemsetAsync(s->bc_flag, 0, s->n, s->stream));
         k_mark_rows<<<g, 256, 0, s->stream>>>(s->bc_flag, s->bc_valn, s->bc_valf, s->bc_rows, s->bc_vals,
                                               s->bc_vfirst, s->nbc);
-        OGS_LAUNCH_CHECK();
-        k_dirichlet_symmetric<<<vec_grid(s->n), 256, 0, s->stream>>>(m->slice_ptr, m->row_len, m->sell_col,
-                                                                      m->diag_pos, s->val, s->b, s->bc_flag,
-                                                                      s->bc_valn, s->bc_valf, s->n);
         OGS_LAUNCH_CHECK();
     }
     // the host staging vectors must outlive the copies above
@@ -670,9 +700,44 @@ extern "C" ogs_status ogs_gpu_set_dirichlet(ogs_system* s, const int64_t* rows, 
     return OGS_OK;
 }
 
-// FP32 inner CG with FP64 residual replacement (mixed.cu); x64 already holds
-// the initial guess with the Dirichlet values, dinv the FP64 Jacobi inverse.
-static ogs_status solve_fp32_refined(ogs_system* s, KState* h)
+// applies the uploaded Dirichlet set to the assembled matrix and b
+// (kernels only)
+static ogs_status dirichlet_apply(ogs_system* s)
+{
+    if (!s->nbc) return OGS_OK;
+    ogs_mesh* m = s->m;
+    if (s->bc_mode == OGS_DIRICHLET_ROW_ONLY)
+    {
+        const int g = std::max(1, std::min(1024, (s->nbc + 255) / 256));
+        k_dirichlet_row_only<<<g, 256, 0, s->stream>>>(m->slice_ptr, m->row_len, m->sell_col, m->diag_pos,
+                                                       s->val, s->b, s->bc_rows, s->bc_vals, s->nbc);
+        OGS_LAUNCH_CHECK();
+    }
+    else
+    {
+        k_dirichlet_symmetric<<<vec_grid(s->n), 256, 0, s->stream>>>(m->slice_ptr, m->row_len, m->sell_col,
+                                                                      m->diag_pos, s->val, s->b, s->bc_flag,
+                                                                      s->bc_valn, s->bc_valf, s->n);
+        OGS_LAUNCH_CHECK();
+    }
+    return OGS_OK;
+}
+
+extern "C" ogs_status ogs_gpu_set_dirichlet(ogs_system* s, const int64_t* rows, const double* values,
+                                            int64_t n_rows, int32_t mode)
+{
+    ogs_status st = dirichlet_upload(s, rows, values, n_rows, mode);
+    if (st) return st;
+    if ((st = dirichlet_apply(s))) return st;
+    OGS_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    return OGS_OK;
+}
+
+// FP32 inner CG with FP64 residual replacement (mixed.cu): buffers, FP32
+// operator, first replacement; x64 already holds the initial guess with the
+// Dirichlet values, dinv the FP64 Jacobi inverse.  Leaves the replacement
+// graph launched; the task loop reads the header next.
+static ogs_status begin_fp32_refined(ogs_system* s, KState* h)
 {
     ogs_mesh* m = s->m;
     const ogs_solver_config& c = s->cfg;
@@ -735,32 +800,6 @@ static ogs_status solve_fp32_refined(ogs_system* s, KState* h)
     }
     OGS_CUDA_TRY(cudaGraphLaunch(s->mp_replace, s->stream));
     count_launches(4);
-    int rounds = 0;  // replacement graphs count 4 launches
-    int chunk_before = -1;  // iteration count when the pending chunk was launched
-    for (;;)
-    {
-        OGS_CUDA_TRY(cudaMemcpyAsync(h, s->st, kStateHeader, cudaMemcpyDeviceToHost, s->stream));
-        OGS_CUDA_TRY(cudaStreamSynchronize(s->stream));
-        if (chunk_before >= 0)
-        {
-            if (s->prof_on) accumulate_prof(s, std::min(ogs_system::kChunk, h->iter - chunk_before));
-            chunk_before = -1;
-        }
-        if (h->done) break;
-        if (++rounds > 4 * c.max_iter + 64) { set_error("solve: mixed-precision state did not finish"); return OGS_CUDA_ERROR; }
-        if (h->replace)
-        {
-            OGS_CUDA_TRY(cudaGraphLaunch(s->mp_replace, s->stream));
-            count_launches(4);
-        }
-        else
-        {
-            chunk_before = h->iter;
-            OGS_CUDA_TRY(cudaGraphLaunch(s->mp_chunk, s->stream));
-            count_launches(3 * ogs_system::kChunk);
-        }
-    }
-    // the events of the last chunk are read at the next header read
     return OGS_OK;
 }
 
@@ -797,7 +836,39 @@ static ogs_status ilu_factor(ogs_system* s)
     return OGS_OK;
 }
 
-extern "C" ogs_status ogs_gpu_solve(ogs_system* s, double* x_inout, ogs_solve_stats* stats)
+// x = v everywhere (no-preconditioner Jacobi inverse of the FP32 mode)
+__global__ void k_fill(double* x, double v, int n)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) x[i] = v;
+}
+
+// ------------------------------------------------------------------
+// A solve as a resumable task.  solve_begin enqueues the start of the
+// solve (initial guess, Dirichlet values, preconditioner, first residual,
+// first chunk of iterations or the first FP64 replacement) and the copy of
+// the solver header behind it; solve_advance waits for (or, non-blocking,
+// checks) that copy, reads the header and enqueues what comes next -- a
+// chunk of iterations, a residual replacement, or the copy of x out.  No
+// host synchronisation between the launches of one solve, so one host
+// thread can keep many systems' solves in flight (the request server);
+// ogs_gpu_solve is begin + blocking advances, the same launches in the same
+// order.
+// ------------------------------------------------------------------
+static ogs_status task_fail(ogs_system* s, ogs_status st)
+{
+    s->task.phase = 3;
+    s->task.status = st;
+    return st;
+}
+
+static ogs_status enqueue_header(ogs_system* s)
+{
+    OGS_CUDA_TRY(cudaMemcpyAsync(s->h_st, s->st, kStateHeader, cudaMemcpyDeviceToHost, s->stream));
+    OGS_CUDA_TRY(cudaEventRecord(s->task.ev, s->stream));
+    return OGS_OK;
+}
+
+static ogs_status solve_begin(ogs_system* s, double* x_inout)
 {
     if (!s || !x_inout) { set_error("solve: NULL argument"); return OGS_BAD_ARG; }
     const ogs_solver_config& c = s->cfg;
@@ -811,16 +882,26 @@ extern "C" ogs_status ogs_gpu_solve(ogs_system* s, double* x_inout, ogs_solve_st
         set_error("solve: the FP32-inner / FP64-refinement mode takes Jacobi or no preconditioner");
         return OGS_BAD_ARG;
     }
+    if (s->task.phase == 1 || s->task.phase == 2)
+    {
+        set_error("solve: a solve of this system is still in flight");
+        return OGS_BAD_ARG;
+    }
+    SolveTask& T = s->task;
+    T = SolveTask{T.ev};
+    if (!T.ev) OGS_CUDA_TRY(cudaEventCreateWithFlags(&T.ev, cudaEventDisableTiming));
+    T.x_out = x_inout;
+    T.xdev = is_device_ptr(x_inout);
+    T.mixed = c.precision == OGS_PRECISION_FP32_REFINED;
+    T.kind = c.method == OGS_LS_CG ? SK_CG : SK_BICGSTAB;
     if (c.precond == OGS_PRECOND_ILU0)
     {
         ogs_status st = ilu_factor(s);
         if (st) return st;
     }
-    const int kind = c.method == OGS_LS_CG ? SK_CG : SK_BICGSTAB;
     const size_t nb = (size_t)s->n * sizeof(double);
-    const bool xdev = is_device_ptr(x_inout);
     OGS_CUDA_TRY(cudaEventRecord(s->ev0, s->stream));
-    OGS_CUDA_TRY(cudaMemcpyAsync(s->x, x_inout, nb, xdev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+    OGS_CUDA_TRY(cudaMemcpyAsync(s->x, x_inout, nb, T.xdev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
                                  s->stream));
     if (s->nbc)
     {
@@ -829,18 +910,16 @@ extern "C" ogs_status ogs_gpu_solve(ogs_system* s, double* x_inout, ogs_solve_st
         OGS_LAUNCH_CHECK();
     }
     SolveArgs a = make_solve_args(s);
-    const bool mixed = c.precision == OGS_PRECISION_FP32_REFINED;
     if (a.precond == OGS_PRECOND_JACOBI)
     {
         launch_dinv(s->val, s->m->diag_pos, s->dinv, s->n, s->stream);
         OGS_LAUNCH_CHECK();
     }
-    else if (mixed)
+    else if (T.mixed)
     {
         // no preconditioner: M^-1 = I
-        std::vector<double> ones(s->n, 1.0);
-        OGS_CUDA_TRY(cudaMemcpyAsync(s->dinv, ones.data(), nb, cudaMemcpyHostToDevice, s->stream));
-        OGS_CUDA_TRY(cudaStreamSynchronize(s->stream));
+        k_fill<<<vec_grid(s->n), kThreads, 0, s->stream>>>(s->dinv, 1.0, s->n);
+        OGS_LAUNCH_CHECK();
     }
     KState* h = s->h_st;
     std::memset(h, 0, kStateHeader);
@@ -849,9 +928,9 @@ extern "C" ogs_status ogs_gpu_solve(ogs_system* s, double* x_inout, ogs_solve_st
     h->error = 1.0e10;
     h->max_iter = c.max_iter;
     h->alpha = h->omega = h->rho0 = 1.0;
-    if (mixed)
+    if (T.mixed)
     {
-        ogs_status st = solve_fp32_refined(s, h);
+        ogs_status st = begin_fp32_refined(s, h);
         if (st) return st;
     }
     else
@@ -859,62 +938,184 @@ extern "C" ogs_status ogs_gpu_solve(ogs_system* s, double* x_inout, ogs_solve_st
         h->nb_spmv = vec_grid(s->n);
         h->nb_upd = red_grid(s->n);
         OGS_CUDA_TRY(cudaMemcpyAsync(s->st, h, kStateHeader, cudaMemcpyHostToDevice, s->stream));
-        launch_krylov_init(a, kind, s->stream);
+        launch_krylov_init(a, T.kind, s->stream);
         OGS_LAUNCH_CHECK();
-        count_launches(krylov_init_launches(kind, a.precond) - 1);
-        cudaGraphExec_t ge;
-        int per = 0;
-        ogs_status st = get_chunk(s, kind, a, &ge, &per);
+        count_launches(krylov_init_launches(T.kind, a.precond) - 1);
+        ogs_status st = get_chunk(s, T.kind, a, &T.ge, &T.per);
         if (st) return st;
-        int launched = 0;
-        int chunk_before = -1;
-        for (;;)
+    }
+    {
+        ogs_status st = enqueue_header(s);
+        if (st) return st;
+    }
+    T.phase = 1;
+    return OGS_OK;
+}
+
+// One step of the task.  block: wait for the pending header copy; else
+// return at once (finished = false) while it is in flight.
+static ogs_status solve_advance(ogs_system* s, bool block, bool* finished)
+{
+    SolveTask& T = s->task;
+    *finished = false;
+    if (T.phase == 0 || T.phase == 3)
+    {
+        *finished = T.phase == 3;
+        return OGS_OK;
+    }
+    if (block)
+    {
+        cudaError_t e = cudaEventSynchronize(T.ev);
+        if (e != cudaSuccess) { set_error("solve: %s", cudaGetErrorString(e)); return task_fail(s, OGS_CUDA_ERROR); }
+    }
+    else
+    {
+        cudaError_t e = cudaEventQuery(T.ev);
+        if (e == cudaErrorNotReady) return OGS_OK;
+        if (e != cudaSuccess) { set_error("solve: %s", cudaGetErrorString(e)); return task_fail(s, OGS_CUDA_ERROR); }
+    }
+    const ogs_solver_config& c = s->cfg;
+    KState* h = s->h_st;
+    if (T.phase == 2)
+    {
+        // x has landed: close the solve
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, s->ev0, s->ev1);
+        s->bnorm_prev = h->bnorm;
+        if (s->prof_on)
         {
-            OGS_CUDA_TRY(cudaMemcpyAsync(h, s->st, kStateHeader, cudaMemcpyDeviceToHost, s->stream));
-            OGS_CUDA_TRY(cudaStreamSynchronize(s->stream));
-            if (chunk_before >= 0 && s->prof_on)
-                accumulate_prof(s, std::min(per, h->iter - chunk_before + (kind == SK_BICGSTAB && h->done ? 1 : 0)));
-            chunk_before = -1;
-            if (h->done || launched > c.max_iter + per) break;
-            chunk_before = h->iter;
-            OGS_CUDA_TRY(cudaGraphLaunch(ge, s->stream));
-            count_launches((int64_t)per * kernels_per_iteration(kind, a.precond));
-            launched += per;
+            s->prof_solve_ms += ms;
+            s->prof_solves += 1;
+        }
+        T.ms = ms;
+        T.status = (ogs_status)h->status;
+        T.phase = 3;
+        *finished = true;
+        return OGS_OK;
+    }
+    // phase 1: a header copy has landed
+    if (T.mixed)
+    {
+        if (T.chunk_before >= 0)
+        {
+            if (s->prof_on) accumulate_prof(s, std::min(ogs_system::kChunk, h->iter - T.chunk_before));
+            T.chunk_before = -1;
         }
         if (!h->done)
         {
-            set_error("solve: solver state did not finish");
-            return OGS_CUDA_ERROR;
+            if (++T.rounds > 4 * c.max_iter + 64)
+            {
+                set_error("solve: mixed-precision state did not finish");
+                return task_fail(s, OGS_CUDA_ERROR);
+            }
+            if (h->replace)
+            {
+                if (cudaGraphLaunch(s->mp_replace, s->stream) != cudaSuccess) return task_fail(s, OGS_CUDA_ERROR);
+                count_launches(4);
+            }
+            else
+            {
+                T.chunk_before = h->iter;
+                if (cudaGraphLaunch(s->mp_chunk, s->stream) != cudaSuccess) return task_fail(s, OGS_CUDA_ERROR);
+                count_launches(3 * ogs_system::kChunk);
+            }
+            if (enqueue_header(s)) return task_fail(s, OGS_CUDA_ERROR);
+            return OGS_OK;
+        }
+    }
+    else
+    {
+        if (T.chunk_before >= 0 && s->prof_on)
+            accumulate_prof(s, std::min(T.per, h->iter - T.chunk_before + (T.kind == SK_BICGSTAB && h->done ? 1 : 0)));
+        T.chunk_before = -1;
+        if (!h->done)
+        {
+            if (T.launched > c.max_iter + T.per)
+            {
+                set_error("solve: solver state did not finish");
+                return task_fail(s, OGS_CUDA_ERROR);
+            }
+            T.chunk_before = h->iter;
+            if (cudaGraphLaunch(T.ge, s->stream) != cudaSuccess) return task_fail(s, OGS_CUDA_ERROR);
+            count_launches((int64_t)T.per * kernels_per_iteration(T.kind, s->cfg.precond));
+            T.launched += T.per;
+            if (enqueue_header(s)) return task_fail(s, OGS_CUDA_ERROR);
+            return OGS_OK;
         }
         if (h->finish_s)
         {
+            SolveArgs a = make_solve_args(s);
             launch_bicgstab_finish(a, s->stream);
-            OGS_LAUNCH_CHECK();
+            if (cudaGetLastError() != cudaSuccess) return task_fail(s, OGS_CUDA_ERROR);
+            count_launches(1);
         }
     }
-    OGS_CUDA_TRY(cudaMemcpyAsync(x_inout, s->x, nb, xdev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
-                                 s->stream));
-    OGS_CUDA_TRY(cudaEventRecord(s->ev1, s->stream));
-    OGS_CUDA_TRY(cudaStreamSynchronize(s->stream));
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, s->ev0, s->ev1);
-    s->bnorm_prev = h->bnorm;
-    if (s->prof_on)
+    // done: x out, then close at the next advance
+    const size_t nb = (size_t)s->n * sizeof(double);
+    if (cudaMemcpyAsync(T.x_out, s->x, nb, T.xdev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                        s->stream) != cudaSuccess ||
+        cudaEventRecord(s->ev1, s->stream) != cudaSuccess || cudaEventRecord(T.ev, s->stream) != cudaSuccess)
     {
-        s->prof_solve_ms += ms;
-        s->prof_solves += 1;
+        set_error("solve: copying x out failed");
+        return task_fail(s, OGS_CUDA_ERROR);
     }
+    T.phase = 2;
+    return OGS_OK;
+}
+
+static ogs_status solve_end(ogs_system* s, ogs_solve_stats* stats)
+{
+    SolveTask& T = s->task;
+    const KState* h = s->h_st;
     if (stats)
     {
         std::memset(stats, 0, sizeof *stats);
         stats->iterations = h->iter;
-        stats->status = h->status;
+        stats->status = T.status;
         stats->rel_residual = h->error;
         stats->b_norm = h->bnorm;
         stats->refinements = h->replacements;
-        stats->solve_ms = ms;
+        stats->solve_ms = T.ms;
     }
-    return h->status == OGS_OK ? OGS_OK : (ogs_status)h->status;
+    const ogs_status st = T.status;
+    T.phase = 0;
+    return st;
+}
+
+extern "C" ogs_status ogs_gpu_solve(ogs_system* s, double* x_inout, ogs_solve_stats* stats)
+{
+    ogs_status st = solve_begin(s, x_inout);
+    if (st) return st;
+    bool fin = false;
+    while (!fin)
+    {
+        st = solve_advance(s, true, &fin);
+        if (st) { s->task.phase = 0; return st; }
+    }
+    return solve_end(s, stats);
+}
+
+extern "C" ogs_status ogs_gpu_solve_begin(ogs_system* s, double* x_inout) { return solve_begin(s, x_inout); }
+
+extern "C" ogs_status ogs_gpu_solve_poll(ogs_system* s, int32_t* finished)
+{
+    if (!s || !finished) { set_error("solve_poll: NULL argument"); return OGS_BAD_ARG; }
+    bool fin = false;
+    ogs_status st = solve_advance(s, false, &fin);
+    *finished = fin ? 1 : 0;
+    return st;
+}
+
+extern "C" ogs_status ogs_gpu_solve_end(ogs_system* s, ogs_solve_stats* stats)
+{
+    if (!s) { set_error("solve_end: NULL system"); return OGS_BAD_ARG; }
+    bool fin = s->task.phase == 3;
+    while (!fin && s->task.phase != 0)
+    {
+        ogs_status st = solve_advance(s, true, &fin);
+        if (st) { s->task.phase = 0; return st; }
+    }
+    return solve_end(s, stats);
 }
 
 extern "C" ogs_status ogs_gpu_spmv(ogs_system* s, const double* x, double* y)
@@ -1027,3 +1228,67 @@ extern "C" ogs_status ogs_gpu_profile(ogs_system* s, int32_t enable, ogs_profile
     }
     return OGS_OK;
 }
+
+// ------------------------------------------------------------------
+// Internal entry points of the request server (server.cu): the pieces of
+// one solve request, enqueued on the system's stream without host waits.
+// ------------------------------------------------------------------
+namespace ogs {
+
+cudaStream_t system_stream(ogs_system* s) { return s->stream; }
+
+int64_t system_rows(const ogs_system* s) { return s->n; }
+
+// device bytes of a system on mesh m (matrix values, Krylov vectors,
+// solver state, Dirichlet arrays, FP32-mode block when fp32)
+size_t system_bytes(const ogs_mesh* m, bool fp32)
+{
+    const size_t n = (size_t)m->n_nodes;
+    const size_t vec = ((n * 8 + 255) & ~size_t(255)) * 11;
+    size_t b = (size_t)m->sell_nnz * 8 + vec + sizeof(KState) + 3 * n * 8 + n;
+    if (fp32)
+    {
+        const size_t v4 = (n * 4 + 255) & ~size_t(255);
+        const bool dia = m->n_up == 14 || m->n_up == 8 || m->n_up == 5;
+        b += 7 * v4 + (dia ? (size_t)m->n_up * n * 4 : (size_t)m->sell_nnz * 4);
+    }
+    return b;
+}
+
+// a fresh Linear_EQS for every request: bNorm = 1.0 (equation_class.cpp:
+// 85-143), tolerance of the request
+void system_reset_request(ogs_system* s, double tol)
+{
+    s->bnorm_prev = 1.0;
+    s->cfg.tol = tol;
+}
+
+ogs_status system_upload_dirichlet(ogs_system* s, const int64_t* rows, const double* vals, int64_t n, int32_t mode)
+{
+    return dirichlet_upload(s, rows, vals, n, mode);
+}
+
+// Initialize + element assembly + the uploaded Dirichlet set, enqueued
+ogs_status system_enqueue_assembly(ogs_system* s, const ogs_assembly_params* p, const double* elem_k,
+                                   const double* u0, const double* gpv)
+{
+    ogs_status st = ogs_gpu_initialize(s);
+    if (st) return st;
+    if ((st = enqueue_element_kernel(s, p, elem_k, u0, gpv, p->pcs_type == OGS_PCS_MASS_TRANSPORT ? 1 : 0,
+                                     nullptr)))
+        return st;
+    return dirichlet_apply(s);
+}
+
+// Gauss-point Darcy flux into the device array q (enqueued)
+ogs_status system_enqueue_velocity(ogs_system* s, const ogs_assembly_params* p, const double* elem_k,
+                                   const double* u, double* q)
+{
+    return enqueue_element_kernel(s, p, elem_k, u, nullptr, 2, q);
+}
+
+// singular-Jacobian flag of the last element kernel (valid once the stream
+// has passed it)
+ogs_status system_element_status(const ogs_system* s) { return element_flag_status(s); }
+
+}  // namespace ogs

@@ -1,0 +1,379 @@
+// server.cu -- request server with continuous batching (serving extension;
+// no counterpart in the reference, where one ogs process runs one deck).
+//
+// Flow and transport solve requests arrive at any time.  Each request
+// belongs to a class (mesh, kind, Dirichlet set) registered once; its own
+// data is a conductivity field on the device, a tolerance and an output
+// array.  The server keeps a pool of equation systems ("slots") per class,
+// each with its own CUDA stream, matrices and Krylov state resident on the
+// device, and walks one scheduling round per ogs_gpu_server_progress call:
+//
+//   * every running request is polled without blocking (ogs_gpu_solve_poll:
+//     the next chunk of iterations is enqueued as soon as the GPU reached the
+//     previous decision point), finished ones release their slot;
+//   * queued requests are admitted in arrival order as slots free up: an
+//     idle slot of the class is reused, or a new one is created while the
+//     device bytes of all slots stay within the HBM budget (idle slots of
+//     other classes are released, least recently used first, to make room);
+//   * admission enqueues the whole request -- initial guess, assembly,
+//     Dirichlet elimination, (for transport) Gauss-point flux, start of the
+//     solve -- on the slot's stream with no host wait.
+//
+// So requests that arrive while others run join at the next round, and the
+// work of all admitted requests overlaps on the GPU (one stream each).  A
+// request runs exactly the kernels, launch shapes and order of the
+// single-system API on a system of its own, so its result does not depend on
+// what else is in flight.
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <deque>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+
+namespace ogs {
+cudaStream_t system_stream(ogs_system* s);
+int64_t system_rows(const ogs_system* s);
+size_t system_bytes(const ogs_mesh* m, bool fp32);
+void system_reset_request(ogs_system* s, double tol);
+ogs_status system_upload_dirichlet(ogs_system* s, const int64_t* rows, const double* vals, int64_t n, int32_t mode);
+ogs_status system_enqueue_assembly(ogs_system* s, const ogs_assembly_params* p, const double* elem_k,
+                                   const double* u0, const double* gpv);
+ogs_status system_enqueue_velocity(ogs_system* s, const ogs_assembly_params* p, const double* elem_k,
+                                   const double* u, double* q);
+ogs_status system_element_status(const ogs_system* s);
+}  // namespace ogs
+
+using namespace ogs;
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct SrvClass
+{
+    ogs_server_class c;
+    std::vector<int64_t> bc_rows;
+    std::vector<double> bc_vals;
+    double* x0 = nullptr;      // initial guess (Dirichlet values, else 0), device
+    double* u_flow = nullptr;  // transport: head field of the Gauss-point flux, device
+    size_t bytes = 0;          // device bytes of one slot
+    int64_t n = 0, ngp = 0, ne = 0;
+};
+
+struct SrvSlot
+{
+    int cls = -1;
+    ogs_system* sys = nullptr;
+    double* q = nullptr;       // transport: Gauss-point flux
+    bool busy = false;
+    int64_t last_used = 0;
+};
+
+struct SrvReq
+{
+    int cls = 0;
+    const double* elem_k = nullptr;
+    double* out = nullptr;
+    double tol = 0.0;
+    int state = 0;             // 0 queued, 1 running, 2 done
+    int slot = -1;
+    ogs_status status = OGS_OK;
+    ogs_solve_stats st{};
+    Clock::time_point t_submit, t_admit, t_done;
+};
+
+}  // namespace
+
+struct ogs_server
+{
+    size_t budget = 0, used = 0;
+    int max_active = 0;
+    std::vector<SrvClass> classes;
+    std::vector<SrvSlot> slots;
+    std::vector<SrvReq> reqs;
+    std::deque<int64_t> queue;
+    std::vector<int64_t> running;
+    int64_t tick = 0;
+    int64_t completed = 0;
+};
+
+namespace {
+
+void release_slot(ogs_server* S, size_t k)
+{
+    SrvSlot& sl = S->slots[k];
+    if (sl.sys) ogs_gpu_system_destroy(sl.sys);
+    cudaFree(sl.q);
+    S->used -= S->classes[sl.cls].bytes;
+    S->slots.erase(S->slots.begin() + k);
+    for (int64_t id : S->running)
+        if (S->reqs[id].slot > (int)k) S->reqs[id].slot -= 1;
+}
+
+// a slot of class c: idle one, or a new one within the budget
+int acquire_slot(ogs_server* S, int c)
+{
+    for (size_t k = 0; k < S->slots.size(); k++)
+        if (!S->slots[k].busy && S->slots[k].cls == c) return (int)k;
+    if ((int)S->running.size() >= S->max_active) return -1;
+    const SrvClass& C = S->classes[c];
+    while (S->used + C.bytes > S->budget)
+    {
+        int lru = -1;
+        for (size_t k = 0; k < S->slots.size(); k++)
+            if (!S->slots[k].busy && (lru < 0 || S->slots[k].last_used < S->slots[lru].last_used)) lru = (int)k;
+        if (lru < 0) return -1;
+        release_slot(S, lru);
+    }
+    SrvSlot sl;
+    sl.cls = c;
+    if (ogs_gpu_system_create(C.c.mesh, nullptr, &sl.sys)) return -2;
+    if (ogs_gpu_configure(sl.sys, &C.c.solver) ||
+        system_upload_dirichlet(sl.sys, C.bc_rows.data(), C.bc_vals.data(), (int64_t)C.bc_rows.size(),
+                                C.c.bc_mode))
+    {
+        ogs_gpu_system_destroy(sl.sys);
+        return -2;
+    }
+    if (C.c.kind == OGS_REQUEST_TRANSPORT && cudaMalloc(&sl.q, (size_t)C.ne * C.ngp * 3 * sizeof(double)) != cudaSuccess)
+    {
+        cudaGetLastError();
+        ogs_gpu_system_destroy(sl.sys);
+        set_error("server: no device memory for a transport slot");
+        return -2;
+    }
+    S->used += C.bytes;
+    S->slots.push_back(sl);
+    return (int)S->slots.size() - 1;
+}
+
+ogs_status start(ogs_server* S, int64_t id, int k)
+{
+    SrvReq& R = S->reqs[id];
+    SrvSlot& sl = S->slots[k];
+    const SrvClass& C = S->classes[R.cls];
+    ogs_system* s = sl.sys;
+    cudaStream_t st = system_stream(s);
+    system_reset_request(s, R.tol);
+    OGS_CUDA_TRY(cudaMemcpyAsync(R.out, C.x0, C.n * sizeof(double), cudaMemcpyDefault, st));
+    ogs_status e;
+    if (C.c.kind == OGS_REQUEST_TRANSPORT)
+    {
+        if ((e = system_enqueue_velocity(s, &C.c.flow_params, R.elem_k, C.u_flow, sl.q))) return e;
+        if ((e = system_enqueue_assembly(s, &C.c.params, nullptr, C.x0, sl.q))) return e;
+    }
+    else if ((e = system_enqueue_assembly(s, &C.c.params, R.elem_k, C.x0, nullptr)))
+        return e;
+    return ogs_gpu_solve_begin(s, R.out);
+}
+
+double ms_between(Clock::time_point a, Clock::time_point b)
+{
+    return std::chrono::duration<double, std::milli>(b - a).count();
+}
+
+}  // namespace
+
+extern "C" ogs_status ogs_gpu_server_create(int64_t hbm_budget_bytes, int32_t max_active, ogs_server** out)
+{
+    if (!out || max_active <= 0) { set_error("server_create: bad arguments"); return OGS_BAD_ARG; }
+    ogs_server* S = new ogs_server;
+    if (hbm_budget_bytes <= 0)
+    {
+        size_t fr = 0, tot = 0;
+        if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) { delete S; set_error("server_create: no device"); return OGS_CUDA_ERROR; }
+        S->budget = (size_t)(0.8 * (double)fr);
+    }
+    else
+        S->budget = (size_t)hbm_budget_bytes;
+    S->max_active = max_active;
+    *out = S;
+    return OGS_OK;
+}
+
+extern "C" ogs_status ogs_gpu_server_destroy(ogs_server* S)
+{
+    if (!S) return OGS_OK;
+    for (SrvSlot& sl : S->slots)
+    {
+        if (sl.sys) ogs_gpu_system_destroy(sl.sys);
+        cudaFree(sl.q);
+    }
+    for (SrvClass& C : S->classes)
+    {
+        cudaFree(C.x0);
+        cudaFree(C.u_flow);
+    }
+    delete S;
+    return OGS_OK;
+}
+
+extern "C" ogs_status ogs_gpu_server_add_class(ogs_server* S, const ogs_server_class* c, int32_t* class_id)
+{
+    if (!S || !c || !c->mesh || !class_id || c->n_bc < 0 || (c->n_bc && (!c->bc_rows || !c->bc_values)))
+    {
+        set_error("server_add_class: bad arguments");
+        return OGS_BAD_ARG;
+    }
+    if (c->kind != OGS_REQUEST_FLOW && c->kind != OGS_REQUEST_TRANSPORT)
+    {
+        set_error("server_add_class: kind %d", c->kind);
+        return OGS_BAD_ARG;
+    }
+    SrvClass C;
+    C.c = *c;
+    int64_t n = 0, nnz = 0;
+    ogs_gpu_mesh_info(c->mesh, &n, &nnz);
+    C.n = n;
+    C.ngp = ogs_gpu_mesh_gauss_points(c->mesh);
+    C.ne = c->n_elements;
+    C.bc_rows.assign(c->bc_rows, c->bc_rows + c->n_bc);
+    C.bc_vals.assign(c->bc_values, c->bc_values + c->n_bc);
+    std::vector<double> x0(n, 0.0);
+    for (int64_t q = 0; q < c->n_bc; q++)
+        if (c->bc_rows[q] >= 0 && c->bc_rows[q] < n) x0[c->bc_rows[q]] = c->bc_values[q];
+    OGS_CUDA_TRY(cudaMalloc(&C.x0, std::max<int64_t>(1, n) * sizeof(double)));
+    OGS_CUDA_TRY(cudaMemcpy(C.x0, x0.data(), n * sizeof(double), cudaMemcpyHostToDevice));
+    if (c->kind == OGS_REQUEST_TRANSPORT)
+    {
+        if (!c->flow_head || C.ne <= 0)
+        {
+            cudaFree(C.x0);
+            set_error("server_add_class: transport needs flow_head and n_elements");
+            return OGS_BAD_ARG;
+        }
+        OGS_CUDA_TRY(cudaMalloc(&C.u_flow, std::max<int64_t>(1, n) * sizeof(double)));
+        OGS_CUDA_TRY(cudaMemcpy(C.u_flow, c->flow_head, n * sizeof(double), cudaMemcpyDefault));
+    }
+    C.bytes = system_bytes(c->mesh, c->solver.precision == OGS_PRECISION_FP32_REFINED);
+    if (c->kind == OGS_REQUEST_TRANSPORT) C.bytes += (size_t)C.ne * C.ngp * 3 * sizeof(double);
+    C.c.bc_rows = nullptr;
+    C.c.bc_values = nullptr;
+    C.c.flow_head = nullptr;
+    S->classes.push_back(std::move(C));
+    *class_id = (int32_t)S->classes.size() - 1;
+    return OGS_OK;
+}
+
+extern "C" ogs_status ogs_gpu_server_submit(ogs_server* S, int32_t class_id, const double* elem_k, double tol,
+                                            double* out, int64_t* request_id)
+{
+    if (!S || !out || !request_id || class_id < 0 || class_id >= (int32_t)S->classes.size() || !(tol > 0.0) ||
+        !elem_k)
+    {
+        set_error("server_submit: bad arguments");
+        return OGS_BAD_ARG;
+    }
+    SrvReq R;
+    R.cls = class_id;
+    R.elem_k = elem_k;
+    R.out = out;
+    R.tol = tol;
+    R.t_submit = Clock::now();
+    S->reqs.push_back(R);
+    *request_id = (int64_t)S->reqs.size() - 1;
+    S->queue.push_back(*request_id);
+    return OGS_OK;
+}
+
+extern "C" ogs_status ogs_gpu_server_progress(ogs_server* S, int32_t* n_running, int32_t* n_queued)
+{
+    if (!S) { set_error("server_progress: NULL server"); return OGS_BAD_ARG; }
+    S->tick += 1;
+    // running requests: non-blocking polls
+    for (size_t q = 0; q < S->running.size();)
+    {
+        const int64_t id = S->running[q];
+        SrvReq& R = S->reqs[id];
+        SrvSlot& sl = S->slots[R.slot];
+        int32_t fin = 0;
+        ogs_status st = ogs_gpu_solve_poll(sl.sys, &fin);
+        if (st == OGS_OK && !fin)
+        {
+            q++;
+            continue;
+        }
+        ogs_status es = ogs_gpu_solve_end(sl.sys, &R.st);
+        R.status = st != OGS_OK ? st : es;
+        if (R.status == OGS_OK || R.status == OGS_NONFINITE)
+        {
+            const ogs_status ef = system_element_status(sl.sys);
+            if (ef) R.status = ef;
+        }
+        R.t_done = Clock::now();
+        R.state = 2;
+        sl.busy = false;
+        sl.last_used = S->tick;
+        S->completed += 1;
+        S->running.erase(S->running.begin() + q);
+    }
+    // admission in arrival order
+    while (!S->queue.empty())
+    {
+        const int64_t id = S->queue.front();
+        SrvReq& R = S->reqs[id];
+        const int k = acquire_slot(S, R.cls);
+        if (k == -2) return OGS_OOM;
+        if (k < 0) break;
+        S->queue.pop_front();
+        S->slots[k].busy = true;
+        R.slot = k;
+        R.state = 1;
+        R.t_admit = Clock::now();
+        ogs_status st = start(S, id, k);
+        if (st)
+        {
+            // the request fails on its own; its slot goes back to the pool
+            R.status = st;
+            R.state = 2;
+            R.t_done = Clock::now();
+            S->slots[k].busy = false;
+            S->completed += 1;
+            cudaStreamSynchronize(system_stream(S->slots[k].sys));
+            continue;
+        }
+        S->running.push_back(id);
+    }
+    if (n_running) *n_running = (int32_t)S->running.size();
+    if (n_queued) *n_queued = (int32_t)S->queue.size();
+    return OGS_OK;
+}
+
+extern "C" ogs_status ogs_gpu_server_result(const ogs_server* S, int64_t request_id, ogs_server_result* r)
+{
+    if (!S || !r || request_id < 0 || request_id >= (int64_t)S->reqs.size())
+    {
+        set_error("server_result: bad arguments");
+        return OGS_BAD_ARG;
+    }
+    const SrvReq& R = S->reqs[request_id];
+    std::memset(r, 0, sizeof *r);
+    r->state = R.state;
+    r->status = R.status;
+    if (R.state == 2)
+    {
+        r->iterations = R.st.iterations;
+        r->refinements = R.st.refinements;
+        r->rel_residual = R.st.rel_residual;
+        r->latency_ms = ms_between(R.t_submit, R.t_done);
+        r->queue_ms = R.slot >= 0 ? ms_between(R.t_submit, R.t_admit) : r->latency_ms;
+        r->solve_ms = R.st.solve_ms;
+    }
+    return OGS_OK;
+}
+
+extern "C" ogs_status ogs_gpu_server_info(const ogs_server* S, ogs_server_info* info)
+{
+    if (!S || !info) { set_error("server_info: bad arguments"); return OGS_BAD_ARG; }
+    std::memset(info, 0, sizeof *info);
+    info->slots = (int32_t)S->slots.size();
+    info->running = (int32_t)S->running.size();
+    info->queued = (int32_t)S->queue.size();
+    info->completed = S->completed;
+    info->bytes_used = (int64_t)S->used;
+    info->bytes_budget = (int64_t)S->budget;
+    return OGS_OK;
+}
