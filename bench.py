@@ -388,6 +388,187 @@ def batch_leg(capi, torch, steps=2, n_real=BATCH_REALS, n_hi=96, plain=True, tol
     return out
 
 
+# ------------------------------------------------------------------
+# Serving: Poisson arrivals of flow and transport requests
+# ------------------------------------------------------------------
+SERVE_RATE = 200.0        # requests per second
+SERVE_REQUESTS = 400
+SERVE_SEED = 5
+SERVE_DOF = (1e4, 2e6)
+SERVE_CLASSES = 5         # log-spaced size classes per mesh type (meshes are cached)
+SERVE_WARM_SLOTS = 4      # slots per class created before the timed run
+SERVE_WORKLOAD = ("Poisson arrivals 200/s of flow (steady GWF, heads 10/0 m on the x faces) and transport "
+                  "(one MASS_TRANSPORT step, flux from a linear head field) requests on quad, hex and "
+                  "hex-split-tet meshes, 1e4-2e6 DOF log-uniform (5 size classes per type), log-normal K "
+                  "per request, tol 1e-6 or 1e-10")
+
+
+def serve_meshes(n_classes=SERVE_CLASSES):
+    """Mesh of every (type, size class): quad n x n cells, hex and tet n^3 cells."""
+    from ogs5_gb300 import mesh as M
+    dofs = np.geomspace(SERVE_DOF[0], SERVE_DOF[1], n_classes)
+    out = {}
+    for t in ("quad", "hex", "tet"):
+        for c, d in enumerate(dofs):
+            if t == "quad":
+                n = max(4, int(round(np.sqrt(d))) - 1)
+                out[(t, c)] = M.structured_quad(n, n)
+            else:
+                n = max(3, int(round(np.cbrt(d))) - 1)
+                out[(t, c)] = M.structured_hex(n, n, n) if t == "hex" else M.structured_tet(n, n, n)
+    return dofs, out
+
+
+def serve_requests(torch, dofs, meshes, n_req=SERVE_REQUESTS, rate=SERVE_RATE, seed=SERVE_SEED):
+    from ogs5_gb300 import fields
+    rng = np.random.default_rng(seed)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, n_req))
+    reqs = []
+    for q in range(n_req):
+        t = ("quad", "hex", "tet")[rng.integers(3)]
+        d = np.exp(rng.uniform(np.log(SERVE_DOF[0]), np.log(SERVE_DOF[1])))
+        c = int(np.argmin(np.abs(np.log(dofs) - np.log(d))))
+        kind = int(rng.integers(2))
+        tol = 1e-6 if rng.integers(2) else 1e-10
+        m = meshes[(t, c)]
+        var = float(rng.uniform(0.5, 1.5))
+        k = fields.lognormal_k_device(m.shape, np.log(1e-5), var, 8.0, seed=seed * 100000 + q)
+        if k.numel() != m.n_elements:  # tets: the field of the parent hex
+            k = k.repeat_interleave(m.n_elements // k.numel())
+        reqs.append({"t": float(arrivals[q]), "key": (t, c), "kind": kind, "tol": tol, "k": k})
+    return reqs
+
+
+def serve_class_setup(capi, m, kind):
+    lf, rf = m.face_nodes(0, 0), m.face_nodes(0, 1)
+    if kind == 0:
+        rows = np.concatenate([lf, rf])
+        vals = np.concatenate([np.full(len(lf), 10.0), np.zeros(len(rf))])
+        p = capi.make_params(capi.GROUNDWATER_FLOW, steady=1)
+        return rows, vals, capi.DIRICHLET_SYMMETRIC, p, None, None
+    p = capi.make_params(capi.MASS_TRANSPORT, dt=3600.0, porosity=0.3, alpha_l=1.0, alpha_t=0.1, diffusion=1e-9)
+    head = 10.0 * (1.0 - m.x / m.x.max())
+    return lf, np.ones(len(lf)), capi.DIRICHLET_ROW_ONLY, p, capi.make_params(capi.GROUNDWATER_FLOW), head
+
+
+def serve_leg(capi, torch, n_req=SERVE_REQUESTS):
+    t_setup = time.perf_counter()
+    dofs, meshes = serve_meshes()
+    gms = {key: capi.GpuMesh(m) for key, m in meshes.items()}
+    reqs = serve_requests(torch, dofs, meshes, n_req=n_req)
+    print(f"serve: meshes and fields {time.perf_counter() - t_setup:.1f} s", file=sys.stderr)
+    srv = capi.Server(max_active=128)
+    cls = {}
+    for key, m in meshes.items():
+        for kind in (0, 1):
+            rows, vals, mode, p, fp, head = serve_class_setup(capi, m, kind)
+            cfg = (capi.solver_config(capi.LS_CG, capi.PRECOND_JACOBI, 20000,
+                                      precision=capi.PRECISION_FP32_REFINED) if kind == 0 else
+                   capi.solver_config(capi.LS_BICGSTAB, capi.PRECOND_JACOBI, 5000))
+            cls[(key, kind)] = srv.add_class(gms[key], kind, p, rows, vals, mode, cfg, flow_params=fp,
+                                             flow_head=head)
+    outs = [torch.zeros(meshes[r["key"]].n_nodes, dtype=torch.float64, device="cuda") for r in reqs]
+    # warm-up: SERVE_WARM_SLOTS concurrent requests of every class, so each
+    # class starts with that many slots whose buffers and graphs exist
+    warm_out = []
+    for (key, kind), cid in cls.items():
+        k = next((r["k"] for r in reqs if r["key"] == key), None)
+        if k is None:
+            continue
+        for _ in range(SERVE_WARM_SLOTS):
+            warm_out.append(torch.zeros(meshes[key].n_nodes, dtype=torch.float64, device="cuda"))
+            srv.submit(cid, k, 1e-6, warm_out[-1])
+    srv.drain()
+    del warm_out
+    torch.cuda.synchronize()
+    print(f"serve: warm-up done {time.perf_counter() - t_setup:.1f} s", file=sys.stderr)
+    # served run in real time
+    ids = []
+    t0 = time.perf_counter()
+    for q, r in enumerate(reqs):
+        while time.perf_counter() - t0 < r["t"]:
+            srv.progress()
+        ids.append(srv.submit(cls[(r["key"], r["kind"])], r["k"], r["tol"], outs[q]))
+        srv.progress()
+    srv.drain()
+    makespan = time.perf_counter() - t0
+    res = [srv.result(i) for i in ids]
+    lat = [x["latency_ms"] for x in res]
+    ok = sum(1 for x in res if x["status"] == capi.OK)
+    fails = {}
+    for r, x in zip(reqs, res):
+        if x["status"] != capi.OK:
+            key = f"{r['key'][0]}{r['key'][1]}-{'flow' if r['kind'] == 0 else 'mt'}-{r['tol']:g}-s{x['status']}"
+            fails[key] = fails.get(key, 0) + 1
+    info = srv.info()
+    served = {"value": round(n_req / makespan, 3), "unit": "solves/s",
+              "p50_latency_ms": round(float(np.percentile(lat, 50)), 3),
+              "p99_latency_ms": round(float(np.percentile(lat, 99)), 3),
+              "ok": ok, "failed": fails, "slots": info["slots"], "hbm_bytes_used": info["bytes_used"]}
+    # plain FP64 path: the same requests one after another through the
+    # blocking single-system API (FP64 CG / BiCGStab + Jacobi), queued in
+    # arrival order behind one another
+    eqs_by = {}
+    svc = []
+    err = {1e-6: 0.0, 1e-10: 0.0}
+    worst = []
+    for q, r in enumerate(reqs):
+        key, kind = r["key"], r["kind"]
+        m = meshes[key]
+        if (key, kind) not in eqs_by:
+            e = capi.LinearEQS(gms[key])
+            rows, vals, mode, p, fp, head = serve_class_setup(capi, m, kind)
+            x0 = np.zeros(m.n_nodes)
+            x0[rows] = vals
+            eqs_by[(key, kind)] = (e, rows, vals, mode, p, fp,
+                                   None if head is None else torch.tensor(head, device="cuda"),
+                                   torch.tensor(x0, device="cuda"), torch.tensor(rows, device="cuda"),
+                                   torch.tensor(vals, device="cuda"))
+        e, rows, vals, mode, p, fp, head, x0, rows_d, vals_d = eqs_by[(key, kind)]
+        torch.cuda.synchronize()
+        ts = time.perf_counter()
+        if kind == 0:
+            e.ConfigNumerics(capi.LS_CG, capi.PRECOND_JACOBI, 20000, r["tol"], check_norm_rhs=False)
+            e.Initialize()
+            e.GlobalAssembly(p, r["k"], x0)
+        else:
+            e.ConfigNumerics(capi.LS_BICGSTAB, capi.PRECOND_JACOBI, 5000, r["tol"], check_norm_rhs=False)
+            qbuf = torch.empty((m.n_elements, gms[key].n_gauss, 3), dtype=torch.float64, device="cuda")
+            e.gp_velocity(fp, r["k"], head, qbuf)
+            e.Initialize()
+            e.GlobalAssembly(p, None, x0, qbuf)
+        e.SetKnownX(rows_d, vals_d, mode)
+        x = x0.clone()
+        e.Solver(x)
+        torch.cuda.synchronize()
+        svc.append(time.perf_counter() - ts)
+        ref = x
+        eq = float((outs[q] - ref).abs().max() / ref.abs().max())
+        if res[q]["status"] == capi.OK:
+            err[r["tol"]] = max(err[r["tol"]], eq)
+        worst.append((eq, f"{r['key'][0]}{r['key'][1]}-{'flow' if r['kind'] == 0 else 'mt'}-{r['tol']:g}",
+                      res[q]["status"], res[q]["iterations"], e.stats()["iterations"]))
+    done = 0.0
+    lat64 = []
+    for r, sv in zip(reqs, svc):
+        start = max(done, r["t"])
+        done = start + sv
+        lat64.append((done - r["t"]) * 1e3)
+    fp64 = {"value": round(n_req / done, 3), "unit": "solves/s",
+            "p50_latency_ms": round(float(np.percentile(lat64, 50)), 3),
+            "p99_latency_ms": round(float(np.percentile(lat64, 99)), 3),
+            "busy_s": round(sum(svc), 3),
+            "how": "same requests, blocking single-system API one after another (FP64 CG / BiCGStab + "
+                   "Jacobi), FIFO queue behind the measured service times"}
+    srv.close()
+    return {"workload": SERVE_WORKLOAD, "requests": n_req, "rate_per_s": SERVE_RATE,
+            "classes": len(cls), "served": served, "fp64_path": fp64,
+            "speedup_vs_fp64_path": round(served["value"] / fp64["value"], 3),
+            "max_rel_err_vs_fp64": {"tol_1e-6": err[1e-6], "tol_1e-10": err[1e-10]},
+            "worst": sorted(worst, reverse=True)[:8],
+            "served_value": served["value"]}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -395,13 +576,15 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--path", default="both", choices=["both", "fp64", "mixed", "batch"],
+    ap.add_argument("--path", default="both", choices=["both", "fp64", "mixed", "batch", "serve"],
                     help="fp64 / mixed / batch: time one path only (profiling driver)")
     ap.add_argument("--batch-reals", type=int, default=BATCH_REALS)
     ap.add_argument("--batch-max-n", type=int, default=96)
     ap.add_argument("--batch-tol", type=float, default=BATCH_TOL)
     ap.add_argument("--batch-plain", action="store_true", help="--path batch: also time the FP64 path")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--serve-requests", type=int, default=SERVE_REQUESTS)
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -415,6 +598,10 @@ def main():
     B.build()
     from ogs5_gb300 import capi
 
+    if args.path == "serve":
+        from ogs5_gb300 import capi
+        print(json.dumps(serve_leg(capi, torch, n_req=args.serve_requests)))
+        return
     if args.path == "batch":
         from ogs5_gb300 import capi
         print(json.dumps(batch_leg(capi, torch, steps=max(1, args.steps), n_real=args.batch_reals,
@@ -507,6 +694,8 @@ def main():
                      "launches": pr["spmv_launches"], "peak_kind": peak_kind},
         "clocks": clk.summary(),
     }
+    if not args.no_serve:
+        out["serve"] = serve_leg(capi, torch, n_req=args.serve_requests)
     if not args.no_batch:
         out["batch"] = batch_leg(capi, torch, n_real=args.batch_reals, n_hi=args.batch_max_n,
                                  tol=args.batch_tol)

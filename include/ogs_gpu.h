@@ -160,7 +160,10 @@ typedef struct
     double rel_residual;       /* |r| / |b| at exit (Linear_EQS::error)        */
     double b_norm;             /* |b| at entry (Linear_EQS::bNorm)             */
     int32_t refinements;       /* FP32 mode: FP64 residual replacements        */
-    int32_t pad0;
+    int32_t fp64_fallback;     /* FP32 mode: 1 if a replacement cycle lowered
+                                  the FP64 residual by less than 4x and the
+                                  solve finished in FP64 CG (iterations then
+                                  count both phases)                          */
     double solve_ms;           /* device time of the solve, CUDA events        */
 } ogs_solve_stats;
 
@@ -457,6 +460,9 @@ typedef struct
 ogs_status ogs_gpu_server_create(int64_t hbm_budget_bytes, int32_t max_active, ogs_server** out);
 ogs_status ogs_gpu_server_destroy(ogs_server* srv);
 ogs_status ogs_gpu_server_add_class(ogs_server* srv, const ogs_server_class* cls, int32_t* class_id);
+/* Creates idle slots of a class up to n_slots in total (within the budget),
+ * so that the first requests do not pay for allocation and graph capture. */
+ogs_status ogs_gpu_server_reserve(ogs_server* srv, int32_t class_id, int32_t n_slots);
 /* Queues a request.  elem_k: device array (n_elements) that stays valid
  * until the request is done; out: n_nodes doubles (device or pinned host),
  * written when the request is done. */

@@ -48,7 +48,7 @@ EXPORTS = [
     "ogs_gpu_batch_set_tuning", "ogs_gpu_batch_solve", "ogs_gpu_batch_get_heads", "ogs_gpu_batch_info",
     "ogs_gpu_solve_begin", "ogs_gpu_solve_poll", "ogs_gpu_solve_end",
     "ogs_gpu_server_create", "ogs_gpu_server_destroy", "ogs_gpu_server_add_class", "ogs_gpu_server_submit",
-    "ogs_gpu_server_progress", "ogs_gpu_server_result", "ogs_gpu_server_info",
+    "ogs_gpu_server_progress", "ogs_gpu_server_result", "ogs_gpu_server_info", "ogs_gpu_server_reserve",
 ]
 REQUEST_FLOW, REQUEST_TRANSPORT = 0, 1
 NOALLOC_MAX_ROWS = 524288
@@ -94,7 +94,7 @@ class Profile(C.Structure):
 
 class SolveStats(C.Structure):
     _fields_ = [("iterations", C.c_int32), ("status", C.c_int32), ("rel_residual", C.c_double),
-                ("b_norm", C.c_double), ("refinements", C.c_int32), ("pad0", C.c_int32),
+                ("b_norm", C.c_double), ("refinements", C.c_int32), ("fp64_fallback", C.c_int32),
                 ("solve_ms", C.c_double)]
 
 
@@ -220,6 +220,8 @@ def lib():
         L.ogs_gpu_server_progress.argtypes = [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
         L.ogs_gpu_server_result.argtypes = [vp, C.c_int64, C.POINTER(ServerResult)]
         L.ogs_gpu_server_info.argtypes = [vp, C.POINTER(ServerInfo)]
+        L.ogs_gpu_server_reserve.argtypes = [vp, C.c_int32, C.c_int32]
+        L.ogs_gpu_server_reserve.restype = st
         for name in ("ogs_gpu_solve_begin", "ogs_gpu_solve_poll", "ogs_gpu_solve_end", "ogs_gpu_server_create",
                      "ogs_gpu_server_destroy", "ogs_gpu_server_add_class", "ogs_gpu_server_submit",
                      "ogs_gpu_server_progress", "ogs_gpu_server_result", "ogs_gpu_server_info"):
@@ -358,7 +360,8 @@ class LinearEQS:
     def stats(self) -> dict:
         s = self.last_stats
         return {"iterations": s.iterations, "status": s.status, "rel_residual": s.rel_residual,
-                "b_norm": s.b_norm, "refinements": s.refinements, "solve_ms": s.solve_ms}
+                "b_norm": s.b_norm, "refinements": s.refinements, "fp64_fallback": s.fp64_fallback,
+                "solve_ms": s.solve_ms}
 
     def gp_velocity(self, params: AssemblyParams, elem_k, u, out=None):
         ng = self.gmesh.n_gauss
@@ -560,6 +563,9 @@ class Server:
         cid = C.c_int32()
         _check(lib().ogs_gpu_server_add_class(self.h, C.byref(c), C.byref(cid)))
         return cid.value
+
+    def reserve(self, class_id, n_slots):
+        _check(lib().ogs_gpu_server_reserve(self.h, class_id, n_slots))
 
     def submit(self, class_id, elem_k, tol, out) -> int:
         rid = C.c_int64()

@@ -153,6 +153,7 @@ struct SolveTask
     int kind = 0;
     cudaGraphExec_t ge = nullptr;
     int per = 0, launched = 0, rounds = 0, chunk_before = -1;
+    int fp32_iters = 0, fp32_repl = 0;  // FP32 phase of a solve that fell back to FP64
     double* x_out = nullptr;
     ogs_status status = OGS_OK;
     float ms = 0.f;
@@ -213,65 +214,6 @@ struct ogs_system
 namespace {
 
 constexpr size_t kStateHeader = offsetof(KState, ticket);
-
-// Keeps the Krylov vectors L2-resident (GB300: 126 MB L2) while the SELL
-// matrix streams through with evict-first loads.  The set-aside is a limit
-// of this process's context; OGS_GPU_L2_PERSIST=0 turns it off.
-void set_l2_window_region(ogs_system* s, void* base, size_t bytes)
-{
-    const char* env = getenv("OGS_GPU_L2_PERSIST");
-    if (env && env[0] == '0') return;
-    int dev = 0, max_win = 0, max_persist = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&max_win, cudaDevAttrMaxAccessPolicyWindowSize, dev);
-    cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, dev);
-    if (max_win <= 0 || max_persist <= 0) return;
-    const size_t want = std::min<size_t>((size_t)max_win, bytes);
-    size_t cur = 0;
-    cudaDeviceGetLimit(&cur, cudaLimitPersistingL2CacheSize);
-    const size_t setaside = std::min<size_t>((size_t)max_persist, std::max(cur, want));
-    if (setaside > cur && cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, setaside) != cudaSuccess)
-    {
-        cudaGetLastError();
-        return;
-    }
-    cudaStreamAttrValue v{};
-    v.accessPolicyWindow.base_ptr = base;
-    v.accessPolicyWindow.num_bytes = want;
-    v.accessPolicyWindow.hitRatio = (float)std::min(1.0, (double)setaside / (double)want);
-    v.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
-    v.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
-    if (cudaStreamSetAttribute(s->stream, cudaStreamAttributeAccessPolicyWindow, &v) != cudaSuccess)
-        cudaGetLastError();
-}
-
-void set_l2_window(ogs_system* s)
-{
-    const char* env = getenv("OGS_GPU_L2_PERSIST");
-    if (env && env[0] == '0') return;
-    int dev = 0, max_win = 0, max_persist = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&max_win, cudaDevAttrMaxAccessPolicyWindowSize, dev);
-    cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, dev);
-    if (max_win <= 0 || max_persist <= 0) return;
-    const size_t want = std::min<size_t>((size_t)max_win, s->vec_stride * 5);  // p r s x dinv
-    size_t cur = 0;
-    cudaDeviceGetLimit(&cur, cudaLimitPersistingL2CacheSize);
-    const size_t setaside = std::min<size_t>((size_t)max_persist, std::max(cur, want));
-    if (setaside > cur && cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, setaside) != cudaSuccess)
-    {
-        cudaGetLastError();
-        return;
-    }
-    cudaStreamAttrValue v{};
-    v.accessPolicyWindow.base_ptr = s->vec_block;
-    v.accessPolicyWindow.num_bytes = want;
-    v.accessPolicyWindow.hitRatio = (float)std::min(1.0, (double)setaside / (double)want);
-    v.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
-    v.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
-    if (cudaStreamSetAttribute(s->stream, cudaStreamAttributeAccessPolicyWindow, &v) != cudaSuccess)
-        cudaGetLastError();
-}
 
 ogs_status stage_in(ogs_system* s, const double* src, size_t n, double** scratch, const double** out)
 {
@@ -382,12 +324,7 @@ extern "C" ogs_status ogs_gpu_system_destroy(ogs_system* s)
 {
     if (!s) return OGS_OK;
     drop_graphs(s);
-    if (s->vec_block)
-    {
-        cudaStreamSynchronize(s->stream);
-        cudaCtxResetPersistingL2Cache();  // hand the persisting lines back
-        cudaGetLastError();
-    }
+    if (s->vec_block) cudaStreamSynchronize(s->stream);
     double* bufs[] = {s->val,     s->ek,      s->u0,      s->gpv,     s->qbuf,     s->vec_in,
                       s->vec_out, s->bc_vals, s->bc_valn, s->bc_valf, s->bc_vfirst};
     for (double* p : bufs) cudaFree(p);
@@ -436,8 +373,7 @@ extern "C" ogs_status ogs_gpu_system_create(ogs_mesh* m, void* stream, ogs_syste
     const size_t nb = (size_t)s->n * sizeof(double);
     double** vecs[] = {&s->p, &s->r, &s->s, &s->x, &s->dinv, &s->ph, &s->sh, &s->r0, &s->v, &s->t, &s->b};
     cudaError_t e = cudaMalloc(&s->val, std::max<int64_t>(1, m->sell_nnz) * sizeof(double));
-    // Krylov vectors in one block, most-reused first, so that one L2
-    // access-policy window can keep them resident while the matrix streams
+    // Krylov vectors in one allocation (one cudaMalloc per system)
     const size_t nvec = sizeof(vecs) / sizeof(vecs[0]);
     const size_t stride = (nb + 255) & ~size_t(255);
     if (e == cudaSuccess) e = cudaMalloc(&s->vec_block, stride * nvec);
@@ -463,7 +399,6 @@ extern "C" ogs_status ogs_gpu_system_create(ogs_mesh* m, void* stream, ogs_syste
         ogs_gpu_system_destroy(s);
         return e == cudaErrorMemoryAllocation ? OGS_OOM : OGS_CUDA_ERROR;
     }
-    set_l2_window(s);
     // CNumerics defaults (rf_num_new.cpp:77-165): BiCGStab, Jacobi, 1000, 1e-12
     s->cfg.method = OGS_LS_BICGSTAB;
     s->cfg.precond = OGS_PRECOND_JACOBI;
@@ -768,7 +703,6 @@ static ogs_status begin_fp32_refined(ogs_system* s, KState* h)
     a.d32 = s->d32; a.x = s->x; a.b = s->b; a.r64 = s->r;
     a.x32 = s->x32; a.r32 = s->r32; a.p32 = s->p32; a.s32 = s->s32; a.u32 = s->u32; a.w32 = s->w32;
     a.st = s->st; a.n = n;
-    set_l2_window_region(s, s->f32_block, s->f32_bytes);
     launch_mp_convert(a, m->row_len, m->slot_up, s->U, s->val32, s->dinv, s->d32, s->stream);
     OGS_LAUNCH_CHECK();
     OGS_CUDA_TRY(cudaMemsetAsync(s->x32, 0, (size_t)n * sizeof(float), s->stream));
@@ -994,6 +928,34 @@ static ogs_status solve_advance(ogs_system* s, bool block, bool* finished)
         return OGS_OK;
     }
     // phase 1: a header copy has landed
+    if (T.mixed && h->done && h->fallback)
+    {
+        // FP32 cycles stopped gaining: continue with FP64 CG from x64
+        T.fp32_iters = h->iter;
+        T.fp32_repl = h->replacements;
+        T.mixed = false;
+        T.kind = SK_CG;
+        T.chunk_before = -1;
+        const double bn = h->bnorm;
+        std::memset(h, 0, kStateHeader);
+        h->bnorm = bn;  // |b| / bn = 1: CheckNormRHS does not return early
+        h->tol = c.tol;
+        h->error = 1.0e10;
+        h->max_iter = std::max(1, c.max_iter - T.fp32_iters);
+        h->alpha = h->omega = h->rho0 = 1.0;
+        h->nb_spmv = vec_grid(s->n);
+        h->nb_upd = red_grid(s->n);
+        SolveArgs a = make_solve_args(s);
+        if (cudaMemcpyAsync(s->st, h, kStateHeader, cudaMemcpyHostToDevice, s->stream) != cudaSuccess)
+            return task_fail(s, OGS_CUDA_ERROR);
+        launch_krylov_init(a, SK_CG, s->stream);
+        if (cudaGetLastError() != cudaSuccess) return task_fail(s, OGS_CUDA_ERROR);
+        count_launches(krylov_init_launches(SK_CG, a.precond));
+        ogs_status st = get_chunk(s, SK_CG, a, &T.ge, &T.per);
+        if (st) return task_fail(s, st);
+        if (enqueue_header(s)) return task_fail(s, OGS_CUDA_ERROR);
+        return OGS_OK;
+    }
     if (T.mixed)
     {
         if (T.chunk_before >= 0)
@@ -1070,11 +1032,12 @@ static ogs_status solve_end(ogs_system* s, ogs_solve_stats* stats)
     if (stats)
     {
         std::memset(stats, 0, sizeof *stats);
-        stats->iterations = h->iter;
+        stats->iterations = h->iter + T.fp32_iters;
         stats->status = T.status;
         stats->rel_residual = h->error;
         stats->b_norm = h->bnorm;
-        stats->refinements = h->replacements;
+        stats->refinements = h->replacements + T.fp32_repl;
+        stats->fp64_fallback = T.fp32_iters > 0 || T.fp32_repl > 0 ? 1 : 0;
         stats->solve_ms = T.ms;
     }
     const ogs_status st = T.status;

@@ -25,7 +25,13 @@ struct KState
     int replace;                 // 1: the FP64 residual replacement is due
     int replacements;
     int first;                   // first restart of a solve (p = z)
-    int pad2;
+    int fallback;                // FP32 cycles stopped gaining: finish in FP64 CG
+    double err_prev;             // |r64| / |b| at the previous replacement
+    double rn_req;               // |r32| when the pending replacement was asked for
+    double rbest[2];             // smallest |r32| of the cycle up to iteration k, at [k & 1]
+    int itbest[2];               // the iteration where it was reached, at [k & 1]
+    int stalled;                 // the pending replacement was forced by a plateau
+    int pad4;
     // ticket-free CG: r.z of the iteration after `base_iter` comes from
     // rz_base (initial residual or the last replacement), later ones from
     // the parity-buffered partials of the update kernel

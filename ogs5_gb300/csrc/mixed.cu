@@ -140,6 +140,14 @@ __global__ void __launch_bounds__(kThreads) k_mp_accumulate(MixedArgs a)
     }
 }
 
+// a full replacement cycle that lowers |r64| by less than 4x, or a short
+// one that gains less than a quarter of what the FP32 recurrence claimed,
+// hands over to FP64
+constexpr double kMinCycleGain = 4.0;
+constexpr double kCycleSlack = 0.25;
+// iterations without a new smallest FP32 residual that count as a plateau
+constexpr int kPlateau = 64;
+
 // r64 = b - A64 x64 ; |r64| ; convergence on the FP64 residual ; new scale
 __global__ void __launch_bounds__(kThreads) k_mp_residual(MixedArgs a)
 {
@@ -171,6 +179,20 @@ __global__ void __launch_bounds__(kThreads) k_mp_residual(MixedArgs a)
         if (!isfinite(st->error)) { st->status = OGS_NONFINITE; st->done = 1; return; }
         if (st->error < st->tol) { st->status = OGS_OK; st->done = 1; return; }
         if (st->iter >= st->max_iter) { st->status = OGS_NOT_CONVERGED; st->done = 1; return; }
+        // A cycle of FP32 iterations lowers the true residual about as much
+        // as the FP32 recurrence claims (rmax / rn_req: 1/delta for a full
+        // cycle).  When the FP32 operator is too coarse for the system's
+        // conditioning (cond(A) near 1/eps_fp32) the true gain falls far
+        // behind the claimed one; the solve then finishes in FP64 CG from x64.
+        const double claimed = st->rn_req > 0.0 ? st->rmax / st->rn_req : 1.0;
+        const double gain = st->err_prev / st->error;
+        if (st->stalled || (!st->first && gain < fmin(kMinCycleGain, kCycleSlack * claimed)))
+        {
+            st->fallback = 1;
+            st->done = 1;
+            return;
+        }
+        st->err_prev = st->error;
         const double ns = rn > DBL_MIN ? 1.0 / rn : 1.0;
         st->ratio = st->first ? 1.0 : ns / st->scale;
         st->scale = ns;
@@ -209,6 +231,7 @@ __global__ void __launch_bounds__(kThreads) k_mp_restart(MixedArgs a)
         st->base_iter = it;
         st->rmax = -1.0;  // set from the first rho after the restart
         st->replace = 0;
+        st->stalled = 0;
     }
 }
 
@@ -254,18 +277,34 @@ __global__ void __launch_bounds__(kThreads) k_mp_update(MixedArgs a)
     const double alpha = gamma / eta;
     const double est = rn / st->scale / st->bnorm;  // estimate of |r64| / |b|
     const bool nonfinite = !isfinite(rn) || !isfinite(alpha);
+    // plateau: no new smallest |r32| in the cycle for max(64, half the
+    // cycle) iterations (parity slots of the previous iteration: written by
+    // block 0 of the previous launch)
+    const double rb_prev = fresh ? rn : ((it - 1) & 1 ? st->rbest[1] : st->rbest[0]);
+    const int ib_prev = fresh ? it : ((it - 1) & 1 ? st->itbest[1] : st->itbest[0]);
+    const bool better = rn < rb_prev;
+    const double rb = better ? rn : rb_prev;
+    const int ib = better ? it : ib_prev;
+    const bool stalled = it - ib > max(kPlateau, (it - st->base_iter) / 2);
     // right after a replacement r32 is the true residual (checked in FP64 by
     // k_mp_residual), so a fresh iteration never asks for another one
     const bool repl = !nonfinite && !fresh &&
-                      (est < st->tol || rn < st->delta * rmax || it > st->max_iter);
+                      (est < st->tol || rn < st->delta * rmax || it > st->max_iter || stalled);
     if (blockIdx.x == 0 && threadIdx.x == 0)
     {
+        if (it & 1) { st->rbest[1] = rb; st->itbest[1] = ib; }
+        else { st->rbest[0] = rb; st->itbest[0] = ib; }
         if (fresh) st->rmax = rn;
         st->gam_hist[it & 1] = gamma;
         st->eta_hist[it & 1] = eta;
         st->first = 0;  // read by the replacement kernels only
         if (nonfinite) { st->status = OGS_NONFINITE; st->done = 1; }
-        else if (repl) st->replace = 1;
+        else if (repl)
+        {
+            st->replace = 1;
+            st->rn_req = rn;
+            st->stalled = stalled && !(est < st->tol || rn < st->delta * rmax || it > st->max_iter);
+        }
     }
     if (nonfinite || repl) return;
     const float fb = (float)beta, fa = (float)alpha;

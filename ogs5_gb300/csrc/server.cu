@@ -258,6 +258,28 @@ extern "C" ogs_status ogs_gpu_server_add_class(ogs_server* S, const ogs_server_c
     return OGS_OK;
 }
 
+extern "C" ogs_status ogs_gpu_server_reserve(ogs_server* S, int32_t class_id, int32_t n_slots)
+{
+    if (!S || class_id < 0 || class_id >= (int32_t)S->classes.size() || n_slots < 0)
+    {
+        set_error("server_reserve: bad arguments");
+        return OGS_BAD_ARG;
+    }
+    int have = 0;
+    for (const SrvSlot& sl : S->slots) have += sl.cls == class_id;
+    std::vector<int> made;
+    for (; have < n_slots; have++)
+    {
+        const int k = acquire_slot(S, class_id);
+        if (k == -2) return OGS_OOM;
+        if (k < 0) break;  // budget reached
+        S->slots[k].busy = true;  // keep acquire_slot from handing it out again in this loop
+        made.push_back(k);
+    }
+    for (int k : made) S->slots[k].busy = false;
+    return OGS_OK;
+}
+
 extern "C" ogs_status ogs_gpu_server_submit(ogs_server* S, int32_t class_id, const double* elem_k, double tol,
                                             double* out, int64_t* request_id)
 {

@@ -57,5 +57,5 @@ def lognormal_k_device(shape, mean_ln: float, var: float, ell: float, seed: int,
     noise = torch.complex(torch.randn(ext, generator=gen, device=device, dtype=torch.float64),
                           torch.randn(ext, generator=gen, device=device, dtype=torch.float64))
     f = torch.fft.ifftn(torch.sqrt(lam / n) * noise * n).real
-    f = f[: sh[0], : sh[1], : sh[2]]
+    f = f[tuple(slice(0, m) for m in sh)]
     return torch.exp(mean_ln + f).reshape(-1).contiguous()
