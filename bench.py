@@ -397,6 +397,12 @@ SERVE_SEED = 5
 SERVE_DOF = (1e4, 2e6)
 SERVE_CLASSES = 5         # log-spaced size classes per mesh type (meshes are cached)
 SERVE_WARM_SLOTS = 4      # slots per class created before the timed run
+# requests in flight at most, and the scheduling policy: smallest class first
+# at admission, higher stream priority for smaller classes (measured on 400
+# requests: p50 267 ms against 508 ms for arrival order with 128 in flight,
+# the same throughput)
+SERVE_MAX_ACTIVE = 16
+SERVE_FLAGS = 3           # capi.SERVER_PRIORITY | capi.SERVER_SJF
 SERVE_WORKLOAD = ("Poisson arrivals 200/s of flow (steady GWF, heads 10/0 m on the x faces) and transport "
                   "(one MASS_TRANSPORT step, flux from a linear head field) requests on quad, hex and "
                   "hex-split-tet meshes, 1e4-2e6 DOF log-uniform (5 size classes per type), log-normal K "
@@ -451,13 +457,15 @@ def serve_class_setup(capi, m, kind):
     return lf, np.ones(len(lf)), capi.DIRICHLET_ROW_ONLY, p, capi.make_params(capi.GROUNDWATER_FLOW), head
 
 
-def serve_leg(capi, torch, n_req=SERVE_REQUESTS):
+def serve_leg(capi, torch, n_req=SERVE_REQUESTS, flags=None, max_active=None, plain=True):
     t_setup = time.perf_counter()
     dofs, meshes = serve_meshes()
     gms = {key: capi.GpuMesh(m) for key, m in meshes.items()}
     reqs = serve_requests(torch, dofs, meshes, n_req=n_req)
     print(f"serve: meshes and fields {time.perf_counter() - t_setup:.1f} s", file=sys.stderr)
-    srv = capi.Server(max_active=128)
+    flags = SERVE_FLAGS if flags is None else flags
+    max_active = SERVE_MAX_ACTIVE if max_active is None else max_active
+    srv = capi.Server(max_active=max_active, flags=flags)
     cls = {}
     for key, m in meshes.items():
         for kind in (0, 1):
@@ -505,6 +513,11 @@ def serve_leg(capi, torch, n_req=SERVE_REQUESTS):
               "p50_latency_ms": round(float(np.percentile(lat, 50)), 3),
               "p99_latency_ms": round(float(np.percentile(lat, 99)), 3),
               "ok": ok, "failed": fails, "slots": info["slots"], "hbm_bytes_used": info["bytes_used"]}
+    policy = {"max_active": max_active, "priority_streams": bool(flags & capi.SERVER_PRIORITY),
+              "admission": "smallest class first" if flags & capi.SERVER_SJF else "arrival order"}
+    if not plain:
+        srv.close()
+        return {"requests": n_req, "served": served, "policy": policy}
     # plain FP64 path: the same requests one after another through the
     # blocking single-system API (FP64 CG / BiCGStab + Jacobi), queued in
     # arrival order behind one another
@@ -562,7 +575,7 @@ def serve_leg(capi, torch, n_req=SERVE_REQUESTS):
                    "Jacobi), FIFO queue behind the measured service times"}
     srv.close()
     return {"workload": SERVE_WORKLOAD, "requests": n_req, "rate_per_s": SERVE_RATE,
-            "classes": len(cls), "served": served, "fp64_path": fp64,
+            "classes": len(cls), "served": served, "policy": policy, "fp64_path": fp64,
             "speedup_vs_fp64_path": round(served["value"] / fp64["value"], 3),
             "max_rel_err_vs_fp64": {"tol_1e-6": err[1e-6], "tol_1e-10": err[1e-10]},
             "worst": sorted(worst, reverse=True)[:8],
@@ -585,6 +598,9 @@ def main():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=SERVE_REQUESTS)
+    ap.add_argument("--serve-flags", type=int, default=None)
+    ap.add_argument("--serve-max-active", type=int, default=None)
+    ap.add_argument("--serve-no-plain", action="store_true")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -600,7 +616,8 @@ def main():
 
     if args.path == "serve":
         from ogs5_gb300 import capi
-        print(json.dumps(serve_leg(capi, torch, n_req=args.serve_requests)))
+        print(json.dumps(serve_leg(capi, torch, n_req=args.serve_requests, flags=args.serve_flags,
+                                   max_active=args.serve_max_active, plain=not args.serve_no_plain)))
         return
     if args.path == "batch":
         from ogs5_gb300 import capi

@@ -456,8 +456,19 @@ typedef struct
     int64_t bytes_used, bytes_budget;
 } ogs_server_info;
 
-/* hbm_budget_bytes <= 0: 80% of the free device memory at creation. */
-ogs_status ogs_gpu_server_create(int64_t hbm_budget_bytes, int32_t max_active, ogs_server** out);
+/* Scheduling policy bits of ogs_gpu_server_create. */
+enum
+{
+    OGS_SERVER_PRIORITY = 1,  /* smaller classes get higher CUDA stream priorities */
+    OGS_SERVER_SJF = 2        /* admit the queued request of the smallest class
+                                 first (arrival order among equals); default:
+                                 arrival order                                 */
+};
+
+/* hbm_budget_bytes <= 0: 80% of the free device memory at creation.
+ * max_active: requests in flight at most.  flags: OGS_SERVER_* bits. */
+ogs_status ogs_gpu_server_create(int64_t hbm_budget_bytes, int32_t max_active, int32_t flags,
+                                 ogs_server** out);
 ogs_status ogs_gpu_server_destroy(ogs_server* srv);
 ogs_status ogs_gpu_server_add_class(ogs_server* srv, const ogs_server_class* cls, int32_t* class_id);
 /* Creates idle slots of a class up to n_slots in total (within the budget),

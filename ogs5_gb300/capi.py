@@ -51,6 +51,7 @@ EXPORTS = [
     "ogs_gpu_server_progress", "ogs_gpu_server_result", "ogs_gpu_server_info", "ogs_gpu_server_reserve",
 ]
 REQUEST_FLOW, REQUEST_TRANSPORT = 0, 1
+SERVER_PRIORITY, SERVER_SJF = 1, 2
 NOALLOC_MAX_ROWS = 524288
 
 
@@ -213,7 +214,7 @@ def lib():
         L.ogs_gpu_solve_begin.argtypes = [vp, vp]
         L.ogs_gpu_solve_poll.argtypes = [vp, C.POINTER(C.c_int32)]
         L.ogs_gpu_solve_end.argtypes = [vp, C.POINTER(SolveStats)]
-        L.ogs_gpu_server_create.argtypes = [C.c_int64, C.c_int32, C.POINTER(vp)]
+        L.ogs_gpu_server_create.argtypes = [C.c_int64, C.c_int32, C.c_int32, C.POINTER(vp)]
         L.ogs_gpu_server_destroy.argtypes = [vp]
         L.ogs_gpu_server_add_class.argtypes = [vp, C.POINTER(ServerClass), C.POINTER(C.c_int32)]
         L.ogs_gpu_server_submit.argtypes = [vp, C.c_int32, vp, C.c_double, vp, C.POINTER(C.c_int64)]
@@ -524,10 +525,10 @@ class Server:
         srv.result(rid)
     """
 
-    def __init__(self, budget_bytes=0, max_active=64):
+    def __init__(self, budget_bytes=0, max_active=64, flags=0):
         self.h = None
         h = C.c_void_p()
-        _check(lib().ogs_gpu_server_create(int(budget_bytes), int(max_active), C.byref(h)))
+        _check(lib().ogs_gpu_server_create(int(budget_bytes), int(max_active), int(flags), C.byref(h)))
         self.h = h
         self._refs = {}
 

@@ -381,16 +381,18 @@ extern "C" ogs_status ogs_gpu_system_create(ogs_mesh* m, void* stream, ogs_syste
         *vecs[k] = (double*)((char*)s->vec_block + k * stride);
     s->vec_stride = stride;
     if (e == cudaSuccess) e = cudaMalloc(&s->st, sizeof(KState));
-    if (e == cudaSuccess) e = cudaMemset(s->st, 0, sizeof(KState));
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->st, 0, sizeof(KState), s->stream);
     if (e == cudaSuccess) e = cudaMalloc(&s->d_bad, sizeof(int));
     if (e == cudaSuccess) e = cudaMallocHost(&s->h_st, sizeof(KState));
     if (e == cudaSuccess) e = cudaMallocHost(&s->h_bad, sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc(&s->bc_flag, std::max(1, s->n));
     if (e == cudaSuccess) e = cudaMalloc(&s->bc_valn, nb);
     if (e == cudaSuccess) e = cudaMalloc(&s->bc_valf, nb);
-    if (e == cudaSuccess) e = cudaMemset(s->val, 0, m->sell_nnz * sizeof(double));
-    if (e == cudaSuccess) e = cudaMemset(s->b, 0, nb);
-    if (e == cudaSuccess) e = cudaMemset(s->x, 0, nb);
+    // stream-ordered: work on the system's (possibly non-blocking) stream
+    // must not overtake these
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->val, 0, m->sell_nnz * sizeof(double), s->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->b, 0, nb, s->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->x, 0, nb, s->stream);
     if (e == cudaSuccess) e = cudaEventCreate(&s->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&s->ev1);
     if (e != cudaSuccess)
@@ -687,7 +689,7 @@ static ogs_status begin_fp32_refined(ogs_system* s, KState* h)
                                       : (size_t)m->sell_nnz * sizeof(float);
         s->f32_bytes = 7 * v4 + op;
         OGS_CUDA_TRY(cudaMalloc(&s->f32_block, s->f32_bytes));
-        OGS_CUDA_TRY(cudaMemset(s->f32_block, 0, s->f32_bytes));
+        OGS_CUDA_TRY(cudaMemsetAsync(s->f32_block, 0, s->f32_bytes, s->stream));
         char* p = (char*)s->f32_block;
         s->p32 = (float*)p; s->r32 = (float*)(p + v4); s->x32 = (float*)(p + 2 * v4);
         s->s32 = (float*)(p + 3 * v4); s->d32 = (float*)(p + 4 * v4);
@@ -1107,6 +1109,15 @@ extern "C" ogs_status ogs_gpu_spmv(ogs_system* s, const double* x, double* y)
     return OGS_OK;
 }
 
+// device array of the system -> caller's array (host or device), ordered on
+// the system's stream, complete on return
+static ogs_status copy_out(const ogs_system* s, void* dst, const void* src, size_t bytes)
+{
+    OGS_CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, s->stream));
+    OGS_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    return OGS_OK;
+}
+
 extern "C" ogs_status ogs_gpu_get_csr(const ogs_system* s, int64_t* row_ptr, int64_t* col, double* val)
 {
     if (!s) { set_error("get_csr: NULL system"); return OGS_BAD_ARG; }
@@ -1128,9 +1139,8 @@ extern "C" ogs_status ogs_gpu_get_csr(const ogs_system* s, int64_t* row_ptr, int
             s->val, m->csr2sell, tmp, m->nnz);
         cudaError_t e = cudaGetLastError();
         if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
-        if (e == cudaSuccess)
-            e = cudaMemcpy(val, tmp, m->nnz * sizeof(double),
-                           is_device_ptr(val) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(val, tmp, m->nnz * sizeof(double), cudaMemcpyDefault, s->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
         cudaFree(tmp);
         if (e != cudaSuccess) { set_error("get_csr: %s", cudaGetErrorString(e)); return OGS_CUDA_ERROR; }
     }
@@ -1140,29 +1150,20 @@ extern "C" ogs_status ogs_gpu_get_csr(const ogs_system* s, int64_t* row_ptr, int
 extern "C" ogs_status ogs_gpu_get_rhs(const ogs_system* s, double* b)
 {
     if (!s || !b) { set_error("get_rhs: NULL argument"); return OGS_BAD_ARG; }
-    OGS_CUDA_TRY(cudaStreamSynchronize(s->stream));
-    OGS_CUDA_TRY(cudaMemcpy(b, s->b, (size_t)s->n * sizeof(double),
-                            is_device_ptr(b) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost));
-    return OGS_OK;
+    return copy_out(s, b, s->b, (size_t)s->n * sizeof(double));
 }
 
 extern "C" ogs_status ogs_gpu_get_x(const ogs_system* s, double* x)
 {
     if (!s || !x) { set_error("get_x: NULL argument"); return OGS_BAD_ARG; }
-    OGS_CUDA_TRY(cudaStreamSynchronize(s->stream));
-    OGS_CUDA_TRY(cudaMemcpy(x, s->x, (size_t)s->n * sizeof(double),
-                            is_device_ptr(x) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost));
-    return OGS_OK;
+    return copy_out(s, x, s->x, (size_t)s->n * sizeof(double));
 }
 
 extern "C" ogs_status ogs_gpu_get_ilu0(const ogs_system* s, double* lu)
 {
     if (!s || !lu) { set_error("get_ilu0: NULL argument"); return OGS_BAD_ARG; }
     if (!s->lu) { set_error("get_ilu0: no ILU(0) factorisation yet (solve with ls_precond 100 first)"); return OGS_BAD_ARG; }
-    OGS_CUDA_TRY(cudaStreamSynchronize(s->stream));
-    OGS_CUDA_TRY(cudaMemcpy(lu, s->lu, (size_t)s->m->nnz * sizeof(double),
-                            is_device_ptr(lu) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost));
-    return OGS_OK;
+    return copy_out(s, lu, s->lu, (size_t)s->m->nnz * sizeof(double));
 }
 
 extern "C" ogs_status ogs_gpu_profile(ogs_system* s, int32_t enable, ogs_profile* out)

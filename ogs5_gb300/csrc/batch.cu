@@ -1050,13 +1050,20 @@ extern "C" ogs_status ogs_gpu_batch_create(const ogs_batch_config* cfg, const og
     {
         const BReal& R = B->real[r];
         const size_t ne = (size_t)(R.nx - 1) * (R.ny - 1) * (R.nz - 1);
-        e = cudaMemcpy(B->ek + R.elem0, reals[r].elem_k, ne * sizeof(double), cudaMemcpyDefault);
+        e = cudaMemcpyAsync(B->ek + R.elem0, reals[r].elem_k, ne * sizeof(double), cudaMemcpyDefault, B->stream);
         if (e != cudaSuccess)
         {
             set_error("batch_create: copying elem_k of realisation %d: %s", r, cudaGetErrorString(e));
             ogs_gpu_batch_destroy(B);
             return OGS_CUDA_ERROR;
         }
+    }
+    // the caller may release its arrays when this returns
+    if ((e = cudaStreamSynchronize(B->stream)) != cudaSuccess)
+    {
+        set_error("batch_create: %s", cudaGetErrorString(e));
+        ogs_gpu_batch_destroy(B);
+        return OGS_CUDA_ERROR;
     }
     // default launch shape; ogs_gpu_batch_autotune refines it
     B->tune.tile_rows = 4096;
@@ -1184,7 +1191,8 @@ extern "C" ogs_status ogs_gpu_batch_get_heads(const ogs_batch* B, double* h)
 {
     if (!B || !h) { set_error("batch_get_heads: NULL argument"); return OGS_BAD_ARG; }
     OGS_CUDA_TRY(cudaStreamSynchronize(B->stream));
-    OGS_CUDA_TRY(cudaMemcpy(h, B->x64, B->rows * sizeof(double), cudaMemcpyDefault));
+    OGS_CUDA_TRY(cudaMemcpyAsync(h, B->x64, B->rows * sizeof(double), cudaMemcpyDefault, B->stream));
+    OGS_CUDA_TRY(cudaStreamSynchronize(B->stream));
     return OGS_OK;
 }
 

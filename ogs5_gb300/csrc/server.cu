@@ -61,6 +61,7 @@ struct SrvClass
     double* u_flow = nullptr;  // transport: head field of the Gauss-point flux, device
     size_t bytes = 0;          // device bytes of one slot
     int64_t n = 0, ngp = 0, ne = 0;
+    int priority = 0;          // CUDA stream priority of its slots
 };
 
 struct SrvSlot
@@ -68,6 +69,7 @@ struct SrvSlot
     int cls = -1;
     ogs_system* sys = nullptr;
     double* q = nullptr;       // transport: Gauss-point flux
+    cudaStream_t stream = nullptr;  // owned by the server, priority by class size
     bool busy = false;
     int64_t last_used = 0;
 };
@@ -91,6 +93,7 @@ struct ogs_server
 {
     size_t budget = 0, used = 0;
     int max_active = 0;
+    int flags = 0;             // OGS_SERVER_* policy bits
     std::vector<SrvClass> classes;
     std::vector<SrvSlot> slots;
     std::vector<SrvReq> reqs;
@@ -107,6 +110,7 @@ void release_slot(ogs_server* S, size_t k)
     SrvSlot& sl = S->slots[k];
     if (sl.sys) ogs_gpu_system_destroy(sl.sys);
     cudaFree(sl.q);
+    if (sl.stream) cudaStreamDestroy(sl.stream);
     S->used -= S->classes[sl.cls].bytes;
     S->slots.erase(S->slots.begin() + k);
     for (int64_t id : S->running)
@@ -130,18 +134,30 @@ int acquire_slot(ogs_server* S, int c)
     }
     SrvSlot sl;
     sl.cls = c;
-    if (ogs_gpu_system_create(C.c.mesh, nullptr, &sl.sys)) return -2;
+    if (cudaStreamCreateWithPriority(&sl.stream, cudaStreamNonBlocking, C.priority) != cudaSuccess)
+    {
+        cudaGetLastError();
+        set_error("server: stream creation failed");
+        return -2;
+    }
+    if (ogs_gpu_system_create(C.c.mesh, sl.stream, &sl.sys))
+    {
+        cudaStreamDestroy(sl.stream);
+        return -2;
+    }
     if (ogs_gpu_configure(sl.sys, &C.c.solver) ||
         system_upload_dirichlet(sl.sys, C.bc_rows.data(), C.bc_vals.data(), (int64_t)C.bc_rows.size(),
                                 C.c.bc_mode))
     {
         ogs_gpu_system_destroy(sl.sys);
+        cudaStreamDestroy(sl.stream);
         return -2;
     }
     if (C.c.kind == OGS_REQUEST_TRANSPORT && cudaMalloc(&sl.q, (size_t)C.ne * C.ngp * 3 * sizeof(double)) != cudaSuccess)
     {
         cudaGetLastError();
         ogs_gpu_system_destroy(sl.sys);
+        cudaStreamDestroy(sl.stream);
         set_error("server: no device memory for a transport slot");
         return -2;
     }
@@ -170,6 +186,33 @@ ogs_status start(ogs_server* S, int64_t id, int k)
     return ogs_gpu_solve_begin(s, R.out);
 }
 
+// Smaller systems get higher stream priorities: their short kernels are
+// scheduled ahead of the blocks of large solves, so a small request is not
+// time-sliced behind every large one in flight (shortest job first at the
+// block scheduler).  Classes are ranked by rows, spread over the device's
+// priority range in factors of four.
+void assign_priorities(ogs_server* S)
+{
+    int least = 0, greatest = 0;
+    if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return;
+    }
+    const int levels = least - greatest + 1;  // greatest is the most negative
+    int64_t nmin = INT64_MAX;
+    for (const SrvClass& C : S->classes) nmin = std::min(nmin, C.n);
+    nmin = std::max<int64_t>(1, nmin);
+    for (SrvClass& C : S->classes)
+    {
+        // factors of four above the smallest class; the smallest get the
+        // greatest priority
+        int step = 0;
+        for (int64_t v = C.n; v >= 4 * nmin && step < levels - 1; v /= 4) step++;
+        C.priority = greatest + step;
+    }
+}
+
 double ms_between(Clock::time_point a, Clock::time_point b)
 {
     return std::chrono::duration<double, std::milli>(b - a).count();
@@ -177,7 +220,8 @@ double ms_between(Clock::time_point a, Clock::time_point b)
 
 }  // namespace
 
-extern "C" ogs_status ogs_gpu_server_create(int64_t hbm_budget_bytes, int32_t max_active, ogs_server** out)
+extern "C" ogs_status ogs_gpu_server_create(int64_t hbm_budget_bytes, int32_t max_active, int32_t flags,
+                                            ogs_server** out)
 {
     if (!out || max_active <= 0) { set_error("server_create: bad arguments"); return OGS_BAD_ARG; }
     ogs_server* S = new ogs_server;
@@ -190,6 +234,7 @@ extern "C" ogs_status ogs_gpu_server_create(int64_t hbm_budget_bytes, int32_t ma
     else
         S->budget = (size_t)hbm_budget_bytes;
     S->max_active = max_active;
+    S->flags = flags;
     *out = S;
     return OGS_OK;
 }
@@ -201,6 +246,7 @@ extern "C" ogs_status ogs_gpu_server_destroy(ogs_server* S)
     {
         if (sl.sys) ogs_gpu_system_destroy(sl.sys);
         cudaFree(sl.q);
+        if (sl.stream) cudaStreamDestroy(sl.stream);
     }
     for (SrvClass& C : S->classes)
     {
@@ -247,6 +293,9 @@ extern "C" ogs_status ogs_gpu_server_add_class(ogs_server* S, const ogs_server_c
         }
         OGS_CUDA_TRY(cudaMalloc(&C.u_flow, std::max<int64_t>(1, n) * sizeof(double)));
         OGS_CUDA_TRY(cudaMemcpy(C.u_flow, c->flow_head, n * sizeof(double), cudaMemcpyDefault));
+        // a device-to-device copy returns before it completes: finish it
+        // before slots on other streams read the field
+        OGS_CUDA_TRY(cudaStreamSynchronize(cudaStreamLegacy));
     }
     C.bytes = system_bytes(c->mesh, c->solver.precision == OGS_PRECISION_FP32_REFINED);
     if (c->kind == OGS_REQUEST_TRANSPORT) C.bytes += (size_t)C.ne * C.ngp * 3 * sizeof(double);
@@ -255,6 +304,7 @@ extern "C" ogs_status ogs_gpu_server_add_class(ogs_server* S, const ogs_server_c
     C.c.flow_head = nullptr;
     S->classes.push_back(std::move(C));
     *class_id = (int32_t)S->classes.size() - 1;
+    if (S->flags & OGS_SERVER_PRIORITY) assign_priorities(S);
     return OGS_OK;
 }
 
@@ -332,15 +382,20 @@ extern "C" ogs_status ogs_gpu_server_progress(ogs_server* S, int32_t* n_running,
         S->completed += 1;
         S->running.erase(S->running.begin() + q);
     }
-    // admission in arrival order
+    // admission: arrival order, or smallest class first (arrival order
+    // among equals) with OGS_SERVER_SJF
     while (!S->queue.empty())
     {
-        const int64_t id = S->queue.front();
+        size_t pick = 0;
+        if (S->flags & OGS_SERVER_SJF)
+            for (size_t q = 1; q < S->queue.size(); q++)
+                if (S->classes[S->reqs[S->queue[q]].cls].n < S->classes[S->reqs[S->queue[pick]].cls].n) pick = q;
+        const int64_t id = S->queue[pick];
         SrvReq& R = S->reqs[id];
         const int k = acquire_slot(S, R.cls);
         if (k == -2) return OGS_OOM;
         if (k < 0) break;
-        S->queue.pop_front();
+        S->queue.erase(S->queue.begin() + pick);
         S->slots[k].busy = true;
         R.slot = k;
         R.state = 1;

@@ -58,7 +58,7 @@ def _k(torch, m, seed):
 
 
 def test_server_mix_equals_alone_and_blocking_api(gpu):
-    srv = gpu.Server(max_active=64)
+    srv = gpu.Server(max_active=64, flags=gpu.SERVER_PRIORITY | gpu.SERVER_SJF)
     torch, classes = _classes(gpu, srv)
     reqs = []
     for q in range(16):
