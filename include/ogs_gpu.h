@@ -160,10 +160,12 @@ typedef struct
     double rel_residual;       /* |r| / |b| at exit (Linear_EQS::error)        */
     double b_norm;             /* |b| at entry (Linear_EQS::bNorm)             */
     int32_t refinements;       /* FP32 mode: FP64 residual replacements        */
-    int32_t fp64_fallback;     /* FP32 mode: 1 if a replacement cycle lowered
-                                  the FP64 residual by less than 4x and the
-                                  solve finished in FP64 CG (iterations then
-                                  count both phases)                          */
+    int32_t fp64_fallback;     /* FP32 mode: 1 if the FP32 cycles stopped
+                                  gaining (a plateau of the FP32 residual, or
+                                  a replacement that lowered the FP64
+                                  residual far less than the FP32 recurrence
+                                  claimed) and the solve finished in FP64 CG
+                                  from x (iterations count both phases)       */
     double solve_ms;           /* device time of the solve, CUDA events        */
 } ogs_solve_stats;
 

@@ -93,3 +93,27 @@ def test_profile_counts_spmv_launches(gpu, mixed):
     assert pr["solves"] == 1 and pr["spmv_ms"] > 0
     # the SpMV of every fourth iteration of a chunk is timed
     assert abs(pr["spmv_launches"] - it / 4) <= it / 16 + 3
+
+
+def test_fp32_stall_falls_back_to_fp64(gpu):
+    """Steady heterogeneous 375 x 375 quads: the FP32 recurrence stalls
+    (cond(A) near 1/eps_fp32 for the Jacobi-scaled operator); the solve
+    detects the stalled cycle, finishes in FP64 CG from the accumulated x64
+    and still meets the tolerance and the FP64 path's heads."""
+    m = M.structured_quad(375, 375)
+    ek = fields.lognormal_k(m.shape, np.log(1e-5), 1.0, 8.0, seed=3)
+    eqs, x0 = _deck(gpu, m, ek, steady=True)
+    x64, it64, x32, it32, st = _both(gpu, eqs, x0)
+    assert st["status"] == gpu.OK and st["rel_residual"] < 1e-10
+    assert st["fp64_fallback"] == 1
+    assert rel_max_err(x32, x64) < MIXED_RTOL
+
+
+def test_fp32_no_fallback_when_cycles_gain(gpu):
+    """Transient hex deck: every FP32 cycle gains about 1/delta, no fallback."""
+    m = M.structured_hex(24, 20, 12)
+    ek = fields.lognormal_k(m.shape, np.log(1e-5), 1.0, 4.0, seed=6)
+    eqs, x0 = _deck(gpu, m, ek)
+    x64, it64, x32, it32, st = _both(gpu, eqs, x0)
+    assert st["status"] == gpu.OK and st["fp64_fallback"] == 0
+    assert rel_max_err(x32, x64) < MIXED_RTOL
