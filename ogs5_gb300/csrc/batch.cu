@@ -413,8 +413,18 @@ __device__ void phase_a(const BatchArgs& a, int g)
         const float* U = a.U32 + 14 * r0;
         const float* u = a.u32 + r0;
         float v[3] = {0.f, 0.f, 0.f};
-        for (int i = T.i0 + threadIdx.x; i < T.i1; i += NT)
+        for (int c = T.i0; c < T.i1; c += NT)
         {
+            // bulk L2 prefetch of the next chunk of every other operator
+            // stream (as the single-system FP32 SpMV)
+            const int d = 2 * threadIdx.x, nb = c + NT;
+            if (d < 14 && nb < T.i1)
+            {
+                const float* seg = U + (size_t)d * R.n;
+                bulk_prefetch_l2(seg + nb, (size_t)min(NT, T.i1 - nb) * sizeof(float), seg, seg + R.n);
+            }
+            const int i = c + threadIdx.x;
+            if (i >= T.i1) continue;
             const float w = row32(U, R.nx, nxy, R.n, i, u);
             a.w32[r0 + i] = w;
             const float ui = u[i], ri = a.r32[r0 + i];

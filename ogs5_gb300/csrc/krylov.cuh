@@ -231,6 +231,18 @@ __device__ __forceinline__ void reduce_partials(const double* part, int nb, doub
     __syncthreads();
 }
 
+// cp.async.bulk.prefetch.L2 of [p, p + bytes), widened to 16-byte
+// boundaries (the instruction's alignment rule) and clipped to [lo, hi)
+__device__ __forceinline__ void bulk_prefetch_l2(const void* p, size_t bytes, const void* lo, const void* hi)
+{
+    size_t b = (size_t)p & ~(size_t)15;
+    size_t e = ((size_t)p + bytes + 15) & ~(size_t)15;
+    const size_t l = ((size_t)lo + 15) & ~(size_t)15, h = (size_t)hi & ~(size_t)15;
+    if (b < l) b = l;
+    if (e > h) e = h;
+    if (e > b) asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(b), "r"((unsigned)(e - b)) : "memory");
+}
+
 // Arguments of the FP32-inner / FP64-refinement kernels (mixed.cu).
 struct MixedArgs
 {
