@@ -258,7 +258,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_mp_spmv(MixedArgs a)
     write_partials<3, float>(v, st->cg_ps);
 }
 
-constexpr int kU32 = 4;  // elements per thread per step, loaded before use
+constexpr int kU32 = 8;  // elements per thread per step, loaded before use
 
 // V: scalars from the S partials ; replacement test ; p, s, x32, r32, u32
 __global__ void __launch_bounds__(kThreads) k_mp_update(MixedArgs a)
