@@ -232,6 +232,73 @@ def cpu_baseline_sample():
 
 
 # ------------------------------------------------------------------
+# Transport on the Kuhn-tet split of the deck (flow -> Darcy flux ->
+# MASS_TRANSPORT with BiCGStab + ILU(0))
+# ------------------------------------------------------------------
+TRANSPORT_WORKLOAD = ("hex 128x128x64 split into 6 Kuhn tets (6,291,456 tets, 1,081,665 nodes), conductivity "
+                      "of the parent hex; one transient flow step (CG + Jacobi, FP32 inner) -> Gauss-point "
+                      "Darcy flux -> one MASS_TRANSPORT step (dt 3600 s, porosity 0.3, alpha_L/alpha_T "
+                      "1.0/0.1 m, D 1e-9 m2/s, c = 1 on x = 0), BiCGStab 1e-10")
+
+
+def transport_leg(capi, torch, steps=3):
+    """One MASS_TRANSPORT step per measured step, ILU(0) and Jacobi."""
+    from ogs5_gb300 import fields
+    from ogs5_gb300 import mesh as M
+    m = M.structured_tet(NX, NY, NZ)
+    ek = torch.tensor(np.repeat(fields.lognormal_k((NX, NY, NZ), np.log(1e-5), 1.0, 8.0, seed=SEED), 6),
+                      device="cuda")
+    gm = capi.GpuMesh(m)
+    lf, rf = m.face_nodes(0, 0), m.face_nodes(0, 1)
+    # flow step from h0 (heads 10 / 0 on the x faces)
+    flow = capi.LinearEQS(gm)
+    flow.ConfigNumerics(capi.LS_CG, capi.PRECOND_JACOBI, 20000, TOL, precision=capi.PRECISION_FP32_REFINED)
+    h0 = np.zeros(m.n_nodes)
+    h0[lf] = 10.0
+    h = torch.tensor(h0, device="cuda")
+    flow.Initialize()
+    flow.GlobalAssembly(capi.make_params(capi.GROUNDWATER_FLOW, dt=DT, storage=SS), ek, h)
+    flow.SetKnownX(np.concatenate([lf, rf]), np.concatenate([np.full(len(lf), 10.0), np.zeros(len(rf))]),
+                   capi.DIRICHLET_SYMMETRIC)
+    flow_it = flow.Solver(h)
+    q = torch.empty((m.n_elements, gm.n_gauss, 3), dtype=torch.float64, device="cuda")
+    flow.gp_velocity(capi.make_params(capi.GROUNDWATER_FLOW), ek, h, q)
+    del flow
+    p = capi.make_params(capi.MASS_TRANSPORT, dt=DT, porosity=0.3, alpha_l=1.0, alpha_t=0.1, diffusion=1e-9)
+    mt = capi.LinearEQS(gm)
+    c0 = torch.zeros(m.n_nodes, dtype=torch.float64, device="cuda")
+    rows = torch.tensor(lf, device="cuda")
+    vals = torch.ones(len(lf), dtype=torch.float64, device="cuda")
+    out = {"workload": TRANSPORT_WORKLOAD, "nodes": m.n_nodes, "elements": m.n_elements,
+           "flow_fp32_iterations": flow_it}
+    res = {}
+    for name, pre in (("ilu0", capi.PRECOND_ILU0), ("jacobi", capi.PRECOND_JACOBI)):
+        mt.ConfigNumerics(capi.LS_BICGSTAB, pre, 5000, TOL, check_norm_rhs=False)
+        times, its = [], []
+        for k in range(steps + 1):
+            x = c0.clone()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            mt.Initialize()
+            mt.GlobalAssembly(p, None, c0, q)
+            mt.SetKnownX(rows, vals, capi.DIRICHLET_ROW_ONLY)
+            its.append(mt.Solver(x))
+            e1.record()
+            e1.synchronize()
+            if k:  # the first step builds the graphs and factor buffers
+                times.append(e0.elapsed_time(e1))
+        st = mt.stats()
+        res[name] = x
+        out[name] = {"value": round(1e3 / statistics.median(times), 3), "unit": "solves/s",
+                     "ms_per_step": round(statistics.median(times), 3), "iterations": its[-1],
+                     "solve_ms": round(st["solve_ms"], 3), "rel_residual": st["rel_residual"]}
+    out["max_rel_diff_ilu0_vs_jacobi"] = float((res["ilu0"] - res["jacobi"]).abs().max()
+                                               / res["jacobi"].abs().max())
+    return out
+
+
+# ------------------------------------------------------------------
 # Monte-Carlo batch (512 steady realisations of uneven size)
 # ------------------------------------------------------------------
 BATCH_REALS = 512
@@ -589,7 +656,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--path", default="both", choices=["both", "fp64", "mixed", "batch", "serve"],
+    ap.add_argument("--path", default="both", choices=["both", "fp64", "mixed", "batch", "serve", "transport"],
                     help="fp64 / mixed / batch: time one path only (profiling driver)")
     ap.add_argument("--batch-reals", type=int, default=BATCH_REALS)
     ap.add_argument("--batch-max-n", type=int, default=96)
@@ -597,6 +664,7 @@ def main():
     ap.add_argument("--batch-plain", action="store_true", help="--path batch: also time the FP64 path")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-transport", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=SERVE_REQUESTS)
     ap.add_argument("--serve-flags", type=int, default=None)
     ap.add_argument("--serve-max-active", type=int, default=None)
@@ -614,6 +682,10 @@ def main():
     B.build()
     from ogs5_gb300 import capi
 
+    if args.path == "transport":
+        from ogs5_gb300 import capi
+        print(json.dumps(transport_leg(capi, torch, steps=max(1, args.steps))))
+        return
     if args.path == "serve":
         from ogs5_gb300 import capi
         print(json.dumps(serve_leg(capi, torch, n_req=args.serve_requests, flags=args.serve_flags,
@@ -711,6 +783,8 @@ def main():
                      "launches": pr["spmv_launches"], "peak_kind": peak_kind},
         "clocks": clk.summary(),
     }
+    if not args.no_transport:
+        out["transport"] = transport_leg(capi, torch)
     if not args.no_serve:
         out["serve"] = serve_leg(capi, torch, n_req=args.serve_requests)
     if not args.no_batch:
