@@ -127,7 +127,10 @@ typedef struct
     double gravity;            /* gravity_constant; < DBL_EPSILON = HEAD form  */
     int32_t gravity_on;        /* coordinate_system % 10 == 2 and
                                   FluidProp->CheckGravityCalculation()         */
-    int32_t pad0;
+    int32_t mass_lumping;      /* m_num->ele_mass_lumping (rf_num_new.cpp:125,
+                                  684): the mass matrix becomes diagonal,
+                                  CalCoefMass * element volume / nodes
+                                  (CalcLumpedMass, fem_ele_std.cpp:4598-4660) */
     double alpha_l;            /* MT: mass_dispersion_longitudinal             */
     double alpha_t;            /* MT: mass_dispersion_transverse               */
     double diffusion;          /* MT: Daq * TortuosityFunction                 */

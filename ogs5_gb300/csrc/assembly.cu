@@ -152,6 +152,55 @@ __device__ __forceinline__ double flow_mat(const ogs_assembly_params& p, double 
     return k * p.time_unit_factor * 1.0;
 }
 
+// CElem::calcVolume (MSH/msh_elem.cpp:1511-1576) with ComputeDetTri /
+// ComputeDetTex (FEM/mathlib.cpp:2911-2955): quads as two triangles,
+// hexahedra as six tetrahedra in the mesh's node order
+__device__ __forceinline__ double vol_tri(const double* X, const double* Y, const double* Z, int a, int b, int c)
+{
+    const double u0 = X[c] - X[a], u1 = Y[c] - Y[a], u2 = Z[c] - Z[a];
+    const double v0 = X[b] - X[a], v1 = Y[b] - Y[a], v2 = Z[b] - Z[a];
+    const double z0 = u1 * v2 - u2 * v1, z1 = u2 * v0 - u0 * v2, z2 = u0 * v1 - u1 * v0;
+    return 0.5 * sqrt(z0 * z0 + z1 * z1 + z2 * z2);
+}
+
+__device__ __forceinline__ double vol_tet(const double* X, const double* Y, const double* Z, int a, int b, int c,
+                                          int d)
+{
+    const double ax = X[a] - X[d], ay = Y[a] - Y[d], az = Z[a] - Z[d];
+    const double bx = X[b] - X[d], by = Y[b] - Y[d], bz = Z[b] - Z[d];
+    const double cx = X[c] - X[d], cy = Y[c] - Y[d], cz = Z[c] - Z[d];
+    return fabs(ax * (by * cz - bz * cy) - ay * (bx * cz - bz * cx) + az * (bx * cy - by * cx)) / 6.0;
+}
+
+template <int ET>
+__device__ __forceinline__ double element_volume(const double* X, const double* Y, const double* Z)
+{
+    if (ET == OGS_ELEM_QUAD4) return vol_tri(X, Y, Z, 0, 1, 2) + vol_tri(X, Y, Z, 2, 3, 0);
+    if (ET == OGS_ELEM_TET4) return vol_tet(X, Y, Z, 0, 1, 2, 3);
+    double v = vol_tet(X, Y, Z, 4, 7, 5, 0);
+    v += vol_tet(X, Y, Z, 5, 3, 1, 0);
+    v += vol_tet(X, Y, Z, 5, 7, 3, 0);
+    v += vol_tet(X, Y, Z, 5, 7, 6, 2);
+    v += vol_tet(X, Y, Z, 1, 3, 5, 2);
+    v += vol_tet(X, Y, Z, 3, 7, 5, 2);
+    return v;
+}
+
+// CalcLumpedMass (fem_ele_std.cpp:4598-4660), selected by
+// m_num->ele_mass_lumping: the packed lower-triangle mass becomes
+// diag(CalCoefMass * ElementVolumeMultiplyer (1) * volume / nnodes)
+template <int ET, int NN>
+__device__ __forceinline__ void lump_mass(const double* X, const double* Y, const double* Z, double cm, double* Ml)
+{
+    double f = cm;
+    f *= 1.0;
+    f *= element_volume<ET>(X, Y, Z) / (double)NN;
+#pragma unroll
+    for (int i = 0; i < NN; i++)
+#pragma unroll
+        for (int j = 0; j <= i; j++) Ml[i * (i + 1) / 2 + j] = i == j ? f : 0.0;
+}
+
 // CalCoefMass for GWF (StorageFunction) and LIQUID_FLOW (Ss + n drho/dp)
 __device__ __forceinline__ double flow_mass_coef(const ogs_assembly_params& p)
 {
@@ -293,6 +342,7 @@ __global__ void __launch_bounds__(128) k_flow_general(AsmArgs a)
             }
         }
         if (!ok) { flag_bad(a.bad_elem, e); continue; }
+        if (a.p.mass_lumping) lump_mass<ET, NN>(X, Y, Z, cm, Ml);
         flow_combine<NN>(a, e, nd, U, Ml, Ll, grav);
     }
 }
@@ -343,6 +393,7 @@ __global__ void __launch_bounds__(128) k_flow_affine(AsmArgs a)
                 Ll[l] = s;
                 Ml[l] = md * sM0[i * NN + j];
             }
+        if (a.p.mass_lumping) lump_mass<ET, NN>(X, Y, Z, cm, Ml);
 #pragma unroll
         for (int i = 0; i < NN; i++) grav[i] = 0.0;
         if (a.p.pcs_type == OGS_PCS_LIQUID_FLOW && a.p.gravity_on)
@@ -472,6 +523,7 @@ __global__ void __launch_bounds__(128) k_mt_general(AsmArgs a)
             }
         }
         if (!ok) { flag_bad(a.bad_elem, e); continue; }
+        if (p.mass_lumping) lump_mass<ET, NN>(X, Y, Z, cm, Ml);
         mt_combine<NN>(a, e, nd, U, Ml, L, A, St);
     }
 }
@@ -548,6 +600,7 @@ __global__ void __launch_bounds__(128) k_mt_tet_affine(AsmArgs a)
                 Ml[l] = cm * det * sM0[i * NN + j];
                 St[l] = cs * det * sM0[i * NN + j];
             }
+        if (p.mass_lumping) lump_mass<OGS_ELEM_TET4, NN>(X, Y, Z, cm, Ml);
         mt_combine<NN>(a, e, nd, U, Ml, L, A, St);
     }
 }

@@ -371,6 +371,53 @@ static void dispersion_tensor(int dim, const ogs_assembly_params* p,
         for (int i = 0; i < dim * dim; i++) D[i] = md[i];
 }
 
+/* ComputeDetTri (FEM/mathlib.cpp:2911-2928): area of the triangle */
+static double det_tri(const double* x1, const double* x2, const double* x3)
+{
+    double u[3], v[3], z[3];
+    for (int k = 0; k < 3; k++)
+    {
+        u[k] = x3[k] - x1[k];
+        v[k] = x2[k] - x1[k];
+    }
+    z[0] = u[1] * v[2] - u[2] * v[1];
+    z[1] = u[2] * v[0] - u[0] * v[2];
+    z[2] = u[0] * v[1] - u[1] * v[0];
+    return 0.5 * sqrt(z[0] * z[0] + z[1] * z[1] + z[2] * z[2]);
+}
+
+/* ComputeDetTex (FEM/mathlib.cpp:2945-2955): volume of the tetrahedron */
+static double det_tex(const double* x1, const double* x2, const double* x3, const double* x4)
+{
+    return fabs((x1[0] - x4[0]) * ((x2[1] - x4[1]) * (x3[2] - x4[2]) - (x2[2] - x4[2]) * (x3[1] - x4[1])) -
+                (x1[1] - x4[1]) * ((x2[0] - x4[0]) * (x3[2] - x4[2]) - (x2[2] - x4[2]) * (x3[0] - x4[0])) +
+                (x1[2] - x4[2]) * ((x2[0] - x4[0]) * (x3[1] - x4[1]) - (x2[1] - x4[1]) * (x3[0] - x4[0]))) /
+           6.0;
+}
+
+/* CElem::calcVolume (MSH/msh_elem.cpp:1511-1576): quads as two triangles,
+ * hexahedra as six tetrahedra, in the node order of the mesh */
+double orc_element_volume(int etype, const double* X, const double* Y, const double* Z)
+{
+    double P[8][3];
+    const int nn = orc_nodes_per_element(etype);
+    for (int i = 0; i < nn; i++)
+    {
+        P[i][0] = X[i];
+        P[i][1] = Y[i];
+        P[i][2] = Z ? Z[i] : 0.0;
+    }
+    if (etype == OGS_ELEM_QUAD4) return det_tri(P[0], P[1], P[2]) + det_tri(P[2], P[3], P[0]);
+    if (etype == OGS_ELEM_TET4) return det_tex(P[0], P[1], P[2], P[3]);
+    double v = det_tex(P[4], P[7], P[5], P[0]);
+    v += det_tex(P[5], P[3], P[1], P[0]);
+    v += det_tex(P[5], P[7], P[3], P[0]);
+    v += det_tex(P[5], P[7], P[6], P[2]);
+    v += det_tex(P[1], P[3], P[5], P[2]);
+    v += det_tex(P[3], P[7], P[5], P[2]);
+    return v;
+}
+
 /* Local matrices of one element:
  *   CalcMass (fem_ele_std.cpp:3753-3900) with CalCoefMass (:1569-1717),
  *   CalcLaplace (:4948-5070) with CalCoefLaplace (:2202-2384, :2545-2562),
@@ -493,6 +540,16 @@ int orc_element_matrices(int etype, int ngauss, int dim, const double* X,
     for (int i = 0; i < nn; i++)
         for (int j = 0; j < nn; j++)
             if (i > j) m->mass[j * nn + i] = m->mass[i * nn + j];
+    if (p->mass_lumping)
+    {
+        /* CalcLumpedMass (fem_ele_std.cpp:4598-4660): factor = CalCoefMass()
+         * * ElementVolumeMultiplyer (1) * volume / nnodes on the diagonal */
+        double factor = c_mass;
+        factor *= 1.0;
+        factor *= orc_element_volume(etype, X3, Y3, Z3) / (double)nn;
+        for (int i = 0; i < nn * nn; i++) m->mass[i] = 0.0;
+        for (int i = 0; i < nn; i++) m->mass[i * nn + i] = factor;
+    }
     return 0;
 }
 

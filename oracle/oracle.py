@@ -46,7 +46,7 @@ class AssemblyParams(C.Structure):
         ("time_unit_factor", C.c_double), ("storage", C.c_double),
         ("porosity", C.c_double), ("drho_dp", C.c_double),
         ("viscosity", C.c_double), ("density", C.c_double),
-        ("gravity", C.c_double), ("gravity_on", C.c_int32), ("pad0", C.c_int32),
+        ("gravity", C.c_double), ("gravity_on", C.c_int32), ("mass_lumping", C.c_int32),
         ("alpha_l", C.c_double), ("alpha_t", C.c_double),
         ("diffusion", C.c_double), ("decay", C.c_double),
         ("retardation", C.c_double), ("saturation", C.c_double),

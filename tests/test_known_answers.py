@@ -131,3 +131,30 @@ def test_ilu0_reproduces_matrix_on_pattern(oracle):
         for k in range(trp[i], trp[i + 1]):
             (L if tcol[k] < i else U)[i, tcol[k]] = tlu[k]
     assert np.allclose(L @ U, T, rtol=1e-13, atol=1e-14)
+
+
+@pytest.mark.parametrize("et,vol", [(0, 1.0), (1, 1.0), (2, None)])
+def test_lumped_mass_is_volume_over_nodes(oracle, et, vol):
+    """ele_mass_lumping: the mass matrix is diag(c * V_e / n) (CalcLumpedMass),
+    V_e from the mesh's volume decomposition; its sum equals the consistent
+    mass's sum, c * V_e."""
+    c = unit_elem(et)
+    nn = c.shape[0]
+    cons = oracle.element_matrices(et, c, oracle.make_params(pcs_type=0, storage=2.5), k_e=1.0)["mass"]
+    lump = oracle.element_matrices(et, c, oracle.make_params(pcs_type=0, storage=2.5, mass_lumping=1),
+                                   k_e=1.0)["mass"]
+    assert np.count_nonzero(lump - np.diag(np.diag(lump))) == 0
+    assert np.allclose(np.diag(lump), lump[0, 0], rtol=0, atol=0)
+    assert abs(lump.sum() - cons.sum()) < 1e-13 * abs(cons.sum())
+    if vol is not None:
+        assert abs(lump[0, 0] - 2.5 * vol / nn) < 1e-14
+    # distorted hexahedron: the six-tetrahedra volume, not the Gauss volume
+    if et == 1:
+        d = c.copy()
+        d[6] += np.array([0.3, 0.2, 0.1])
+        tets = [(4, 7, 5, 0), (5, 3, 1, 0), (5, 7, 3, 0), (5, 7, 6, 2), (1, 3, 5, 2), (3, 7, 5, 2)]
+        v = sum(abs(np.linalg.det(np.array([d[a] - d[q], d[b] - d[q], d[cc] - d[q]]))) / 6
+                for a, b, cc, q in tets)
+        lm = oracle.element_matrices(1, d, oracle.make_params(pcs_type=0, storage=1.0, mass_lumping=1),
+                                     k_e=1.0)["mass"]
+        assert abs(lm[0, 0] - v / 8) < 1e-14

@@ -118,6 +118,33 @@ def test_assembly_mass_transport(gpu, oracle, kind, distorted):
 
 @pytest.mark.parametrize("kind", ["quad", "hex", "tet"])
 @pytest.mark.parametrize("distorted", [False, True])
+@pytest.mark.parametrize("pcs", ["flow", "transport"])
+def test_assembly_mass_lumping(gpu, oracle, kind, distorted, pcs):
+    """ele_mass_lumping on the affine and per-Gauss-point kernels, flow and
+    transport: every entry within 1e-12 of the oracle's CalcLumpedMass."""
+    m = small_mesh(kind)
+    if distorted:
+        m = distort(m, 0.2, seed=5)
+    rng = np.random.default_rng(21)
+    u0 = rng.uniform(0, 1, m.n_nodes)
+    if pcs == "flow":
+        p = gpu.make_params(gpu.GROUNDWATER_FLOW, dt=600.0, storage=1e-3, mass_lumping=1)
+        out = run_assembly(gpu, oracle, m, p, k_field(m, 6), u0)
+    else:
+        ngp = {"quad": 9, "hex": 27, "tet": 5}[kind]
+        gpv = rng.normal(0, 1e-5, (m.n_elements, ngp, 3))
+        if m.dim == 2:
+            gpv[:, :, 2] = 0.0
+        p = gpu.make_params(gpu.MASS_TRANSPORT, dt=600.0, theta=0.7, porosity=0.3, alpha_l=1.0,
+                            alpha_t=0.1, diffusion=1e-9, decay=1e-7, retardation=1.5, mass_lumping=1)
+        out = run_assembly(gpu, oracle, m, p, None, u0, gpv)
+    _, _, (rp, col, val, b), (oval, ob) = out
+    assert_matrix_close(rp, val, oval)
+    assert_vector_close(b, ob)
+
+
+@pytest.mark.parametrize("kind", ["quad", "hex", "tet"])
+@pytest.mark.parametrize("distorted", [False, True])
 def test_gp_velocity(gpu, oracle, kind, distorted):
     m = small_mesh(kind)
     if distorted:
