@@ -137,6 +137,19 @@ typedef struct
     double decay;              /* MT: CalcElementDecayRateNew                  */
     double retardation;        /* MT: CalcElementRetardationFactorNew          */
     double saturation;         /* MT: SATURATION1 of the flow process (1)      */
+    int32_t supg_method;       /* MT: m_num->ele_supg_method (rf_num_new.cpp:704):
+                                  0 off, 1 tau from the Langevin function,
+                                  2 tau with the time step
+                                  (CalcSUPGCoefficient, fem_ele_std.cpp:3908) */
+    int32_t supg_length;       /* ele_supg_method_length: 0 longest edge,
+                                  1 shortest, 2 "average" (the reference sums
+                                  edges 1..n-1 and divides by n)
+                                  (CalcSUPGEffectiveElemenetLength, :4034)     */
+    int32_t supg_diffusivity;  /* ele_supg_method_diffusivity: 0 largest entry
+                                  of the dispersion tensor, 1 smallest, 2 the
+                                  last diagonal entry (the reference assigns
+                                  rather than sums the squares)                */
+    int32_t pad1;
 } ogs_assembly_params;
 
 /* Linear_EQS::ConfigNumerics inputs (CNumerics, FEM/rf_num_new.h:34-60). */

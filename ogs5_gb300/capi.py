@@ -79,6 +79,8 @@ class AssemblyParams(C.Structure):
         ("alpha_l", C.c_double), ("alpha_t", C.c_double),
         ("diffusion", C.c_double), ("decay", C.c_double),
         ("retardation", C.c_double), ("saturation", C.c_double),
+        ("supg_method", C.c_int32), ("supg_length", C.c_int32), ("supg_diffusivity", C.c_int32),
+        ("pad1", C.c_int32),
     ]
 
 

@@ -110,8 +110,8 @@ __device__ __forceinline__ void grad_global(const double* iJ, const double* dN, 
 // MassDispersionTensorNew (FEM/rf_mmp_new.cpp:3090-3328), isotropic
 // tortuosity: D = n S Daq tau I + alpha_T |q| I + (alpha_L - alpha_T) q q^T / |q|
 template <int DIM>
-__device__ __forceinline__ void dispersion(const ogs_assembly_params& p, const double* v,
-                                           double* D)
+__device__ __forceinline__ void dispersion_raw(const ogs_assembly_params& p, const double* v,
+                                               double* D)
 {
     const double dm = p.diffusion * p.porosity * p.saturation;
     const double vg = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
@@ -134,8 +134,115 @@ __device__ __forceinline__ void dispersion(const ogs_assembly_params& p, const d
 #pragma unroll
         for (int i = 0; i < DIM; i++) D[i * DIM + i] = dm;
     }
+}
+
+template <int DIM>
+__device__ __forceinline__ void dispersion(const ogs_assembly_params& p, const double* v, double* D)
+{
+    dispersion_raw<DIM>(p, v, D);
 #pragma unroll
     for (int i = 0; i < DIM * DIM; i++) D[i] = D[i] * 1.0 * p.time_unit_factor;
+}
+
+// MLangevin (FEM/mathlib.cpp:3009-3021): coth(v) - 1/v, its series below 0.01
+__device__ __forceinline__ double langevin(double v)
+{
+    double s = 0.0;
+    if (v < 0.01)
+        s = v * (1.0 / 3.0 + v * v * (-1.0 / 45.0 + 18.0 / 8505.0 * v * v));
+    else if (0.01 <= v && v < 20)
+        s = (exp(v) + exp(-v)) / (exp(v) - exp(-v)) - 1 / v;
+    else if (20 <= v)
+        s = 1.0;
+    return s;
+}
+
+// CalcSUPGEffectiveElemenetLength (fem_ele_std.cpp:4034-4095) over the edges
+// of CElem::GetLocalIndicesOfEdgeNodes (MSH/msh_elem.cpp:984-1052)
+template <int ET>
+__device__ __forceinline__ double supg_length(const double* X, const double* Y, const double* Z, int method)
+{
+    constexpr int NE = ET == OGS_ELEM_HEX8 ? 12 : ET == OGS_ELEM_QUAD4 ? 4 : 6;
+    double len[NE];
+#pragma unroll
+    for (int e = 0; e < NE; e++)
+    {
+        int a, b;
+        if (ET == OGS_ELEM_QUAD4) { a = e; b = (e + 1) % 4; }
+        else if (ET == OGS_ELEM_HEX8)
+        {
+            if (e < 8) { a = e; b = (e + 1) % 4 + 4 * (e / 4); }
+            else { a = e % 4; b = e % 4 + 4; }
+        }
+        else if (e < 3) { a = e; b = (e + 1) % 3; }
+        else { a = 3; b = (e + 1) % 3; }
+        const double dx = X[b] - X[a], dy = Y[b] - Y[a], dz = Z[b] - Z[a];
+        len[e] = sqrt(dx * dx + dy * dy + dz * dz);
+    }
+    double L = 0.0;
+    if (method == 1)
+    {
+        double mn = len[0];
+#pragma unroll
+        for (int e = 1; e < NE; e++) { L = len[e]; if (L < mn) mn = L; }
+        L = mn;
+    }
+    else if (method == 2)
+    {
+        double t = 0.0;
+#pragma unroll
+        for (int e = 1; e < NE; e++) t += len[e];  // the reference starts at edge 1
+        L = t / NE;
+    }
+    else
+    {
+        double mx = len[0];
+#pragma unroll
+        for (int e = 1; e < NE; e++) { L = len[e]; if (L > mx) mx = L; }
+        L = mx;
+    }
+    return L;
+}
+
+// CalcSUPGCoefficient (fem_ele_std.cpp:3908-3995), MASS_TRANSPORT; D is the
+// raw MassDispersionTensorNew of the Gauss point
+template <int DIM>
+__device__ __forceinline__ double supg_tau(const ogs_assembly_params& p, const double* vel, const double* D, double L)
+{
+    const double v_mag = sqrt(vel[0] * vel[0] + vel[1] * vel[1] + vel[2] * vel[2]);
+    if (v_mag == 0.0) return 0.0;
+    double diff;
+    if (p.supg_diffusivity == 1)
+    {
+        diff = D[0];
+#pragma unroll
+        for (int i = 1; i < DIM * DIM; i++)
+            if (D[i] < diff) diff = D[i];
+    }
+    else if (p.supg_diffusivity == 2)
+    {
+        double t = 0.0;
+#pragma unroll
+        for (int i = 0; i < DIM; i++) t = D[i + i * DIM] * D[i + i * DIM];  // the reference assigns
+        diff = sqrt(t);
+    }
+    else
+    {
+        diff = D[0];
+#pragma unroll
+        for (int i = 1; i < DIM * DIM; i++)
+            if (D[i] > diff) diff = D[i];
+    }
+    double tau = 0.0;
+    if (p.supg_method == 1)
+    {
+        const double alpha = 0.5 * v_mag * L / diff;
+        tau = 0.5 * L / v_mag * langevin(alpha);
+    }
+    else if (p.supg_method == 2)
+        tau = 1.0 / sqrt((2.0 / p.dt) * (2.0 / p.dt) + (2.0 * v_mag / L) * (2.0 * v_mag / L) +
+                         (4.0 * diff / (L * L)) * (4.0 * diff / (L * L)));
+    return tau;
 }
 
 // flow coefficient of the Laplace term: CalCoefLaplace GWF (:2308-2384,
@@ -424,8 +531,9 @@ template <int NN>
 __device__ __forceinline__ void mt_combine(const AsmArgs& a, int64_t e, const int* nd,
                                            const double* U, const double* Ml,
                                            const double* L, const double* A,
-                                           const double* St)
+                                           const double* St, const double* Mx = nullptr)
 {
+    // Mx: the non-symmetric SUPG mass term (full NN x NN), added to the mass
     // AssembleMixedHyperbolicParabolicEquation (fem_ele_std.cpp:8592-8692)
     const double dt_inverse = 1.0 / a.p.dt;
     const double th = a.p.theta;
@@ -439,12 +547,13 @@ __device__ __forceinline__ void mt_combine(const AsmArgs& a, int64_t e, const in
         {
             const int l = i >= j ? i * (i + 1) / 2 + j : j * (j + 1) / 2 + i;
             const int k = i * NN + j;
-            double s = Ml[l] * dt_inverse;
+            const double mij = Mx ? Ml[l] + Mx[k] : Ml[l];
+            double s = mij * dt_inverse;
             s += L[k] * th;
             s += A[k] * th;
             s += St[l] * th;
             S[k] = s;
-            double q = Ml[l] * dt_inverse;
+            double q = mij * dt_inverse;
             q += L[k] * (-(1.0 - th));
             q += A[k] * (-(1.0 - th));
             q += St[l] * (-(1.0 - th));
@@ -453,7 +562,8 @@ __device__ __forceinline__ void mt_combine(const AsmArgs& a, int64_t e, const in
     scatter<NN>(a, e, nd, S, r);
 }
 
-template <int ET, int NGP>
+// SUPG: with the streamline-upwind terms of ele_supg_method > 0
+template <int ET, int NGP, bool SUPG>
 __global__ void __launch_bounds__(128) k_mt_general(AsmArgs a)
 {
     constexpr int NN = ElemTraits<ET>::NN, DIM = ElemTraits<ET>::DIM;
@@ -472,10 +582,14 @@ __global__ void __launch_bounds__(128) k_mt_general(AsmArgs a)
         double X[NN], Y[NN], Z[NN], U[NN];
         gather<NN>(a, e, nd, X, Y, Z, U);
         double Ml[NN * (NN + 1) / 2], St[NN * (NN + 1) / 2], L[NN * NN], A[NN * NN];
+        double Mx[SUPG ? NN * NN : 1];
 #pragma unroll
         for (int l = 0; l < NN * (NN + 1) / 2; l++) Ml[l] = St[l] = 0.0;
 #pragma unroll
         for (int k = 0; k < NN * NN; k++) L[k] = A[k] = 0.0;
+#pragma unroll
+        for (int k = 0; k < (SUPG ? NN * NN : 1); k++) Mx[k] = 0.0;
+        const double Lsupg = SUPG ? supg_length<ET>(X, Y, Z, p.supg_length) : 0.0;
         bool ok = true;
         const double* ve = a.gpv + e * NGP * 3;
 #pragma unroll 1
@@ -521,10 +635,40 @@ __global__ void __launch_bounds__(128) k_mt_general(AsmArgs a)
                     A[i * NN + j] = t;
                 }
             }
+            if constexpr (SUPG)
+            {
+                // CalcSUPGWeightingFunction (fem_ele_std.cpp:4004-4025): w_i =
+                // v . grad N_i with the raw flux; SUPG mass (CalcMass :3856-3879)
+                // and advection (CalcAdvection :5467-5490) terms
+                double Dr[DIM * DIM], wf[NN];
+                dispersion_raw<DIM>(p, v, Dr);
+                const double tau = supg_tau<DIM>(p, v, Dr, Lsupg);
+#pragma unroll
+                for (int i = 0; i < NN; i++)
+                {
+                    wf[i] = 0.0;
+#pragma unroll
+                    for (int k = 0; k < DIM; k++) wf[i] += dNg[k * NN + i] * v[k];
+                }
+#pragma unroll
+                for (int i = 0; i < NN; i++)
+#pragma unroll
+                    for (int j = 0; j < NN; j++)
+                    {
+                        Mx[i * NN + j] += mf * tau * wf[i] * sf[j];
+                        A[i * NN + j] += fkt * (1.0 * p.time_unit_factor) * tau * wf[i] * wf[j];
+                    }
+            }
         }
         if (!ok) { flag_bad(a.bad_elem, e); continue; }
-        if (p.mass_lumping) lump_mass<ET, NN>(X, Y, Z, cm, Ml);
-        mt_combine<NN>(a, e, nd, U, Ml, L, A, St);
+        if (p.mass_lumping)
+        {
+            // CalcLumpedMass has no SUPG term
+            lump_mass<ET, NN>(X, Y, Z, cm, Ml);
+            mt_combine<NN>(a, e, nd, U, Ml, L, A, St);
+        }
+        else
+            mt_combine<NN>(a, e, nd, U, Ml, L, A, St, SUPG ? Mx : nullptr);
     }
 }
 
@@ -675,10 +819,13 @@ template <int ET, int NGP>
 static void launch_mt(const AsmArgs& a, bool affine, cudaStream_t s)
 {
     const int g = grid_for(a.E, 128);
-    if (ET == OGS_ELEM_TET4 && affine)
+    // the affine tet kernel folds the Gauss points away; SUPG needs them
+    if (ET == OGS_ELEM_TET4 && affine && a.p.supg_method == 0)
         k_mt_tet_affine<<<g, 128, 0, s>>>(a);
+    else if (a.p.supg_method > 0)
+        k_mt_general<ET, NGP, true><<<g, 128, 0, s>>>(a);
     else
-        k_mt_general<ET, NGP><<<g, 128, 0, s>>>(a);
+        k_mt_general<ET, NGP, false><<<g, 128, 0, s>>>(a);
 }
 
 template <int ET, int NGP>

@@ -418,6 +418,113 @@ double orc_element_volume(int etype, const double* X, const double* Y, const dou
     return v;
 }
 
+/* MLangevin (FEM/mathlib.cpp:3009-3021): coth(v) - 1/v, its series
+ * v/3 - v^3/45 + 2 v^5/945 below 0.01, 1 from 20 on */
+static double langevin(double v)
+{
+    double s = 0.0;
+    if (v < 0.01)
+        s = v * (1.0 / 3.0 + v * v * (-1.0 / 45.0 + 18.0 / 8505.0 * v * v));
+    else if (0.01 <= v && v < 20)
+        s = (exp(v) + exp(-v)) / (exp(v) - exp(-v)) - 1 / v;
+    else if (20 <= v)
+        s = 1.0;
+    return s;
+}
+
+/* CalcSUPGEffectiveElemenetLength (fem_ele_std.cpp:4034-4095) over the
+ * edges of CElem::GetLocalIndicesOfEdgeNodes (MSH/msh_elem.cpp:984-1052) */
+double orc_supg_length(int etype, const double* X, const double* Y, const double* Z, int method)
+{
+    int ne, a[12], b[12];
+    if (etype == OGS_ELEM_QUAD4)
+    {
+        ne = 4;
+        for (int e = 0; e < 4; e++) { a[e] = e; b[e] = (e + 1) % 4; }
+    }
+    else if (etype == OGS_ELEM_HEX8)
+    {
+        ne = 12;
+        for (int e = 0; e < 12; e++)
+        {
+            if (e < 8) { a[e] = e; b[e] = (e + 1) % 4 + 4 * (e / 4); }
+            else { a[e] = e % 4; b[e] = e % 4 + 4; }
+        }
+    }
+    else
+    {
+        ne = 6;
+        for (int e = 0; e < 6; e++)
+        {
+            if (e < 3) { a[e] = e; b[e] = (e + 1) % 3; }
+            else { a[e] = 3; b[e] = (e + 1) % 3; }
+        }
+    }
+    double len[12];
+    for (int e = 0; e < ne; e++)
+    {
+        const double dx = X[b[e]] - X[a[e]], dy = Y[b[e]] - Y[a[e]], dz = (Z ? Z[b[e]] - Z[a[e]] : 0.0);
+        len[e] = sqrt(dx * dx + dy * dy + dz * dz);
+    }
+    double L = 0.0;
+    if (method == 1)
+    {
+        double mn = len[0];
+        for (int e = 1; e < ne; e++) { L = len[e]; if (L < mn) mn = L; }
+        L = mn;
+    }
+    else if (method == 2)
+    {
+        double t = 0.0;
+        for (int e = 1; e < ne; e++) t += len[e];  /* the reference starts at edge 1 */
+        L = t / ne;
+    }
+    else
+    {
+        double mx = len[0];
+        for (int e = 1; e < ne; e++) { L = len[e]; if (L > mx) mx = L; }
+        L = mx;
+    }
+    return L;
+}
+
+/* CalcSUPGCoefficient (fem_ele_std.cpp:3908-3995) for MASS_TRANSPORT:
+ * D is the raw MassDispersionTensorNew of the Gauss point */
+static double supg_tau(const ogs_assembly_params* p, int dim, const double* vel, const double* D, double L)
+{
+    const double v_mag = sqrt(vel[0] * vel[0] + vel[1] * vel[1] + vel[2] * vel[2]);
+    if (v_mag == 0.0) return 0.0;
+    double diff;
+    if (p->supg_diffusivity == 1)
+    {
+        diff = D[0];
+        for (int i = 1; i < dim * dim; i++)
+            if (D[i] < diff) diff = D[i];
+    }
+    else if (p->supg_diffusivity == 2)
+    {
+        double t = 0.0;
+        for (int i = 0; i < dim; i++) t = D[i + i * dim] * D[i + i * dim];
+        diff = sqrt(t);
+    }
+    else
+    {
+        diff = D[0];
+        for (int i = 1; i < dim * dim; i++)
+            if (D[i] > diff) diff = D[i];
+    }
+    double tau = 0.0;
+    if (p->supg_method == 1)
+    {
+        const double alpha = 0.5 * v_mag * L / diff;
+        tau = 0.5 * L / v_mag * langevin(alpha);
+    }
+    else if (p->supg_method == 2)
+        tau = 1.0 / sqrt((2.0 / p->dt) * (2.0 / p->dt) + (2.0 * v_mag / L) * (2.0 * v_mag / L) +
+                         (4.0 * diff / (L * L)) * (4.0 * diff / (L * L)));
+    return tau;
+}
+
 /* Local matrices of one element:
  *   CalcMass (fem_ele_std.cpp:3753-3900) with CalCoefMass (:1569-1717),
  *   CalcLaplace (:4948-5070) with CalCoefLaplace (:2202-2384, :2545-2562),
@@ -469,6 +576,11 @@ int orc_element_matrices(int etype, int ngauss, int dim, const double* X,
         Y3[i] = Y[i];
         Z3[i] = Z ? Z[i] : 0.0;
     }
+    /* SUPG (transport): non-symmetric mass term kept apart from the
+     * mirrored consistent mass */
+    const int supg = pcs == OGS_PCS_MASS_TRANSPORT && p->supg_method > 0;
+    double msupg[64] = {0};
+    const double L_supg = supg ? orc_supg_length(etype, X3, Y3, Z3, p->supg_length) : 0.0;
 
     for (int gp = 0; gp < ngp; gp++)
     {
@@ -523,6 +635,28 @@ int orc_element_matrices(int etype, int ngauss, int dim, const double* X,
                 for (int j = 0; j < nn; j++)
                     m->storage[i * nn + j] += fs * sf[i] * sf[j];
         }
+        if (supg)
+        {
+            /* CalcSUPGWeightingFunction (:4004-4025): w_i = v . grad N_i with the
+             * raw Gauss-point flux; CalcMass SUPG term (:3856-3879) and
+             * CalcAdvection SUPG term (:5467-5490) */
+            double v[3] = {vel[gp * 3 + 0], vel[gp * 3 + 1], vel[gp * 3 + 2]};
+            double D[9], wf[8];
+            dispersion_tensor(dim, p, v, D);
+            const double tau = supg_tau(p, dim, v, D, L_supg);
+            for (int i = 0; i < nn; i++)
+            {
+                wf[i] = 0.0;
+                for (int k = 0; k < dim; k++) wf[i] += dNg[k * nn + i] * v[k];
+            }
+            const double mat_fac = c_mass * fkt * 1.0;
+            for (int i = 0; i < nn; i++)
+                for (int j = 0; j < nn; j++)
+                {
+                    msupg[i * nn + j] += mat_fac * tau * wf[i] * sf[j];
+                    m->advection[i * nn + j] += fkt * (1.0 * p->time_unit_factor) * tau * wf[i] * wf[j];
+                }
+        }
         if (pcs == OGS_PCS_LIQUID_FLOW && p->gravity_on)
         {
             double rho = p->density;
@@ -540,6 +674,8 @@ int orc_element_matrices(int etype, int ngauss, int dim, const double* X,
     for (int i = 0; i < nn; i++)
         for (int j = 0; j < nn; j++)
             if (i > j) m->mass[j * nn + i] = m->mass[i * nn + j];
+    if (supg)
+        for (int i = 0; i < nn * nn; i++) m->mass[i] += msupg[i];
     if (p->mass_lumping)
     {
         /* CalcLumpedMass (fem_ele_std.cpp:4598-4660): factor = CalCoefMass()

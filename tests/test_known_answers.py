@@ -158,3 +158,36 @@ def test_lumped_mass_is_volume_over_nodes(oracle, et, vol):
         lm = oracle.element_matrices(1, d, oracle.make_params(pcs_type=0, storage=1.0, mass_lumping=1),
                                      k_e=1.0)["mass"]
         assert abs(lm[0, 0] - v / 8) < 1e-14
+
+
+@pytest.mark.parametrize("method", [1, 2])
+def test_supg_terms_on_a_tet(oracle, method):
+    """SUPG (ele_supg_method) on the reference tet with a constant flux:
+    w_i = v . grad N_i and tau are constant, so the added advection is
+    V tau w_i w_j and the added mass c tau w_i V / 4 (the 5-point rule
+    integrates N_j exactly); tau from the longest edge and the largest
+    dispersion entry."""
+    c = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]], dtype=float)
+    vol = 1 / 6
+    g = np.array([[-1, -1, -1], [1, 0, 0], [0, 1, 0], [0, 0, 1]], dtype=float)
+    v = np.array([2e-5, -1e-5, 5e-6])
+    vel = np.tile(v, (5, 1))
+    kw = dict(pcs_type=2, dt=600.0, porosity=0.3, alpha_l=1.0, alpha_t=0.1, diffusion=1e-9,
+              retardation=1.2)
+    off = oracle.element_matrices(2, c, oracle.make_params(**kw), vel=vel)
+    on = oracle.element_matrices(2, c, oracle.make_params(supg_method=method, **kw), vel=vel)
+    vm = np.linalg.norm(v)
+    D = 0.1 * vm * np.eye(3) + (1.0 - 0.1) * np.outer(v, v) / vm + 1e-9 * 0.3 * np.eye(3)
+    diff = D.max()
+    L = np.sqrt(2.0)  # longest edge of the reference tet
+    if method == 1:
+        a = 0.5 * vm * L / diff
+        tau = 0.5 * L / vm * (1 / np.tanh(a) - 1 / a if a < 20 else 1.0)
+    else:
+        tau = 1 / np.sqrt((2 / 600.0) ** 2 + (2 * vm / L) ** 2 + (4 * diff / L ** 2) ** 2)
+    w = g @ v
+    cm = 0.3 * 1.0 * 1.2
+    assert np.allclose(on["advection"] - off["advection"], vol * tau * np.outer(w, w), rtol=1e-10, atol=0)
+    assert np.allclose(on["mass"] - off["mass"], cm * tau * np.outer(w, np.full(4, vol / 4)), rtol=1e-10,
+                       atol=0)
+    assert np.allclose(on["laplace"], off["laplace"], rtol=0, atol=0)

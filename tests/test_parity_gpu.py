@@ -144,6 +144,29 @@ def test_assembly_mass_lumping(gpu, oracle, kind, distorted, pcs):
 
 
 @pytest.mark.parametrize("kind", ["quad", "hex", "tet"])
+@pytest.mark.parametrize("opts", [(1, 0, 0), (2, 1, 1), (2, 2, 2), (1, 2, 0)])
+def test_assembly_supg(gpu, oracle, kind, opts):
+    """ele_supg_method / _length / _diffusivity on transport: the SUPG mass
+    and advection terms on distorted meshes, every entry within 1e-12 of the
+    oracle (also through the affine-tet dispatch, which SUPG bypasses)."""
+    method, length, diffusivity = opts
+    m = distort(small_mesh(kind), 0.15, seed=8) if kind != "tet" else small_mesh(kind)
+    ngp = {"quad": 9, "hex": 27, "tet": 5}[kind]
+    rng = np.random.default_rng(23)
+    gpv = rng.normal(0, 1e-5, (m.n_elements, ngp, 3))
+    if m.dim == 2:
+        gpv[:, :, 2] = 0.0
+    gpv[1, :, :] = 0.0  # tau = 0 branch
+    c0 = rng.uniform(0, 1, m.n_nodes)
+    p = gpu.make_params(gpu.MASS_TRANSPORT, dt=600.0, theta=0.8, porosity=0.3, alpha_l=1.0, alpha_t=0.1,
+                        diffusion=1e-9, decay=1e-7, retardation=1.5, supg_method=method,
+                        supg_length=length, supg_diffusivity=diffusivity)
+    _, _, (rp, col, val, b), (oval, ob) = run_assembly(gpu, oracle, m, p, None, c0, gpv)
+    assert_matrix_close(rp, val, oval)
+    assert_vector_close(b, ob)
+
+
+@pytest.mark.parametrize("kind", ["quad", "hex", "tet"])
 @pytest.mark.parametrize("distorted", [False, True])
 def test_gp_velocity(gpu, oracle, kind, distorted):
     m = small_mesh(kind)
