@@ -503,6 +503,43 @@ ogs_status ogs_gpu_server_progress(ogs_server* srv, int32_t* n_running, int32_t*
 ogs_status ogs_gpu_server_result(const ogs_server* srv, int64_t request_id, ogs_server_result* r);
 ogs_status ogs_gpu_server_info(const ogs_server* srv, ogs_server_info* info);
 
+/* ---- Input decks (host only, no GPU call) --------------------------------
+ * Reads an OGS-5 deck's mesh (.msh), geometry (.gli) and boundary
+ * conditions (.bc) and yields what the GPU path consumes: the mesh
+ * description for ogs_gpu_mesh_create and the Dirichlet rows and values for
+ * ogs_gpu_set_dirichlet.  Replaces, for quad/hex/tet meshes and CONSTANT
+ * conditions on points, polylines and planar surfaces:
+ *   CFEMesh::Read (MSH/msh_mesh.cpp:421-495), CElem::Read
+ *   (MSH/msh_elem.cpp:578-736);
+ *   GEOLIB's readGLIFileV4 points/polylines/surfaces
+ *   (FileIO/OGSIOVer4.cpp:54-503);
+ *   BCRead / CBoundaryCondition::Read (FEM/rf_bc_new.cpp:250-560) and the
+ *   node search of CBoundaryConditionsGroup::Set
+ *   (FEM/rf_bc_new.cpp:1272-1560): GetNODOnPNT, GetNODOnPLY, GetNODOnSFC
+ *   (MSH/msh_mesh.cpp:1434, 1562, 1779). */
+typedef struct ogs_deck ogs_deck;
+
+/* gli_path and bc_path may be NULL.  Errors (unreadable file, element type
+ * off the GPU path, mixed element types, unsupported $DIS_TYPE or geometry)
+ * return OGS_BAD_ARG with the reason in ogs_gpu_last_error. */
+ogs_status ogs_deck_read(const char* msh_path, const char* gli_path, const char* bc_path,
+                         ogs_deck** out);
+ogs_status ogs_deck_destroy(ogs_deck* deck);
+/* The mesh; the arrays stay owned by the deck.  min_edge_length (may be
+ * NULL): CFEMesh::getMinEdgeLength. */
+ogs_status ogs_deck_mesh(const ogs_deck* deck, ogs_mesh_desc* desc, double* min_edge_length);
+/* Mesh nodes of one geometry ("POINT" | "POLYLINE" | "SURFACE", name) as a
+ * CONSTANT condition without $EPSILON selects them.  rows NULL: *n gets the
+ * count only; otherwise capacity >= *n. */
+ogs_status ogs_deck_geo_nodes(const ogs_deck* deck, const char* geo_type, const char* name,
+                              int64_t* rows, int64_t capacity, int64_t* n);
+/* Dirichlet rows and values of every condition whose $PCS_TYPE equals
+ * pcs_type (and $PRIMARY_VARIABLE / $COMP_NAME primary_variable unless
+ * NULL), in the order CRFProcess::bc_node_value holds them: file order, and
+ * within a condition the node order of its search.  rows NULL: count only. */
+ogs_status ogs_deck_dirichlet(const ogs_deck* deck, const char* pcs_type, const char* primary_variable,
+                              int64_t* rows, double* values, int64_t capacity, int64_t* n);
+
 #ifdef __cplusplus
 }
 #endif

@@ -49,6 +49,7 @@ EXPORTS = [
     "ogs_gpu_solve_begin", "ogs_gpu_solve_poll", "ogs_gpu_solve_end",
     "ogs_gpu_server_create", "ogs_gpu_server_destroy", "ogs_gpu_server_add_class", "ogs_gpu_server_submit",
     "ogs_gpu_server_progress", "ogs_gpu_server_result", "ogs_gpu_server_info", "ogs_gpu_server_reserve",
+    "ogs_deck_read", "ogs_deck_destroy", "ogs_deck_mesh", "ogs_deck_geo_nodes", "ogs_deck_dirichlet",
 ]
 REQUEST_FLOW, REQUEST_TRANSPORT = 0, 1
 SERVER_PRIORITY, SERVER_SJF = 1, 2
@@ -228,6 +229,16 @@ def lib():
         for name in ("ogs_gpu_solve_begin", "ogs_gpu_solve_poll", "ogs_gpu_solve_end", "ogs_gpu_server_create",
                      "ogs_gpu_server_destroy", "ogs_gpu_server_add_class", "ogs_gpu_server_submit",
                      "ogs_gpu_server_progress", "ogs_gpu_server_result", "ogs_gpu_server_info"):
+            getattr(L, name).restype = st
+        cp = C.c_char_p
+        i64p = C.POINTER(C.c_int64)
+        L.ogs_deck_read.argtypes = [cp, cp, cp, C.POINTER(vp)]
+        L.ogs_deck_destroy.argtypes = [vp]
+        L.ogs_deck_mesh.argtypes = [vp, C.POINTER(MeshDesc), C.POINTER(C.c_double)]
+        L.ogs_deck_geo_nodes.argtypes = [vp, cp, cp, vp, C.c_int64, i64p]
+        L.ogs_deck_dirichlet.argtypes = [vp, cp, cp, vp, vp, C.c_int64, i64p]
+        for name in ("ogs_deck_read", "ogs_deck_destroy", "ogs_deck_mesh", "ogs_deck_geo_nodes",
+                     "ogs_deck_dirichlet"):
             getattr(L, name).restype = st
         L.ogs_gpu_kernel_launches.argtypes = [C.c_int32]
         L.ogs_gpu_kernel_launches.restype = C.c_int64
@@ -599,3 +610,68 @@ class Server:
         _check(lib().ogs_gpu_server_info(self.h, C.byref(i)))
         return {"slots": i.slots, "running": i.running, "queued": i.queued, "completed": i.completed,
                 "bytes_used": i.bytes_used, "bytes_budget": i.bytes_budget}
+
+
+class Deck:
+    """An OGS-5 input deck read by the library's native reader (host only):
+    mesh (.msh), geometry (.gli) and CONSTANT Dirichlet conditions (.bc).
+
+    ``mesh`` is a :class:`ogs5_gb300.mesh.Mesh` ready for :class:`GpuMesh`;
+    ``dirichlet(pcs_type)`` gives the rows and values for
+    ``LinearEQS.SetKnownX`` in the order CRFProcess::bc_node_value holds them
+    (FEM/rf_bc_new.cpp:1272-1560)."""
+
+    def __init__(self, msh: str, gli: str | None = None, bc: str | None = None):
+        h = C.c_void_p()
+        enc = (lambda p: None if p is None else os.fsencode(p))
+        _check(lib().ogs_deck_read(enc(msh), enc(gli), enc(bc), C.byref(h)))
+        self.h = h
+
+    @property
+    def min_edge_length(self) -> float:
+        d, h = MeshDesc(), C.c_double()
+        lib().ogs_deck_mesh(self.h, C.byref(d), C.byref(h))  # h is set even off the GPU path
+        return h.value
+
+    @property
+    def mesh(self):
+        from . import mesh as M
+        d = MeshDesc()
+        _check(lib().ogs_deck_mesh(self.h, C.byref(d), None))
+        nn, ne = d.n_nodes, d.n_elements
+        npe = M.NODES_PER_ELEMENT[d.elem_type]
+        f64 = C.POINTER(C.c_double)
+        x = np.ctypeslib.as_array(C.cast(d.x, f64), (nn,)).copy()
+        y = np.ctypeslib.as_array(C.cast(d.y, f64), (nn,)).copy()
+        z = (np.ctypeslib.as_array(C.cast(d.z, f64), (nn,)).copy() if d.z else np.zeros(nn))
+        conn = np.ctypeslib.as_array(C.cast(d.connectivity, C.POINTER(C.c_int32)), (ne * npe,))
+        return M.Mesh(d.elem_type, d.dim, x, y, z, conn.reshape(ne, npe).copy())
+
+    def geo_nodes(self, geo_type: str, name: str) -> np.ndarray:
+        n = C.c_int64()
+        _check(lib().ogs_deck_geo_nodes(self.h, geo_type.encode(), name.encode(), None, 0, C.byref(n)))
+        rows = np.empty(n.value, dtype=np.int64)
+        _check(lib().ogs_deck_geo_nodes(self.h, geo_type.encode(), name.encode(), _ptr(rows), len(rows),
+                                        C.byref(n)))
+        return rows
+
+    def dirichlet(self, pcs_type: str, primary_variable: str | None = None):
+        n = C.c_int64()
+        pv = None if primary_variable is None else primary_variable.encode()
+        _check(lib().ogs_deck_dirichlet(self.h, pcs_type.encode(), pv, None, None, 0, C.byref(n)))
+        rows = np.empty(n.value, dtype=np.int64)
+        vals = np.empty(n.value, dtype=np.float64)
+        _check(lib().ogs_deck_dirichlet(self.h, pcs_type.encode(), pv, _ptr(rows), _ptr(vals), len(rows),
+                                        C.byref(n)))
+        return rows, vals
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().ogs_deck_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -3,12 +3,15 @@
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
 bench.py's CPU-baseline leg, never by the ogs5_gb300 product path.
 
-Two libraries are wrapped:
+Three libraries are wrapped:
   * ``_build/libogs_oracle.so`` -- the C restatement of the OGS-5 path
     (ogs_oracle.c), always built;
   * ``_ref/libogs5ref.so`` -- the reference's own FEM/mathlib.cpp,
     FEM/matrix_class.cpp and FEM/equation_class.cpp behind ref_harness.cpp,
-    built only where the reference sources are present.
+    built only where the reference sources are present;
+  * ``_ref/libogs5geo.so`` -- the reference's own GEOLIB surface, polygon
+    and polyline code behind ref_geo_harness.cpp (node searches of the deck
+    reader), built only where the reference sources are present.
 """
 from __future__ import annotations
 
@@ -21,6 +24,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libogs_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libogs5ref.so")
+GEO_SO = os.path.join(HERE, "_ref", "libogs5geo.so")
 
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _i64p = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
@@ -251,10 +255,58 @@ def solve(row_ptr, col, val, b, x0, method=2, precond=1, max_iter=1000, tol=1e-1
 # --------------------------------------------------------------------------
 
 _ref = None
+_ref_geo = None
 
 
 def ref_available() -> bool:
     return os.path.exists(REF_SO)
+
+
+def has_ref_geo() -> bool:
+    return os.path.exists(GEO_SO)
+
+
+def ref_geo():
+    """The reference's GEOLIB/MathLib geometry behind ref_geo_harness.cpp,
+    with numpy front ends: surface_nodes, polyline_nodes, point_in_polygon."""
+    global _ref_geo
+    if _ref_geo is None:
+        L = C.CDLL(GEO_SO)
+        L.ref_geo_surface_nodes.argtypes = [C.c_int, _dp, C.c_int64, _dp, C.c_double, C.c_void_p]
+        L.ref_geo_polyline_nodes.argtypes = [C.c_int, _dp, C.c_int64, _dp, C.c_double, _i64p, _dp]
+        L.ref_geo_polyline_nodes.restype = C.c_int64
+        L.ref_geo_point_in_polygon.argtypes = [C.c_int, _dp, C.c_int64, _dp, C.c_void_p]
+        _ref_geo = L
+    return _ref_geo
+
+
+def _xyz(a):
+    return np.ascontiguousarray(np.asarray(a, dtype=np.float64).reshape(-1, 3))
+
+
+def ref_surface_nodes(polygon, nodes, eps):
+    """Mesh nodes on the surface of a closed polygon (GetNODOnSFC loop)."""
+    P, X = _xyz(polygon), _xyz(nodes)
+    mask = np.zeros(len(X), dtype=np.uint8)
+    if ref_geo().ref_geo_surface_nodes(len(P), P.ravel(), len(X), X.ravel(), eps, mask.ctypes.data) != 0:
+        raise RuntimeError("Surface::createSurface failed")
+    return np.flatnonzero(mask)
+
+
+def ref_polyline_nodes(points, nodes, radius):
+    """Mesh nodes along a polyline in MeshNodesAlongPolyline order."""
+    P, X = _xyz(points), _xyz(nodes)
+    ids = np.zeros(len(X), dtype=np.int64)
+    dist = np.zeros(len(X))
+    n = ref_geo().ref_geo_polyline_nodes(len(P), P.ravel(), len(X), X.ravel(), radius, ids, dist)
+    return ids[:n], dist[:n]
+
+
+def ref_point_in_polygon(polygon, points):
+    P, X = _xyz(polygon), _xyz(points)
+    mask = np.zeros(len(X), dtype=np.uint8)
+    ref_geo().ref_geo_point_in_polygon(len(P), P.ravel(), len(X), X.ravel(), mask.ctypes.data)
+    return mask.astype(bool)
 
 
 def ref():

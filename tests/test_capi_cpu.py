@@ -11,7 +11,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def header_functions():
     txt = open(os.path.join(ROOT, "include", "ogs_gpu.h")).read()
-    return sorted(set(re.findall(r"\b(ogs_gpu_\w+)\s*\(", txt)))
+    return sorted(set(re.findall(r"\b(ogs_(?:gpu|deck)_\w+)\s*\(", txt)))
 
 
 @pytest.fixture(scope="module")
