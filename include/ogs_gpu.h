@@ -149,7 +149,16 @@ typedef struct
                                   of the dispersion tensor, 1 smallest, 2 the
                                   last diagonal entry (the reference assigns
                                   rather than sums the squares)                */
-    int32_t pad1;
+    int32_t memory_type;       /* MT: pcs->Memory_Type ($MEMORY_TYPE, rf_pcs.cpp
+                                  :2142-2146, 972).  0: element matrices recomputed
+                                  every assembly.  > 0: the first assembly
+                                  after creation or ogs_gpu_cache_reset stores
+                                  the mass and the Laplace + advection +
+                                  storage operators, later assemblies combine
+                                  the stored ones with this call's dt, theta
+                                  and u0 and ignore gp_velocity, porosity and
+                                  the other material values
+                                  (fem_ele_std.cpp:8534-8588)                  */
 } ogs_assembly_params;
 
 /* Linear_EQS::ConfigNumerics inputs (CNumerics, FEM/rf_num_new.h:34-60). */
@@ -216,6 +225,11 @@ ogs_status ogs_gpu_system_destroy(ogs_system* sys);
 
 /* Linear_EQS::ConfigNumerics (FEM/equation_class.cpp:191-318). */
 ogs_status ogs_gpu_configure(ogs_system* sys, const ogs_solver_config* cfg);
+
+/* Forgets the transport operators stored under memory_type > 0, so that the
+ * next such assembly computes and stores them again: the reference's first
+ * time step (aktueller_zeitschritt == 1, fem_ele_std.cpp:8534). */
+ogs_status ogs_gpu_cache_reset(ogs_system* sys);
 
 /* Linear_EQS::Initialize (FEM/equation_class.cpp:325-332): A = 0, b = 0. */
 ogs_status ogs_gpu_initialize(ogs_system* sys);

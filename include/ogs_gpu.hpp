@@ -145,6 +145,9 @@ public:
         check(ogs_gpu_assemble(h_, &p, elem_k, u0, gp_velocity), "ogs_gpu_assemble");
     }
 
+    // forget the transport operators stored under memory_type > 0
+    void ResetOperators() { check(ogs_gpu_cache_reset(h_), "ogs_gpu_cache_reset"); }
+
     void SetKnownX_i(long i, double x)
     {
         known_rows_.push_back((int64_t)i);

@@ -49,6 +49,7 @@ EXPORTS = [
     "ogs_gpu_solve_begin", "ogs_gpu_solve_poll", "ogs_gpu_solve_end",
     "ogs_gpu_server_create", "ogs_gpu_server_destroy", "ogs_gpu_server_add_class", "ogs_gpu_server_submit",
     "ogs_gpu_server_progress", "ogs_gpu_server_result", "ogs_gpu_server_info", "ogs_gpu_server_reserve",
+    "ogs_gpu_cache_reset",
     "ogs_deck_read", "ogs_deck_destroy", "ogs_deck_mesh", "ogs_deck_geo_nodes", "ogs_deck_dirichlet",
 ]
 REQUEST_FLOW, REQUEST_TRANSPORT = 0, 1
@@ -81,7 +82,7 @@ class AssemblyParams(C.Structure):
         ("diffusion", C.c_double), ("decay", C.c_double),
         ("retardation", C.c_double), ("saturation", C.c_double),
         ("supg_method", C.c_int32), ("supg_length", C.c_int32), ("supg_diffusivity", C.c_int32),
-        ("pad1", C.c_int32),
+        ("memory_type", C.c_int32),
     ]
 
 
@@ -230,6 +231,8 @@ def lib():
                      "ogs_gpu_server_destroy", "ogs_gpu_server_add_class", "ogs_gpu_server_submit",
                      "ogs_gpu_server_progress", "ogs_gpu_server_result", "ogs_gpu_server_info"):
             getattr(L, name).restype = st
+        L.ogs_gpu_cache_reset.argtypes = [vp]
+        L.ogs_gpu_cache_reset.restype = st
         cp = C.c_char_p
         i64p = C.POINTER(C.c_int64)
         L.ogs_deck_read.argtypes = [cp, cp, cp, C.POINTER(vp)]
@@ -355,6 +358,11 @@ class LinearEQS:
     def GlobalAssembly(self, params: AssemblyParams, elem_k=None, u0=None, gp_velocity=None):
         ek, u, gv = _f64(elem_k), _f64(u0), _f64(gp_velocity)
         _check(lib().ogs_gpu_assemble(self.h, C.byref(params), _ptr(ek), _ptr(u), _ptr(gv)))
+
+    # forget the transport operators stored under memory_type > 0 (the
+    # reference's first time step recomputes them)
+    def ResetOperators(self):
+        _check(lib().ogs_gpu_cache_reset(self.h))
 
     # SetKnownX_i over a node set (IncorporateBoundaryConditions)
     def SetKnownX(self, rows, values, mode=DIRICHLET_ROW_ONLY):

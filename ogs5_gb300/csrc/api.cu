@@ -43,6 +43,30 @@ struct SellRow
     __device__ __forceinline__ int slot(int j) const { return beg + (j << 5); }
 };
 
+// Transport assembly from the stored operators (memory_type > 0, after the
+// first assembly): the element loop of AssembleMixedHyperbolicParabolicEquation
+// with EleMat's matrices (fem_ele_std.cpp:8575-8640) summed over elements --
+// A += M / dt + theta K,  b += (M / dt - (1 - theta) K) u0, one thread a row.
+__global__ void k_mt_from_operators(const int32_t* __restrict__ slice_ptr, const int32_t* __restrict__ row_len,
+                                    const int32_t* __restrict__ col, const double* __restrict__ M,
+                                    const double* __restrict__ K, const double* __restrict__ u, double dt_inverse,
+                                    double th, double* val, double* b, int n)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    {
+        const SellRow R(slice_ptr, row_len, i);
+        double bi = 0.0;
+        for (int j = 0; j < R.len; j++)
+        {
+            const int k = R.slot(j);
+            const double m = M[k] * dt_inverse, kk = K[k];
+            val[k] += m + kk * th;
+            if (u) bi += (m + kk * (-(1.0 - th))) * u[col[k]];
+        }
+        b[i] += bi;
+    }
+}
+
 __global__ void k_dirichlet_row_only(const int32_t* __restrict__ slice_ptr, const int32_t* __restrict__ row_len,
                                      const int32_t* __restrict__ col, const int32_t* __restrict__ diag_pos,
                                      double* val, double* b, const int32_t* __restrict__ rows,
@@ -169,6 +193,10 @@ struct ogs_system
     double *r = nullptr, *r0 = nullptr, *p = nullptr, *ph = nullptr, *s = nullptr, *sh = nullptr,
            *t = nullptr, *v = nullptr, *dinv = nullptr;
     double* lu = nullptr;     // ILU(0) factors on the CSR pattern (allocated on first use)
+    // transport operators stored under memory_type > 0 (SELL order, allocated
+    // on first use): mass, and Laplace + advection + storage
+    double *op_mass = nullptr, *op_k = nullptr;
+    bool op_valid = false;
     int* d_ilu_bad = nullptr;
     double *ek = nullptr, *u0 = nullptr, *gpv = nullptr, *qbuf = nullptr, *vec_in = nullptr,
            *vec_out = nullptr;
@@ -331,6 +359,8 @@ extern "C" ogs_status ogs_gpu_system_destroy(ogs_system* s)
     cudaFree(s->vec_block);
     cudaFree(s->f32_block);
     cudaFree(s->lu);
+    cudaFree(s->op_mass);
+    cudaFree(s->op_k);
     cudaFree(s->d_ilu_bad);
     cudaFree(s->st);
     cudaFree(s->d_bad);
@@ -461,7 +491,8 @@ constexpr int kNoBadElement = 0x7fffffff;
 // point flux); the singular-Jacobian flag lands in s->h_bad (pinned) once
 // the stream has passed this point.
 static ogs_status enqueue_element_kernel(ogs_system* s, const ogs_assembly_params* p, const double* elem_k,
-                                         const double* u0, const double* gpv, int kind, double* q_out)
+                                         const double* u0, const double* gpv, int kind, double* q_out,
+                                         double* val = nullptr, double* val2 = nullptr)
 {
     ogs_mesh* m = s->m;
     AsmArgs a;
@@ -472,8 +503,9 @@ static ogs_status enqueue_element_kernel(ogs_system* s, const ogs_assembly_param
     a.slot_t = m->slot_t;
     a.tab = m->tab;
     a.aff = m->aff;
-    a.val = s->val;
+    a.val = val ? val : s->val;
     a.b = s->b;
+    a.val2 = val2;
     a.q_out = q_out;
     a.bad_elem = s->d_bad;
     a.p = *p;
@@ -519,8 +551,45 @@ extern "C" ogs_status ogs_gpu_assemble(ogs_system* s, const ogs_assembly_params*
     ogs_status st = check_params(p);
     if (st) return st;
     if (p->pcs_type != OGS_PCS_MASS_TRANSPORT && !elem_k) { set_error("assemble: flow needs elem_k"); return OGS_BAD_ARG; }
-    if (p->pcs_type == OGS_PCS_MASS_TRANSPORT && !gp_velocity) { set_error("assemble: transport needs gp_velocity"); return OGS_BAD_ARG; }
-    return run_element_kernel(s, p, elem_k, u0, gp_velocity, p->pcs_type == OGS_PCS_MASS_TRANSPORT ? 1 : 0, nullptr);
+    const bool stored = p->pcs_type == OGS_PCS_MASS_TRANSPORT && p->memory_type > 0;
+    if (p->pcs_type == OGS_PCS_MASS_TRANSPORT && !gp_velocity && !(stored && s->op_valid))
+    {
+        set_error("assemble: transport needs gp_velocity");
+        return OGS_BAD_ARG;
+    }
+    if (!stored) return run_element_kernel(s, p, elem_k, u0, gp_velocity, p->pcs_type == OGS_PCS_MASS_TRANSPORT ? 1 : 0, nullptr);
+    // Memory_Type > 0: the reference computes and stores the element
+    // matrices on the first time step and reuses them afterwards
+    // (fem_ele_std.cpp:8534-8588); here the first assembly scatters the
+    // mass and the theta-weighted operator into two stored matrices
+    const ogs_mesh* m = s->m;
+    const size_t bytes = (size_t)std::max<int64_t>(1, m->sell_nnz) * sizeof(double);
+    if (!s->op_valid)
+    {
+        if (!s->op_mass) OGS_CUDA_TRY(cudaMalloc(&s->op_mass, bytes));
+        if (!s->op_k) OGS_CUDA_TRY(cudaMalloc(&s->op_k, bytes));
+        OGS_CUDA_TRY(cudaMemsetAsync(s->op_mass, 0, bytes, s->stream));
+        OGS_CUDA_TRY(cudaMemsetAsync(s->op_k, 0, bytes, s->stream));
+        st = enqueue_element_kernel(s, p, elem_k, u0, gp_velocity, 1, nullptr, s->op_mass, s->op_k);
+        if (st) return st;
+        OGS_CUDA_TRY(cudaStreamSynchronize(s->stream));
+        if ((st = element_flag_status(s))) return st;
+        s->op_valid = true;
+    }
+    const double* du;
+    if ((st = stage_in(s, u0, m->n_nodes, &s->u0, &du))) return st;
+    k_mt_from_operators<<<vec_grid(s->n), 256, 0, s->stream>>>(m->slice_ptr, m->row_len, m->sell_col, s->op_mass,
+                                                             s->op_k, du, 1.0 / p->dt, p->theta, s->val, s->b, s->n);
+    OGS_LAUNCH_CHECK();
+    OGS_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    return OGS_OK;
+}
+
+extern "C" ogs_status ogs_gpu_cache_reset(ogs_system* s)
+{
+    if (!s) { set_error("cache_reset: NULL system"); return OGS_BAD_ARG; }
+    s->op_valid = false;
+    return OGS_OK;
 }
 
 extern "C" ogs_status ogs_gpu_gp_velocity(ogs_system* s, const ogs_assembly_params* p, const double* elem_k,

@@ -527,7 +527,9 @@ __global__ void __launch_bounds__(128) k_flow_affine(AsmArgs a)
 // ------------------------------------------------------------------
 // MASS_TRANSPORT
 // ------------------------------------------------------------------
-template <int NN>
+// STORE: the kernel may be the one that fills the stored operators (the SUPG
+// instantiation, whose extra terms vanish with supg_method 0)
+template <int NN, bool STORE = false>
 __device__ __forceinline__ void mt_combine(const AsmArgs& a, int64_t e, const int* nd,
                                            const double* U, const double* Ml,
                                            const double* L, const double* A,
@@ -535,6 +537,24 @@ __device__ __forceinline__ void mt_combine(const AsmArgs& a, int64_t e, const in
 {
     // Mx: the non-symmetric SUPG mass term (full NN x NN), added to the mass
     // AssembleMixedHyperbolicParabolicEquation (fem_ele_std.cpp:8592-8692)
+    if (STORE && a.val2)
+    {
+        // the operators stored for memory_type > 0 (EleMat->SetMass_notsym,
+        // SetLaplace, SetAdvection, SetStorage; fem_ele_std.cpp:8565-8573),
+        // scattered: their time weights are applied per assembly
+#pragma unroll
+        for (int i = 0; i < NN; i++)
+#pragma unroll
+            for (int j = 0; j < NN; j++)
+            {
+                const int l = i >= j ? i * (i + 1) / 2 + j : j * (j + 1) / 2 + i;
+                const int k = i * NN + j;
+                const int32_t slot = __ldg(a.slot_t + (int64_t)k * a.E + e);
+                atomicAdd(a.val + slot, Mx ? Ml[l] + Mx[k] : Ml[l]);
+                atomicAdd(a.val2 + slot, L[k] + A[k] + St[l]);
+            }
+        return;
+    }
     const double dt_inverse = 1.0 / a.p.dt;
     const double th = a.p.theta;
     double S[NN * NN], r[NN];
@@ -665,10 +685,10 @@ __global__ void __launch_bounds__(128) k_mt_general(AsmArgs a)
         {
             // CalcLumpedMass has no SUPG term
             lump_mass<ET, NN>(X, Y, Z, cm, Ml);
-            mt_combine<NN>(a, e, nd, U, Ml, L, A, St);
+            mt_combine<NN, SUPG>(a, e, nd, U, Ml, L, A, St);
         }
         else
-            mt_combine<NN>(a, e, nd, U, Ml, L, A, St, SUPG ? Mx : nullptr);
+            mt_combine<NN, SUPG>(a, e, nd, U, Ml, L, A, St, SUPG ? Mx : nullptr);
     }
 }
 
@@ -819,8 +839,12 @@ template <int ET, int NGP>
 static void launch_mt(const AsmArgs& a, bool affine, cudaStream_t s)
 {
     const int g = grid_for(a.E, 128);
-    // the affine tet kernel folds the Gauss points away; SUPG needs them
-    if (ET == OGS_ELEM_TET4 && affine && a.p.supg_method == 0)
+    // the affine tet kernel folds the Gauss points away; SUPG needs them.
+    // Filling the stored operators (a.val2) goes through the SUPG kernel,
+    // exact for supg_method 0 too (tau = 0 adds zeros).
+    if (a.val2)
+        k_mt_general<ET, NGP, true><<<g, 128, 0, s>>>(a);
+    else if (ET == OGS_ELEM_TET4 && affine && a.p.supg_method == 0)
         k_mt_tet_affine<<<g, 128, 0, s>>>(a);
     else if (a.p.supg_method > 0)
         k_mt_general<ET, NGP, true><<<g, 128, 0, s>>>(a);

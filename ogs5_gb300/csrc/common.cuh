@@ -106,6 +106,9 @@ struct AsmArgs
     const double* gpv;  // [e][gp][3]
     double* val;
     double* b;
+    double* val2;       // transport with memory_type > 0, first assembly:
+                        // val gets the mass, val2 the Laplace + advection +
+                        // storage operator, b nothing
     double* q_out;      // velocity kernel output [e][gp][3]
     int* bad_elem;      // first element with a singular Jacobian + 1
     ogs_assembly_params p;

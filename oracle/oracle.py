@@ -55,7 +55,7 @@ class AssemblyParams(C.Structure):
         ("diffusion", C.c_double), ("decay", C.c_double),
         ("retardation", C.c_double), ("saturation", C.c_double),
         ("supg_method", C.c_int32), ("supg_length", C.c_int32), ("supg_diffusivity", C.c_int32),
-        ("pad1", C.c_int32),
+        ("memory_type", C.c_int32),
     ]
 
 

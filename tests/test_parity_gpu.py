@@ -144,6 +144,45 @@ def test_assembly_mass_lumping(gpu, oracle, kind, distorted, pcs):
 
 
 @pytest.mark.parametrize("kind", ["quad", "hex", "tet"])
+@pytest.mark.parametrize("opts", [{}, {"mass_lumping": 1}, {"supg_method": 1}])
+def test_transport_stored_operators(gpu, oracle, kind, opts):
+    """$MEMORY_TYPE 1 (fem_ele_std.cpp:8534-8588): the first assembly stores
+    the operators; a later one with another dt, theta, u0 and velocity field
+    combines the stored ones -- the oracle's assembly with the first
+    velocities and the later dt, theta, u0 -- also without gp_velocity; after
+    ResetOperators the new velocities are taken."""
+    m = distort(small_mesh(kind), 0.15, seed=4) if kind != "tet" else small_mesh(kind)
+    ngp = {"quad": 9, "hex": 27, "tet": 5}[kind]
+    rng = np.random.default_rng(31)
+    gpv1, gpv2 = rng.normal(0, 1e-5, (2, m.n_elements, ngp, 3))
+    if m.dim == 2:
+        gpv1[:, :, 2] = gpv2[:, :, 2] = 0.0
+    c1, c2 = rng.uniform(0, 1, (2, m.n_nodes))
+    base = dict(porosity=0.3, alpha_l=1.0, alpha_t=0.1, diffusion=1e-9, decay=1e-7, retardation=1.5, **opts)
+    p1 = gpu.make_params(gpu.MASS_TRANSPORT, dt=600.0, theta=0.7, memory_type=1, **base)
+    p2 = gpu.make_params(gpu.MASS_TRANSPORT, dt=1800.0, theta=0.55, memory_type=1, **base)
+    eqs = gpu.LinearEQS(gpu.GpuMesh(m))
+    orp, ocol = oracle.build_pattern(m.n_nodes, m.conn)
+
+    def check(p, c, gpv_gpu, gpv_oracle):
+        eqs.Initialize()
+        eqs.GlobalAssembly(p, None, c, gpv_gpu)
+        rp, _, val = eqs.get_csr()
+        oval, ob = oracle.assemble(m, orp, ocol, oracle_params(oracle, p), u0=c, gp_vel=gpv_oracle)
+        assert_matrix_close(rp, val, oval)
+        assert_vector_close(eqs.get_rhs(), ob)
+
+    check(p1, c1, gpv1, gpv1)
+    check(p2, c2, gpv2, gpv1)
+    check(p2, c2, None, gpv1)
+    eqs.ResetOperators()
+    check(p2, c2, gpv2, gpv2)
+    with pytest.raises(gpu.OgsError):
+        eqs.ResetOperators()
+        eqs.GlobalAssembly(p2, None, c2, None)
+
+
+@pytest.mark.parametrize("kind", ["quad", "hex", "tet"])
 @pytest.mark.parametrize("opts", [(1, 0, 0), (2, 1, 1), (2, 2, 2), (1, 2, 0)])
 def test_assembly_supg(gpu, oracle, kind, opts):
     """ele_supg_method / _length / _diffusivity on transport: the SUPG mass
