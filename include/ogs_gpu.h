@@ -175,8 +175,19 @@ typedef struct
     int32_t check_norm_rhs;    /* 1: keep Linear_EQS::CheckNormRHS, i.e.
                                   return at once when |b|/|b_prev| < tol
                                   (equation_class.cpp:1104-1121)               */
-    int32_t pad0;
+    int32_t schedule;          /* FP32 mode: OGS_SCHEDULE_GRAPH (0) two
+                                  kernels per iteration in captured graphs;
+                                  OGS_SCHEDULE_PERSISTENT (1) many iterations
+                                  in one cooperative launch with two grid
+                                  barriers per iteration (graph schedule where
+                                  the device cannot launch it)               */
 } ogs_solver_config;
+
+enum
+{
+    OGS_SCHEDULE_GRAPH = 0,
+    OGS_SCHEDULE_PERSISTENT = 1
+};
 
 typedef struct
 {
@@ -325,6 +336,9 @@ typedef struct
     int64_t spmv_launches;     /* SpMV launches that did work                 */
     double solve_ms;           /* summed device time of the solves            */
     int64_t solves;
+    double persist_ms;         /* summed time of the persistent FP32 CG
+                                  launches (OGS_SCHEDULE_PERSISTENT)          */
+    int64_t persist_iters;     /* FP32 iterations those launches ran          */
 } ogs_profile;
 
 /* enable != 0 turns the timing on (graphs are re-captured with the events);

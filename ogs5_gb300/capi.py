@@ -35,6 +35,7 @@ DIRICHLET_ROW_ONLY, DIRICHLET_SYMMETRIC = 0, 1
 LS_BICGSTAB, LS_CG = 2, 5
 PRECOND_NONE, PRECOND_JACOBI, PRECOND_ILU0 = 0, 1, 100
 PRECISION_FP64, PRECISION_FP32_REFINED = 0, 1
+SCHEDULE_GRAPH, SCHEDULE_PERSISTENT = 0, 1
 
 # every entry point include/ogs_gpu.h declares
 EXPORTS = [
@@ -89,12 +90,12 @@ class AssemblyParams(C.Structure):
 class SolverConfig(C.Structure):
     _fields_ = [("method", C.c_int32), ("precond", C.c_int32), ("max_iter", C.c_int32),
                 ("precision", C.c_int32), ("tol", C.c_double), ("inner_tol", C.c_double),
-                ("check_norm_rhs", C.c_int32), ("pad0", C.c_int32)]
+                ("check_norm_rhs", C.c_int32), ("schedule", C.c_int32)]
 
 
 class Profile(C.Structure):
     _fields_ = [("spmv_ms", C.c_double), ("spmv_launches", C.c_int64), ("solve_ms", C.c_double),
-                ("solves", C.c_int64)]
+                ("solves", C.c_int64), ("persist_ms", C.c_double), ("persist_iters", C.c_int64)]
 
 
 class SolveStats(C.Structure):
@@ -345,9 +346,10 @@ class LinearEQS:
     # Linear_EQS::ConfigNumerics
     def ConfigNumerics(self, ls_method=LS_BICGSTAB, ls_precond=PRECOND_JACOBI,
                        ls_max_iterations=1000, ls_error_tolerance=1e-12,
-                       precision=PRECISION_FP64, inner_tol=0.0, check_norm_rhs=True):
+                       precision=PRECISION_FP64, inner_tol=0.0, check_norm_rhs=True,
+                       schedule=SCHEDULE_GRAPH):
         c = SolverConfig(ls_method, ls_precond, ls_max_iterations, precision, ls_error_tolerance,
-                         inner_tol, 1 if check_norm_rhs else 0, 0)
+                         inner_tol, 1 if check_norm_rhs else 0, schedule)
         _check(lib().ogs_gpu_configure(self.h, C.byref(c)))
 
     # Linear_EQS::Initialize
@@ -398,7 +400,7 @@ class LinearEQS:
         p = Profile()
         _check(lib().ogs_gpu_profile(self.h, 1 if enable else 0, C.byref(p)))
         return {"spmv_ms": p.spmv_ms, "spmv_launches": p.spmv_launches, "solve_ms": p.solve_ms,
-                "solves": p.solves}
+                "solves": p.solves, "persist_ms": p.persist_ms, "persist_iters": p.persist_iters}
 
     def get_csr(self):
         nnz = self.gmesh.nnz
@@ -531,8 +533,10 @@ class Batch:
 
 
 def solver_config(method=LS_CG, precond=PRECOND_JACOBI, max_iter=20000, tol=1e-10,
-                  precision=PRECISION_FP64, inner_tol=0.0, check_norm_rhs=True) -> SolverConfig:
-    return SolverConfig(method, precond, max_iter, precision, tol, inner_tol, 1 if check_norm_rhs else 0, 0)
+                  precision=PRECISION_FP64, inner_tol=0.0, check_norm_rhs=True,
+                  schedule=SCHEDULE_GRAPH) -> SolverConfig:
+    return SolverConfig(method, precond, max_iter, precision, tol, inner_tol, 1 if check_norm_rhs else 0,
+                        schedule)
 
 
 class Server:

@@ -22,6 +22,8 @@ void launch_mp_convert(const MixedArgs& a, const int32_t* row_len, const int8_t*
                        float* val32, const double* dinv64, float* d32, cudaStream_t s);
 void launch_mp_replace(const MixedArgs& a, cudaStream_t s);
 void launch_mp_iteration(const MixedArgs& a, cudaStream_t s, cudaEvent_t eb, cudaEvent_t ee);
+int mp_persist_grid(const MixedArgs& a);
+cudaError_t launch_mp_persist(const MixedArgs& a, int grid, int iters, cudaStream_t s);
 int kernels_per_iteration(int kind, int precond);
 int krylov_init_launches(int kind, int precond);
 bool ilu_cluster_ok();
@@ -229,6 +231,12 @@ struct ogs_system
           *val32 = nullptr, *u32 = nullptr, *w32 = nullptr;
     int fmt = -1;
     cudaGraphExec_t mp_chunk = nullptr, mp_replace = nullptr;
+    // persistent FP32 CG (OGS_SCHEDULE_PERSISTENT): the arguments of the
+    // direct cooperative launches and their grid (0: graph schedule)
+    MixedArgs mp_args{};
+    int mp_grid = 0;
+    double prof_persist_ms = 0.0;
+    int64_t prof_persist_iters = 0;
     // SpMV timing inside the chunk graphs (ogs_gpu_profile)
     static constexpr int kChunk = 16;
     bool prof_on = false;
@@ -292,6 +300,8 @@ void drop_graphs(ogs_system* s)
 // (one pair per iteration slowed the chunk by ~10%); the sampled launches
 // give the average SpMV duration.
 constexpr int kProfEvery = 4;
+// FP32 iterations per persistent launch (a due replacement ends it sooner)
+constexpr int kPersistIters = 64;
 
 void accumulate_prof(ogs_system* s, int executed)
 {
@@ -459,6 +469,11 @@ extern "C" ogs_status ogs_gpu_configure(ogs_system* s, const ogs_solver_config* 
     if (c->precision != OGS_PRECISION_FP64 && c->precision != OGS_PRECISION_FP32_REFINED)
     {
         set_error("configure: unknown precision %d", c->precision);
+        return OGS_BAD_ARG;
+    }
+    if (c->schedule != OGS_SCHEDULE_PERSISTENT && c->schedule != OGS_SCHEDULE_GRAPH)
+    {
+        set_error("configure: unknown schedule %d", c->schedule);
         return OGS_BAD_ARG;
     }
     s->cfg = *c;
@@ -792,7 +807,9 @@ static ogs_status begin_fp32_refined(ogs_system* s, KState* h)
         ogs_status st = capture(s, &s->mp_replace, [&]() { launch_mp_replace(a, s->stream); });
         if (st) return st;
     }
-    if (!s->mp_chunk)
+    s->mp_args = a;
+    s->mp_grid = c.schedule == OGS_SCHEDULE_PERSISTENT ? mp_persist_grid(a) : 0;
+    if (!s->mp_chunk && s->mp_grid == 0)
     {
         ogs_status st = capture(s, &s->mp_chunk, [&]() {
             for (int i = 0; i < ogs_system::kChunk; i++)
@@ -1031,7 +1048,19 @@ static ogs_status solve_advance(ogs_system* s, bool block, bool* finished)
     {
         if (T.chunk_before >= 0)
         {
-            if (s->prof_on) accumulate_prof(s, std::min(ogs_system::kChunk, h->iter - T.chunk_before));
+            if (s->prof_on && s->mp_grid > 0)
+            {
+                float ms = 0.f;
+                if (cudaEventElapsedTime(&ms, s->prof_b[0], s->prof_e[0]) == cudaSuccess)
+                {
+                    s->prof_persist_ms += ms;
+                    s->prof_persist_iters += h->iter - T.chunk_before;
+                }
+                else
+                    cudaGetLastError();
+            }
+            else if (s->prof_on)
+                accumulate_prof(s, std::min(ogs_system::kChunk, h->iter - T.chunk_before));
             T.chunk_before = -1;
         }
         if (!h->done)
@@ -1045,6 +1074,21 @@ static ogs_status solve_advance(ogs_system* s, bool block, bool* finished)
             {
                 if (cudaGraphLaunch(s->mp_replace, s->stream) != cudaSuccess) return task_fail(s, OGS_CUDA_ERROR);
                 count_launches(4);
+            }
+            else if (s->mp_grid > 0)
+            {
+                // one cooperative launch runs up to kPersistIters iterations;
+                // it returns early when a replacement is due or the solve ended
+                T.chunk_before = h->iter;
+                if (s->prof_on) cudaEventRecord(s->prof_b[0], s->stream);
+                if (launch_mp_persist(s->mp_args, s->mp_grid, kPersistIters, s->stream) != cudaSuccess)
+                {
+                    set_error("solve: cooperative launch of the FP32 CG kernel failed: %s",
+                              cudaGetErrorString(cudaGetLastError()));
+                    return task_fail(s, OGS_CUDA_ERROR);
+                }
+                if (s->prof_on) cudaEventRecord(s->prof_e[0], s->stream);
+                count_launches(1);
             }
             else
             {
@@ -1244,9 +1288,11 @@ extern "C" ogs_status ogs_gpu_profile(ogs_system* s, int32_t enable, ogs_profile
         out->spmv_launches = s->prof_spmv_n;
         out->solve_ms = s->prof_solve_ms;
         out->solves = s->prof_solves;
+        out->persist_ms = s->prof_persist_ms;
+        out->persist_iters = s->prof_persist_iters;
     }
-    s->prof_spmv_ms = s->prof_solve_ms = 0.0;
-    s->prof_spmv_n = s->prof_solves = 0;
+    s->prof_spmv_ms = s->prof_solve_ms = s->prof_persist_ms = 0.0;
+    s->prof_spmv_n = s->prof_solves = s->prof_persist_iters = 0;
     const bool on = enable != 0;
     if (on && !s->prof_b[0])
         for (int i = 0; i < ogs_system::kChunk; i++)

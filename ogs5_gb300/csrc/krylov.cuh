@@ -41,6 +41,9 @@ struct KState
     int base_iter;
     int nb_spmv, nb_upd;         // producer grid sizes (partials to add)
     int pad3;
+    // grid barrier of the persistent FP32 CG kernel (reset with the header)
+    unsigned int bar_count, bar_gen;
+    int bar_err, pad5;
     unsigned int ticket[8];
     double part[8][2 * kMaxBlocks];
     double cg_ps[3 * kMaxBlocks];        // per SpMV block: p . s (FP64 CG); r.u, w.u, r.r (FP32 CG)

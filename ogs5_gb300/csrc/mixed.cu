@@ -48,14 +48,27 @@ namespace ogs {
 // kernel is latency-bound otherwise); out-of-range neighbours are
 // predicated off.  Summation order: diagonal, then per offset the upper and
 // the mirrored lower entry.
-template <int NU>
-__device__ __forceinline__ float dia_row(const MixedArgs& a, const float* __restrict__ x, int i)
+//
+// X_NC: x is read through the non-coherent read-only path (__ldg), valid
+// only when x does not change during the launch; the persistent kernel,
+// which rewrites x between its grid barriers, reads it with plain loads.
+template <bool X_NC>
+__device__ __forceinline__ float ldx(const float* x, int i)
+{
+    if constexpr (X_NC)
+        return __ldg(x + i);
+    else
+        return x[i];
+}
+
+template <int NU, bool X_NC = true>
+__device__ __forceinline__ float dia_row(const MixedArgs& a, const float* x, int i)
 {
     constexpr int K = 2 * NU - 1;
     const int n = a.n;
     float uv[K], xv[K];
     uv[0] = __ldg(a.U + i);
-    xv[0] = __ldg(x + i);
+    xv[0] = ldx<X_NC>(x, i);
 #pragma unroll
     for (int d = 1; d < NU; d++)
     {
@@ -63,9 +76,9 @@ __device__ __forceinline__ float dia_row(const MixedArgs& a, const float* __rest
         const float* Ud = a.U + (size_t)d * n;
         const bool up = i + o < n, lo = i - o >= 0;
         uv[2 * d - 1] = up ? __ldg(Ud + i) : 0.f;
-        xv[2 * d - 1] = up ? __ldg(x + i + o) : 0.f;
+        xv[2 * d - 1] = up ? ldx<X_NC>(x, i + o) : 0.f;
         uv[2 * d] = lo ? __ldg(Ud + i - o) : 0.f;
-        xv[2 * d] = lo ? __ldg(x + i - o) : 0.f;
+        xv[2 * d] = lo ? ldx<X_NC>(x, i - o) : 0.f;
     }
     float acc = 0.f;
 #pragma unroll
@@ -73,7 +86,8 @@ __device__ __forceinline__ float dia_row(const MixedArgs& a, const float* __rest
     return acc;
 }
 
-__device__ __forceinline__ float sell32_row(const MixedArgs& a, const float* __restrict__ x, int row)
+template <bool X_NC = true>
+__device__ __forceinline__ float sell32_row(const MixedArgs& a, const float* x, int row)
 {
     const int s = row >> 5;
     const int b0 = __ldg(a.A.slice_ptr + s), b1 = __ldg(a.A.slice_ptr + s + 1);
@@ -84,19 +98,19 @@ __device__ __forceinline__ float sell32_row(const MixedArgs& a, const float* __r
     for (int j = 0; j < w; j++)
     {
         const int k = beg + (j << 5);
-        acc += __ldg(a.val32 + k) * __ldg(x + __ldg(a.A.col + k));
+        acc += __ldg(a.val32 + k) * ldx<X_NC>(x, __ldg(a.A.col + k));
     }
     return acc;
 }
 
 // NU > 0: diagonal-offset operator with NU stored offsets; NU == 0: SELL-32
-template <int NU>
-__device__ __forceinline__ float op_row(const MixedArgs& a, const float* __restrict__ x, int i)
+template <int NU, bool X_NC = true>
+__device__ __forceinline__ float op_row(const MixedArgs& a, const float* x, int i)
 {
     if constexpr (NU > 0)
-        return dia_row<NU>(a, x, i);
+        return dia_row<NU, X_NC>(a, x, i);
     else
-        return sell32_row(a, x, i);
+        return sell32_row<X_NC>(a, x, i);
 }
 
 
@@ -345,6 +359,181 @@ __global__ void __launch_bounds__(kThreads) k_mp_update(MixedArgs a)
 }
 
 // ------------------------------------------------------------------
+// Persistent FP32 CG: the S and V steps of many iterations in one
+// cooperative launch (all blocks resident), two grid barriers per
+// iteration -- after the partial sums and after the vector update, whose u
+// the next product reads at neighbouring rows.  Every block adds the
+// partials itself in the same order, so all hold the same scalars and take
+// the same branch; block 0 publishes the state the replacement kernels and
+// the host read.  A thread owns the rows gtid + k * stride in both steps,
+// so w is read back by the thread that wrote it.
+// ------------------------------------------------------------------
+constexpr unsigned kBarSpinLimit = 1u << 24;
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p)
+{
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release(unsigned* p, unsigned v)
+{
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// false in every thread of the block once any block gave up waiting
+__device__ bool mp_grid_barrier(KState* st)
+{
+    __shared__ int s_go;
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        int go = 1;
+        const unsigned gen = ld_acquire(&st->bar_gen);
+        __threadfence();
+        if (atomicAdd(&st->bar_count, 1u) + 1u == gridDim.x)
+        {
+            st->bar_count = 0u;
+            __threadfence();
+            st_release(&st->bar_gen, gen + 1u);
+        }
+        else
+        {
+            unsigned spins = 0;
+            while (ld_acquire(&st->bar_gen) == gen)
+            {
+                if (++spins > kBarSpinLimit || *(volatile int*)&st->bar_err)
+                {
+                    atomicExch(&st->bar_err, 1);
+                    go = 0;
+                    break;
+                }
+                if (spins > 64) __nanosleep(32);
+            }
+        }
+        __threadfence();
+        s_go = go;
+    }
+    __syncthreads();
+    return s_go != 0;
+}
+
+template <int NU>
+__global__ void __launch_bounds__(kThreads) k_mp_persist(MixedArgs a, int iters)
+{
+    KState* st = a.st;
+    // launch-time state: nothing writes it before every block has passed the
+    // first barrier, which comes after these reads
+    if (st->done || st->replace) return;
+    const int it0 = st->iter, base_iter = st->base_iter, max_iter = st->max_iter;
+    const double scale = st->scale, bnorm = st->bnorm, tol = st->tol, dlt = st->delta;
+    double rmax = st->rmax;
+    double gam_prev = st->gam_hist[it0 & 1], eta_prev = st->eta_hist[it0 & 1];
+    double rb_prev = (it0 & 1) ? st->rbest[1] : st->rbest[0];
+    int ib_prev = (it0 & 1) ? st->itbest[1] : st->itbest[0];
+    const int n = a.n, stride = gridDim.x * blockDim.x, gtid = blockIdx.x * blockDim.x + threadIdx.x;
+    for (int t = 0; t < iters; t++)
+    {
+        const int it = it0 + t + 1;
+        // S: w32 = A32 u32 ; partials of r.u, w.u, r.r
+        float v[3] = {0.f, 0.f, 0.f};
+        for (int i = gtid; i < n; i += stride)
+        {
+            const float w = op_row<NU, false>(a, a.u32, i);
+            a.w32[i] = w;
+            const float u = a.u32[i], r = a.r32[i];
+            v[0] += r * u;
+            v[1] += w * u;
+            v[2] += r * r;
+        }
+        write_partials<3, float>(v, st->cg_ps);
+        if (!mp_grid_barrier(st)) break;
+        double g[3];
+        reduce_partials<3>(st->cg_ps, gridDim.x, g);
+        // V: the scalars of k_mp_update from this block's copies
+        const double gamma = g[0], delta = g[1], rn = sqrt(g[2]);
+        const bool first = it == 1;
+        const bool fresh = it == base_iter + 1;
+        if (fresh) rmax = rn;
+        const double beta = first ? 0.0 : gamma / gam_prev;
+        const double eta = first ? delta : delta - beta * beta * eta_prev;
+        const double alpha = gamma / eta;
+        const double est = rn / scale / bnorm;
+        const bool nonfinite = !isfinite(rn) || !isfinite(alpha);
+        const double rbp = fresh ? rn : rb_prev;
+        const int ibp = fresh ? it : ib_prev;
+        const bool better = rn < rbp;
+        const double rb = better ? rn : rbp;
+        const int ib = better ? it : ibp;
+        const bool stalled = it - ib > max(kPlateau, (it - base_iter) / 2);
+        const bool repl = !nonfinite && !fresh && (est < tol || rn < dlt * rmax || it > max_iter || stalled);
+        if (blockIdx.x == 0 && threadIdx.x == 0)
+        {
+            st->iter = it;
+            if (it & 1) { st->rbest[1] = rb; st->itbest[1] = ib; }
+            else { st->rbest[0] = rb; st->itbest[0] = ib; }
+            if (fresh) st->rmax = rn;
+            st->gam_hist[it & 1] = gamma;
+            st->eta_hist[it & 1] = eta;
+            st->first = 0;
+            if (nonfinite) { st->status = OGS_NONFINITE; st->done = 1; }
+            else if (repl)
+            {
+                st->replace = 1;
+                st->rn_req = rn;
+                st->stalled = stalled && !(est < tol || rn < dlt * rmax || it > max_iter);
+            }
+        }
+        if (nonfinite || repl) break;
+        gam_prev = gamma;
+        eta_prev = eta;
+        rb_prev = rb;
+        ib_prev = ib;
+        const float fb = (float)beta, fa = (float)alpha;
+        for (int base = gtid; base < n; base += kU32 * stride)
+        {
+            float uv[kU32], wv[kU32], pv[kU32], sv[kU32], xv[kU32], rv[kU32], dv[kU32];
+#pragma unroll
+            for (int k = 0; k < kU32; k++)
+            {
+                const int i = base + k * stride;
+                const bool in = i < n;
+                uv[k] = in ? a.u32[i] : 0.f;
+                wv[k] = in ? a.w32[i] : 0.f;
+                pv[k] = in ? a.p32[i] : 0.f;
+                sv[k] = in ? a.s32[i] : 0.f;
+                xv[k] = in ? a.x32[i] : 0.f;
+                rv[k] = in ? a.r32[i] : 0.f;
+                dv[k] = in ? a.d32[i] : 0.f;
+            }
+#pragma unroll
+            for (int k = 0; k < kU32; k++)
+            {
+                const int i = base + k * stride;
+                if (i < n)
+                {
+                    const float p = uv[k] + fb * pv[k];
+                    const float s = wv[k] + fb * sv[k];
+                    const float r = rv[k] - fa * s;
+                    a.p32[i] = p;
+                    a.s32[i] = s;
+                    a.x32[i] = xv[k] + fa * p;
+                    a.r32[i] = r;
+                    a.u32[i] = r * dv[k];
+                }
+            }
+        }
+        if (!mp_grid_barrier(st)) break;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0 && *(volatile int*)&st->bar_err)
+    {
+        st->status = OGS_CUDA_ERROR;
+        st->done = 1;
+    }
+}
+
+// ------------------------------------------------------------------
 // launchers
 // ------------------------------------------------------------------
 int vec_grid(int n);
@@ -375,6 +564,57 @@ void launch_mp_replace(const MixedArgs& a, cudaStream_t s)
     k_mp_accumulate<<<g, kThreads, 0, s>>>(a);
     k_mp_residual<<<g, kThreads, 0, s>>>(a);
     k_mp_restart<<<g, kThreads, 0, s>>>(a);
+}
+
+// resident blocks of the persistent kernel for the operator format (0 when
+// the device cannot launch it cooperatively)
+template <int NU>
+static int persist_grid_for(int n)
+{
+    int dev = 0, sms = 152, coop = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+    if (!coop) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mp_persist<NU>, kThreads, 0) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return 0;
+    }
+    const int need = (n + kThreads - 1) / kThreads;
+    return std::max(1, std::min(need, std::min(per_sm * sms, kMaxBlocks)));
+}
+
+int mp_persist_grid(const MixedArgs& a)
+{
+    switch (a.fmt == 0 ? a.n_up : 0)
+    {
+        case 14: return persist_grid_for<14>(a.n);
+        case 8: return persist_grid_for<8>(a.n);
+        case 5: return persist_grid_for<5>(a.n);
+        default: return persist_grid_for<0>(a.n);
+    }
+}
+
+// up to `iters` FP32 iterations in one cooperative launch of `grid` blocks
+cudaError_t launch_mp_persist(const MixedArgs& a, int grid, int iters, cudaStream_t s)
+{
+    cudaLaunchConfig_t lc = {};
+    lc.gridDim = dim3(grid);
+    lc.blockDim = dim3(kThreads);
+    lc.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    lc.attrs = at;
+    lc.numAttrs = 1;
+    switch (a.fmt == 0 ? a.n_up : 0)
+    {
+        case 14: return cudaLaunchKernelEx(&lc, k_mp_persist<14>, a, iters);
+        case 8: return cudaLaunchKernelEx(&lc, k_mp_persist<8>, a, iters);
+        case 5: return cudaLaunchKernelEx(&lc, k_mp_persist<5>, a, iters);
+        default: return cudaLaunchKernelEx(&lc, k_mp_persist<0>, a, iters);
+    }
 }
 
 void launch_mp_iteration(const MixedArgs& a, cudaStream_t s, cudaEvent_t eb, cudaEvent_t ee)

@@ -78,21 +78,74 @@ def test_fp32_refined_rejects_bicgstab(gpu):
     assert ei.value.status == gpu.BAD_ARG
 
 
-@pytest.mark.parametrize("mixed", [False, True])
-def test_profile_counts_spmv_launches(gpu, mixed):
-    """ogs_gpu_profile times one SpMV per executed Krylov iteration."""
+@pytest.mark.parametrize("mixed,schedule", [(False, 0), (True, 0), (True, 1)])
+def test_profile_counts_spmv_launches(gpu, mixed, schedule):
+    """ogs_gpu_profile times one SpMV in four iterations of the graph
+    schedules, and every launch of the persistent FP32 kernel with the
+    iterations it ran."""
     m = M.structured_hex(16, 12, 8)
     ek = fields.lognormal_k(m.shape, np.log(1e-5), 1.0, 4.0, seed=1)
     eqs, x0 = _deck(gpu, m, ek)
     eqs.ConfigNumerics(gpu.LS_CG, gpu.PRECOND_JACOBI, 5000, 1e-10,
-                       precision=gpu.PRECISION_FP32_REFINED if mixed else gpu.PRECISION_FP64)
+                       precision=gpu.PRECISION_FP32_REFINED if mixed else gpu.PRECISION_FP64,
+                       schedule=schedule)
     eqs.profile(True)
     x = x0.copy()
     it = eqs.Solver(x)
     pr = eqs.profile(False)
-    assert pr["solves"] == 1 and pr["spmv_ms"] > 0
-    # the SpMV of every fourth iteration of a chunk is timed
-    assert abs(pr["spmv_launches"] - it / 4) <= it / 16 + 3
+    assert pr["solves"] == 1
+    if mixed and schedule == gpu.SCHEDULE_PERSISTENT:
+        # an iteration that asks for a replacement is redone after it
+        rep = eqs.stats()["refinements"]
+        assert pr["persist_ms"] > 0 and it <= pr["persist_iters"] <= it + rep + 1
+        assert pr["spmv_launches"] == 0
+    else:
+        assert pr["spmv_ms"] > 0 and pr["persist_iters"] == 0
+        assert abs(pr["spmv_launches"] - it / 4) <= it / 16 + 3
+
+
+@pytest.mark.parametrize("kind", ["hex", "tet", "hex_renumbered", "quad"])
+def test_fp32_schedules_agree(gpu, kind):
+    """The persistent cooperative kernel and the two-kernel graph schedule
+    run the same recurrence: heads within the FP32 bar of each other and of
+    FP64, iteration counts within a few (their dot products add the block
+    partials of different grids)."""
+    if kind == "tet":
+        m = M.structured_tet(14, 10, 8)
+        ek = np.repeat(fields.lognormal_k((14, 10, 8), np.log(1e-5), 1.0, 4.0, seed=5), 6)
+    elif kind == "quad":
+        m = M.structured_quad(120, 90)
+        ek = fields.lognormal_k(m.shape, np.log(1e-5), 1.0, 6.0, seed=5)
+    else:
+        m = M.structured_hex(30, 22, 14)
+        ek = fields.lognormal_k(m.shape, np.log(1e-5), 1.0, 4.0, seed=5)
+    if kind == "hex_renumbered":
+        m, _ = renumber(m, 7)  # SELL-32 FP32 operator
+    eqs, x0 = _deck(gpu, m, ek)
+    eqs.ConfigNumerics(gpu.LS_CG, gpu.PRECOND_JACOBI, 20000, 1e-10, check_norm_rhs=False)
+    x64 = x0.copy()
+    eqs.Solver(x64)
+    out = {}
+    for sch in (gpu.SCHEDULE_GRAPH, gpu.SCHEDULE_PERSISTENT):
+        eqs.ConfigNumerics(gpu.LS_CG, gpu.PRECOND_JACOBI, 20000, 1e-10, precision=gpu.PRECISION_FP32_REFINED,
+                           check_norm_rhs=False, schedule=sch)
+        x = x0.copy()
+        it = eqs.Solver(x)
+        st = eqs.stats()
+        assert st["status"] == gpu.OK and st["rel_residual"] < 1e-10
+        assert rel_max_err(x, x64) < MIXED_RTOL
+        out[sch] = (x, it)
+    (xg, itg), (xp, itp) = out[gpu.SCHEDULE_GRAPH], out[gpu.SCHEDULE_PERSISTENT]
+    assert rel_max_err(xp, xg) < MIXED_RTOL
+    assert abs(itp - itg) <= max(5, itg // 20)
+
+
+def test_schedule_rejects_unknown(gpu):
+    m = M.structured_hex(4, 4, 4)
+    eqs, _ = _deck(gpu, m, np.ones(m.n_elements))
+    with pytest.raises(gpu.OgsError):
+        eqs.ConfigNumerics(gpu.LS_CG, gpu.PRECOND_JACOBI, 100, 1e-10, precision=gpu.PRECISION_FP32_REFINED,
+                           schedule=7)
 
 
 def test_fp32_stall_falls_back_to_fp64(gpu):
