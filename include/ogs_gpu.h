@@ -86,7 +86,15 @@ enum
 enum
 {
     OGS_PRECISION_FP64 = 0,
-    OGS_PRECISION_FP32_REFINED = 1 /* FP32 matrix + inner sweeps, FP64 IR */
+    OGS_PRECISION_FP32_REFINED = 1, /* FP32 matrix + inner sweeps, FP64 IR */
+    OGS_PRECISION_FP32_CELLS = 2    /* as FP32_REFINED, but on a regular hex
+                                       lattice whose matrix is a sum of
+                                       scaled box-element matrices (flow
+                                       without mass lumping) the inner CG
+                                       applies the operator from one FP32
+                                       coefficient per cell (4 B per cell
+                                       instead of 56 B per row); elsewhere
+                                       the stored FP32 operator            */
 };
 
 /* Mesh description: the data CFEMesh hands to SparseTable and the element
@@ -203,6 +211,11 @@ typedef struct
                                   claimed) and the solve finished in FP64 CG
                                   from x (iterations count both phases)       */
     double solve_ms;           /* device time of the solve, CUDA events        */
+    int32_t fp32_operator;     /* FP32 mode: the inner CG's operator, 0 FP32
+                                  diagonal offsets, 1 FP32 SELL-32, 2 one
+                                  coefficient per cell of a regular hex
+                                  lattice; -1 in FP64 mode                    */
+    int32_t pad0;
 } ogs_solve_stats;
 
 typedef struct ogs_mesh ogs_mesh;

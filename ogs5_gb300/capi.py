@@ -34,7 +34,7 @@ GROUNDWATER_FLOW, LIQUID_FLOW, MASS_TRANSPORT = 0, 1, 2
 DIRICHLET_ROW_ONLY, DIRICHLET_SYMMETRIC = 0, 1
 LS_BICGSTAB, LS_CG = 2, 5
 PRECOND_NONE, PRECOND_JACOBI, PRECOND_ILU0 = 0, 1, 100
-PRECISION_FP64, PRECISION_FP32_REFINED = 0, 1
+PRECISION_FP64, PRECISION_FP32_REFINED, PRECISION_FP32_CELLS = 0, 1, 2
 SCHEDULE_GRAPH, SCHEDULE_PERSISTENT = 0, 1
 
 # every entry point include/ogs_gpu.h declares
@@ -101,7 +101,7 @@ class Profile(C.Structure):
 class SolveStats(C.Structure):
     _fields_ = [("iterations", C.c_int32), ("status", C.c_int32), ("rel_residual", C.c_double),
                 ("b_norm", C.c_double), ("refinements", C.c_int32), ("fp64_fallback", C.c_int32),
-                ("solve_ms", C.c_double)]
+                ("solve_ms", C.c_double), ("fp32_operator", C.c_int32), ("pad0", C.c_int32)]
 
 
 class BatchRealisation(C.Structure):
@@ -385,7 +385,7 @@ class LinearEQS:
         s = self.last_stats
         return {"iterations": s.iterations, "status": s.status, "rel_residual": s.rel_residual,
                 "b_norm": s.b_norm, "refinements": s.refinements, "fp64_fallback": s.fp64_fallback,
-                "solve_ms": s.solve_ms}
+                "solve_ms": s.solve_ms, "fp32_operator": s.fp32_operator}
 
     def gp_velocity(self, params: AssemblyParams, elem_k, u, out=None):
         ng = self.gmesh.n_gauss

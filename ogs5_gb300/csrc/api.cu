@@ -23,6 +23,13 @@ void launch_mp_convert(const MixedArgs& a, const int32_t* row_len, const int8_t*
 void launch_mp_replace(const MixedArgs& a, cudaStream_t s);
 void launch_mp_iteration(const MixedArgs& a, cudaStream_t s, cudaEvent_t eb, cudaEvent_t ee);
 int mp_persist_grid(const MixedArgs& a);
+void launch_mp_convert_cells(const MixedArgs& a, const double* coef, int64_t cells, float* alpha32, float* beta32,
+                             unsigned char* mask, float* dbc, const int32_t* diag_pos, const double* dinv64,
+                             float* d32, int bc_mode, const unsigned char* bc_flag, const int32_t* bc_rows, int nbc,
+                             cudaStream_t s);
+void launch_mp_check(const MixedArgs& a, unsigned* out, cudaStream_t s);
+int cell_spmv_grid(int nx, int ny, int nz);
+void launch_flow_cell_coef(const AsmArgs& a, double* coef, cudaStream_t s);
 cudaError_t launch_mp_persist(const MixedArgs& a, int grid, int iters, cudaStream_t s);
 int kernels_per_iteration(int kind, int precond);
 int krylov_init_launches(int kind, int precond);
@@ -180,6 +187,7 @@ struct SolveTask
     cudaGraphExec_t ge = nullptr;
     int per = 0, launched = 0, rounds = 0, chunk_before = -1;
     int fp32_iters = 0, fp32_repl = 0;  // FP32 phase of a solve that fell back to FP64
+    int fp32_fmt = -1;                  // operator format of the FP32 phase
     double* x_out = nullptr;
     ogs_status status = OGS_OK;
     float ms = 0.f;
@@ -235,6 +243,18 @@ struct ogs_system
     // direct cooperative launches and their grid (0: graph schedule)
     MixedArgs mp_args{};
     int mp_grid = 0;
+    // cell coefficients of the flow operator on a hex lattice (mesh grid):
+    // alpha per cell, beta at [cells], summed over the assemblies since
+    // Initialize; mf_state 1 while the assembled matrix has that form
+    double* mf_coef = nullptr;
+    int mf_state = 0;
+    // the assembled matrix is symmetric (flow assembly, symmetric Dirichlet
+    // elimination); the FP32 upper-half diagonal operator needs it
+    bool symmetric = true;
+    float *mf_alpha32 = nullptr, *mf_beta32 = nullptr, *mf_dbc = nullptr;
+    unsigned char* mf_mask = nullptr;
+    unsigned* d_check = nullptr;
+    unsigned* h_check = nullptr;  // pinned
     double prof_persist_ms = 0.0;
     int64_t prof_persist_iters = 0;
     // SpMV timing inside the chunk graphs (ogs_gpu_profile)
@@ -371,6 +391,9 @@ extern "C" ogs_status ogs_gpu_system_destroy(ogs_system* s)
     cudaFree(s->lu);
     cudaFree(s->op_mass);
     cudaFree(s->op_k);
+    cudaFree(s->mf_coef);
+    cudaFree(s->d_check);
+    if (s->h_check) cudaFreeHost(s->h_check);
     cudaFree(s->d_ilu_bad);
     cudaFree(s->st);
     cudaFree(s->d_bad);
@@ -388,6 +411,20 @@ extern "C" ogs_status ogs_gpu_system_destroy(ogs_system* s)
     if (s->ev1) cudaEventDestroy(s->ev1);
     if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
     delete s;
+    return OGS_OK;
+}
+
+// cell-coefficient record of a new assembly cycle (Initialize)
+static ogs_status mf_reset(ogs_system* s)
+{
+    const ogs_mesh* m = s->m;
+    s->symmetric = true;
+    s->mf_state = 0;
+    if (!m->grid || m->ngauss < 2) return OGS_OK;  // one Gauss point under-integrates L_box
+    const size_t cells = (size_t)(m->gx - 1) * (m->gy - 1) * (m->gz - 1);
+    if (!s->mf_coef) OGS_CUDA_TRY(cudaMalloc(&s->mf_coef, (cells + 1) * sizeof(double)));
+    OGS_CUDA_TRY(cudaMemsetAsync(s->mf_coef, 0, (cells + 1) * sizeof(double), s->stream));
+    s->mf_state = 1;
     return OGS_OK;
 }
 
@@ -448,6 +485,11 @@ extern "C" ogs_status ogs_gpu_system_create(ogs_mesh* m, void* stream, ogs_syste
     s->cfg.tol = 1e-12;
     s->cfg.check_norm_rhs = 1;
     s->configured = true;
+    if (mf_reset(s) != OGS_OK)
+    {
+        ogs_gpu_system_destroy(s);
+        return OGS_CUDA_ERROR;
+    }
     *out = s;
     return OGS_OK;
 }
@@ -466,7 +508,8 @@ extern "C" ogs_status ogs_gpu_configure(ogs_system* s, const ogs_solver_config* 
         return OGS_BAD_ARG;
     }
     if (c->max_iter < 0 || !(c->tol >= 0.0)) { set_error("configure: bad max_iter/tol"); return OGS_BAD_ARG; }
-    if (c->precision != OGS_PRECISION_FP64 && c->precision != OGS_PRECISION_FP32_REFINED)
+    if (c->precision != OGS_PRECISION_FP64 && c->precision != OGS_PRECISION_FP32_REFINED &&
+        c->precision != OGS_PRECISION_FP32_CELLS)
     {
         set_error("configure: unknown precision %d", c->precision);
         return OGS_BAD_ARG;
@@ -486,7 +529,7 @@ extern "C" ogs_status ogs_gpu_initialize(ogs_system* s)
     if (!s) { set_error("initialize: NULL system"); return OGS_BAD_ARG; }
     OGS_CUDA_TRY(cudaMemsetAsync(s->val, 0, s->m->sell_nnz * sizeof(double), s->stream));
     OGS_CUDA_TRY(cudaMemsetAsync(s->b, 0, (size_t)s->n * sizeof(double), s->stream));
-    return OGS_OK;
+    return mf_reset(s);
 }
 
 static ogs_status check_params(const ogs_assembly_params* p)
@@ -536,6 +579,22 @@ static ogs_status enqueue_element_kernel(ogs_system* s, const ogs_assembly_param
         return OGS_BAD_ARG;
     }
     OGS_LAUNCH_CHECK();
+    // the cell-coefficient form holds for flow without mass lumping
+    if (kind == 0 && s->mf_state == 1)
+    {
+        if (p->mass_lumping)
+            s->mf_state = 0;
+        else
+        {
+            launch_flow_cell_coef(a, s->mf_coef, s->stream);
+            OGS_LAUNCH_CHECK();
+        }
+    }
+    if (kind == 1)
+    {
+        s->mf_state = 0;
+        s->symmetric = false;  // advection
+    }
     OGS_CUDA_TRY(cudaMemcpyAsync(s->h_bad, s->d_bad, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
     return OGS_OK;
 }
@@ -591,6 +650,8 @@ extern "C" ogs_status ogs_gpu_assemble(ogs_system* s, const ogs_assembly_params*
         if ((st = element_flag_status(s))) return st;
         s->op_valid = true;
     }
+    s->mf_state = 0;
+    s->symmetric = false;
     const double* du;
     if ((st = stage_in(s, u0, m->n_nodes, &s->u0, &du))) return st;
     k_mt_from_operators<<<vec_grid(s->n), 256, 0, s->stream>>>(m->slice_ptr, m->row_len, m->sell_col, s->op_mass,
@@ -749,6 +810,7 @@ extern "C" ogs_status ogs_gpu_set_dirichlet(ogs_system* s, const int64_t* rows, 
 {
     ogs_status st = dirichlet_upload(s, rows, values, n_rows, mode);
     if (st) return st;
+    if (mode == OGS_DIRICHLET_ROW_ONLY && n_rows > 0) s->symmetric = false;  // the columns stay
     if ((st = dirichlet_apply(s))) return st;
     OGS_CUDA_TRY(cudaStreamSynchronize(s->stream));
     return OGS_OK;
@@ -763,14 +825,29 @@ static ogs_status begin_fp32_refined(ogs_system* s, KState* h)
     ogs_mesh* m = s->m;
     const ogs_solver_config& c = s->cfg;
     const int n = s->n;
+    // FP32 operator: cell coefficients on a hex lattice whose matrix has
+    // that form (fmt 2, on request), else for symmetric matrices the upper
+    // half of the diagonal-offset form for the hex (14), Kuhn-tet (8) and
+    // quad (5) patterns (fmt 0), else SELL-32 with FP32 values (fmt 1)
+    const bool cells_ok = c.precision == OGS_PRECISION_FP32_CELLS && s->mf_state == 1 &&
+                          cell_spmv_grid(m->gx, m->gy, m->gz) <= kMaxBlocks;
+    const int want = cells_ok ? 2 : s->symmetric && (m->n_up == 14 || m->n_up == 8 || m->n_up == 5) ? 0 : 1;
+    const size_t cells = m->grid ? (size_t)(m->gx - 1) * (m->gy - 1) * (m->gz - 1) : 0;
+    if (s->fmt != want && s->fmt >= 0)
+    {
+        cudaFree(s->f32_block);
+        s->f32_block = nullptr;
+        s->fmt = -1;
+        drop_graphs(s);  // the captured iterations hold the operator format
+    }
     if (s->fmt < 0)
     {
-        // diagonal-offset kernels exist for the hex (14), Kuhn-tet (8) and
-        // quad (5) patterns; anything else runs SELL-32 with FP32 values
-        s->fmt = (m->n_up == 14 || m->n_up == 8 || m->n_up == 5) ? 0 : 1;
-        const size_t v4 = ((size_t)n * sizeof(float) + 255) & ~size_t(255);
+        s->fmt = want;
+        auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
+        const size_t v4 = al((size_t)n * sizeof(float));
         const size_t op = s->fmt == 0 ? (size_t)m->n_up * n * sizeof(float)
-                                      : (size_t)m->sell_nnz * sizeof(float);
+                        : s->fmt == 1 ? (size_t)m->sell_nnz * sizeof(float)
+                                      : al(cells * sizeof(float)) + 256 + v4 + al((size_t)n);
         s->f32_bytes = 7 * v4 + op;
         OGS_CUDA_TRY(cudaMalloc(&s->f32_block, s->f32_bytes));
         OGS_CUDA_TRY(cudaMemsetAsync(s->f32_block, 0, s->f32_bytes, s->stream));
@@ -778,8 +855,17 @@ static ogs_status begin_fp32_refined(ogs_system* s, KState* h)
         s->p32 = (float*)p; s->r32 = (float*)(p + v4); s->x32 = (float*)(p + 2 * v4);
         s->s32 = (float*)(p + 3 * v4); s->d32 = (float*)(p + 4 * v4);
         s->u32 = (float*)(p + 5 * v4); s->w32 = (float*)(p + 6 * v4);
-        float* opb = (float*)(p + 7 * v4);
-        if (s->fmt == 0) s->U = opb; else s->val32 = opb;
+        char* opb = p + 7 * v4;
+        s->U = nullptr; s->val32 = nullptr;
+        if (s->fmt == 0) s->U = (float*)opb;
+        else if (s->fmt == 1) s->val32 = (float*)opb;
+        else
+        {
+            s->mf_alpha32 = (float*)opb;
+            s->mf_beta32 = (float*)(opb + al(cells * sizeof(float)));
+            s->mf_dbc = (float*)(opb + al(cells * sizeof(float)) + 256);
+            s->mf_mask = (unsigned char*)(opb + al(cells * sizeof(float)) + 256 + v4);
+        }
     }
     MixedArgs a;
     std::memset(&a, 0, sizeof a);
@@ -789,13 +875,62 @@ static ogs_status begin_fp32_refined(ogs_system* s, KState* h)
     a.d32 = s->d32; a.x = s->x; a.b = s->b; a.r64 = s->r;
     a.x32 = s->x32; a.r32 = s->r32; a.p32 = s->p32; a.s32 = s->s32; a.u32 = s->u32; a.w32 = s->w32;
     a.st = s->st; a.n = n;
-    launch_mp_convert(a, m->row_len, m->slot_up, s->U, s->val32, s->dinv, s->d32, s->stream);
-    OGS_LAUNCH_CHECK();
+    if (s->fmt == 2)
+    {
+        a.gx = m->gx; a.gy = m->gy; a.gz = m->gz;
+        a.mf_alpha = s->mf_alpha32; a.mf_beta = s->mf_beta32; a.mf_mask = s->mf_mask; a.mf_dbc = s->mf_dbc;
+        // unit-coefficient box matrices by corner-equality pattern (bit 0 x,
+        // 1 y, 2 z): 1-D stiffness +-1/h and mass h/3 | h/6, tensor products
+        const double hs[3] = {m->ghx, m->ghy, m->ghz};
+        for (int pat = 0; pat < 8; pat++)
+        {
+            double K1[3], M1[3];
+            for (int d = 0; d < 3; d++)
+            {
+                const bool eq = (pat >> d) & 1;
+                K1[d] = (eq ? 1.0 : -1.0) / hs[d];
+                M1[d] = hs[d] * (eq ? 1.0 / 3.0 : 1.0 / 6.0);
+            }
+            a.mf_L[pat] = (float)(K1[0] * M1[1] * M1[2] + M1[0] * K1[1] * M1[2] + M1[0] * M1[1] * K1[2]);
+            a.mf_M[pat] = (float)(M1[0] * M1[1] * M1[2]);
+        }
+        for (int d = 0; d < 3; d++)
+        {
+            a.mf_m1[2 * d] = (float)(hs[d] / 3.0);
+            a.mf_m1[2 * d + 1] = (float)(hs[d] / 6.0);
+        }
+        launch_mp_convert_cells(a, s->mf_coef, (int64_t)cells, s->mf_alpha32, s->mf_beta32, s->mf_mask, s->mf_dbc,
+                                m->diag_pos, s->dinv, s->d32, s->bc_mode, s->bc_flag, s->bc_rows, s->nbc,
+                                s->stream);
+        OGS_LAUNCH_CHECK();
+        // the FP32 operator must reproduce the assembled FP64 matrix (up to
+        // FP32 rounding); a matrix changed by other means falls back
+        if (!s->d_check) OGS_CUDA_TRY(cudaMalloc(&s->d_check, 2 * sizeof(unsigned)));
+        if (!s->h_check) OGS_CUDA_TRY(cudaMallocHost(&s->h_check, 2 * sizeof(unsigned)));
+        launch_mp_check(a, s->d_check, s->stream);
+        OGS_LAUNCH_CHECK();
+        OGS_CUDA_TRY(cudaMemcpyAsync(s->h_check, s->d_check, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost,
+                                     s->stream));
+        OGS_CUDA_TRY(cudaStreamSynchronize(s->stream));
+        float dmax, smax;
+        std::memcpy(&dmax, &s->h_check[0], sizeof(float));
+        std::memcpy(&smax, &s->h_check[1], sizeof(float));
+        if (!(dmax <= 1e-5f * smax))
+        {
+            s->mf_state = 0;
+            return begin_fp32_refined(s, h);
+        }
+    }
+    else
+    {
+        launch_mp_convert(a, m->row_len, m->slot_up, s->U, s->val32, s->dinv, s->d32, s->stream);
+        OGS_LAUNCH_CHECK();
+    }
     OGS_CUDA_TRY(cudaMemsetAsync(s->x32, 0, (size_t)n * sizeof(float), s->stream));
     h->scale = 1.0;
     h->ratio = 1.0;
     h->first = 1;
-    h->nb_spmv = mp_spmv_grid(n);
+    h->nb_spmv = s->fmt == 2 ? cell_spmv_grid(m->gx, m->gy, m->gz) : mp_spmv_grid(n);
     h->nb_upd = red_grid(n);
     h->delta = c.inner_tol > 0.0 ? c.inner_tol : 1e-2;
     OGS_CUDA_TRY(cudaMemcpyAsync(s->st, h, kStateHeader, cudaMemcpyHostToDevice, s->stream));
@@ -822,6 +957,7 @@ static ogs_status begin_fp32_refined(ogs_system* s, KState* h)
     }
     OGS_CUDA_TRY(cudaGraphLaunch(s->mp_replace, s->stream));
     count_launches(4);
+    s->task.fp32_fmt = s->fmt;
     return OGS_OK;
 }
 
@@ -894,12 +1030,12 @@ static ogs_status solve_begin(ogs_system* s, double* x_inout)
 {
     if (!s || !x_inout) { set_error("solve: NULL argument"); return OGS_BAD_ARG; }
     const ogs_solver_config& c = s->cfg;
-    if (c.precision == OGS_PRECISION_FP32_REFINED && c.method != OGS_LS_CG)
+    if (c.precision != OGS_PRECISION_FP64 && c.method != OGS_LS_CG)
     {
         set_error("solve: the FP32-inner / FP64-refinement mode runs CG (ls_method 5)");
         return OGS_BAD_ARG;
     }
-    if (c.precision == OGS_PRECISION_FP32_REFINED && c.precond == OGS_PRECOND_ILU0)
+    if (c.precision != OGS_PRECISION_FP64 && c.precond == OGS_PRECOND_ILU0)
     {
         set_error("solve: the FP32-inner / FP64-refinement mode takes Jacobi or no preconditioner");
         return OGS_BAD_ARG;
@@ -914,7 +1050,7 @@ static ogs_status solve_begin(ogs_system* s, double* x_inout)
     if (!T.ev) OGS_CUDA_TRY(cudaEventCreateWithFlags(&T.ev, cudaEventDisableTiming));
     T.x_out = x_inout;
     T.xdev = is_device_ptr(x_inout);
-    T.mixed = c.precision == OGS_PRECISION_FP32_REFINED;
+    T.mixed = c.precision != OGS_PRECISION_FP64;
     T.kind = c.method == OGS_LS_CG ? SK_CG : SK_BICGSTAB;
     if (c.precond == OGS_PRECOND_ILU0)
     {
@@ -1154,6 +1290,7 @@ static ogs_status solve_end(ogs_system* s, ogs_solve_stats* stats)
         stats->refinements = h->replacements + T.fp32_repl;
         stats->fp64_fallback = T.fp32_iters > 0 || T.fp32_repl > 0 ? 1 : 0;
         stats->solve_ms = T.ms;
+        stats->fp32_operator = T.fp32_fmt;
     }
     const ogs_status st = T.status;
     T.phase = 0;

@@ -858,6 +858,28 @@ static void launch_vel(const AsmArgs& a, cudaStream_t s)
     k_gp_velocity<ET, NGP><<<grid_for(a.E, 128), 128, 0, s>>>(a);
 }
 
+// Cell coefficients of the flow operator on a regular hex lattice.  Without
+// mass lumping the left-hand side flow_combine scatters is
+// sum_c (alpha_c L_box + beta M_box) with alpha_c = relax0 * mat(K_c) and
+// beta = CalCoefMass / dt, L_box and M_box the Laplace and mass matrices of
+// the unit-coefficient box; the FP32 inner CG applies the operator from
+// these (summed over the assemblies since Initialize).  beta sits at
+// coef[E].
+__global__ void k_flow_cell_coef(ogs_assembly_params p, const double* __restrict__ elem_k, int64_t E,
+                                 double* coef)
+{
+    double relax0 = p.nls_relaxation;
+    if (relax0 < DBL_MIN) relax0 = 1.0;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < E; e += (int64_t)gridDim.x * blockDim.x)
+        coef[e] += relax0 * flow_mat(p, __ldg(elem_k + e));
+    if (blockIdx.x == 0 && threadIdx.x == 0) coef[E] += flow_mass_coef(p) * (1.0 / p.dt);
+}
+
+void launch_flow_cell_coef(const AsmArgs& a, double* coef, cudaStream_t s)
+{
+    k_flow_cell_coef<<<grid_for(a.E, 256), 256, 0, s>>>(a.p, a.elem_k, a.E, coef);
+}
+
 // dispatch on (element type, Gauss points); returns false for an
 // unsupported combination
 bool launch_assembly(const ogs_mesh* m, const AsmArgs& a, bool affine, int kind,

@@ -132,6 +132,13 @@ struct ogs_mesh
     int64_t sell_nnz = 0;     // SELL-32 slots including padding
     int n_slices = 0;
     bool affine = false;      // every element has a constant Jacobian
+    // regular lattice of hexahedra: node i = ix + gx (iy + gy iz) at
+    // (x0 + ix hx, ...), cell c = cx + (gx-1) (cy + (gy-1) cz) in the OGS
+    // corner order; the FP32 inner CG can then apply the operator from one
+    // coefficient per cell instead of stored matrix values
+    bool grid = false;
+    int gx = 0, gy = 0, gz = 0;
+    double ghx = 0.0, ghy = 0.0, ghz = 0.0;
     int device = 0;
     // device arrays
     double *x = nullptr, *y = nullptr, *z = nullptr;

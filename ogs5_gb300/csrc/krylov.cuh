@@ -263,6 +263,14 @@ struct MixedArgs
     float *x32, *r32, *p32, *s32, *u32, *w32;
     KState* st;
     int n;
+    // fmt 2: operator from one coefficient per cell of a regular hex lattice
+    int gx, gy, gz;
+    const float* mf_alpha;          // [cells] Laplace coefficient
+    const float* mf_beta;           // mass coefficient (one value)
+    const unsigned char* mf_mask;   // [n] bit 0: Dirichlet row, bit 1: column eliminated
+    const float* mf_dbc;            // [n] kept diagonal of Dirichlet rows
+    float mf_L[8], mf_M[8];         // box Laplace / mass entries by corner-equality pattern
+    float mf_m1[6];                 // 1-D mass entries per axis: (x: same, other), (y: ...), (z: ...)
 };
 
 }  // namespace ogs

@@ -8,6 +8,7 @@
 // position of (node_i, node_j); the assembly kernels scatter through it
 // without searching.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -323,6 +324,54 @@ extern "C" ogs_status ogs_gpu_mesh_destroy(ogs_mesh* m)
     return OGS_OK;
 }
 
+// Is the hex mesh a regular lattice in lexicographic node order (x fastest)
+// with uniform spacing and cells in lexicographic order with the OGS corner
+// order (bottom face counter-clockwise, then the top face)?
+static void detect_grid(const ogs_mesh_desc* d, ogs_mesh* m)
+{
+    m->grid = false;
+    if (d->elem_type != OGS_ELEM_HEX8) return;
+    const int64_t N = d->n_nodes, E = d->n_elements;
+    const double *x = d->x, *y = d->y, *z = d->z;
+    int64_t nx = 1;
+    while (nx < N && x[nx] != x[0]) nx++;
+    if (nx < 2 || N % nx) return;
+    int64_t ny = 1;
+    while (ny * nx < N && y[ny * nx] != y[0]) ny++;
+    if (ny < 2 || N % (nx * ny)) return;
+    const int64_t nz = N / (nx * ny);
+    if (nz < 2 || E != (nx - 1) * (ny - 1) * (nz - 1)) return;
+    const double hx = x[1] - x[0], hy = y[nx] - y[0], hz = z[nx * ny] - z[0];
+    if (!(hx > 0.0 && hy > 0.0 && hz > 0.0)) return;
+    std::atomic<bool> ok{true};
+    parallel_for(N, [&](int64_t lo, int64_t hi) {
+        for (int64_t i = lo; i < hi && ok.load(std::memory_order_relaxed); i++)
+        {
+            const int64_t ix = i % nx, t = i / nx, iy = t % ny, iz = t / ny;
+            if (std::fabs(x[i] - (x[0] + ix * hx)) > 1e-9 * hx || std::fabs(y[i] - (y[0] + iy * hy)) > 1e-9 * hy ||
+                std::fabs(z[i] - (z[0] + iz * hz)) > 1e-9 * hz)
+                ok = false;
+        }
+    });
+    if (!ok) return;
+    const int32_t* conn = d->connectivity;
+    parallel_for(E, [&](int64_t lo, int64_t hi) {
+        for (int64_t e = lo; e < hi && ok.load(std::memory_order_relaxed); e++)
+        {
+            const int64_t cx = e % (nx - 1), t = e / (nx - 1), cy = t % (ny - 1), cz = t / (ny - 1);
+            const int64_t n0 = cx + nx * (cy + ny * cz);
+            const int64_t want[8] = {n0, n0 + 1, n0 + 1 + nx, n0 + nx, n0 + nx * ny, n0 + 1 + nx * ny,
+                                     n0 + 1 + nx + nx * ny, n0 + nx + nx * ny};
+            for (int k = 0; k < 8; k++)
+                if (conn[e * 8 + k] != want[k]) ok = false;
+        }
+    });
+    if (!ok) return;
+    m->grid = true;
+    m->gx = (int)nx; m->gy = (int)ny; m->gz = (int)nz;
+    m->ghx = hx; m->ghy = hy; m->ghz = hz;
+}
+
 extern "C" ogs_status ogs_gpu_mesh_create(const ogs_mesh_desc* d, ogs_mesh** out)
 {
     if (!d || !out) { set_error("mesh_create: NULL argument"); return OGS_BAD_ARG; }
@@ -355,6 +404,7 @@ extern "C" ogs_status ogs_gpu_mesh_create(const ogs_mesh_desc* d, ogs_mesh** out
     m->ngp = num_gauss_points(et, ng);
     m->n_nodes = N; m->n_elem = E;
     cudaGetDevice(&m->device);
+    detect_grid(d, m);
 
     // node -> element incidence
     std::vector<int64_t> ne_ptr(N + 1, 0);

@@ -104,13 +104,81 @@ __device__ __forceinline__ float sell32_row(const MixedArgs& a, const float* x, 
 }
 
 // NU > 0: diagonal-offset operator with NU stored offsets; NU == 0: SELL-32
+// Operator from cell coefficients on a regular hex lattice (fmt 2): row i
+// of sum_c (alpha_c L_box + beta M_box) over the up to eight cells around
+// node i, with the eliminated columns of the Dirichlet set dropped and the
+// Dirichlet rows reduced to their kept diagonal.  L_box and M_box entries
+// depend only on which corner coordinates of the two nodes agree (three
+// bits), so the 64 corner pairs read two 8-entry tables.  Per row: 27
+// values of x, 27 mask bytes and up to 8 coefficients instead of 27
+// stored matrix values.
+template <bool X_NC>
+__device__ __forceinline__ float mf_row(const MixedArgs& a, const float* x, int i)
+{
+    const unsigned char mk = __ldg(a.mf_mask + i);
+    if (mk & 1) return __ldg(a.mf_dbc + i) * ldx<X_NC>(x, i);
+    const int nx = a.gx, ny = a.gy;
+    const int ix = i % nx, t = i / nx, iy = t % ny, iz = t / ny;
+    const bool vx0 = ix > 0, vx1 = ix < nx - 1, vy0 = iy > 0, vy1 = iy < ny - 1, vz0 = iz > 0,
+               vz1 = iz < a.gz - 1;
+    float xv[27];
+#pragma unroll
+    for (int dz = -1; dz <= 1; dz++)
+#pragma unroll
+        for (int dy = -1; dy <= 1; dy++)
+#pragma unroll
+            for (int dx = -1; dx <= 1; dx++)
+            {
+                const bool in = (dx < 0 ? vx0 : dx > 0 ? vx1 : true) && (dy < 0 ? vy0 : dy > 0 ? vy1 : true) &&
+                                (dz < 0 ? vz0 : dz > 0 ? vz1 : true);
+                const int j = i + dx + nx * (dy + ny * dz);
+                const float v = in ? ldx<X_NC>(x, j) : 0.f;
+                const int mk = in ? (int)__ldg(a.mf_mask + j) : 2;
+                xv[(dx + 1) + 3 * ((dy + 1) + 3 * (dz + 1))] = (mk & 2) ? 0.f : v;
+            }
+    const int ncx = nx - 1, ncy = ny - 1;
+    float accL = 0.f, accM = 0.f;
+#pragma unroll
+    for (int ez = 0; ez < 2; ez++)
+#pragma unroll
+        for (int ey = 0; ey < 2; ey++)
+#pragma unroll
+            for (int ex = 0; ex < 2; ex++)
+            {
+                // the cell with corner (ix - 1 + ex, iy - 1 + ey, iz - 1 + ez);
+                // node i is its corner (1 - ex, 1 - ey, 1 - ez)
+                if (!((ex ? vx1 : vx0) && (ey ? vy1 : vy0) && (ez ? vz1 : vz0))) continue;
+                const int c = (ix - 1 + ex) + ncx * ((iy - 1 + ey) + ncy * (iz - 1 + ez));
+                float sL = 0.f, sM = 0.f;
+#pragma unroll
+                for (int bz = 0; bz < 2; bz++)
+#pragma unroll
+                    for (int by = 0; by < 2; by++)
+#pragma unroll
+                        for (int bx = 0; bx < 2; bx++)
+                        {
+                            const int pat = ((1 - ex) == bx ? 1 : 0) | ((1 - ey) == by ? 2 : 0) | ((1 - ez) == bz ? 4 : 0);
+                            const float xb = xv[(ex + bx) + 3 * ((ey + by) + 3 * (ez + bz))];
+                            sL += a.mf_L[pat] * xb;
+                            sM += a.mf_M[pat] * xb;
+                        }
+                accL += __ldg(a.mf_alpha + c) * sL;
+                accM += sM;
+            }
+    return accL + __ldg(a.mf_beta) * accM;
+}
+
+// NU > 0: diagonal-offset operator with NU stored offsets; NU == 0: SELL-32;
+// NU == -1: cell coefficients of a regular hex lattice
 template <int NU, bool X_NC = true>
 __device__ __forceinline__ float op_row(const MixedArgs& a, const float* x, int i)
 {
     if constexpr (NU > 0)
         return dia_row<NU, X_NC>(a, x, i);
-    else
+    else if constexpr (NU == 0)
         return sell32_row<X_NC>(a, x, i);
+    else
+        return mf_row<X_NC>(a, x, i);
 }
 
 
@@ -136,6 +204,79 @@ __global__ void k_mp_convert(MixedArgs a, const int32_t* __restrict__ row_len,
                 val32[k] = (float)a.A.val[k];
         }
     }
+}
+
+// fmt 2: FP32 cell coefficients, the Dirichlet mask and kept diagonals,
+// and the Jacobi inverse
+__global__ void k_mp_convert_cells(const double* __restrict__ coef, int64_t cells, float* alpha32, float* beta32)
+{
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < cells; c += (int64_t)gridDim.x * blockDim.x)
+        alpha32[c] = (float)coef[c];
+    if (blockIdx.x == 0 && threadIdx.x == 0) *beta32 = (float)coef[cells];
+}
+
+// mask from the Dirichlet set: SYMMETRIC (row flags) eliminates rows and
+// columns, ROW_ONLY (row list) only rows
+__global__ void k_mp_mask_symmetric(const unsigned char* __restrict__ flag, unsigned char* mask, int n)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        mask[i] = flag[i] ? 3 : 0;
+}
+
+__global__ void k_mp_mask_rows(const int32_t* __restrict__ rows, int nbc, unsigned char* mask)
+{
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nbc; q += gridDim.x * blockDim.x) mask[rows[q]] = 1;
+}
+
+__global__ void k_mp_dbc(MixedArgs a, const int32_t* __restrict__ diag_pos, const double* __restrict__ dinv64,
+                         float* d32, float* dbc)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x)
+    {
+        d32[i] = (float)dinv64[i];
+        const int dp = diag_pos[i];
+        dbc[i] = (a.mf_mask[i] & 1) && dp >= 0 ? (float)a.A.val[dp] : 0.f;
+    }
+}
+
+// Check of an FP32 operator against the FP64 matrix on a fixed test vector
+// v (in w32): out[0] = max |y32 - y64|, out[1] = max sum_j |a_ij v_j|, as
+// float bits (non-negative floats order like their bits)
+__device__ __forceinline__ float test_vector(int i)
+{
+    unsigned h = (unsigned)i * 2654435761u;
+    h ^= h >> 15;
+    return 0.5f + (float)(h & 0xffffu) * (1.0f / 65536.0f);
+}
+
+__global__ void k_mp_check_fill(float* v, int n)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) v[i] = test_vector(i);
+}
+
+template <int NU>
+__global__ void k_mp_check(MixedArgs a, unsigned* out)
+{
+    float dmax = 0.f, smax = 0.f;
+    for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < a.n; row += gridDim.x * blockDim.x)
+    {
+        const float y32 = op_row<NU>(a, a.w32, row);
+        const int s = row >> 5;
+        const int b0 = a.A.slice_ptr[s], b1 = a.A.slice_ptr[s + 1];
+        const int beg = b0 + (row & 31);
+        double y = 0.0, sa = 0.0;
+        for (int j = 0; j < (b1 - b0) >> 5; j++)
+        {
+            const int k = beg + (j << 5);
+            const double t = a.A.val[k] * (double)a.w32[a.A.col[k]];
+            y += t;
+            sa += fabs(t);
+        }
+        dmax = fmaxf(dmax, (float)fabs((double)y32 - y));
+        smax = fmaxf(smax, (float)sa);
+    }
+    atomicMax(out, __float_as_uint(dmax));
+    atomicMax(out + 1, __float_as_uint(smax));
 }
 
 // ------------------------------------------------------------------
@@ -270,6 +411,276 @@ __global__ void __launch_bounds__(kThreads, 3) k_mp_spmv(MixedArgs a)
         v[2] += r * r;
     }
     write_partials<3, float>(v, st->cg_ps);
+}
+
+// fmt 2 product on the lattice: blocks of 4 warps, a warp holds 32
+// consecutive x-columns of one y-line and marches up kCellZ planes in z.
+// x at ix +- 1 comes from the neighbouring lanes (loads at the warp edges
+// only); three planes of the 3 x 3 neighbourhood and two layers of 2 x 2
+// cells stay in registers, so a node costs one x, one mask byte per line
+// and plane step, two cell coefficients and its r instead of the 27 + 27
+// + 8 loads of mf_row.
+constexpr int kCellZ = 16;
+constexpr int kCellWarps = 4;
+
+struct CellGrid
+{
+    int bx, by, bz;  // blocks along x (32 columns), y (kCellWarps lines), z (kCellZ planes)
+};
+
+__host__ __device__ inline CellGrid cell_grid(int nx, int ny, int nz)
+{
+    return {(nx + 31) / 32, (ny + kCellWarps - 1) / kCellWarps, (nz + kCellZ - 1) / kCellZ};
+}
+
+// Raw loads of one line (iy, z) of a plane: x and mask at ix, and at ix - 1
+// (lane 0) / ix + 1 (lane 31) -- issued one plane step ahead of their use,
+// without depending on each other.  cell_line_finish masks them and takes
+// the neighbours of the inner lanes from the shuffles.
+struct LineRaw
+{
+    float xc, xe;   // x at ix, and at the warp-edge neighbour
+    int mc, me;     // mask bytes (2 = eliminated or outside)
+};
+
+__device__ __forceinline__ void cell_line_fetch(const MixedArgs& a, const float* x, int ix, int iy, int z, bool lv,
+                                                LineRaw& R)
+{
+    const int nx = a.gx, lane = threadIdx.x & 31;
+    const int j = ix + nx * (iy + a.gy * z);
+    const bool in = lv && ix < nx;
+    R.xc = in ? x[j] : 0.f;
+    R.mc = in ? (int)__ldg(a.mf_mask + j) : 2;
+    const int je = lane == 0 ? j - 1 : j + 1;
+    const bool ein = lv && (lane == 0 ? (ix >= 1 && ix - 1 < nx) : (lane == 31 && ix + 1 < nx));
+    R.xe = ein ? x[je] : 0.f;
+    R.me = ein ? (int)__ldg(a.mf_mask + je) : 2;
+}
+
+__device__ __forceinline__ void cell_line_finish(const LineRaw& R, float& l, float& c, float& r)
+{
+    const int lane = threadIdx.x & 31;
+    const float v = (R.mc & 2) ? 0.f : R.xc;
+    const float e = (R.me & 2) ? 0.f : R.xe;
+    float lf = __shfl_up_sync(0xffffffffu, v, 1), rt = __shfl_down_sync(0xffffffffu, v, 1);
+    if (lane == 0) lf = e;
+    if (lane == 31) rt = e;
+    l = lf;
+    c = v;
+    r = rt;
+}
+
+// cell coefficients (cx, cy, cz), cx in {ix - 1, ix}, cy in {iy - 1, iy}:
+// raw loads (own column, and ix - 1 on lane 0), then the shuffle
+struct LayerRaw
+{
+    float v[2], e[2];
+};
+
+__device__ __forceinline__ void cell_layer_fetch(const MixedArgs& a, int ix, int iy, int cz, LayerRaw& R)
+{
+    const int ncx = a.gx - 1, ncy = a.gy - 1, lane = threadIdx.x & 31;
+    const bool zin = cz >= 0 && cz < a.gz - 1;
+#pragma unroll
+    for (int ey = 0; ey < 2; ey++)
+    {
+        const int cy = iy - 1 + ey;
+        const bool yin = zin && cy >= 0 && cy < ncy;
+        const int base = ncx * (cy + ncy * cz);
+        R.v[ey] = yin && ix < ncx ? __ldg(a.mf_alpha + base + ix) : 0.f;
+        R.e[ey] = lane == 0 && yin && ix >= 1 && ix - 1 < ncx ? __ldg(a.mf_alpha + base + ix - 1) : 0.f;
+    }
+}
+
+__device__ __forceinline__ void cell_layer_finish(const LayerRaw& R, float (&A)[2][2])
+{
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int ey = 0; ey < 2; ey++)
+    {
+        float lf = __shfl_up_sync(0xffffffffu, R.v[ey], 1);
+        if (lane == 0) lf = R.e[ey];
+        A[ey][1] = R.v[ey];
+        A[ey][0] = lf;
+    }
+}
+
+// per-thread constants of the fmt 2 product
+struct CellCtx
+{
+    const float* x;
+    int ix, iy, nx, ny, nz, z1;
+    bool act, px0, px1, py0, py1;
+    bool lv[3];
+    float beta;
+};
+
+// One node of the column: planes z-1, z, z+1 in P[A], P[B], P[C] (P[C] is
+// filled here from the prefetched raw loads), cell layers z-1 and z in
+// Ac[J0], Ac[J1] (Ac[J1] filled here); then the loads of plane z+2 and
+// layer z+1 are issued for the next step.  The slots rotate with the step,
+// so the window is never copied.
+// The node's own u, mask byte and r come one step ahead too (NU: u and mask
+// of node z + 1 from the raw line loads, rn: its r).
+struct NodeNext
+{
+    float u, r;
+    int m;
+};
+
+template <int A, int B, int C, int J0, int J1>
+__device__ __forceinline__ void cell_step(const MixedArgs& a, const CellCtx& t, int z, float (&P)[3][3][3],
+                                          float (&Ac)[2][2][2], LineRaw (&NR)[3], LayerRaw& NA, NodeNext& nn,
+                                          float (&v)[3])
+{
+    const float u = nn.u, r = nn.r;
+    const int mk = nn.m;
+    const int i = t.ix + t.nx * (t.iy + t.ny * z);
+    nn.u = NR[1].xc;  // node z + 1 (raw, unmasked)
+    nn.m = NR[1].mc;
+#pragma unroll
+    for (int l = 0; l < 3; l++) cell_line_finish(NR[l], P[C][l][0], P[C][l][1], P[C][l][2]);
+    cell_layer_finish(NA, Ac[J1]);
+    if (z + 1 < t.z1)
+    {
+#pragma unroll
+        for (int l = 0; l < 3; l++)
+            cell_line_fetch(a, t.x, t.ix, t.iy + l - 1, z + 2, t.lv[l] && z + 2 < t.nz, NR[l]);
+        cell_layer_fetch(a, t.ix, t.iy, z + 1, NA);
+        nn.r = t.act ? a.r32[i + t.nx * t.ny] : 0.f;
+    }
+    if (!t.act) return;  // lanes past the lattice: only the shuffles above
+    float w;
+    if (mk & 1)
+        w = __ldg(a.mf_dbc + i) * u;
+    else
+    {
+        const int pl[3] = {A, B, C};
+        const int jl[2] = {J0, J1};
+        // Laplace: per cell around the node (absent cells have alpha 0)
+        float accL = 0.f;
+#pragma unroll
+        for (int ez = 0; ez < 2; ez++)
+#pragma unroll
+            for (int ey = 0; ey < 2; ey++)
+#pragma unroll
+                for (int ex = 0; ex < 2; ex++)
+                {
+                    float sL = 0.f;
+#pragma unroll
+                    for (int bz = 0; bz < 2; bz++)
+#pragma unroll
+                        for (int by = 0; by < 2; by++)
+#pragma unroll
+                            for (int bx = 0; bx < 2; bx++)
+                            {
+                                const int pat = ((1 - ex) == bx ? 1 : 0) | ((1 - ey) == by ? 2 : 0) |
+                                                ((1 - ez) == bz ? 4 : 0);
+                                sL += a.mf_L[pat] * P[pl[ez + bz]][ey + by][ex + bx];
+                            }
+                    accL += Ac[jl[ez]][ey][ex] * sL;
+                }
+        // mass: M_box and the presence of the cells are tensor products, so
+        // the sum over the present cells is the 3 x 3 x 3 stencil
+        // mx (x) my (x) mz with per-axis weights -- summed axis by axis
+        const bool pz0 = z > 0, pz1 = z < t.nz - 1;
+        const float mx0 = t.px0 ? a.mf_m1[1] : 0.f, mx2 = t.px1 ? a.mf_m1[1] : 0.f;
+        const float mx1 = (t.px0 ? a.mf_m1[0] : 0.f) + (t.px1 ? a.mf_m1[0] : 0.f);
+        const float my0 = t.py0 ? a.mf_m1[3] : 0.f, my2 = t.py1 ? a.mf_m1[3] : 0.f;
+        const float my1 = (t.py0 ? a.mf_m1[2] : 0.f) + (t.py1 ? a.mf_m1[2] : 0.f);
+        const float mz0 = pz0 ? a.mf_m1[5] : 0.f, mz2 = pz1 ? a.mf_m1[5] : 0.f;
+        const float mz1 = (pz0 ? a.mf_m1[4] : 0.f) + (pz1 ? a.mf_m1[4] : 0.f);
+        float accM = 0.f;
+#pragma unroll
+        for (int q = 0; q < 3; q++)
+        {
+            float sy = 0.f;
+#pragma unroll
+            for (int l = 0; l < 3; l++)
+            {
+                const float* row = P[pl[q]][l];
+                const float sx = mx0 * row[0] + mx1 * row[1] + mx2 * row[2];
+                sy += (l == 0 ? my0 : l == 1 ? my1 : my2) * sx;
+            }
+            accM += (q == 0 ? mz0 : q == 1 ? mz1 : mz2) * sy;
+        }
+        w = accL + t.beta * accM;
+    }
+    a.w32[i] = w;
+    v[0] += r * u;
+    v[1] += w * u;
+    v[2] += r * r;
+}
+
+// S for fmt 2: iter += 1 ; w32 = A32 u32 ; partials of r.u, w.u, r.r
+__global__ void __launch_bounds__(32 * kCellWarps) k_mp_spmv_cells(MixedArgs a)
+{
+    KState* st = a.st;
+    if (st->done || st->replace) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) st->iter += 1;  // no block of this kernel reads iter
+    CellCtx t;
+    t.nx = a.gx; t.ny = a.gy; t.nz = a.gz;
+    const CellGrid G = cell_grid(t.nx, t.ny, t.nz);
+    const int b = blockIdx.x, bxi = b % G.bx, byi = (b / G.bx) % G.by, bzi = b / (G.bx * G.by);
+    t.ix = bxi * 32 + (threadIdx.x & 31);
+    t.iy = byi * kCellWarps + (threadIdx.x >> 5);
+    const int z0 = bzi * kCellZ;
+    t.z1 = min(t.nz, z0 + kCellZ);
+    const bool yv = t.iy < t.ny;
+    t.act = yv && t.ix < t.nx;
+    t.x = a.u32;
+    t.beta = __ldg(a.mf_beta);
+    t.px0 = t.ix > 0; t.px1 = t.ix < t.nx - 1; t.py0 = t.iy > 0; t.py1 = t.iy < t.ny - 1;
+#pragma unroll
+    for (int dy = -1; dy <= 1; dy++) t.lv[dy + 1] = yv && t.iy + dy >= 0 && t.iy + dy < t.ny;
+    // P[slot][line dy+1][dx+1]: three rotating plane slots; Ac[slot][ey][ex]
+    float P[3][3][3];
+    float Ac[2][2][2];
+    LineRaw NR[3];
+    LayerRaw NA;
+    // planes z0 - 1 -> slot 0, z0 -> slot 1; layer z0 - 1 -> slot 0
+#pragma unroll
+    for (int q = 0; q < 2; q++)
+    {
+        const int z = z0 - 1 + q;
+        const bool zv = z >= 0 && z < t.nz;
+#pragma unroll
+        for (int l = 0; l < 3; l++) cell_line_fetch(a, t.x, t.ix, t.iy + l - 1, z, t.lv[l] && zv, NR[l]);
+#pragma unroll
+        for (int l = 0; l < 3; l++) cell_line_finish(NR[l], P[q][l][0], P[q][l][1], P[q][l][2]);
+    }
+    cell_layer_fetch(a, t.ix, t.iy, z0 - 1, NA);
+    cell_layer_finish(NA, Ac[0]);
+    // node z0: u and mask from the raw center line of plane z0 (still in NR)
+    NodeNext nn;
+    nn.u = NR[1].xc;
+    nn.m = NR[1].mc;
+    nn.r = t.act ? a.r32[t.ix + t.nx * (t.iy + t.ny * z0)] : 0.f;
+#pragma unroll
+    for (int l = 0; l < 3; l++) cell_line_fetch(a, t.x, t.ix, t.iy + l - 1, z0 + 1, t.lv[l] && z0 + 1 < t.nz, NR[l]);
+    cell_layer_fetch(a, t.ix, t.iy, z0, NA);
+    float v[3] = {0.f, 0.f, 0.f};
+    for (int z = z0; z < t.z1; z += 6)
+    {
+        cell_step<0, 1, 2, 0, 1>(a, t, z, P, Ac, NR, NA, nn, v);
+        if (z + 1 >= t.z1) break;
+        cell_step<1, 2, 0, 1, 0>(a, t, z + 1, P, Ac, NR, NA, nn, v);
+        if (z + 2 >= t.z1) break;
+        cell_step<2, 0, 1, 0, 1>(a, t, z + 2, P, Ac, NR, NA, nn, v);
+        if (z + 3 >= t.z1) break;
+        cell_step<0, 1, 2, 1, 0>(a, t, z + 3, P, Ac, NR, NA, nn, v);
+        if (z + 4 >= t.z1) break;
+        cell_step<1, 2, 0, 0, 1>(a, t, z + 4, P, Ac, NR, NA, nn, v);
+        if (z + 5 >= t.z1) break;
+        cell_step<2, 0, 1, 1, 0>(a, t, z + 5, P, Ac, NR, NA, nn, v);
+    }
+    write_partials<3, float>(v, st->cg_ps);
+}
+
+int cell_spmv_grid(int nx, int ny, int nz)
+{
+    const CellGrid G = cell_grid(nx, ny, nz);
+    return G.bx * G.by * G.bz;
 }
 
 constexpr int kU32 = 8;  // elements per thread per step, loaded before use
@@ -546,6 +957,44 @@ void launch_mp_convert(const MixedArgs& a, const int32_t* row_len, const int8_t*
 
 int red_grid(int n);
 
+// fmt 2 operator: FP32 coefficients, mask, kept diagonals, Jacobi inverse.
+// bc_mode / bc_flag / bc_rows describe the Dirichlet set (nbc rows).
+void launch_mp_convert_cells(const MixedArgs& a, const double* coef, int64_t cells, float* alpha32, float* beta32,
+                             unsigned char* mask, float* dbc, const int32_t* diag_pos, const double* dinv64,
+                             float* d32, int bc_mode, const unsigned char* bc_flag, const int32_t* bc_rows, int nbc,
+                             cudaStream_t s)
+{
+    const int g = vec_grid(a.n);
+    k_mp_convert_cells<<<vec_grid((int)std::min<int64_t>(cells, 1 << 30)), kThreads, 0, s>>>(coef, cells, alpha32,
+                                                                                             beta32);
+    cudaMemsetAsync(mask, 0, (size_t)a.n, s);
+    if (nbc > 0)
+    {
+        if (bc_mode == OGS_DIRICHLET_SYMMETRIC)
+            k_mp_mask_symmetric<<<g, kThreads, 0, s>>>(bc_flag, mask, a.n);
+        else
+            k_mp_mask_rows<<<std::max(1, std::min(1024, (nbc + kThreads - 1) / kThreads)), kThreads, 0, s>>>(
+                bc_rows, nbc, mask);
+    }
+    k_mp_dbc<<<g, kThreads, 0, s>>>(a, diag_pos, dinv64, d32, dbc);
+}
+
+// enqueues the operator check; out (2 unsigned, device) is zeroed first
+void launch_mp_check(const MixedArgs& a, unsigned* out, cudaStream_t s)
+{
+    const int g = vec_grid(a.n);
+    cudaMemsetAsync(out, 0, 2 * sizeof(unsigned), s);
+    k_mp_check_fill<<<g, kThreads, 0, s>>>(a.w32, a.n);
+    switch (a.fmt == 0 ? a.n_up : a.fmt == 2 ? -1 : 0)
+    {
+        case 14: k_mp_check<14><<<g, kThreads, 0, s>>>(a, out); break;
+        case 8: k_mp_check<8><<<g, kThreads, 0, s>>>(a, out); break;
+        case 5: k_mp_check<5><<<g, kThreads, 0, s>>>(a, out); break;
+        case -1: k_mp_check<-1><<<g, kThreads, 0, s>>>(a, out); break;
+        default: k_mp_check<0><<<g, kThreads, 0, s>>>(a, out); break;
+    }
+}
+
 // grids of the FP32 CG kernels (the update/p kernels add this many SpMV
 // partials, the p kernel this many update partials)
 int mp_spmv_grid(int n)
@@ -587,11 +1036,12 @@ static int persist_grid_for(int n)
 
 int mp_persist_grid(const MixedArgs& a)
 {
-    switch (a.fmt == 0 ? a.n_up : 0)
+    switch (a.fmt == 0 ? a.n_up : a.fmt == 2 ? -1 : 0)
     {
         case 14: return persist_grid_for<14>(a.n);
         case 8: return persist_grid_for<8>(a.n);
         case 5: return persist_grid_for<5>(a.n);
+        case -1: return persist_grid_for<-1>(a.n);
         default: return persist_grid_for<0>(a.n);
     }
 }
@@ -608,11 +1058,12 @@ cudaError_t launch_mp_persist(const MixedArgs& a, int grid, int iters, cudaStrea
     at[0].val.cooperative = 1;
     lc.attrs = at;
     lc.numAttrs = 1;
-    switch (a.fmt == 0 ? a.n_up : 0)
+    switch (a.fmt == 0 ? a.n_up : a.fmt == 2 ? -1 : 0)
     {
         case 14: return cudaLaunchKernelEx(&lc, k_mp_persist<14>, a, iters);
         case 8: return cudaLaunchKernelEx(&lc, k_mp_persist<8>, a, iters);
         case 5: return cudaLaunchKernelEx(&lc, k_mp_persist<5>, a, iters);
+        case -1: return cudaLaunchKernelEx(&lc, k_mp_persist<-1>, a, iters);
         default: return cudaLaunchKernelEx(&lc, k_mp_persist<0>, a, iters);
     }
 }
@@ -621,11 +1072,14 @@ void launch_mp_iteration(const MixedArgs& a, cudaStream_t s, cudaEvent_t eb, cud
 {
     const int gs = mp_spmv_grid(a.n), gr = red_grid(a.n);
     if (eb) cudaEventRecordWithFlags(eb, s, cudaEventRecordExternal);
-    switch (a.fmt == 0 ? a.n_up : 0)
+    switch (a.fmt == 0 ? a.n_up : a.fmt == 2 ? -1 : 0)
     {
         case 14: k_mp_spmv<14><<<gs, kThreads, 0, s>>>(a); break;  // hex, 27-point
         case 8: k_mp_spmv<8><<<gs, kThreads, 0, s>>>(a); break;    // Kuhn tets, 15-point
         case 5: k_mp_spmv<5><<<gs, kThreads, 0, s>>>(a); break;    // quads, 9-point
+        case -1:  // hex lattice, cell coefficients
+            k_mp_spmv_cells<<<cell_spmv_grid(a.gx, a.gy, a.gz), 32 * kCellWarps, 0, s>>>(a);
+            break;
         default: k_mp_spmv<0><<<gs, kThreads, 0, s>>>(a); break;   // SELL-32 FP32
     }
     if (ee) cudaEventRecordWithFlags(ee, s, cudaEventRecordExternal);

@@ -297,7 +297,7 @@ extern "C" ogs_status ogs_gpu_server_add_class(ogs_server* S, const ogs_server_c
         // before slots on other streams read the field
         OGS_CUDA_TRY(cudaStreamSynchronize(cudaStreamLegacy));
     }
-    C.bytes = system_bytes(c->mesh, c->solver.precision == OGS_PRECISION_FP32_REFINED);
+    C.bytes = system_bytes(c->mesh, c->solver.precision != OGS_PRECISION_FP64);
     if (c->kind == OGS_REQUEST_TRANSPORT) C.bytes += (size_t)C.ne * C.ngp * 3 * sizeof(double);
     C.c.bc_rows = nullptr;
     C.c.bc_values = nullptr;

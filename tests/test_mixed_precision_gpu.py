@@ -29,11 +29,12 @@ def _deck(gpu, m, ek, left=10.0, right=0.0, steady=False):
     return eqs, x0
 
 
-def _both(gpu, eqs, x0, tol=1e-10):
+def _both(gpu, eqs, x0, tol=1e-10, precision=None):
     eqs.ConfigNumerics(gpu.LS_CG, gpu.PRECOND_JACOBI, 20000, tol, check_norm_rhs=False)
     x64 = x0.copy()
     it64 = eqs.Solver(x64)
-    eqs.ConfigNumerics(gpu.LS_CG, gpu.PRECOND_JACOBI, 20000, tol, precision=gpu.PRECISION_FP32_REFINED,
+    eqs.ConfigNumerics(gpu.LS_CG, gpu.PRECOND_JACOBI, 20000, tol,
+                       precision=gpu.PRECISION_FP32_REFINED if precision is None else precision,
                        check_norm_rhs=False)
     x32 = x0.copy()
     it32 = eqs.Solver(x32)
@@ -170,3 +171,78 @@ def test_fp32_no_fallback_when_cycles_gain(gpu):
     x64, it64, x32, it32, st = _both(gpu, eqs, x0)
     assert st["status"] == gpu.OK and st["fp64_fallback"] == 0
     assert rel_max_err(x32, x64) < MIXED_RTOL
+
+
+def _solve_pair(gpu, eqs, x0, tol=1e-10):
+    x64, _, x32, _, st = _both(gpu, eqs, x0, tol, precision=gpu.PRECISION_FP32_CELLS)
+    assert st["status"] == gpu.OK and st["rel_residual"] < tol
+    assert rel_max_err(x32, x64) < MIXED_RTOL
+    return st
+
+
+def _hex_system(gpu, m, ek, params, mode, repeat=1, reassemble_after_bc=False, gauss=3):
+    eqs = gpu.LinearEQS(gpu.GpuMesh(m, gauss_points=gauss))
+    eqs.Initialize()
+    for _ in range(repeat):
+        eqs.GlobalAssembly(params, ek, np.zeros(m.n_nodes))
+    lf, rf = m.face_nodes(0, 0), m.face_nodes(0, 1)
+    rows = np.concatenate([lf, rf])
+    vals = np.concatenate([np.full(len(lf), 10.0), np.full(len(rf), 2.0)])
+    eqs.SetKnownX(rows, vals, mode)
+    if reassemble_after_bc:
+        eqs.GlobalAssembly(params, ek, np.zeros(m.n_nodes))
+    x0 = np.zeros(m.n_nodes)
+    x0[lf] = 10.0
+    return eqs, x0
+
+
+@pytest.mark.parametrize("case", ["symmetric", "row_only", "twice", "liquid_gravity", "steady", "spacing"])
+def test_cell_coefficient_operator(gpu, case):
+    """PRECISION_FP32_CELLS on a regular hex lattice: the FP32 inner CG
+    applies the operator from one coefficient per cell (fp32_operator 2);
+    heads within 1e-8 of the FP64 path for symmetric and row-only Dirichlet
+    sets, two assemblies summed, LIQUID_FLOW with gravity, steady flow and
+    anisotropic spacing.  PRECISION_FP32_REFINED keeps the stored diagonal
+    operator (fp32_operator 0) on the same system."""
+    m = M.structured_hex(30, 22, 14, *((2.0, 0.5, 0.75) if case == "spacing" else (1.0, 1.0, 1.0)))
+    ek = fields.lognormal_k(m.shape, np.log(1e-5), 1.0, 4.0, seed=9)
+    if case == "liquid_gravity":
+        p = gpu.make_params(gpu.LIQUID_FLOW, dt=3600.0, storage=1e-4, porosity=0.2, drho_dp=1e-7,
+                            viscosity=1e-3, density=1000.0, gravity=9.81, gravity_on=1)
+        ek = ek * 1e-7
+    else:
+        p = gpu.make_params(gpu.GROUNDWATER_FLOW, dt=3600.0, storage=1e-4, steady=1 if case == "steady" else 0)
+    mode = gpu.DIRICHLET_ROW_ONLY if case == "row_only" else gpu.DIRICHLET_SYMMETRIC
+    eqs, x0 = _hex_system(gpu, m, ek, p, mode, repeat=2 if case == "twice" else 1)
+    st = _solve_pair(gpu, eqs, x0)
+    assert st["fp32_operator"] == 2
+    # the stored FP32 operator: upper-half diagonal offsets for symmetric
+    # matrices, SELL-32 once row-only Dirichlet rows break the symmetry
+    x64, _, x32, _, st = _both(gpu, eqs, x0)
+    assert st["fp32_operator"] == (1 if case == "row_only" else 0)
+    assert rel_max_err(x32, x64) < MIXED_RTOL
+
+
+@pytest.mark.parametrize("case", ["lumping", "one_gauss_point", "reassembled_after_bc", "stretched"])
+def test_cell_coefficient_operator_falls_back(gpu, case):
+    """Matrices without the cell-coefficient form keep the stored FP32
+    operator: mass lumping, one Gauss point (under-integrated Laplace), an
+    assembly added after the Dirichlet elimination (caught by the check of
+    the FP32 operator against the FP64 matrix), a non-uniform lattice."""
+    if case == "stretched":
+        m = M.structured_hex(20, 12, 8)
+        m.x = m.x ** 1.1  # graded in x
+    else:
+        m = M.structured_hex(20, 12, 8)
+    ek = fields.lognormal_k(m.shape, np.log(1e-5), 1.0, 4.0, seed=2)
+    p = gpu.make_params(gpu.GROUNDWATER_FLOW, dt=3600.0, storage=1e-4, mass_lumping=1 if case == "lumping" else 0)
+    eqs, x0 = _hex_system(gpu, m, ek, p, gpu.DIRICHLET_SYMMETRIC,
+                          reassemble_after_bc=case == "reassembled_after_bc",
+                          gauss=1 if case == "one_gauss_point" else 3)
+    x64, _, x32, _, st = _both(gpu, eqs, x0, precision=gpu.PRECISION_FP32_CELLS)
+    assert st["status"] == gpu.OK and st["fp32_operator"] == 0 and st["rel_residual"] < 1e-10
+    if case != "one_gauss_point":  # hourglass modes: heads as ill-conditioned as the system
+        assert rel_max_err(x32, x64) < MIXED_RTOL
+    eqs.ConfigNumerics(gpu.LS_CG, gpu.PRECOND_JACOBI, 20000, 1e-10, check_norm_rhs=False)
+    eqs.Solver(x0.copy())
+    assert eqs.stats()["fp32_operator"] == -1
