@@ -44,6 +44,10 @@ struct KState
     // grid barrier of the persistent FP32 CG kernel (reset with the header)
     unsigned int bar_count, bar_gen;
     int bar_err, pad5;
+    // FP32 CG: the last block of the product adds the block partials into
+    // r.u, w.u, r.r for the update kernel (reset with the header)
+    unsigned int mp_ticket, pad6;
+    double mp_g[3];
     unsigned int ticket[8];
     double part[8][2 * kMaxBlocks];
     double cg_ps[3 * kMaxBlocks];        // per SpMV block: p . s (FP64 CG); r.u, w.u, r.r (FP32 CG)

@@ -391,8 +391,22 @@ __global__ void __launch_bounds__(kThreads) k_mp_restart(MixedArgs a)
 }
 
 // ------------------------------------------------------------------
-// FP32 CG iteration (Chronopoulos-Gear, ticket-free, see krylov.cuh)
+// FP32 CG iteration (Chronopoulos-Gear)
 // ------------------------------------------------------------------
+// r.u, w.u, r.r of the product: block partials, added by the last block
+// (fixed order, see grid_sum) into st->mp_g for the update kernel, which
+// then streams without a reduction prologue
+__device__ __forceinline__ void mp_sum_products(const float (&v)[3], KState* st)
+{
+    double g[3];
+    if (grid_sum<3, float>(v, g, st->cg_ps, &st->mp_ticket) && threadIdx.x == 0)
+    {
+        st->mp_g[0] = g[0];
+        st->mp_g[1] = g[1];
+        st->mp_g[2] = g[2];
+    }
+}
+
 // S: iter += 1 ; w32 = A32 u32 ; partials of r.u, w.u, r.r
 template <int NU>
 __global__ void __launch_bounds__(kThreads, 3) k_mp_spmv(MixedArgs a)
@@ -410,7 +424,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_mp_spmv(MixedArgs a)
         v[1] += w * u;
         v[2] += r * r;
     }
-    write_partials<3, float>(v, st->cg_ps);
+    mp_sum_products(v, st);
 }
 
 // fmt 2 product on the lattice: blocks of 4 warps, a warp holds 32
@@ -674,7 +688,7 @@ __global__ void __launch_bounds__(32 * kCellWarps) k_mp_spmv_cells(MixedArgs a)
         if (z + 5 >= t.z1) break;
         cell_step<2, 0, 1, 1, 0>(a, t, z + 5, P, Ac, NR, NA, nn, v);
     }
-    write_partials<3, float>(v, st->cg_ps);
+    mp_sum_products(v, st);
 }
 
 int cell_spmv_grid(int nx, int ny, int nz)
@@ -691,9 +705,7 @@ __global__ void __launch_bounds__(kThreads) k_mp_update(MixedArgs a)
     KState* st = a.st;
     if (st->done || st->replace) return;
     const int it = st->iter;
-    double g[3];
-    reduce_partials<3>(st->cg_ps, st->nb_spmv, g);
-    const double gamma = g[0], delta = g[1], rn = sqrt(g[2]);
+    const double gamma = st->mp_g[0], delta = st->mp_g[1], rn = sqrt(st->mp_g[2]);
     const bool first = it == 1;                  // no search direction yet: beta = 0
     const bool fresh = it == st->base_iter + 1;  // first iteration after a (re)start
     const double rmax = fresh ? rn : st->rmax;
@@ -1070,7 +1082,7 @@ cudaError_t launch_mp_persist(const MixedArgs& a, int grid, int iters, cudaStrea
 
 void launch_mp_iteration(const MixedArgs& a, cudaStream_t s, cudaEvent_t eb, cudaEvent_t ee)
 {
-    const int gs = mp_spmv_grid(a.n), gr = red_grid(a.n);
+    const int gs = mp_spmv_grid(a.n);
     if (eb) cudaEventRecordWithFlags(eb, s, cudaEventRecordExternal);
     switch (a.fmt == 0 ? a.n_up : a.fmt == 2 ? -1 : 0)
     {
@@ -1083,7 +1095,7 @@ void launch_mp_iteration(const MixedArgs& a, cudaStream_t s, cudaEvent_t eb, cud
         default: k_mp_spmv<0><<<gs, kThreads, 0, s>>>(a); break;   // SELL-32 FP32
     }
     if (ee) cudaEventRecordWithFlags(ee, s, cudaEventRecordExternal);
-    k_mp_update<<<gr, kThreads, 0, s>>>(a);
+    k_mp_update<<<red_grid(a.n), kThreads, 0, s>>>(a);
 }
 
 }  // namespace ogs
