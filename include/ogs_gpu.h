@@ -55,7 +55,8 @@ typedef enum
 {
     OGS_PCS_GROUNDWATER_FLOW = 0,
     OGS_PCS_LIQUID_FLOW = 1,
-    OGS_PCS_MASS_TRANSPORT = 2
+    OGS_PCS_MASS_TRANSPORT = 2,
+    OGS_PCS_RICHARDS_FLOW = 3  /* through ogs_gpu_assemble_richards only */
 } ogs_pcs_type;
 
 /* Dirichlet treatment.  ROW_ONLY is CSparseMatrix::Diagonize of the SP
@@ -249,6 +250,74 @@ ogs_status ogs_gpu_system_destroy(ogs_system* sys);
 
 /* Linear_EQS::ConfigNumerics (FEM/equation_class.cpp:191-318). */
 ogs_status ogs_gpu_configure(ogs_system* sys, const ogs_solver_config* cfg);
+
+/* ---- RICHARDS_FLOW -------------------------------------------------------
+ * Material curves of the unsaturated medium (CMediumProperties, the $MMP
+ * keywords $CAPILLARY_PRESSURE and $PERMEABILITY_SATURATION). */
+typedef struct
+{
+    int32_t capillary_model;   /* capillary_pressure_model: 4 van Genuchten,
+                                  6 Brooks-Corey                               */
+    int32_t permeability_model;/* permeability_saturation_model[0]: 4 van
+                                  Genuchten-Mualem, 6 Brooks-Corey             */
+    double pb;                 /* capillary_pressure_values[0]: entry pressure */
+    double slr, slm;           /* capillary_pressure_values[1], [2]: residual and
+                                  maximum saturation of the pressure curve    */
+    double m;                  /* capillary_pressure_values[3]: exponent      */
+    double kr_slr, kr_slm;     /* residual_saturation[0], maximum_saturation[0] */
+    double kr_m;               /* saturation_exponent[0]                      */
+    double kr_min;             /* minimum_relative_permeability               */
+} ogs_richards_params;
+
+/* One RICHARDS_FLOW assembly (fem_ele_std.cpp:9470-9481:
+ * AssembleParabolicEquation + Assemble_Gravity) with the storage and
+ * conductivity of the iterate p_iter at every Gauss point (CalCoefMass
+ * :1721-1770, CalCoefLaplace :2614-2640, saturation curves
+ * rf_mmp_new.cpp:5243-5520 and 2490-2640), added to A and b:
+ *   A += M(p_iter) / dt + relax0 L(p_iter)
+ *   b += (M(p_iter) / dt - relax1 L(p_iter)) p_old + gravity(p_iter).
+ * p uses pcs_type OGS_PCS_RICHARDS_FLOW, dt, nls_relaxation,
+ * time_unit_factor, storage, porosity, drho_dp, viscosity, density, gravity,
+ * gravity_on, mass_lumping (the lumped storage taken at the element centre,
+ * CalcLumpedMass).  elem_k: intrinsic permeability per element. */
+ogs_status ogs_gpu_assemble_richards(ogs_system* sys, const ogs_assembly_params* p, const ogs_richards_params* r,
+                                     const double* elem_k, const double* p_old, const double* p_iter);
+
+/* $NON_LINEAR_ITERATIONS of a Picard process (CNumerics). */
+typedef struct
+{
+    int32_t error_method;      /* FiniteElement::ErrorMethod: 1 LMAX, 2 ENORM,
+                                  3 EVNORM, 4 ERNORM                           */
+    int32_t max_iterations;    /* nls_max_iterations                          */
+    double tolerance;          /* nls_error_tolerance[0]                      */
+} ogs_picard_config;
+
+typedef struct
+{
+    int32_t iterations;        /* Picard iterations run                       */
+    int32_t converged;         /* error / tolerance <= 1 reached              */
+    int32_t diverged;          /* two iterations in a row gained < 1 %        */
+    int32_t linear_iterations; /* Krylov iterations, all Picard iterations    */
+    double error;              /* last error / tolerance                       */
+    double solve_ms;           /* device time of the whole step               */
+} ogs_picard_stats;
+
+/* One time step of RICHARDS_FLOW by Picard iteration: the loop of
+ * CRFProcess::ExecuteNonLinear with nls_method PICARD (rf_pcs.cpp:9636-9960)
+ * around CRFProcess::Execute (:4695-5080).  Each iteration: A = 0, b = 0,
+ * ogs_gpu_assemble_richards at the iterate, the Dirichlet set (mode as
+ * ogs_gpu_set_dirichlet), the configured linear solve from the iterate,
+ * the error of CalcIterationNODError (:9170-9600) divided by the
+ * tolerance, and the update iterate = (1 - theta) iterate + theta x with
+ * theta = 1 - nls_relaxation (1 once converged).  Stops when the error is
+ * <= 1, after two iterations that each lowered it by less than 1 %, or after
+ * max_iterations.  p_iter: the first iterate in, the last one out (host or
+ * device, n_nodes doubles).  Returns OGS_NOT_CONVERGED when the loop ended
+ * unconverged. */
+ogs_status ogs_gpu_richards_step(ogs_system* sys, const ogs_assembly_params* p, const ogs_richards_params* r,
+                                 const double* elem_k, const double* p_old, double* p_iter,
+                                 const int64_t* bc_rows, const double* bc_values, int64_t n_bc, int32_t bc_mode,
+                                 const ogs_picard_config* nls, ogs_picard_stats* stats);
 
 /* Forgets the transport operators stored under memory_type > 0, so that the
  * next such assembly computes and stores them again: the reference's first

@@ -50,10 +50,12 @@ EXPORTS = [
     "ogs_gpu_solve_begin", "ogs_gpu_solve_poll", "ogs_gpu_solve_end",
     "ogs_gpu_server_create", "ogs_gpu_server_destroy", "ogs_gpu_server_add_class", "ogs_gpu_server_submit",
     "ogs_gpu_server_progress", "ogs_gpu_server_result", "ogs_gpu_server_info", "ogs_gpu_server_reserve",
-    "ogs_gpu_cache_reset",
+    "ogs_gpu_cache_reset", "ogs_gpu_assemble_richards", "ogs_gpu_richards_step",
     "ogs_deck_read", "ogs_deck_destroy", "ogs_deck_mesh", "ogs_deck_geo_nodes", "ogs_deck_dirichlet",
 ]
 REQUEST_FLOW, REQUEST_TRANSPORT = 0, 1
+RICHARDS_FLOW = 3
+LMAX, ENORM, EVNORM, ERNORM = 1, 2, 3, 4
 SERVER_PRIORITY, SERVER_SJF = 1, 2
 NOALLOC_MAX_ROWS = 524288
 
@@ -141,6 +143,32 @@ class ServerResult(C.Structure):
 class ServerInfo(C.Structure):
     _fields_ = [("slots", C.c_int32), ("running", C.c_int32), ("queued", C.c_int32), ("pad0", C.c_int32),
                 ("completed", C.c_int64), ("bytes_used", C.c_int64), ("bytes_budget", C.c_int64)]
+
+
+class RichardsParams(C.Structure):
+    _fields_ = [("capillary_model", C.c_int32), ("permeability_model", C.c_int32), ("pb", C.c_double),
+                ("slr", C.c_double), ("slm", C.c_double), ("m", C.c_double), ("kr_slr", C.c_double),
+                ("kr_slm", C.c_double), ("kr_m", C.c_double), ("kr_min", C.c_double)]
+
+
+class PicardConfig(C.Structure):
+    _fields_ = [("error_method", C.c_int32), ("max_iterations", C.c_int32), ("tolerance", C.c_double)]
+
+
+class PicardStats(C.Structure):
+    _fields_ = [("iterations", C.c_int32), ("converged", C.c_int32), ("diverged", C.c_int32),
+                ("linear_iterations", C.c_int32), ("error", C.c_double), ("solve_ms", C.c_double)]
+
+
+def richards_params(**kw) -> RichardsParams:
+    """ogs_richards_params; defaults: van Genuchten curves, pb 1e4 Pa,
+    residual 0.1, maximum 1, exponent 0.5, minimum k_rel 1e-9."""
+    r = RichardsParams(4, 4, 1.0e4, 0.1, 1.0, 0.5, 0.1, 1.0, 0.5, 1e-9)
+    for k, v in kw.items():
+        if not hasattr(r, k):
+            raise AttributeError(k)
+        setattr(r, k, v)
+    return r
 
 
 def make_params(pcs_type=GROUNDWATER_FLOW, **kw) -> AssemblyParams:
@@ -234,6 +262,13 @@ def lib():
             getattr(L, name).restype = st
         L.ogs_gpu_cache_reset.argtypes = [vp]
         L.ogs_gpu_cache_reset.restype = st
+        L.ogs_gpu_assemble_richards.argtypes = [vp, C.POINTER(AssemblyParams), C.POINTER(RichardsParams), vp, vp,
+                                                vp]
+        L.ogs_gpu_assemble_richards.restype = st
+        L.ogs_gpu_richards_step.argtypes = [vp, C.POINTER(AssemblyParams), C.POINTER(RichardsParams), vp, vp, vp,
+                                            vp, vp, C.c_int64, C.c_int32, C.POINTER(PicardConfig),
+                                            C.POINTER(PicardStats)]
+        L.ogs_gpu_richards_step.restype = st
         cp = C.c_char_p
         i64p = C.POINTER(C.c_int64)
         L.ogs_deck_read.argtypes = [cp, cp, cp, C.POINTER(vp)]
@@ -360,6 +395,29 @@ class LinearEQS:
     def GlobalAssembly(self, params: AssemblyParams, elem_k=None, u0=None, gp_velocity=None):
         ek, u, gv = _f64(elem_k), _f64(u0), _f64(gp_velocity)
         _check(lib().ogs_gpu_assemble(self.h, C.byref(params), _ptr(ek), _ptr(u), _ptr(gv)))
+
+    # RICHARDS_FLOW: AssembleParabolicEquation + Assemble_Gravity at the iterate
+    def AssembleRichards(self, params: AssemblyParams, r: RichardsParams, elem_k, p_old, p_iter):
+        ek, po, pi = _f64(elem_k), _f64(p_old), _f64(p_iter)
+        _check(lib().ogs_gpu_assemble_richards(self.h, C.byref(params), C.byref(r), _ptr(ek), _ptr(po), _ptr(pi)))
+
+    # one RICHARDS_FLOW time step by Picard iteration (ExecuteNonLinear);
+    # p_iter (numpy float64 or device tensor) is updated in place
+    def RichardsStep(self, params: AssemblyParams, r: RichardsParams, elem_k, p_old, p_iter, rows, values,
+                     mode=DIRICHLET_SYMMETRIC, error_method=ENORM, max_iterations=20, tolerance=1e-6,
+                     allow_fail=False) -> dict:
+        ek, po = _f64(elem_k), _f64(p_old)
+        rr = rows if hasattr(rows, "data_ptr") else np.ascontiguousarray(rows, dtype=np.int64)
+        vv = _f64(values)
+        cfg = PicardConfig(error_method, max_iterations, tolerance)
+        stt = PicardStats()
+        status = lib().ogs_gpu_richards_step(self.h, C.byref(params), C.byref(r), _ptr(ek), _ptr(po), _ptr(p_iter),
+                                             _ptr(rr), _ptr(vv), len(rr), mode, C.byref(cfg), C.byref(stt))
+        if not allow_fail:
+            _check(status)
+        return {"status": status, "iterations": stt.iterations, "converged": bool(stt.converged),
+                "diverged": bool(stt.diverged), "linear_iterations": stt.linear_iterations, "error": stt.error,
+                "solve_ms": stt.solve_ms}
 
     # forget the transport operators stored under memory_type > 0 (the
     # reference's first time step recomputes them)

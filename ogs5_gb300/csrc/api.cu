@@ -209,7 +209,10 @@ struct ogs_system
     bool op_valid = false;
     int* d_ilu_bad = nullptr;
     double *ek = nullptr, *u0 = nullptr, *gpv = nullptr, *qbuf = nullptr, *vec_in = nullptr,
-           *vec_out = nullptr;
+           *vec_out = nullptr, *u1 = nullptr;
+    // RICHARDS_FLOW Picard step: iterate, solution, old level, reductions
+    double *rich_it = nullptr, *rich_x = nullptr, *rich_old = nullptr, *rich_red = nullptr;
+    double* h_rich = nullptr;  // pinned: sum d^2, sum it^2, max |d|
     KState* st = nullptr;
     KState* h_st = nullptr;   // pinned header copy
     int* d_bad = nullptr;
@@ -392,6 +395,12 @@ extern "C" ogs_status ogs_gpu_system_destroy(ogs_system* s)
     cudaFree(s->op_mass);
     cudaFree(s->op_k);
     cudaFree(s->mf_coef);
+    cudaFree(s->u1);
+    cudaFree(s->rich_it);
+    cudaFree(s->rich_x);
+    cudaFree(s->rich_old);
+    cudaFree(s->rich_red);
+    if (s->h_rich) cudaFreeHost(s->h_rich);
     cudaFree(s->d_check);
     if (s->h_check) cudaFreeHost(s->h_check);
     cudaFree(s->d_ilu_bad);
@@ -535,7 +544,13 @@ extern "C" ogs_status ogs_gpu_initialize(ogs_system* s)
 static ogs_status check_params(const ogs_assembly_params* p)
 {
     if (!p) { set_error("assemble: NULL params"); return OGS_BAD_ARG; }
-    if (p->pcs_type < 0 || p->pcs_type > 2) { set_error("assemble: bad pcs_type %d", p->pcs_type); return OGS_BAD_ARG; }
+    if (p->pcs_type < 0 || p->pcs_type > 2)
+    {
+        set_error(p->pcs_type == OGS_PCS_RICHARDS_FLOW ? "assemble: RICHARDS_FLOW goes through ogs_gpu_assemble_richards"
+                                                       : "assemble: bad pcs_type %d",
+                  p->pcs_type);
+        return OGS_BAD_ARG;
+    }
     if (!(p->dt > 0.0)) { set_error("assemble: dt must be > 0"); return OGS_BAD_ARG; }
     if (!(p->time_unit_factor != 0.0)) { set_error("assemble: time_unit_factor must be non-zero"); return OGS_BAD_ARG; }
     return OGS_OK;
@@ -550,7 +565,8 @@ constexpr int kNoBadElement = 0x7fffffff;
 // the stream has passed this point.
 static ogs_status enqueue_element_kernel(ogs_system* s, const ogs_assembly_params* p, const double* elem_k,
                                          const double* u0, const double* gpv, int kind, double* q_out,
-                                         double* val = nullptr, double* val2 = nullptr)
+                                         double* val = nullptr, double* val2 = nullptr,
+                                         const double* u1 = nullptr, const ogs_richards_params* rp = nullptr)
 {
     ogs_mesh* m = s->m;
     AsmArgs a;
@@ -571,6 +587,8 @@ static ogs_status enqueue_element_kernel(ogs_system* s, const ogs_assembly_param
     if ((st = stage_in(s, elem_k, m->n_elem, &s->ek, &a.elem_k))) return st;
     if ((st = stage_in(s, u0, m->n_nodes, &s->u0, &a.u0))) return st;
     if ((st = stage_in(s, gpv, (size_t)m->n_elem * m->ngp * 3, &s->gpv, &a.gpv))) return st;
+    if ((st = stage_in(s, u1, m->n_nodes, &s->u1, &a.u1))) return st;
+    if (rp) a.r = *rp;
     k_set_int<<<1, 1, 0, s->stream>>>(s->d_bad, kNoBadElement);
     OGS_LAUNCH_CHECK();
     if (!launch_assembly(m, a, m->affine, kind, s->stream))
@@ -595,6 +613,7 @@ static ogs_status enqueue_element_kernel(ogs_system* s, const ogs_assembly_param
         s->mf_state = 0;
         s->symmetric = false;  // advection
     }
+    if (kind == 3) s->mf_state = 0;  // coefficients vary inside the cells
     OGS_CUDA_TRY(cudaMemcpyAsync(s->h_bad, s->d_bad, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
     return OGS_OK;
 }
@@ -665,6 +684,178 @@ extern "C" ogs_status ogs_gpu_cache_reset(ogs_system* s)
 {
     if (!s) { set_error("cache_reset: NULL system"); return OGS_BAD_ARG; }
     s->op_valid = false;
+    return OGS_OK;
+}
+
+// ------------------------------------------------------------------
+// RICHARDS_FLOW
+// ------------------------------------------------------------------
+static ogs_status dirichlet_upload(ogs_system* s, const int64_t* rows, const double* values, int64_t n_rows,
+                                   int32_t mode);
+static ogs_status dirichlet_apply(ogs_system* s);
+
+static ogs_status check_richards(const ogs_assembly_params* p, const ogs_richards_params* r)
+{
+    if (!p || !r) { set_error("richards: NULL params"); return OGS_BAD_ARG; }
+    if (p->pcs_type != OGS_PCS_RICHARDS_FLOW) { set_error("richards: pcs_type must be OGS_PCS_RICHARDS_FLOW"); return OGS_BAD_ARG; }
+    if (!(p->dt > 0.0) || !(p->time_unit_factor != 0.0) || !(p->viscosity > 0.0))
+    {
+        set_error("richards: dt, time_unit_factor and viscosity must be set (> 0)");
+        return OGS_BAD_ARG;
+    }
+    if ((r->capillary_model != 4 && r->capillary_model != 6) || (r->permeability_model != 4 && r->permeability_model != 6))
+    {
+        set_error("richards: capillary model %d / permeability model %d not supported (4 van Genuchten, 6 Brooks-Corey)",
+                  r->capillary_model, r->permeability_model);
+        return OGS_BAD_ARG;
+    }
+    const bool vg_ok = r->capillary_model != 4 || (r->m > 0.0 && r->m < 1.0);
+    const bool kr_ok = r->permeability_model != 4 || (r->kr_m > 0.0 && r->kr_m <= 1.0);
+    if (!(r->pb > 0.0) || !(r->slm > r->slr) || !(r->m > 0.0) || !vg_ok || !(r->kr_slm > r->kr_slr) ||
+        !(r->kr_m > 0.0) || !kr_ok)
+    {
+        set_error("richards: bad curve parameters (pb > 0, slm > slr, van Genuchten 0 < m < 1)");
+        return OGS_BAD_ARG;
+    }
+    return OGS_OK;
+}
+
+extern "C" ogs_status ogs_gpu_assemble_richards(ogs_system* s, const ogs_assembly_params* p, const ogs_richards_params* r,
+                                                const double* elem_k, const double* p_old, const double* p_iter)
+{
+    if (!s || !elem_k || !p_iter) { set_error("assemble_richards: NULL argument"); return OGS_BAD_ARG; }
+    ogs_status st = check_richards(p, r);
+    if (st) return st;
+    if ((st = enqueue_element_kernel(s, p, elem_k, p_old, nullptr, 3, nullptr, nullptr, nullptr, p_iter, r))) return st;
+    OGS_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    return element_flag_status(s);
+}
+
+// sum (it - x)^2, sum it^2 (grid_sum, fixed order) and max |it - x| of a
+// Picard iteration; out[0..2]
+__global__ void k_picard_error(const double* __restrict__ it, const double* __restrict__ x, int n, double* part,
+                               unsigned* ticket, double* out)
+{
+    double v[2] = {0.0, 0.0}, mx = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    {
+        const double d = it[i] - x[i];
+        v[0] += d * d;
+        v[1] += it[i] * it[i];
+        mx = fmax(mx, fabs(d));
+    }
+    atomicMax((unsigned long long*)(out + 2), (unsigned long long)__double_as_longlong(mx));
+    double o[2];
+    if (grid_sum<2, double>(v, o, part, ticket) && threadIdx.x == 0)
+    {
+        out[0] = o[0];
+        out[1] = o[1];
+    }
+}
+
+// iterate = (1 - theta) iterate + theta x  (the new value itself for theta 1)
+__global__ void k_picard_update(double* it, const double* __restrict__ x, int n, double theta)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        it[i] = theta == 1.0 ? x[i] : (1.0 - theta) * it[i] + theta * x[i];
+}
+
+extern "C" ogs_status ogs_gpu_richards_step(ogs_system* s, const ogs_assembly_params* p, const ogs_richards_params* r,
+                                            const double* elem_k, const double* p_old, double* p_iter,
+                                            const int64_t* bc_rows, const double* bc_values, int64_t n_bc,
+                                            int32_t bc_mode, const ogs_picard_config* nls, ogs_picard_stats* stats)
+{
+    if (!s || !elem_k || !p_old || !p_iter || !nls) { set_error("richards_step: NULL argument"); return OGS_BAD_ARG; }
+    ogs_status st = check_richards(p, r);
+    if (st) return st;
+    if (nls->error_method < 1 || nls->error_method > 4 || nls->max_iterations < 1 || !(nls->tolerance > 0.0))
+    {
+        set_error("richards_step: error_method 1..4 (LMAX, ENORM, EVNORM, ERNORM), max_iterations >= 1, tolerance > 0");
+        return OGS_BAD_ARG;
+    }
+    const int n = s->n;
+    const size_t nb = (size_t)n * sizeof(double);
+    if (!s->rich_it)
+    {
+        OGS_CUDA_TRY(cudaMalloc(&s->rich_it, nb));
+        OGS_CUDA_TRY(cudaMalloc(&s->rich_x, nb));
+        OGS_CUDA_TRY(cudaMalloc(&s->rich_old, nb));
+        OGS_CUDA_TRY(cudaMalloc(&s->rich_red, (2 * kMaxBlocks + 4) * sizeof(double)));
+        OGS_CUDA_TRY(cudaMemset(s->rich_red, 0, (2 * kMaxBlocks + 4) * sizeof(double)));
+        OGS_CUDA_TRY(cudaMallocHost(&s->h_rich, 3 * sizeof(double)));
+    }
+    OGS_CUDA_TRY(cudaMemcpyAsync(s->rich_it, p_iter, nb, cudaMemcpyDefault, s->stream));
+    OGS_CUDA_TRY(cudaMemcpyAsync(s->rich_old, p_old, nb, cudaMemcpyDefault, s->stream));
+    if ((st = dirichlet_upload(s, bc_rows, bc_values, n_bc, bc_mode))) return st;
+    double* red = s->rich_red;
+    unsigned* ticket = (unsigned*)(red + 2 * kMaxBlocks + 3);
+    OGS_CUDA_TRY(cudaEventRecord(s->ev0, s->stream));
+    double theta0 = 1.0 - p->nls_relaxation;  // nl_theta (rf_pcs.cpp:9652)
+    if (theta0 < DBL_EPSILON) theta0 = 1.0;
+    ogs_picard_stats out{};
+    double last = 1.0;
+    int fails = 0;
+    for (int it = 0; it < nls->max_iterations; it++)
+    {
+        // CRFProcess::Execute: assembly at the iterate, conditions, solve
+        if ((st = ogs_gpu_initialize(s))) return st;
+        if ((st = enqueue_element_kernel(s, p, elem_k, s->rich_old, nullptr, 3, nullptr, nullptr, nullptr,
+                                         s->rich_it, r)))
+            return st;
+        if ((st = dirichlet_apply(s))) return st;
+        OGS_CUDA_TRY(cudaMemcpyAsync(s->rich_x, s->rich_it, nb, cudaMemcpyDeviceToDevice, s->stream));
+        OGS_CUDA_TRY(cudaStreamSynchronize(s->stream));
+        if ((st = element_flag_status(s))) return st;
+        ogs_solve_stats ls{};
+        st = ogs_gpu_solve(s, s->rich_x, &ls);
+        out.linear_iterations += ls.iterations;
+        if (st != OGS_OK && st != OGS_NOT_CONVERGED) return st;
+        // CalcIterationNODError (PICARD branch): iterate against the solution
+        OGS_CUDA_TRY(cudaMemsetAsync(red + 2 * kMaxBlocks, 0, 3 * sizeof(double), s->stream));
+        k_picard_error<<<red_grid(n), 256, 0, s->stream>>>(s->rich_it, s->rich_x, n, red, ticket, red + 2 * kMaxBlocks);
+        OGS_LAUNCH_CHECK();
+        OGS_CUDA_TRY(cudaMemcpyAsync(s->h_rich, red + 2 * kMaxBlocks, 3 * sizeof(double), cudaMemcpyDeviceToHost,
+                                     s->stream));
+        OGS_CUDA_TRY(cudaStreamSynchronize(s->stream));
+        const double* h = s->h_rich;
+        double abs_err;
+        if (nls->error_method == 1) abs_err = h[2];                                     // LMAX
+        else if (nls->error_method == 4) abs_err = sqrt(h[0]) / (sqrt(h[1]) + DBL_EPSILON);  // ERNORM
+        else abs_err = sqrt(h[0]);                                                      // ENORM, EVNORM
+        const double err = abs_err / nls->tolerance;
+        const double theta = err < 1.0 ? 1.0 : theta0;
+        k_picard_update<<<vec_grid(n), 256, 0, s->stream>>>(s->rich_it, s->rich_x, n, theta);
+        OGS_LAUNCH_CHECK();
+        out.iterations = it + 1;
+        out.error = err;
+        // ExecuteNonLinear, default error branch (rf_pcs.cpp:9735-9760)
+        if (err <= 1.0)
+        {
+            out.converged = 1;
+            break;
+        }
+        const double percent = 100.0 * ((last - err) / last);
+        fails = (it > 0 && percent < 1.0) ? fails + 1 : 0;
+        last = err;
+        if (fails > 1)
+        {
+            out.diverged = 1;
+            break;
+        }
+    }
+    OGS_CUDA_TRY(cudaEventRecord(s->ev1, s->stream));
+    OGS_CUDA_TRY(cudaMemcpyAsync(p_iter, s->rich_it, nb, cudaMemcpyDefault, s->stream));
+    OGS_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, s->ev0, s->ev1);
+    out.solve_ms = ms;
+    if (stats) *stats = out;
+    if (!out.converged)
+    {
+        set_error("richards_step: Picard iteration %s after %d iterations (error/tolerance %.3e)",
+                  out.diverged ? "stagnated" : "did not converge", out.iterations, out.error);
+        return OGS_NOT_CONVERGED;
+    }
     return OGS_OK;
 }
 

@@ -388,7 +388,7 @@ __device__ __forceinline__ void flow_combine(const AsmArgs& a, int64_t e, const 
             S[i * NN + j] = m * dt_inverse + lp * relax0;
             r[i] += (m * dt_inverse - lp * relax1) * U[j];
         }
-    if (a.p.pcs_type == OGS_PCS_LIQUID_FLOW && a.p.gravity_on)
+    if ((a.p.pcs_type == OGS_PCS_LIQUID_FLOW || a.p.pcs_type == OGS_PCS_RICHARDS_FLOW) && a.p.gravity_on)
 #pragma unroll
         for (int i = 0; i < NN; i++) r[i] += grav[i];
     scatter<NN>(a, e, nd, S, r);
@@ -815,6 +815,177 @@ __global__ void __launch_bounds__(128) k_gp_velocity(AsmArgs a)
     }
 }
 
+// ------------------------------------------------------------------
+// RICHARDS_FLOW (fem_ele_std.cpp:9470-9481): AssembleParabolicEquation and
+// Assemble_Gravity with the storage and conductivity of the Picard iterate
+// at each Gauss point
+// ------------------------------------------------------------------
+__device__ __forceinline__ double mrange(double a, double b, double c)
+{
+    return b < a ? a : b > c ? c : b;  // MRange (FEM/mathlib.cpp:447)
+}
+
+// CMediumProperties::SaturationCapillaryPressureFunction, models 4 (van
+// Genuchten) and 6 (Brooks-Corey) (rf_mmp_new.cpp:5243-5328)
+__device__ __forceinline__ double rich_saturation(const ogs_richards_params& r, double pc)
+{
+    double se;
+    if (r.capillary_model == 4)
+    {
+        if (pc < 0.0) pc = 0.0;
+        se = pow(pc / r.pb, 1.0 / (1.0 - r.m)) + 1.0;
+        se = pow(se, -r.m);
+    }
+    else
+    {
+        if (pc < r.pb) pc = r.pb;
+        se = pow(pc / r.pb, -r.m);
+    }
+    const double sl = se * (r.slm - r.slr) + r.slr;
+    return mrange(r.slr + DBL_EPSILON, sl, r.slm - DBL_EPSILON);
+}
+
+// PressureSaturationDependency(Sw, invert = true): dSw/dpc (<= 0), bounded
+// below by -1/DBL_EPSILON (rf_mmp_new.cpp:5425-5520)
+__device__ __forceinline__ double rich_dsdpc(const ogs_richards_params& r, double sl)
+{
+    double dpds;
+    if (r.capillary_model == 4)
+    {
+        sl = mrange(r.slr + DBL_EPSILON, sl, r.slm - DBL_EPSILON);
+        const double v1 = pow((sl - r.slr) / (r.slm - r.slr), -1.0 / r.m);
+        const double v2 = pow(v1 - 1.0, -r.m);
+        dpds = (r.pb * (r.m - 1.0) * v1 * v2) / (r.m * (sl - r.slr));
+    }
+    else
+    {
+        sl = mrange(r.slr + DBL_EPSILON, sl, r.slm);
+        const double v1 = pow((sl - r.slr) / (r.slm - r.slr), -1.0 / r.m);
+        dpds = (r.pb * v1) / (r.m * (r.slr - sl));
+    }
+    double dsdp = 1.0 / dpds;
+    const double lim = (-1.0) / DBL_EPSILON;
+    if (dsdp < lim) dsdp = lim;
+    return dsdp;
+}
+
+// PermeabilitySaturationFunction(Sw, 0), models 4 (van Genuchten-Mualem)
+// and 6 (Brooks-Corey) (rf_mmp_new.cpp:2576-2635)
+__device__ __forceinline__ double rich_krel(const ogs_richards_params& r, double sl)
+{
+    sl = mrange(r.kr_slr, sl, r.kr_slm);
+    const double se = (sl - r.kr_slr) / (r.kr_slm - r.kr_slr);
+    double kr;
+    if (r.permeability_model == 4)
+        kr = sqrt(se) * pow(1.0 - pow(1.0 - pow(se, 1.0 / r.kr_m), r.kr_m), 2);
+    else
+        kr = pow(se, 3.0 + 2.0 / r.kr_m);
+    if (kr < r.kr_min) kr = r.kr_min;
+    return kr;
+}
+
+// CalCoefMass, EPT_RICHARDS_FLOW (fem_ele_std.cpp:1721-1770), isothermal,
+// constant drho_dp
+__device__ __forceinline__ double rich_mass_coef(const ogs_assembly_params& p, const ogs_richards_params& r,
+                                                 double PG)
+{
+    double Sw = 1.0, dSdp = 0.0;
+    if (PG < 0.0)
+    {
+        Sw = rich_saturation(r, -PG);
+        dSdp = -rich_dsdpc(r, Sw);
+    }
+    double val = p.storage * Sw;
+    if (p.density > 0.0) val += p.porosity * Sw * p.drho_dp;
+    if (PG < 0.0) val += p.porosity * dSdp;
+    return val;
+}
+
+// CalCoefLaplace, EPT_RICHARDS_FLOW (fem_ele_std.cpp:2614-2640):
+// K * (time_unit_factor * kr(Sw) / mu) * fac_perm (1)
+__device__ __forceinline__ double rich_lap_coef(const ogs_assembly_params& p, const ogs_richards_params& r,
+                                                double k, double PG)
+{
+    const double Sw = rich_saturation(r, -PG);
+    const double mat_fac = p.time_unit_factor * rich_krel(r, Sw) / p.viscosity;
+    return k * mat_fac * 1.0;
+}
+
+template <int ET, int NGP>
+__global__ void __launch_bounds__(128) k_richards(AsmArgs a)
+{
+    constexpr int NN = ElemTraits<ET>::NN, DIM = ElemTraits<ET>::DIM;
+    __shared__ double sN[NGP * NN], sdN[NGP * NN * DIM], sw[NGP * 3];
+    stage(sN, a.tab, NGP * NN);
+    stage(sdN, a.tab + NGP * NN, NGP * NN * DIM);
+    stage(sw, a.tab + NGP * NN + NGP * NN * DIM, NGP * 3);
+    __syncthreads();
+    const ogs_assembly_params& p = a.p;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < a.E;
+         e += (int64_t)gridDim.x * blockDim.x)
+    {
+        int nd[NN];
+        double X[NN], Y[NN], Z[NN], U[NN], U1[NN];
+        gather<NN>(a, e, nd, X, Y, Z, U);
+#pragma unroll
+        for (int i = 0; i < NN; i++) U1[i] = __ldg(a.u1 + nd[i]);
+        const double ke = __ldg(a.elem_k + e);
+        double Ml[NN * (NN + 1) / 2], Ll[NN * (NN + 1) / 2], grav[NN];
+#pragma unroll
+        for (int l = 0; l < NN * (NN + 1) / 2; l++) Ml[l] = Ll[l] = 0.0;
+#pragma unroll
+        for (int i = 0; i < NN; i++) grav[i] = 0.0;
+        bool ok = true;
+#pragma unroll 1
+        for (int gp = 0; gp < NGP; gp++)
+        {
+            double iJ[DIM * DIM], det, dNg[DIM * NN];
+            if (!jacobian<NN, DIM>(X, Y, Z, sdN + gp * NN * DIM, iJ, det)) { ok = false; break; }
+            grad_global<NN, DIM>(iJ, sdN + gp * NN * DIM, dNg);
+            const double* w = sw + gp * 3;
+            const double fkt = ET == OGS_ELEM_HEX8 ? det * w[0] * w[1] * w[2]
+                             : ET == OGS_ELEM_QUAD4 ? det * w[0] * w[1] : det * w[0];
+            const double* sf = sN + gp * NN;
+            double PG = 0.0;  // interpolate(NodalVal1)
+#pragma unroll
+            for (int i = 0; i < NN; i++) PG += U1[i] * sf[i];
+            const double mat = rich_lap_coef(p, a.r, ke, PG);
+            const double mf = (p.steady ? 0.0 : rich_mass_coef(p, a.r, PG)) * fkt * 1.0;
+#pragma unroll
+            for (int i = 0; i < NN; i++)
+#pragma unroll
+                for (int j = 0; j <= i; j++)
+                {
+                    const int l = i * (i + 1) / 2 + j;
+                    Ml[l] += mf * sf[i] * sf[j];
+                    double s = Ll[l];
+#pragma unroll
+                    for (int k = 0; k < DIM; k++) s += fkt * dNg[k * NN + i] * mat * dNg[k * NN + j];
+                    Ll[l] = s;
+                }
+            if (p.gravity_on)
+            {
+                // Assemble_Gravity (:5859-6000): rho g, or 1 in the head form
+                const double rho = p.gravity < DBL_EPSILON ? 1.0 : p.density * p.gravity;
+                const double fg = fkt * rho;
+#pragma unroll
+                for (int i = 0; i < NN; i++) grav[i] -= fg * dNg[(DIM - 1) * NN + i] * mat;
+            }
+        }
+        if (!ok) { flag_bad(a.bad_elem, e); continue; }
+        if (p.mass_lumping)
+        {
+            // CalcLumpedMass: CalCoefMass at the element centre (equal shape
+            // function values 1/NN there)
+            double PG = 0.0;
+#pragma unroll
+            for (int i = 0; i < NN; i++) PG += U1[i] * (1.0 / NN);
+            lump_mass<ET, NN>(X, Y, Z, p.steady ? 0.0 : rich_mass_coef(p, a.r, PG), Ml);
+        }
+        flow_combine<NN>(a, e, nd, U, Ml, Ll, grav);
+    }
+}
+
 static int grid_for(int64_t E, int threads)
 {
     int dev = 0, sms = 152;
@@ -850,6 +1021,12 @@ static void launch_mt(const AsmArgs& a, bool affine, cudaStream_t s)
         k_mt_general<ET, NGP, true><<<g, 128, 0, s>>>(a);
     else
         k_mt_general<ET, NGP, false><<<g, 128, 0, s>>>(a);
+}
+
+template <int ET, int NGP>
+static void launch_richards(const AsmArgs& a, cudaStream_t s)
+{
+    k_richards<ET, NGP><<<grid_for(a.E, 128), 128, 0, s>>>(a);
 }
 
 template <int ET, int NGP>
@@ -891,6 +1068,7 @@ bool launch_assembly(const ogs_mesh* m, const AsmArgs& a, bool affine, int kind,
     {                                                                \
         if (kind == 0) launch_flow<ET_, NGP_>(a, affine, s);         \
         else if (kind == 1) launch_mt<ET_, NGP_>(a, affine, s);      \
+        else if (kind == 3) launch_richards<ET_, NGP_>(a, s);        \
         else launch_vel<ET_, NGP_>(a, s);                            \
         return true;                                                 \
     }

@@ -112,6 +112,8 @@ struct AsmArgs
     double* q_out;      // velocity kernel output [e][gp][3]
     int* bad_elem;      // first element with a singular Jacobian + 1
     ogs_assembly_params p;
+    const double* u1;   // RICHARDS_FLOW: the Picard iterate (coefficients)
+    ogs_richards_params r;
 };
 
 }  // namespace ogs

@@ -861,6 +861,211 @@ int64_t orc_assemble(int etype, int ngauss, int dim, int64_t n_nodes,
     return 0;
 }
 
+/* ------------------------------------------------------------------ */
+/* RICHARDS_FLOW                                                       */
+/* ------------------------------------------------------------------ */
+
+static double orc_mrange(double a, double b, double c)
+{
+    /* MRange (FEM/mathlib.cpp:447-455) */
+    if (b < a) return a;
+    if (b > c) return c;
+    return b;
+}
+
+/* SaturationCapillaryPressureFunction, models 4 and 6
+ * (FEM/rf_mmp_new.cpp:5243-5328) */
+double orc_rich_saturation(const ogs_richards_params* r, double pc)
+{
+    double se, sl;
+    if (r->capillary_model == 4)
+    {
+        if (pc < 0.0) pc = 0.0;
+        se = pow(pc / r->pb, 1.0 / (1.0 - r->m)) + 1.0;
+        se = pow(se, -r->m);
+    }
+    else
+    {
+        if (pc < r->pb) pc = r->pb;
+        se = pow(pc / r->pb, -r->m);
+    }
+    sl = se * (r->slm - r->slr) + r->slr;
+    return orc_mrange(r->slr + DBL_EPSILON, sl, r->slm - DBL_EPSILON);
+}
+
+/* PressureSaturationDependency(Sw, invert = true) = dSw/dPc
+ * (FEM/rf_mmp_new.cpp:5425-5520) */
+double orc_rich_dsdpc(const ogs_richards_params* r, double sl)
+{
+    double dpds, v1, v2, dsdp;
+    if (r->capillary_model == 4)
+    {
+        sl = orc_mrange(r->slr + DBL_EPSILON, sl, r->slm - DBL_EPSILON);
+        v1 = pow((sl - r->slr) / (r->slm - r->slr), -1.0 / r->m);
+        v2 = pow(v1 - 1.0, -r->m);
+        dpds = (r->pb * (r->m - 1.0) * v1 * v2) / (r->m * (sl - r->slr));
+    }
+    else
+    {
+        sl = orc_mrange(r->slr + DBL_EPSILON, sl, r->slm);
+        v1 = pow((sl - r->slr) / (r->slm - r->slr), -1.0 / r->m);
+        dpds = (r->pb * v1) / (r->m * (r->slr - sl));
+    }
+    dsdp = 1.0 / dpds;
+    if (dsdp < (-1.0) / DBL_EPSILON) dsdp = (-1.0) / DBL_EPSILON;
+    return dsdp;
+}
+
+/* PermeabilitySaturationFunction(Sw, 0), models 4 and 6
+ * (FEM/rf_mmp_new.cpp:2576-2635) */
+double orc_rich_krel(const ogs_richards_params* r, double sl)
+{
+    double se, kr;
+    sl = orc_mrange(r->kr_slr, sl, r->kr_slm);
+    se = (sl - r->kr_slr) / (r->kr_slm - r->kr_slr);
+    if (r->permeability_model == 4)
+        kr = sqrt(se) * pow(1.0 - pow(1.0 - pow(se, 1.0 / r->kr_m), r->kr_m), 2);
+    else
+        kr = pow(se, 3.0 + 2.0 / r->kr_m);
+    if (kr < r->kr_min) kr = r->kr_min;
+    return kr;
+}
+
+/* CalCoefMass, EPT_RICHARDS_FLOW (fem_ele_std.cpp:1721-1770) */
+double orc_rich_mass_coef(const ogs_assembly_params* p, const ogs_richards_params* r, double PG)
+{
+    double Sw = 1.0, dSdp = 0.0, val;
+    if (PG < 0.0)
+    {
+        Sw = orc_rich_saturation(r, -PG);
+        dSdp = -orc_rich_dsdpc(r, Sw);
+    }
+    val = p->storage * Sw;
+    if (p->density > 0.0) val += p->porosity * Sw * p->drho_dp;
+    if (PG < 0.0) val += p->porosity * dSdp;
+    return val;
+}
+
+/* CalCoefLaplace, EPT_RICHARDS_FLOW (fem_ele_std.cpp:2614-2640) */
+double orc_rich_lap_coef(const ogs_assembly_params* p, const ogs_richards_params* r, double k, double PG)
+{
+    const double Sw = orc_rich_saturation(r, -PG);
+    const double mat_fac = p->time_unit_factor * orc_rich_krel(r, Sw) / p->viscosity;
+    return k * mat_fac * 1.0;
+}
+
+/* Element matrices of RICHARDS_FLOW at the nodal iterate u1: CalcMass /
+ * CalcLumpedMass, CalcLaplace and Assemble_Gravity with the coefficients at
+ * each Gauss point (the lumped storage at the element centre). */
+int orc_element_matrices_richards(int etype, int ngauss, int dim, const double* X, const double* Y,
+                                  const double* Z, const ogs_assembly_params* p,
+                                  const ogs_richards_params* r, double k_e, const double* u1,
+                                  orc_elem_mats* m)
+{
+    const int nn = orc_nodes_per_element(etype);
+    double w[ORC_MAX_GP], N[ORC_MAX_GP * 8], dN[ORC_MAX_GP * 24];
+    double w3[ORC_MAX_GP * 3];
+    const int ngp = orc_shape_table(etype, ngauss, NULL, w, N, dN, w3);
+    double X3[8], Y3[8], Z3[8];
+    memset(m, 0, sizeof *m);
+    for (int i = 0; i < nn; i++)
+    {
+        X3[i] = X[i];
+        Y3[i] = Y[i];
+        Z3[i] = Z ? Z[i] : 0.0;
+    }
+    for (int gp = 0; gp < ngp; gp++)
+    {
+        double dNg[24], det, PG = 0.0;
+        if (grad_global(dim, nn, X3, Y3, Z3, dN + gp * nn * dim, dNg, &det)) return -1;
+        const double fkt = etype == OGS_ELEM_HEX8
+                               ? det * w3[gp * 3] * w3[gp * 3 + 1] * w3[gp * 3 + 2]
+                           : etype == OGS_ELEM_QUAD4 ? det * w3[gp * 3] * w3[gp * 3 + 1]
+                                                     : det * w3[gp * 3];
+        const double* sf = N + gp * nn;
+        for (int i = 0; i < nn; i++) PG += u1[i] * sf[i]; /* interpolate(NodalVal1) */
+        const double mat = orc_rich_lap_coef(p, r, k_e, PG);
+        const double mf = (p->steady ? 0.0 : orc_rich_mass_coef(p, r, PG)) * fkt * 1.0;
+        for (int i = 0; i < nn; i++)
+            for (int j = 0; j <= i; j++) m->mass[i * nn + j] += mf * sf[i] * sf[j];
+        for (int i = 0; i < nn; i++)
+            for (int j = 0; j < nn; j++)
+                for (int k = 0; k < dim; k++)
+                    m->laplace[i * nn + j] += fkt * dNg[k * nn + i] * mat * dNg[k * nn + j];
+        if (p->gravity_on)
+        {
+            /* Assemble_Gravity (fem_ele_std.cpp:5859-6000) */
+            double rho = p->density;
+            if (p->gravity < DBL_EPSILON)
+                rho = 1.0;
+            else
+                rho *= p->gravity;
+            const double fg = fkt * rho;
+            for (int i = 0; i < nn; i++) m->rhs_gravity[i] -= fg * dNg[(dim - 1) * nn + i] * mat;
+        }
+    }
+    for (int i = 0; i < nn; i++)
+        for (int j = 0; j < nn; j++)
+            if (i > j) m->mass[j * nn + i] = m->mass[i * nn + j];
+    if (p->mass_lumping)
+    {
+        double PG = 0.0, factor;
+        for (int i = 0; i < nn; i++) PG += u1[i] * (1.0 / nn);
+        factor = p->steady ? 0.0 : orc_rich_mass_coef(p, r, PG);
+        factor *= 1.0;
+        factor *= orc_element_volume(etype, X3, Y3, Z3) / (double)nn;
+        for (int i = 0; i < nn * nn; i++) m->mass[i] = 0.0;
+        for (int i = 0; i < nn; i++) m->mass[i * nn + i] = factor;
+    }
+    return 0;
+}
+
+/* RICHARDS_FLOW global assembly (AssembleParabolicEquation + Assemble_Gravity,
+ * fem_ele_std.cpp:7702-8120, 5859-6000): A += M/dt + relax0 L,
+ * b += (M/dt - relax1 L) u0 + gravity, coefficients at u1. */
+int64_t orc_assemble_richards(int etype, int ngauss, int dim, int64_t n_elem, const double* x, const double* y,
+                              const double* z, const int32_t* conn, const int64_t* row_ptr, const int64_t* col,
+                              const ogs_assembly_params* p, const ogs_richards_params* r, const double* elem_k,
+                              const double* u0, const double* u1, double* val, double* b)
+{
+    const int nn = orc_nodes_per_element(etype);
+    const double dt_inverse = 1.0 / p->dt;
+    double relax0 = p->nls_relaxation;
+    if (relax0 < DBL_MIN) relax0 = 1.0;
+    const double relax1 = 1.0 - relax0;
+    orc_elem_mats m;
+    for (int64_t e = 0; e < n_elem; e++)
+    {
+        double X[8], Y[8], Z[8], Sm[64], Rm[64], u[8], v1[8];
+        const int32_t* en = conn + e * nn;
+        for (int i = 0; i < nn; i++)
+        {
+            X[i] = x[en[i]];
+            Y[i] = y[en[i]];
+            Z[i] = z ? z[en[i]] : 0.0;
+            u[i] = u0 ? u0[en[i]] : 0.0;
+            v1[i] = u1[en[i]];
+        }
+        if (orc_element_matrices_richards(etype, ngauss, dim, X, Y, z ? Z : NULL, p, r, elem_k[e], v1, &m))
+            return -(1 + e);
+        for (int k = 0; k < nn * nn; k++)
+        {
+            Sm[k] = m.mass[k] * dt_inverse + m.laplace[k] * relax0;
+            Rm[k] = m.mass[k] * dt_inverse - m.laplace[k] * relax1;
+        }
+        for (int i = 0; i < nn; i++)
+        {
+            double s = 0.0;
+            for (int j = 0; j < nn; j++) s += Rm[i * nn + j] * u[j];
+            b[en[i]] += s;
+            if (p->gravity_on) b[en[i]] += m.rhs_gravity[i];
+        }
+        for (int i = 0; i < nn; i++)
+            for (int j = 0; j < nn; j++) val[csr_find(row_ptr, col, en[i], en[j])] += Sm[i * nn + j];
+    }
+    return 0;
+}
+
 /* Cal_Velocity scalar branch (fem_ele_std.cpp:6627-6870): per GP
  * q_i = -sum_j mat[i][j] * vel[j] / time_unit_factor with vel = grad u
  * (plus rho*g on the last axis for LIQUID_FLOW with gravity).  Output

@@ -59,6 +59,22 @@ class AssemblyParams(C.Structure):
     ]
 
 
+class RichardsParams(C.Structure):
+    """Mirror of ogs_richards_params (include/ogs_gpu.h)."""
+    _fields_ = [("capillary_model", C.c_int32), ("permeability_model", C.c_int32), ("pb", C.c_double),
+                ("slr", C.c_double), ("slm", C.c_double), ("m", C.c_double), ("kr_slr", C.c_double),
+                ("kr_slm", C.c_double), ("kr_m", C.c_double), ("kr_min", C.c_double)]
+
+
+def richards_params(**kw) -> RichardsParams:
+    r = RichardsParams(4, 4, 1.0e4, 0.1, 1.0, 0.5, 0.1, 1.0, 0.5, 1e-9)
+    for k, v in kw.items():
+        if not hasattr(r, k):
+            raise AttributeError(k)
+        setattr(r, k, v)
+    return r
+
+
 def make_params(**kw) -> AssemblyParams:
     p = AssemblyParams()
     p.dt = 1.0
@@ -113,6 +129,20 @@ def lib():
                                 C.c_int, C.c_double, C.c_void_p, _dp]
         L.orc_ilu0_factor.restype = C.c_int
         L.orc_ilu0_factor.argtypes = [C.c_int64, _i64p, _i64p, _dp, _dp, _i64p]
+        rp = C.POINTER(RichardsParams)
+        for name in ("orc_rich_saturation", "orc_rich_dsdpc", "orc_rich_krel"):
+            getattr(L, name).restype = C.c_double
+            getattr(L, name).argtypes = [rp, C.c_double]
+        L.orc_rich_mass_coef.restype = C.c_double
+        L.orc_rich_mass_coef.argtypes = [C.c_void_p, rp, C.c_double]
+        L.orc_rich_lap_coef.restype = C.c_double
+        L.orc_rich_lap_coef.argtypes = [C.c_void_p, rp, C.c_double, C.c_double]
+        L.orc_element_matrices_richards.restype = C.c_int
+        L.orc_element_matrices_richards.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, C.c_void_p,
+                                                    C.c_void_p, rp, C.c_double, _dp, C.c_void_p]
+        L.orc_assemble_richards.restype = C.c_int64
+        L.orc_assemble_richards.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int64, _dp, _dp, C.c_void_p,
+                                            _i32p, _i64p, _i64p, C.c_void_p, rp, _dp, _dp, _dp, _dp, _dp]
         _lib = L
     return _lib
 
@@ -162,6 +192,95 @@ def element_matrices(etype, coords, params, k_e=1.0, vel=None, ngauss=3):
         out[name] = np.frombuffer(getattr(m, name), dtype=np.float64)[: nn * nn].reshape(nn, nn).copy()
     out["rhs_gravity"] = np.frombuffer(m.rhs_gravity, dtype=np.float64)[:nn].copy()
     return out
+
+
+def rich_curves(r: RichardsParams, pc=None, sw=None):
+    """Saturation S(pc), dS/dpc(S) and k_rel(S) of the medium (scalars)."""
+    L = lib()
+    out = {}
+    if pc is not None:
+        out["saturation"] = L.orc_rich_saturation(C.byref(r), pc)
+    if sw is not None:
+        out["dsdpc"] = L.orc_rich_dsdpc(C.byref(r), sw)
+        out["krel"] = L.orc_rich_krel(C.byref(r), sw)
+    return out
+
+
+def rich_coefficients(params, r: RichardsParams, k, PG):
+    """CalCoefMass and CalCoefLaplace of RICHARDS_FLOW at pressure PG."""
+    L = lib()
+    return (L.orc_rich_mass_coef(C.byref(params), C.byref(r), PG),
+            L.orc_rich_lap_coef(C.byref(params), C.byref(r), k, PG))
+
+
+def element_matrices_richards(etype, coords, params, r, k_e, u1, ngauss=3):
+    nn = 8 if etype == HEX8 else 4
+    dim = 2 if etype == QUAD4 else 3
+    X = np.ascontiguousarray(coords[:, 0], dtype=np.float64)
+    Y = np.ascontiguousarray(coords[:, 1], dtype=np.float64)
+    Z = np.ascontiguousarray(coords[:, 2], dtype=np.float64) if dim == 3 else None
+    m = ElemMats()
+    rc = lib().orc_element_matrices_richards(etype, ngauss, dim, X, Y, _ptr(Z), C.byref(params), C.byref(r),
+                                             k_e, np.ascontiguousarray(u1, dtype=np.float64), C.byref(m))
+    if rc:
+        raise ValueError("singular Jacobian")
+    return {"mass": np.frombuffer(m.mass, dtype=np.float64)[: nn * nn].reshape(nn, nn).copy(),
+            "laplace": np.frombuffer(m.laplace, dtype=np.float64)[: nn * nn].reshape(nn, nn).copy(),
+            "rhs_gravity": np.frombuffer(m.rhs_gravity, dtype=np.float64)[:nn].copy()}
+
+
+def assemble_richards(mesh, row_ptr, col, params, r, elem_k, p_old, p_iter, ngauss=3):
+    """RICHARDS_FLOW global A values (on the pattern) and b at the iterate."""
+    val = np.zeros(len(col))
+    b = np.zeros(mesh.n_nodes)
+    z = mesh.z if mesh.dim == 3 else None
+    f = lambda a: np.ascontiguousarray(a, dtype=np.float64)  # noqa: E731
+    rc = lib().orc_assemble_richards(mesh.elem_type, ngauss, mesh.dim, mesh.n_elements, mesh.x, mesh.y, _ptr(z),
+                                     mesh.conn.ravel(), row_ptr, col, C.byref(params), C.byref(r), f(elem_k),
+                                     f(p_old), f(p_iter), val, b)
+    if rc:
+        raise ValueError(f"singular Jacobian in element {-rc - 1}")
+    return val, b
+
+
+def richards_picard(mesh, row_ptr, col, params, r, elem_k, p_old, p_iter0, rows, vals, symmetric,
+                    error_method=2, tolerance=1e-6, max_iterations=20, method=5, precond=1, max_iter=5000,
+                    tol=1e-12, ngauss=3):
+    """One RICHARDS_FLOW time step by Picard iteration, restating
+    CRFProcess::ExecuteNonLinear (rf_pcs.cpp:9636-9960) with Execute
+    (:4695-5080) and CalcIterationNODError (:9170-9600).  Returns (iterate,
+    info)."""
+    it = np.array(p_iter0, dtype=np.float64)
+    theta0 = 1.0 - params.nls_relaxation
+    if theta0 < np.finfo(float).eps:
+        theta0 = 1.0
+    last, fails, info = 1.0, 0, {"iterations": 0, "converged": False, "diverged": False, "linear": 0}
+    for k in range(max_iterations):
+        val, b = assemble_richards(mesh, row_ptr, col, params, r, elem_k, p_old, it, ngauss)
+        dirichlet(row_ptr, col, val, b, rows, vals, symmetric=symmetric)
+        x, li = solve(row_ptr, col, val, b, it, method=method, precond=precond, max_iter=max_iter, tol=tol)
+        info["linear"] += li["iterations"]
+        d = it - x
+        if error_method == 1:
+            abs_err = np.abs(d).max()
+        elif error_method == 4:
+            abs_err = np.sqrt(np.sum(d * d)) / (np.sqrt(np.sum(it * it)) + np.finfo(float).eps)
+        else:
+            abs_err = np.sqrt(np.sum(d * d))
+        err = abs_err / tolerance
+        theta = 1.0 if err < 1.0 else theta0
+        it = x.copy() if theta == 1.0 else (1.0 - theta) * it + theta * x
+        info["iterations"], info["error"] = k + 1, err
+        if err <= 1.0:
+            info["converged"] = True
+            break
+        percent = 100.0 * ((last - err) / last)
+        fails = fails + 1 if (k > 0 and percent < 1.0) else 0
+        last = err
+        if fails > 1:
+            info["diverged"] = True
+            break
+    return it, info
 
 
 def build_pattern(n_nodes, conn):

@@ -191,3 +191,50 @@ def test_supg_terms_on_a_tet(oracle, method):
     assert np.allclose(on["mass"] - off["mass"], cm * tau * np.outer(w, np.full(4, vol / 4)), rtol=1e-10,
                        atol=0)
     assert np.allclose(on["laplace"], off["laplace"], rtol=0, atol=0)
+
+
+@pytest.mark.parametrize("model", [4, 6])
+def test_richards_curves(oracle, model):
+    """Saturation, dSw/dpc and k_rel of the Richards medium (van Genuchten
+    and Brooks-Corey, rf_mmp_new.cpp:5243-5520, 2576-2635): closed forms,
+    the clamps to [slr + eps, slm - eps], and dSw/dpc(S(pc)) against a
+    centred difference of S(pc)."""
+    m = 0.6 if model == 4 else 2.0
+    r = oracle.richards_params(capillary_model=model, permeability_model=model, pb=2.0e3, slr=0.15, slm=0.95,
+                               m=m, kr_slr=0.15, kr_slm=0.95, kr_m=m, kr_min=1e-8)
+    eps = np.finfo(float).eps
+    for pc in (3.0e3, 1.0e4, 4.0e4):
+        s = oracle.rich_curves(r, pc=pc)["saturation"]
+        if model == 4:
+            se = (1.0 + (pc / 2.0e3) ** (1.0 / (1.0 - m))) ** (-m)
+        else:
+            se = (pc / 2.0e3) ** (-m)
+        assert abs(s - (0.15 + 0.8 * se)) < 1e-14
+        h = pc * 1e-6
+        fd = (oracle.rich_curves(r, pc=pc + h)["saturation"] - oracle.rich_curves(r, pc=pc - h)["saturation"]) / (2 * h)
+        d = oracle.rich_curves(r, sw=s)["dsdpc"]
+        assert d < 0 and abs(d - fd) < 1e-6 * abs(fd)
+        se_k = (s - 0.15) / 0.8
+        kr = (np.sqrt(se_k) * (1 - (1 - se_k ** (1 / m)) ** m) ** 2 if model == 4 else se_k ** (3 + 2 / m))
+        assert abs(oracle.rich_curves(r, sw=s)["krel"] - max(kr, 1e-8)) < 1e-13
+    # full saturation: pc <= 0 (van Genuchten) or pc <= pb (Brooks-Corey)
+    assert oracle.rich_curves(r, pc=-5.0)["saturation"] == 0.95 - eps
+    assert oracle.rich_curves(r, sw=0.1)["krel"] == 1e-8  # below residual: minimum k_rel
+
+
+def test_richards_coefficients(oracle):
+    """CalCoefMass / CalCoefLaplace of RICHARDS_FLOW: saturated (p >= 0)
+    storage Ss + n drho/dp and K / mu; unsaturated adds n dSw/dp (> 0)
+    and scales K by k_rel(S(-p))."""
+    r = oracle.richards_params()
+    p = oracle.make_params(pcs_type=3, storage=1e-6, porosity=0.35, drho_dp=4.4e-10, viscosity=1e-3,
+                           density=1000.0, time_unit_factor=1.0)
+    mc, lc = oracle.rich_coefficients(p, r, 1e-12, 2.0e3)
+    assert abs(mc - (1e-6 + 0.35 * 4.4e-10)) < 1e-20
+    kr_sat = oracle.rich_curves(r, sw=1.0 - np.finfo(float).eps)["krel"]
+    assert abs(lc - 1e-12 * (kr_sat / 1e-3)) < 1e-22
+    mc, lc = oracle.rich_coefficients(p, r, 1e-12, -1.5e4)
+    s = oracle.rich_curves(r, pc=1.5e4)["saturation"]
+    d = -oracle.rich_curves(r, sw=s)["dsdpc"]
+    assert abs(mc - (1e-6 * s + 0.35 * s * 4.4e-10 + 0.35 * d)) < 1e-18
+    assert abs(lc - 1e-12 * (oracle.rich_curves(r, sw=s)["krel"] / 1e-3)) < 1e-24
