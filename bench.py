@@ -320,6 +320,93 @@ def transport_leg(capi, torch, steps=3):
 
 
 # ------------------------------------------------------------------
+# RICHARDS_FLOW: one Picard time step on the deck's hex box
+# ------------------------------------------------------------------
+RICH_SPACING = (0.25, 0.25, 0.0625)  # 32 m x 32 m x 4 m
+RICH_WORKLOAD = ("RICHARDS_FLOW on hex 128x128x64 (1,081,665 nodes), 0.25 x 0.25 x 0.0625 m cells, ln k GRF "
+                 "(mean ln 1e-12 m2, var 0.5, ell 4 cells), van Genuchten pb 5 kPa, m 0.55, Sr 0.08, Smax 0.98, "
+                 "gravity; water table at mid-depth, top raised to -5 kPa; dt 3600 s; Picard ENORM 1 Pa; "
+                 "CG + Jacobi 1e-10")
+
+
+def richards_deck():
+    from ogs5_gb300 import fields
+    from ogs5_gb300 import mesh as M
+    m = M.structured_hex(NX, NY, NZ, *RICH_SPACING)
+    ek = fields.lognormal_k((NX, NY, NZ), np.log(1e-12), 0.5, 4.0, seed=SEED)
+    depth = NZ * RICH_SPACING[2]
+    p_old = 9810.0 * (0.5 * depth - m.z)  # hydrostatic, water table at mid-depth
+    top = np.flatnonzero(m.z == m.z.max())
+    bot = np.flatnonzero(m.z == m.z.min())
+    rows = np.concatenate([top, bot])
+    vals = np.concatenate([np.full(len(top), -5.0e3), p_old[bot]])
+    return m, ek, p_old, rows, vals
+
+
+RICH_MEDIUM = dict(capillary_model=4, permeability_model=4, pb=5.0e3, slr=0.08, slm=0.98, m=0.55, kr_slr=0.08,
+                   kr_slm=0.98, kr_m=0.55, kr_min=1e-9)
+RICH_FLUID = dict(dt=3600.0, storage=1e-6, porosity=0.35, drho_dp=4.4e-10, viscosity=1e-3, density=1000.0,
+                  time_unit_factor=1.0, gravity=9.81, gravity_on=1)
+
+
+def richards_leg(capi, torch, steps=2):
+    """One Picard time step per measured step (the same step repeated from
+    the same state), device time of the whole loop."""
+    m, ek, p_old, rows, vals = richards_deck()
+    gm = capi.GpuMesh(m)
+    eqs = capi.LinearEQS(gm)
+    eqs.ConfigNumerics(capi.LS_CG, capi.PRECOND_JACOBI, 20000, TOL, check_norm_rhs=False)
+    p = capi.make_params(capi.RICHARDS_FLOW, **RICH_FLUID)
+    r = capi.richards_params(**RICH_MEDIUM)
+    ekd = torch.tensor(ek, device="cuda")
+    pod = torch.tensor(p_old, device="cuda")
+    rowsd = torch.tensor(rows, device="cuda")
+    valsd = torch.tensor(vals, device="cuda")
+    times, res = [], None
+    for k in range(steps + 1):
+        it = pod.clone()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = eqs.RichardsStep(p, r, ekd, pod, it, rowsd, valsd, capi.DIRICHLET_SYMMETRIC, error_method=capi.ENORM,
+                               max_iterations=40, tolerance=1.0)
+        torch.cuda.synchronize()
+        if k:  # the first step allocates and captures the solver graphs
+            times.append((time.perf_counter() - t0) * 1e3)
+    ms = statistics.median(times)
+    return {"workload": RICH_WORKLOAD, "value": round(1e3 / ms, 3), "unit": "Picard time steps/s",
+            "ms_per_step": round(ms, 3), "device_ms": round(res["solve_ms"], 3),
+            "picard_iterations": res["iterations"], "linear_iterations": res["linear_iterations"],
+            "final_error_over_tol": res["error"], "converged": res["converged"],
+            "nodes": m.n_nodes, "elements": m.n_elements}
+
+
+def richards_cpu_sample(picard_its, linear_its, t_cg_it):
+    """Oracle Richards assembly of one 16-cell x-slab (seconds per element),
+    extrapolated with the GPU run's Picard and linear iteration counts and
+    the measured oracle CG iteration time: one Picard step on one core."""
+    import copy
+
+    from oracle import oracle as O
+    O.build("/nonexistent")
+    m, ek, p_old, rows, vals = richards_deck()
+    slab = m.conn.reshape(NZ, NY, NX, 8)[:, :, :16, :].reshape(-1, 8)
+    ms = copy.copy(m)
+    ms.conn = np.ascontiguousarray(slab)
+    op = O.make_params(pcs_type=3, **RICH_FLUID)
+    r = O.richards_params(**RICH_MEDIUM)
+    rp, col = O.build_pattern(m.n_nodes, m.conn)
+    eks = ek.reshape(NZ, NY, NX)[:, :, :16].ravel().copy()
+    t0 = time.perf_counter()
+    O.assemble_richards(ms, rp, col, op, r, eks, p_old, p_old)
+    t_el = (time.perf_counter() - t0) / len(slab)
+    s = picard_its * t_el * m.n_elements + linear_its * t_cg_it
+    return {"value": round(1.0 / s, 5), "unit": "Picard time steps/s", "cores": 1, "kind": "port",
+            "sample": f"oracle Richards assembly of a 16-cell slab ({t_el * 1e6:.2f} us per hex) and CG iterations "
+                      f"({t_cg_it * 1e3:.1f} ms each), extrapolated to {picard_its} Picard iterations and "
+                      f"{linear_its} CG iterations of the GPU run"}
+
+
+# ------------------------------------------------------------------
 # Monte-Carlo batch (512 steady realisations of uneven size)
 # ------------------------------------------------------------------
 BATCH_REALS = 512
@@ -677,7 +764,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--path", default="both", choices=["both", "fp64", "mixed", "batch", "serve", "transport"],
+    ap.add_argument("--path", default="both", choices=["both", "fp64", "mixed", "batch", "serve", "transport", "richards"],
                     help="fp64 / mixed / batch: time one path only (profiling driver)")
     ap.add_argument("--batch-reals", type=int, default=BATCH_REALS)
     ap.add_argument("--batch-max-n", type=int, default=96)
@@ -686,6 +773,7 @@ def main():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-transport", action="store_true")
+    ap.add_argument("--no-richards", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=SERVE_REQUESTS)
     ap.add_argument("--serve-flags", type=int, default=None)
     ap.add_argument("--serve-max-active", type=int, default=None)
@@ -703,6 +791,11 @@ def main():
     B.build()
     from ogs5_gb300 import capi
 
+    if args.path == "richards":
+        import torch
+        from ogs5_gb300 import capi
+        print(json.dumps(richards_leg(capi, torch, steps=max(1, args.steps))))
+        return
     if args.path == "transport":
         from ogs5_gb300 import capi
         print(json.dumps(transport_leg(capi, torch, steps=max(1, args.steps))))
@@ -806,6 +899,8 @@ def main():
     }
     if not args.no_transport:
         out["transport"] = transport_leg(capi, torch)
+    if not args.no_richards:
+        out["richards"] = richards_leg(capi, torch)
     if not args.no_serve:
         out["serve"] = serve_leg(capi, torch, n_req=args.serve_requests)
     if not args.no_batch:
@@ -821,6 +916,9 @@ def main():
                                           f"pattern ({t_it*1e3:.1f} ms/iter), extrapolated to "
                                           f"{m.n_elements} elements + {f64['iters'] / k_steps:.0f} "
                                           f"iterations/step")}
+        if "richards" in out:
+            rr = out["richards"]
+            rr["cpu_baseline"] = richards_cpu_sample(rr["picard_iterations"], rr["linear_iterations"], t_it)
     if rank == 0:
         print(json.dumps(out))
 

@@ -789,7 +789,25 @@ extern "C" ogs_status ogs_gpu_richards_step(ogs_system* s, const ogs_assembly_pa
     if ((st = dirichlet_upload(s, bc_rows, bc_values, n_bc, bc_mode))) return st;
     double* red = s->rich_red;
     unsigned* ticket = (unsigned*)(red + 2 * kMaxBlocks + 3);
-    OGS_CUDA_TRY(cudaEventRecord(s->ev0, s->stream));
+    // own events: the linear solves time themselves with ev0 / ev1
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    OGS_CUDA_TRY(cudaEventCreate(&e0));
+    if (cudaEventCreate(&e1) != cudaSuccess)
+    {
+        cudaEventDestroy(e0);
+        set_error("richards_step: cudaEventCreate failed");
+        return OGS_CUDA_ERROR;
+    }
+    struct EvGuard
+    {
+        cudaEvent_t a, b;
+        ~EvGuard()
+        {
+            cudaEventDestroy(a);
+            cudaEventDestroy(b);
+        }
+    } guard{e0, e1};
+    OGS_CUDA_TRY(cudaEventRecord(e0, s->stream));
     double theta0 = 1.0 - p->nls_relaxation;  // nl_theta (rf_pcs.cpp:9652)
     if (theta0 < DBL_EPSILON) theta0 = 1.0;
     ogs_picard_stats out{};
@@ -843,11 +861,11 @@ extern "C" ogs_status ogs_gpu_richards_step(ogs_system* s, const ogs_assembly_pa
             break;
         }
     }
-    OGS_CUDA_TRY(cudaEventRecord(s->ev1, s->stream));
+    OGS_CUDA_TRY(cudaEventRecord(e1, s->stream));
     OGS_CUDA_TRY(cudaMemcpyAsync(p_iter, s->rich_it, nb, cudaMemcpyDefault, s->stream));
     OGS_CUDA_TRY(cudaStreamSynchronize(s->stream));
     float ms = 0.f;
-    cudaEventElapsedTime(&ms, s->ev0, s->ev1);
+    cudaEventElapsedTime(&ms, e0, e1);
     out.solve_ms = ms;
     if (stats) *stats = out;
     if (!out.converged)

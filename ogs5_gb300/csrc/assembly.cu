@@ -901,16 +901,6 @@ __device__ __forceinline__ double rich_mass_coef(const ogs_assembly_params& p, c
     return val;
 }
 
-// CalCoefLaplace, EPT_RICHARDS_FLOW (fem_ele_std.cpp:2614-2640):
-// K * (time_unit_factor * kr(Sw) / mu) * fac_perm (1)
-__device__ __forceinline__ double rich_lap_coef(const ogs_assembly_params& p, const ogs_richards_params& r,
-                                                double k, double PG)
-{
-    const double Sw = rich_saturation(r, -PG);
-    const double mat_fac = p.time_unit_factor * rich_krel(r, Sw) / p.viscosity;
-    return k * mat_fac * 1.0;
-}
-
 template <int ET, int NGP>
 __global__ void __launch_bounds__(128) k_richards(AsmArgs a)
 {
@@ -949,8 +939,20 @@ __global__ void __launch_bounds__(128) k_richards(AsmArgs a)
             double PG = 0.0;  // interpolate(NodalVal1)
 #pragma unroll
             for (int i = 0; i < NN; i++) PG += U1[i] * sf[i];
-            const double mat = rich_lap_coef(p, a.r, ke, PG);
-            const double mf = (p.steady ? 0.0 : rich_mass_coef(p, a.r, PG)) * fkt * 1.0;
+            // CalCoefLaplace (fem_ele_std.cpp:2614-2640): K * (time_unit_factor
+            // * kr(Sw) / mu) * fac_perm (1); CalCoefMass (:1721-1770) reuses
+            // S(-PG), the same call, when unsaturated
+            const double Sw = rich_saturation(a.r, -PG);
+            const double mat = ke * (p.time_unit_factor * rich_krel(a.r, Sw) / p.viscosity) * 1.0;
+            double mc = 0.0;
+            if (!p.steady)
+            {
+                const double Sm = PG < 0.0 ? Sw : 1.0;
+                mc = p.storage * Sm;
+                if (p.density > 0.0) mc += p.porosity * Sm * p.drho_dp;
+                if (PG < 0.0) mc += p.porosity * -rich_dsdpc(a.r, Sw);
+            }
+            const double mf = mc * fkt * 1.0;
 #pragma unroll
             for (int i = 0; i < NN; i++)
 #pragma unroll
