@@ -393,13 +393,21 @@ __global__ void __launch_bounds__(kThreads) k_mp_restart(MixedArgs a)
 // ------------------------------------------------------------------
 // FP32 CG iteration (Chronopoulos-Gear)
 // ------------------------------------------------------------------
-// r.u, w.u, r.r of the product: block partials, added by the last block
-// (fixed order, see grid_sum) into st->mp_g for the update kernel, which
-// then streams without a reduction prologue
+// r.u, w.u, r.r of the product: block partials; one block of
+// k_mp_dots adds them (fixed order) into st->mp_g for the update kernel,
+// which then streams without a reduction prologue
 __device__ __forceinline__ void mp_sum_products(const float (&v)[3], KState* st)
 {
+    write_partials<3, float>(v, st->cg_ps);
+}
+
+__global__ void __launch_bounds__(kThreads) k_mp_dots(MixedArgs a)
+{
+    KState* st = a.st;
+    if (st->done || st->replace) return;
     double g[3];
-    if (grid_sum<3, float>(v, g, st->cg_ps, &st->mp_ticket) && threadIdx.x == 0)
+    reduce_partials<3>(st->cg_ps, st->nb_spmv, g);
+    if (threadIdx.x == 0)
     {
         st->mp_g[0] = g[0];
         st->mp_g[1] = g[1];
@@ -1095,6 +1103,7 @@ void launch_mp_iteration(const MixedArgs& a, cudaStream_t s, cudaEvent_t eb, cud
         default: k_mp_spmv<0><<<gs, kThreads, 0, s>>>(a); break;   // SELL-32 FP32
     }
     if (ee) cudaEventRecordWithFlags(ee, s, cudaEventRecordExternal);
+    k_mp_dots<<<1, kThreads, 0, s>>>(a);
     k_mp_update<<<red_grid(a.n), kThreads, 0, s>>>(a);
 }
 
