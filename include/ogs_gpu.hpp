@@ -15,6 +15,10 @@
 //                                                 -> LinearEQS::GlobalAssembly
 //   CRFProcess::CalIntegrationPointValue (FEM/rf_pcs.cpp:5915)
 //                                                 -> LinearEQS::GaussPointVelocity
+//   CRFProcess::ExecuteNonLinear, RICHARDS_FLOW Picard (FEM/rf_pcs.cpp:9636)
+//                                                 -> LinearEQS::RichardsStep
+//   FEMRead / GEOLIB_Read_GeoLib / BCRead (MSH/msh_mesh.cpp:421,
+//   FileIO/OGSIOVer4.cpp, FEM/rf_bc_new.cpp)      -> ogs_gpu::Deck
 //
 // SetKnownX_i rows are collected and applied as one set (the same result as
 // the reference's row-by-row Diagonize, a row given twice keeping its last
@@ -201,6 +205,22 @@ public:
         return q;
     }
 
+    // RICHARDS_FLOW: one time step by Picard iteration (CRFProcess::
+    // ExecuteNonLinear); the collected SetKnownX_i rows are the Dirichlet
+    // set, x() the first iterate in and the last one out.  Returns the stats;
+    // throws unless the loop converged (or allow_fail).
+    ogs_picard_stats RichardsStep(const ogs_assembly_params& p, const ogs_richards_params& r, const double* elem_k,
+                                  const double* p_old, const ogs_picard_config& nls, bool allow_fail = false)
+    {
+        ogs_picard_stats st{};
+        const ogs_status s = ogs_gpu_richards_step(h_, &p, &r, elem_k, p_old, x_.data(), known_rows_.data(),
+                                                   known_vals_.data(), (int64_t)known_rows_.size(), mode_, &nls, &st);
+        known_rows_.clear();
+        known_vals_.clear();
+        if (s != OGS_OK && !(allow_fail && s == OGS_NOT_CONVERGED)) check(s, "ogs_gpu_richards_step");
+        return st;
+    }
+
     ogs_system* handle() const { return h_; }
 
 private:
@@ -221,6 +241,57 @@ private:
     std::vector<double> known_vals_;
     ogs_dirichlet_mode mode_ = OGS_DIRICHLET_ROW_ONLY;
     ogs_solve_stats stats_{};
+};
+
+// An OGS-5 deck read from disk (FEMRead / GEOLIB / BCRead): the mesh for
+// Mesh, and the CONSTANT Dirichlet rows of a process for SetKnownX_i.
+class Deck
+{
+public:
+    Deck(const std::string& msh, const std::string& gli = "", const std::string& bc = "")
+    {
+        check(ogs_deck_read(msh.c_str(), gli.empty() ? nullptr : gli.c_str(), bc.empty() ? nullptr : bc.c_str(), &h_),
+              "ogs_deck_read");
+    }
+    ~Deck() { ogs_deck_destroy(h_); }
+    Deck(const Deck&) = delete;
+    Deck& operator=(const Deck&) = delete;
+
+    ogs_mesh_desc mesh_desc() const
+    {
+        ogs_mesh_desc d{};
+        check(ogs_deck_mesh(h_, &d, nullptr), "ogs_deck_mesh");
+        return d;
+    }
+
+    double min_edge_length() const
+    {
+        ogs_mesh_desc d{};
+        double h = 0.0;
+        ogs_deck_mesh(h_, &d, &h);
+        return h;
+    }
+
+    // (row, value) pairs of every CONSTANT condition of the process, in the
+    // order CRFProcess::bc_node_value holds them
+    std::vector<std::pair<int64_t, double>> dirichlet(const std::string& pcs_type,
+                                                      const std::string& primary_variable = "") const
+    {
+        const char* pv = primary_variable.empty() ? nullptr : primary_variable.c_str();
+        int64_t n = 0;
+        check(ogs_deck_dirichlet(h_, pcs_type.c_str(), pv, nullptr, nullptr, 0, &n), "ogs_deck_dirichlet");
+        std::vector<int64_t> rows((size_t)n);
+        std::vector<double> vals((size_t)n);
+        check(ogs_deck_dirichlet(h_, pcs_type.c_str(), pv, rows.data(), vals.data(), n, &n), "ogs_deck_dirichlet");
+        std::vector<std::pair<int64_t, double>> out;
+        for (size_t k = 0; k < (size_t)n; k++) out.emplace_back(rows[k], vals[k]);
+        return out;
+    }
+
+    const ogs_deck* handle() const { return h_; }
+
+private:
+    ogs_deck* h_ = nullptr;
 };
 
 // assembly parameters with the defaults of an OGS-5 deck
