@@ -44,10 +44,10 @@ struct KState
     // grid barrier of the persistent FP32 CG kernel (reset with the header)
     unsigned int bar_count, bar_gen;
     int bar_err, pad5;
-    // FP32 CG: the last block of the product adds the block partials into
-    // r.u, w.u, r.r for the update kernel (reset with the header)
+    // FP32 CG: k_mp_dots adds the product's block partials and leaves
+    // alpha and beta of the iteration for the update kernel
     unsigned int mp_ticket, pad6;
-    double mp_g[3];
+    double mp_alpha, mp_beta;
     unsigned int ticket[8];
     double part[8][2 * kMaxBlocks];
     double cg_ps[3 * kMaxBlocks];        // per SpMV block: p . s (FP64 CG); r.u, w.u, r.r (FP32 CG)

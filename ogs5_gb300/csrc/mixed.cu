@@ -393,25 +393,72 @@ __global__ void __launch_bounds__(kThreads) k_mp_restart(MixedArgs a)
 // ------------------------------------------------------------------
 // FP32 CG iteration (Chronopoulos-Gear)
 // ------------------------------------------------------------------
-// r.u, w.u, r.r of the product: block partials; one block of
-// k_mp_dots adds them (fixed order) into st->mp_g for the update kernel,
-// which then streams without a reduction prologue
+// r.u, w.u, r.r of the product: block partials; one block of k_mp_dots
+// adds them (fixed order) and its thread 0 does the scalar work of the
+// iteration, so the update kernel streams after reading alpha and beta
 __device__ __forceinline__ void mp_sum_products(const float (&v)[3], KState* st)
 {
     write_partials<3, float>(v, st->cg_ps);
 }
 
+// V scalars: beta = gamma / gamma_prev ; eta = delta - beta^2 eta_prev ;
+// alpha = gamma / eta ; the replacement test
 __global__ void __launch_bounds__(kThreads) k_mp_dots(MixedArgs a)
 {
     KState* st = a.st;
     if (st->done || st->replace) return;
-    double g[3];
-    reduce_partials<3>(st->cg_ps, st->nb_spmv, g);
+    // thread 0 loads the state it needs (both parity slots) before the
+    // partial sums, so the loads overlap instead of following each other
+    int it = 0, base = 0, max_iter = 0, ibs[2] = {0, 0};
+    double gh[2] = {0.0, 0.0}, eh[2] = {0.0, 0.0}, rbs[2] = {0.0, 0.0};
+    double rmax_prev = 0.0, scale = 1.0, bnorm = 1.0, tol = 0.0, dl = 0.0;
     if (threadIdx.x == 0)
     {
-        st->mp_g[0] = g[0];
-        st->mp_g[1] = g[1];
-        st->mp_g[2] = g[2];
+        it = st->iter; base = st->base_iter; max_iter = st->max_iter;
+        gh[0] = st->gam_hist[0]; gh[1] = st->gam_hist[1];
+        eh[0] = st->eta_hist[0]; eh[1] = st->eta_hist[1];
+        rbs[0] = st->rbest[0]; rbs[1] = st->rbest[1];
+        ibs[0] = st->itbest[0]; ibs[1] = st->itbest[1];
+        rmax_prev = st->rmax; scale = st->scale; bnorm = st->bnorm; tol = st->tol; dl = st->delta;
+    }
+    double g[3];
+    reduce_partials<3>(st->cg_ps, st->nb_spmv, g);
+    if (threadIdx.x != 0) return;
+    const int pp = (it - 1) & 1;                 // parity slot of the previous iteration
+    const double gamma = g[0], delta = g[1], rn = sqrt(g[2]);
+    const bool first = it == 1;                  // no search direction yet: beta = 0
+    const bool fresh = it == base + 1;           // first iteration after a (re)start
+    const double rmax = fresh ? rn : rmax_prev;
+    const double beta = first ? 0.0 : gamma / gh[pp];
+    const double eta = first ? delta : delta - beta * beta * eh[pp];
+    const double alpha = gamma / eta;
+    const double est = rn / scale / bnorm;       // estimate of |r64| / |b|
+    const bool nonfinite = !isfinite(rn) || !isfinite(alpha);
+    // plateau: no new smallest |r32| in the cycle for max(64, half the
+    // cycle) iterations
+    const double rb_prev = fresh ? rn : rbs[pp];
+    const int ib_prev = fresh ? it : ibs[pp];
+    const bool better = rn < rb_prev;
+    const double rb = better ? rn : rb_prev;
+    const int ib = better ? it : ib_prev;
+    const bool stalled = it - ib > max(kPlateau, (it - base) / 2);
+    // right after a replacement r32 is the true residual (checked in FP64 by
+    // k_mp_residual), so a fresh iteration never asks for another one
+    const bool repl = !nonfinite && !fresh && (est < tol || rn < dl * rmax || it > max_iter || stalled);
+    if (it & 1) { st->rbest[1] = rb; st->itbest[1] = ib; }
+    else { st->rbest[0] = rb; st->itbest[0] = ib; }
+    if (fresh) st->rmax = rn;
+    st->gam_hist[it & 1] = gamma;
+    st->eta_hist[it & 1] = eta;
+    st->first = 0;  // read by the replacement kernels only
+    st->mp_alpha = alpha;
+    st->mp_beta = beta;
+    if (nonfinite) { st->status = OGS_NONFINITE; st->done = 1; }
+    else if (repl)
+    {
+        st->replace = 1;
+        st->rn_req = rn;
+        st->stalled = stalled && !(est < tol || rn < dl * rmax || it > max_iter);
     }
 }
 
@@ -706,86 +753,79 @@ int cell_spmv_grid(int nx, int ny, int nz)
 }
 
 constexpr int kU32 = 8;  // elements per thread per step, loaded before use
+constexpr int kU4 = 2;   // 16-byte groups per array, thread and step in k_mp_update
 
-// V: scalars from the S partials ; replacement test ; p, s, x32, r32, u32
+// one row of the Chronopoulos-Gear update
+__device__ __forceinline__ void mp_update_one(float u, float w, float pp, float sp, float xp, float rp, float d, float fa,
+                                              float fb, float& p, float& s, float& x, float& r, float& un)
+{
+    p = u + fb * pp;
+    s = w + fb * sp;
+    r = rp - fa * s;
+    x = xp + fa * p;
+    un = r * d;
+}
+
+// V: p, s, x32, r32, u32 with the alpha and beta of k_mp_dots
 __global__ void __launch_bounds__(kThreads) k_mp_update(MixedArgs a)
 {
     KState* st = a.st;
-    if (st->done || st->replace) return;
-    const int it = st->iter;
-    const double gamma = st->mp_g[0], delta = st->mp_g[1], rn = sqrt(st->mp_g[2]);
-    const bool first = it == 1;                  // no search direction yet: beta = 0
-    const bool fresh = it == st->base_iter + 1;  // first iteration after a (re)start
-    const double rmax = fresh ? rn : st->rmax;
-    const double beta = first ? 0.0 : gamma / st->gam_hist[(it - 1) & 1];
-    const double eta = first ? delta : delta - beta * beta * st->eta_hist[(it - 1) & 1];
-    const double alpha = gamma / eta;
-    const double est = rn / st->scale / st->bnorm;  // estimate of |r64| / |b|
-    const bool nonfinite = !isfinite(rn) || !isfinite(alpha);
-    // plateau: no new smallest |r32| in the cycle for max(64, half the
-    // cycle) iterations (parity slots of the previous iteration: written by
-    // block 0 of the previous launch)
-    const double rb_prev = fresh ? rn : ((it - 1) & 1 ? st->rbest[1] : st->rbest[0]);
-    const int ib_prev = fresh ? it : ((it - 1) & 1 ? st->itbest[1] : st->itbest[0]);
-    const bool better = rn < rb_prev;
-    const double rb = better ? rn : rb_prev;
-    const int ib = better ? it : ib_prev;
-    const bool stalled = it - ib > max(kPlateau, (it - st->base_iter) / 2);
-    // right after a replacement r32 is the true residual (checked in FP64 by
-    // k_mp_residual), so a fresh iteration never asks for another one
-    const bool repl = !nonfinite && !fresh &&
-                      (est < st->tol || rn < st->delta * rmax || it > st->max_iter || stalled);
-    if (blockIdx.x == 0 && threadIdx.x == 0)
-    {
-        if (it & 1) { st->rbest[1] = rb; st->itbest[1] = ib; }
-        else { st->rbest[0] = rb; st->itbest[0] = ib; }
-        if (fresh) st->rmax = rn;
-        st->gam_hist[it & 1] = gamma;
-        st->eta_hist[it & 1] = eta;
-        st->first = 0;  // read by the replacement kernels only
-        if (nonfinite) { st->status = OGS_NONFINITE; st->done = 1; }
-        else if (repl)
-        {
-            st->replace = 1;
-            st->rn_req = rn;
-            st->stalled = stalled && !(est < st->tol || rn < st->delta * rmax || it > st->max_iter);
-        }
-    }
-    if (nonfinite || repl) return;
+    const int done = st->done, repl = st->replace;
+    const double alpha = st->mp_alpha, beta = st->mp_beta;
+    if (done || repl) return;
     const float fb = (float)beta, fa = (float)alpha;
-    const int n = a.n, stride = gridDim.x * blockDim.x;
-    for (int base = blockIdx.x * blockDim.x + threadIdx.x; base < n; base += kU32 * stride)
+    // 16-byte accesses over the first 4 * (n / 4) rows (the FP32 vectors
+    // are 256-byte aligned), kU4 of them per array and thread in flight;
+    // the last n % 4 rows one by one
+    const int n = a.n, n4 = n >> 2, stride = gridDim.x * blockDim.x;
+    const float4 *u4 = (const float4*)a.u32, *w4 = (const float4*)a.w32, *d4 = (const float4*)a.d32;
+    float4 *p4 = (float4*)a.p32, *s4 = (float4*)a.s32, *x4 = (float4*)a.x32, *r4 = (float4*)a.r32;
+    float4* uo4 = (float4*)a.u32;
+    for (int base = blockIdx.x * blockDim.x + threadIdx.x; base < n4; base += kU4 * stride)
     {
-        float uv[kU32], wv[kU32], pv[kU32], sv[kU32], xv[kU32], rv[kU32], dv[kU32];
+        float4 uv[kU4], wv[kU4], pv[kU4], sv[kU4], xv[kU4], rv[kU4], dv[kU4];
+        const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-        for (int k = 0; k < kU32; k++)
+        for (int k = 0; k < kU4; k++)
         {
             const int i = base + k * stride;
-            const bool in = i < n;
-            uv[k] = in ? a.u32[i] : 0.f;
-            wv[k] = in ? a.w32[i] : 0.f;
-            pv[k] = in ? a.p32[i] : 0.f;
-            sv[k] = in ? a.s32[i] : 0.f;
-            xv[k] = in ? a.x32[i] : 0.f;
-            rv[k] = in ? a.r32[i] : 0.f;
-            dv[k] = in ? a.d32[i] : 0.f;
+            const bool in = i < n4;
+            uv[k] = in ? u4[i] : z4;
+            wv[k] = in ? w4[i] : z4;
+            pv[k] = in ? p4[i] : z4;
+            sv[k] = in ? s4[i] : z4;
+            xv[k] = in ? x4[i] : z4;
+            rv[k] = in ? r4[i] : z4;
+            dv[k] = in ? d4[i] : z4;
         }
 #pragma unroll
-        for (int k = 0; k < kU32; k++)
+        for (int k = 0; k < kU4; k++)
         {
             const int i = base + k * stride;
-            if (i < n)
+            if (i < n4)
             {
-                const float p = uv[k] + fb * pv[k];
-                const float s = wv[k] + fb * sv[k];
-                const float r = rv[k] - fa * s;
-                a.p32[i] = p;
-                a.s32[i] = s;
-                a.x32[i] = xv[k] + fa * p;
-                a.r32[i] = r;
-                a.u32[i] = r * dv[k];
+                float4 p, s, x, r, u;
+                mp_update_one(uv[k].x, wv[k].x, pv[k].x, sv[k].x, xv[k].x, rv[k].x, dv[k].x, fa, fb, p.x, s.x, x.x, r.x, u.x);
+                mp_update_one(uv[k].y, wv[k].y, pv[k].y, sv[k].y, xv[k].y, rv[k].y, dv[k].y, fa, fb, p.y, s.y, x.y, r.y, u.y);
+                mp_update_one(uv[k].z, wv[k].z, pv[k].z, sv[k].z, xv[k].z, rv[k].z, dv[k].z, fa, fb, p.z, s.z, x.z, r.z, u.z);
+                mp_update_one(uv[k].w, wv[k].w, pv[k].w, sv[k].w, xv[k].w, rv[k].w, dv[k].w, fa, fb, p.w, s.w, x.w, r.w, u.w);
+                p4[i] = p;
+                s4[i] = s;
+                x4[i] = x;
+                r4[i] = r;
+                uo4[i] = u;
             }
         }
+    }
+    for (int i = 4 * n4 + blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    {
+        float p, s, x, r, u;
+        mp_update_one(a.u32[i], a.w32[i], a.p32[i], a.s32[i], a.x32[i], a.r32[i], a.d32[i], fa, fb, p, s, x, r, u);
+        a.p32[i] = p;
+        a.s32[i] = s;
+        a.x32[i] = x;
+        a.r32[i] = r;
+        a.u32[i] = u;
     }
 }
 
