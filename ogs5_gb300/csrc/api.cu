@@ -242,6 +242,7 @@ struct ogs_system
           *val32 = nullptr, *u32 = nullptr, *w32 = nullptr;
     int fmt = -1;
     cudaGraphExec_t mp_chunk = nullptr, mp_replace = nullptr;
+    int mp_replace_scaled = 0;  // form (MixedArgs::scaled) mp_replace was captured with
     // persistent FP32 CG (OGS_SCHEDULE_PERSISTENT): the arguments of the
     // direct cooperative launches and their grid (0: graph schedule)
     MixedArgs mp_args{};
@@ -1054,7 +1055,7 @@ static ogs_status begin_fp32_refined(ogs_system* s, KState* h)
         s->fmt = want;
         auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
         const size_t v4 = al((size_t)n * sizeof(float));
-        const size_t op = s->fmt == 0 ? (size_t)m->n_up * n * sizeof(float)
+        const size_t op = s->fmt == 0 ? (size_t)m->n_up * ((n + 31) & ~31) * sizeof(float)
                         : s->fmt == 1 ? (size_t)m->sell_nnz * sizeof(float)
                                       : al(cells * sizeof(float)) + 256 + v4 + al((size_t)n);
         s->f32_bytes = 7 * v4 + op;
@@ -1079,9 +1080,14 @@ static ogs_status begin_fp32_refined(ogs_system* s, KState* h)
     MixedArgs a;
     std::memset(&a, 0, sizeof a);
     a.A.slice_ptr = m->slice_ptr; a.A.col = m->sell_col; a.A.val = s->val; a.A.n = n;
-    a.fmt = s->fmt; a.U = s->U; a.up_off = m->up_off; a.n_up = m->n_up; a.val32 = s->val32;
+    a.fmt = s->fmt; a.U = s->U; a.ustride = (n + 31) & ~31; a.up_off = m->up_off; a.n_up = m->n_up;
+    a.val32 = s->val32;
     for (int d = 0; d < 16 && d < (int)m->host_up_off.size(); d++) a.off[d] = m->host_up_off[d];
     a.d32 = s->d32; a.x = s->x; a.b = s->b; a.r64 = s->r;
+    a.dinv64 = s->dinv;
+    // stored FP32 operators iterate on the Jacobi-scaled system; the cell
+    // operator and the persistent kernel use the preconditioned form
+    a.scaled = s->fmt != 2 && c.schedule == OGS_SCHEDULE_GRAPH;
     a.x32 = s->x32; a.r32 = s->r32; a.p32 = s->p32; a.s32 = s->s32; a.u32 = s->u32; a.w32 = s->w32;
     a.st = s->st; a.n = n;
     if (s->fmt == 2)
@@ -1146,8 +1152,14 @@ static ogs_status begin_fp32_refined(ogs_system* s, KState* h)
     SolveArgs sa = make_solve_args(s);
     launch_norm_b(sa, s->stream);
     OGS_LAUNCH_CHECK();
+    if (s->mp_replace && s->mp_replace_scaled != a.scaled)
+    {
+        cudaGraphExecDestroy(s->mp_replace);  // captured for the other form
+        s->mp_replace = nullptr;
+    }
     if (!s->mp_replace)
     {
+        s->mp_replace_scaled = a.scaled;
         ogs_status st = capture(s, &s->mp_replace, [&]() { launch_mp_replace(a, s->stream); });
         if (st) return st;
     }

@@ -48,6 +48,7 @@ struct KState
     // alpha and beta of the iteration for the update kernel
     unsigned int mp_ticket, pad6;
     double mp_alpha, mp_beta;
+    double est_unit;             // |r64| / |b| estimate = est_unit * |r32| (set at each replacement)
     unsigned int ticket[8];
     double part[8][2 * kMaxBlocks];
     double cg_ps[3 * kMaxBlocks];        // per SpMV block: p . s (FP64 CG); r.u, w.u, r.r (FP32 CG)
@@ -255,12 +256,15 @@ struct MixedArgs
 {
     SellView<double> A;       // FP64 matrix
     int fmt;                  // 0: diagonal-offset upper half, 1: SELL-32 FP32
-    const float* U;           // [n_up][n]
+    const float* U;           // [n_up][ustride]
+    int ustride;              // n rounded up to 32 values: every U row starts on a 128-byte line
     const int32_t* up_off;    // [n_up]
     int n_up;
     int off[16];              // up_off by value (diagonal-offset kernels)
     const float* val32;       // SELL-32 FP32 values
-    const float* d32;         // Jacobi inverse, FP32
+    const float* d32;         // Jacobi inverse, FP32 (unscaled form)
+    const double* dinv64;     // Jacobi inverse, FP64
+    int scaled;               // 1: CG on D^-1/2 A D^-1/2 (the iterate u is r itself, no d32)
     double* x;                // FP64 solution
     const double* b;
     double* r64;

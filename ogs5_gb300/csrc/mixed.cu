@@ -18,6 +18,14 @@
 //     r64 = b - A64 x64 (FP64) ; replace r32 by r64 / |r64|, rescale p, s
 //   until |r64| / |b| < tol
 //
+// Jacobi scaling: with the diagonal S = D^-1/2 stored operators hold
+// S A S (unit diagonal) and the inner CG runs unpreconditioned on it with
+// r32 = S r64 scaled to unit norm; u = M^-1 r of the form above becomes r
+// itself, so an iteration reads neither u nor d (the same iterates in
+// exact arithmetic: S^-1 p, S^-1 x are the preconditioned directions).
+// The cell-coefficient operator and the persistent kernel keep the
+// preconditioned form.
+//
 // The FP64 residual replacement (a reliable-update form of iterative
 // refinement) keeps the FP32 Krylov space instead of restarting it, so the
 // iteration count stays close to FP64 CG.  Convergence is only ever
@@ -73,7 +81,7 @@ __device__ __forceinline__ float dia_row(const MixedArgs& a, const float* x, int
     for (int d = 1; d < NU; d++)
     {
         const int o = a.off[d];
-        const float* Ud = a.U + (size_t)d * n;
+        const float* Ud = a.U + (size_t)d * a.ustride;
         const bool up = i + o < n, lo = i - o >= 0;
         uv[2 * d - 1] = up ? __ldg(Ud + i) : 0.f;
         xv[2 * d - 1] = up ? ldx<X_NC>(x, i + o) : 0.f;
@@ -182,7 +190,15 @@ __device__ __forceinline__ float op_row(const MixedArgs& a, const float* x, int 
 }
 
 
-// U[d][i] = (float) A[i][i + off_d]; d32 = (float) (1 / a_ii)
+// S = D^-1/2 of the Jacobi scaling: 1 / sqrt(a_ii), 1 where the Jacobi
+// inverse is not positive (CG needs a positive diagonal anyway)
+__device__ __forceinline__ double jacobi_scale(double dinv)
+{
+    return dinv > 0.0 ? sqrt(dinv) : 1.0;
+}
+
+// U[d][i] = (float) A[i][i + off_d] (times s_i s_j when scaled);
+// d32 = (float) (1 / a_ii)
 __global__ void k_mp_convert(MixedArgs a, const int32_t* __restrict__ row_len,
                              const int8_t* __restrict__ slot_up, float* U, float* val32,
                              const double* __restrict__ dinv64, float* d32)
@@ -190,18 +206,20 @@ __global__ void k_mp_convert(MixedArgs a, const int32_t* __restrict__ row_len,
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x)
     {
         d32[i] = (float)dinv64[i];
+        const double si = a.scaled ? jacobi_scale(dinv64[i]) : 1.0;
         const int beg = a.A.slice_ptr[i >> 5] + (i & 31);
         const int len = row_len[i];
         for (int j = 0; j < len; j++)
         {
             const int k = beg + (j << 5);
+            const double v = a.scaled ? a.A.val[k] * si * jacobi_scale(dinv64[a.A.col[k]]) : a.A.val[k];
             if (a.fmt == 0)
             {
                 const int d = slot_up[k];
-                if (d >= 0) U[(size_t)d * a.n + i] = (float)a.A.val[k];
+                if (d >= 0) U[(size_t)d * a.ustride + i] = (float)v;
             }
             else
-                val32[k] = (float)a.A.val[k];
+                val32[k] = (float)v;
         }
     }
 }
@@ -290,7 +308,8 @@ __global__ void __launch_bounds__(kThreads) k_mp_accumulate(MixedArgs a)
     const double inv = 1.0 / st->scale;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x)
     {
-        a.x[i] += (double)a.x32[i] * inv;
+        const double si = a.scaled ? jacobi_scale(a.dinv64[i]) : 1.0;  // x = S x_scaled
+        a.x[i] += (double)a.x32[i] * inv * si;
         a.x32[i] = 0.f;
     }
 }
@@ -308,7 +327,7 @@ __global__ void __launch_bounds__(kThreads) k_mp_residual(MixedArgs a)
 {
     KState* st = a.st;
     if (st->done) return;
-    double v[1] = {0.0};
+    double v[2] = {0.0, 0.0};  // |r64|^2 ; |S r64|^2 (scaled form)
     for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < a.n; row += gridDim.x * blockDim.x)
     {
         const int s = row >> 5;
@@ -324,11 +343,17 @@ __global__ void __launch_bounds__(kThreads) k_mp_residual(MixedArgs a)
         const double r = a.b[row] - acc;
         a.r64[row] = r;
         v[0] += r * r;
+        if (a.scaled)
+        {
+            const double q = r * jacobi_scale(a.dinv64[row]);
+            v[1] += q * q;
+        }
     }
-    double out[1];
-    if (grid_sum<1, double>(v, out, st->part[0], &st->ticket[0]) && threadIdx.x == 0)
+    double out[2];
+    if (grid_sum<2, double>(v, out, st->part[0], &st->ticket[0]) && threadIdx.x == 0)
     {
         const double rn = sqrt(out[0]);
+        const double rc = a.scaled ? sqrt(out[1]) : rn;  // |r64| in the units of the inner CG
         st->error = rn / st->bnorm;
         st->replacements += 1;
         if (!isfinite(st->error)) { st->status = OGS_NONFINITE; st->done = 1; return; }
@@ -340,15 +365,17 @@ __global__ void __launch_bounds__(kThreads) k_mp_residual(MixedArgs a)
         // conditioning (cond(A) near 1/eps_fp32) the true gain falls far
         // behind the claimed one; the solve then finishes in FP64 CG from x64.
         const double claimed = st->rn_req > 0.0 ? st->rmax / st->rn_req : 1.0;
-        const double gain = st->err_prev / st->error;
+        const double ec = rc / st->bnorm;
+        const double gain = st->err_prev / ec;
         if (st->stalled || (!st->first && gain < fmin(kMinCycleGain, kCycleSlack * claimed)))
         {
             st->fallback = 1;
             st->done = 1;
             return;
         }
-        st->err_prev = st->error;
-        const double ns = rn > DBL_MIN ? 1.0 / rn : 1.0;
+        st->err_prev = ec;
+        st->est_unit = st->error;  // scaled form: r32 starts at unit norm
+        const double ns = rc > DBL_MIN ? 1.0 / rc : 1.0;
         st->ratio = st->first ? 1.0 : ns / st->scale;
         st->scale = ns;
     }
@@ -365,9 +392,14 @@ __global__ void __launch_bounds__(kThreads) k_mp_restart(MixedArgs a)
     const bool first = st->first != 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x)
     {
-        const float r = (float)(a.r64[i] * sc);
-        a.r32[i] = r;
-        a.u32[i] = r * a.d32[i];
+        if (a.scaled)
+            a.r32[i] = (float)(a.r64[i] * jacobi_scale(a.dinv64[i]) * sc);
+        else
+        {
+            const float r = (float)(a.r64[i] * sc);
+            a.r32[i] = r;
+            a.u32[i] = r * a.d32[i];
+        }
         a.p32[i] = first ? 0.f : a.p32[i] * ratio;
         a.s32[i] = first ? 0.f : a.s32[i] * ratio;
     }
@@ -411,7 +443,7 @@ __global__ void __launch_bounds__(kThreads) k_mp_dots(MixedArgs a)
     // partial sums, so the loads overlap instead of following each other
     int it = 0, base = 0, max_iter = 0, ibs[2] = {0, 0};
     double gh[2] = {0.0, 0.0}, eh[2] = {0.0, 0.0}, rbs[2] = {0.0, 0.0};
-    double rmax_prev = 0.0, scale = 1.0, bnorm = 1.0, tol = 0.0, dl = 0.0;
+    double rmax_prev = 0.0, scale = 1.0, bnorm = 1.0, tol = 0.0, dl = 0.0, eu = 0.0;
     if (threadIdx.x == 0)
     {
         it = st->iter; base = st->base_iter; max_iter = st->max_iter;
@@ -420,6 +452,7 @@ __global__ void __launch_bounds__(kThreads) k_mp_dots(MixedArgs a)
         rbs[0] = st->rbest[0]; rbs[1] = st->rbest[1];
         ibs[0] = st->itbest[0]; ibs[1] = st->itbest[1];
         rmax_prev = st->rmax; scale = st->scale; bnorm = st->bnorm; tol = st->tol; dl = st->delta;
+        eu = st->est_unit;
     }
     double g[3];
     reduce_partials<3>(st->cg_ps, st->nb_spmv, g);
@@ -432,7 +465,7 @@ __global__ void __launch_bounds__(kThreads) k_mp_dots(MixedArgs a)
     const double beta = first ? 0.0 : gamma / gh[pp];
     const double eta = first ? delta : delta - beta * beta * eh[pp];
     const double alpha = gamma / eta;
-    const double est = rn / scale / bnorm;       // estimate of |r64| / |b|
+    const double est = a.scaled ? rn * eu : rn / scale / bnorm;  // estimate of |r64| / |b|
     const bool nonfinite = !isfinite(rn) || !isfinite(alpha);
     // plateau: no new smallest |r32| in the cycle for max(64, half the
     // cycle) iterations
@@ -470,11 +503,12 @@ __global__ void __launch_bounds__(kThreads, 3) k_mp_spmv(MixedArgs a)
     if (st->done || st->replace) return;
     if (blockIdx.x == 0 && threadIdx.x == 0) st->iter += 1;  // no block of this kernel reads iter
     float v[3] = {0.f, 0.f, 0.f};
+    const float* xin = a.scaled ? a.r32 : a.u32;  // scaled form: u = r
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x)
     {
-        const float w = op_row<NU>(a, a.u32, i);
+        const float w = op_row<NU>(a, xin, i);
         a.w32[i] = w;
-        const float u = a.u32[i], r = a.r32[i];
+        const float u = xin[i], r = a.r32[i];
         v[0] += r * u;
         v[1] += w * u;
         v[2] += r * r;
@@ -766,7 +800,9 @@ __device__ __forceinline__ void mp_update_one(float u, float w, float pp, float 
     un = r * d;
 }
 
-// V: p, s, x32, r32, u32 with the alpha and beta of k_mp_dots
+// V: p, s, x32, r32 (and u32 = M^-1 r32 in the preconditioned form) with
+// the alpha and beta of k_mp_dots
+template <bool SCALED>
 __global__ void __launch_bounds__(kThreads) k_mp_update(MixedArgs a)
 {
     KState* st = a.st;
@@ -776,9 +812,10 @@ __global__ void __launch_bounds__(kThreads) k_mp_update(MixedArgs a)
     const float fb = (float)beta, fa = (float)alpha;
     // 16-byte accesses over the first 4 * (n / 4) rows (the FP32 vectors
     // are 256-byte aligned), kU4 of them per array and thread in flight;
-    // the last n % 4 rows one by one
+    // the last n % 4 rows one by one.  Scaled form: u is r itself.
     const int n = a.n, n4 = n >> 2, stride = gridDim.x * blockDim.x;
-    const float4 *u4 = (const float4*)a.u32, *w4 = (const float4*)a.w32, *d4 = (const float4*)a.d32;
+    const float4 *w4 = (const float4*)a.w32, *d4 = (const float4*)a.d32;
+    const float4* u4 = (const float4*)(SCALED ? a.r32 : a.u32);
     float4 *p4 = (float4*)a.p32, *s4 = (float4*)a.s32, *x4 = (float4*)a.x32, *r4 = (float4*)a.r32;
     float4* uo4 = (float4*)a.u32;
     for (int base = blockIdx.x * blockDim.x + threadIdx.x; base < n4; base += kU4 * stride)
@@ -790,13 +827,21 @@ __global__ void __launch_bounds__(kThreads) k_mp_update(MixedArgs a)
         {
             const int i = base + k * stride;
             const bool in = i < n4;
-            uv[k] = in ? u4[i] : z4;
             wv[k] = in ? w4[i] : z4;
             pv[k] = in ? p4[i] : z4;
             sv[k] = in ? s4[i] : z4;
             xv[k] = in ? x4[i] : z4;
             rv[k] = in ? r4[i] : z4;
-            dv[k] = in ? d4[i] : z4;
+            if constexpr (SCALED)
+            {
+                uv[k] = rv[k];
+                dv[k] = z4;
+            }
+            else
+            {
+                uv[k] = in ? u4[i] : z4;
+                dv[k] = in ? d4[i] : z4;
+            }
         }
 #pragma unroll
         for (int k = 0; k < kU4; k++)
@@ -813,19 +858,21 @@ __global__ void __launch_bounds__(kThreads) k_mp_update(MixedArgs a)
                 s4[i] = s;
                 x4[i] = x;
                 r4[i] = r;
-                uo4[i] = u;
+                if constexpr (!SCALED) uo4[i] = u;
             }
         }
     }
     for (int i = 4 * n4 + blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
     {
         float p, s, x, r, u;
-        mp_update_one(a.u32[i], a.w32[i], a.p32[i], a.s32[i], a.x32[i], a.r32[i], a.d32[i], fa, fb, p, s, x, r, u);
+        const float ri = a.r32[i];
+        mp_update_one(SCALED ? ri : a.u32[i], a.w32[i], a.p32[i], a.s32[i], a.x32[i], ri, SCALED ? 0.f : a.d32[i], fa,
+                      fb, p, s, x, r, u);
         a.p32[i] = p;
         a.s32[i] = s;
         a.x32[i] = x;
         a.r32[i] = r;
-        a.u32[i] = u;
+        if (!SCALED) a.u32[i] = u;
     }
 }
 
@@ -1144,7 +1191,10 @@ void launch_mp_iteration(const MixedArgs& a, cudaStream_t s, cudaEvent_t eb, cud
     }
     if (ee) cudaEventRecordWithFlags(ee, s, cudaEventRecordExternal);
     k_mp_dots<<<1, kThreads, 0, s>>>(a);
-    k_mp_update<<<red_grid(a.n), kThreads, 0, s>>>(a);
+    if (a.scaled)
+        k_mp_update<true><<<red_grid(a.n), kThreads, 0, s>>>(a);
+    else
+        k_mp_update<false><<<red_grid(a.n), kThreads, 0, s>>>(a);
 }
 
 }  // namespace ogs

@@ -107,10 +107,12 @@ def test_profile_counts_spmv_launches(gpu, mixed, schedule):
 
 @pytest.mark.parametrize("kind", ["hex", "tet", "hex_renumbered", "quad"])
 def test_fp32_schedules_agree(gpu, kind):
-    """The persistent cooperative kernel and the two-kernel graph schedule
-    run the same recurrence: heads within the FP32 bar of each other and of
-    FP64, iteration counts within a few (their dot products add the block
-    partials of different grids)."""
+    """The persistent cooperative kernel (preconditioned form) and the graph
+    schedule (CG on the Jacobi-scaled system) run the same recurrence in
+    exact arithmetic: heads within the FP32 bar of each other and of FP64;
+    iteration counts near FP64 CG's and within one replacement cycle of
+    each other (the last FP64 check can fall on either side of the
+    tolerance)."""
     if kind == "tet":
         m = M.structured_tet(14, 10, 8)
         ek = np.repeat(fields.lognormal_k((14, 10, 8), np.log(1e-5), 1.0, 4.0, seed=5), 6)
@@ -125,7 +127,7 @@ def test_fp32_schedules_agree(gpu, kind):
     eqs, x0 = _deck(gpu, m, ek)
     eqs.ConfigNumerics(gpu.LS_CG, gpu.PRECOND_JACOBI, 20000, 1e-10, check_norm_rhs=False)
     x64 = x0.copy()
-    eqs.Solver(x64)
+    it64 = eqs.Solver(x64)
     out = {}
     for sch in (gpu.SCHEDULE_GRAPH, gpu.SCHEDULE_PERSISTENT):
         eqs.ConfigNumerics(gpu.LS_CG, gpu.PRECOND_JACOBI, 20000, 1e-10, precision=gpu.PRECISION_FP32_REFINED,
@@ -135,10 +137,11 @@ def test_fp32_schedules_agree(gpu, kind):
         st = eqs.stats()
         assert st["status"] == gpu.OK and st["rel_residual"] < 1e-10
         assert rel_max_err(x, x64) < MIXED_RTOL
+        assert it <= 1.3 * it64 + 5
         out[sch] = (x, it)
     (xg, itg), (xp, itp) = out[gpu.SCHEDULE_GRAPH], out[gpu.SCHEDULE_PERSISTENT]
     assert rel_max_err(xp, xg) < MIXED_RTOL
-    assert abs(itp - itg) <= max(5, itg // 20)
+    assert abs(itp - itg) <= max(10, itg // 5)
 
 
 def test_schedule_rejects_unknown(gpu):
