@@ -854,8 +854,11 @@ def main():
     hbm, peak_kind = peaks()
     pr = mix["prof"]
     t_spmv = pr["spmv_ms"] / max(1, pr["spmv_launches"])
-    n_up = 14  # column offsets >= 0 of the 27-point hex pattern, diagonal included
-    spmv_bytes = (4 * n_up + 8) * N
+    # per row: the 13 stored upper off-diagonal values of the 27-point hex
+    # pattern (the Jacobi-scaled operator's unit diagonal is not stored),
+    # the iterate r (4 B) and the product w (4 B)
+    n_vals = 13
+    spmv_bytes = (4 * n_vals + 8) * N
     achieved = spmv_bytes / (t_spmv * 1e-3) / 1e9
     pr64 = f64["prof"]
     t64 = pr64["spmv_ms"] / max(1, pr64["spmv_launches"])
@@ -892,7 +895,7 @@ def main():
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                      "frac": round(achieved / hbm, 4),
                      "traffic": measured_traffic("k_mp_spmv_fp32_diagonal_hex128x128x64.md"),
-                     "kernel": "k_mp_spmv (FP32 upper-diagonal-offset SpMV + fused dots)",
+                     "kernel": "k_mp_spmv (FP32 Jacobi-scaled upper-diagonal-offset SpMV, unit diagonal, + fused dots)",
                      "bytes_per_launch": spmv_bytes, "launch_ms": round(t_spmv, 5),
                      "launches": pr["spmv_launches"], "peak_kind": peak_kind},
         "clocks": clk.summary(),

@@ -69,13 +69,13 @@ __device__ __forceinline__ float ldx(const float* x, int i)
         return x[i];
 }
 
-template <int NU, bool X_NC = true>
+template <int NU, bool X_NC = true, bool UNIT = false>
 __device__ __forceinline__ float dia_row(const MixedArgs& a, const float* x, int i)
 {
     constexpr int K = 2 * NU - 1;
     const int n = a.n;
     float uv[K], xv[K];
-    uv[0] = __ldg(a.U + i);
+    uv[0] = UNIT ? 1.f : __ldg(a.U + i);
     xv[0] = ldx<X_NC>(x, i);
 #pragma unroll
     for (int d = 1; d < NU; d++)
@@ -177,12 +177,15 @@ __device__ __forceinline__ float mf_row(const MixedArgs& a, const float* x, int 
 }
 
 // NU > 0: diagonal-offset operator with NU stored offsets; NU == 0: SELL-32;
-// NU == -1: cell coefficients of a regular hex lattice
-template <int NU, bool X_NC = true>
+// NU == -1: cell coefficients of a regular hex lattice.  UNIT: the
+// diagonal-offset operator of the Jacobi-scaled system, whose diagonal is
+// 1 and is not read (a row whose a_ii was not positive is then off by its
+// diagonal: the inner solve stops gaining and the solve ends in FP64 CG)
+template <int NU, bool X_NC = true, bool UNIT = false>
 __device__ __forceinline__ float op_row(const MixedArgs& a, const float* x, int i)
 {
     if constexpr (NU > 0)
-        return dia_row<NU, X_NC>(a, x, i);
+        return dia_row<NU, X_NC, UNIT>(a, x, i);
     else if constexpr (NU == 0)
         return sell32_row<X_NC>(a, x, i);
     else
@@ -496,7 +499,7 @@ __global__ void __launch_bounds__(kThreads) k_mp_dots(MixedArgs a)
 }
 
 // S: iter += 1 ; w32 = A32 u32 ; partials of r.u, w.u, r.r
-template <int NU>
+template <int NU, bool UNIT = false>
 __global__ void __launch_bounds__(kThreads, 3) k_mp_spmv(MixedArgs a)
 {
     KState* st = a.st;
@@ -506,7 +509,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_mp_spmv(MixedArgs a)
     const float* xin = a.scaled ? a.r32 : a.u32;  // scaled form: u = r
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x)
     {
-        const float w = op_row<NU>(a, xin, i);
+        const float w = op_row<NU, true, UNIT>(a, xin, i);
         a.w32[i] = w;
         const float u = xin[i], r = a.r32[i];
         v[0] += r * u;
@@ -1181,9 +1184,18 @@ void launch_mp_iteration(const MixedArgs& a, cudaStream_t s, cudaEvent_t eb, cud
     if (eb) cudaEventRecordWithFlags(eb, s, cudaEventRecordExternal);
     switch (a.fmt == 0 ? a.n_up : a.fmt == 2 ? -1 : 0)
     {
-        case 14: k_mp_spmv<14><<<gs, kThreads, 0, s>>>(a); break;  // hex, 27-point
-        case 8: k_mp_spmv<8><<<gs, kThreads, 0, s>>>(a); break;    // Kuhn tets, 15-point
-        case 5: k_mp_spmv<5><<<gs, kThreads, 0, s>>>(a); break;    // quads, 9-point
+        case 14:  // hex, 27-point
+            if (a.scaled) k_mp_spmv<14, true><<<gs, kThreads, 0, s>>>(a);
+            else k_mp_spmv<14><<<gs, kThreads, 0, s>>>(a);
+            break;
+        case 8:  // Kuhn tets, 15-point
+            if (a.scaled) k_mp_spmv<8, true><<<gs, kThreads, 0, s>>>(a);
+            else k_mp_spmv<8><<<gs, kThreads, 0, s>>>(a);
+            break;
+        case 5:  // quads, 9-point
+            if (a.scaled) k_mp_spmv<5, true><<<gs, kThreads, 0, s>>>(a);
+            else k_mp_spmv<5><<<gs, kThreads, 0, s>>>(a);
+            break;
         case -1:  // hex lattice, cell coefficients
             k_mp_spmv_cells<<<cell_spmv_grid(a.gx, a.gy, a.gz), 32 * kCellWarps, 0, s>>>(a);
             break;
