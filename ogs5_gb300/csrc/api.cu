@@ -1146,6 +1146,7 @@ static ogs_status begin_fp32_refined(ogs_system* s, KState* h)
     h->ratio = 1.0;
     h->first = 1;
     h->nb_spmv = s->fmt == 2 ? cell_spmv_grid(m->gx, m->gy, m->gz) : mp_spmv_grid(n);
+    a.nb_spmv = h->nb_spmv;
     h->nb_upd = red_grid(n);
     h->delta = c.inner_tol > 0.0 ? c.inner_tol : 1e-2;
     OGS_CUDA_TRY(cudaMemcpyAsync(s->st, h, kStateHeader, cudaMemcpyHostToDevice, s->stream));

@@ -44,10 +44,7 @@ struct KState
     // grid barrier of the persistent FP32 CG kernel (reset with the header)
     unsigned int bar_count, bar_gen;
     int bar_err, pad5;
-    // FP32 CG: k_mp_dots adds the product's block partials and leaves
-    // alpha and beta of the iteration for the update kernel
-    unsigned int mp_ticket, pad6;
-    double mp_alpha, mp_beta;
+    unsigned int mp_ticket, pad6;  // spare
     double est_unit;             // |r64| / |b| estimate = est_unit * |r32| (set at each replacement)
     unsigned int ticket[8];
     double part[8][2 * kMaxBlocks];
@@ -187,6 +184,25 @@ __device__ __forceinline__ bool grid_sum(const T* vin, double* out, double* part
 // last-block step or atomics.  Partial buffers are double-buffered by
 // iteration parity where a kernel reads last iteration's sums.
 // ------------------------------------------------------------------
+// One warp adds nb partials per value in FP64 (each lane a strided share,
+// then the lanes): GB300's FP64 rate makes FP64 work of the whole block
+// cost ~8x the cycles of one warp's.  out[] valid in every lane of warp 0;
+// the other warps leave at once.
+template <int NV>
+__device__ __forceinline__ bool reduce_partials_warp(const double* part, int nb, double* out)
+{
+    if (threadIdx.x >= 32) return false;
+#pragma unroll
+    for (int k = 0; k < NV; k++)
+    {
+        double s = 0.0;
+        for (int q = threadIdx.x; q < nb; q += 32) s += __ldcg(part + k * kMaxBlocks + q);
+        out[k] = s;
+    }
+    warp_allsum<NV, double>(out);
+    return true;
+}
+
 template <int NV, typename T>
 __device__ __forceinline__ void write_partials(const T* vin, double* part)
 {
@@ -271,6 +287,7 @@ struct MixedArgs
     float *x32, *r32, *p32, *s32, *u32, *w32;
     KState* st;
     int n;
+    int nb_spmv;              // blocks of the product (partials to add)
     // fmt 2: operator from one coefficient per cell of a regular hex lattice
     int gx, gy, gz;
     const float* mf_alpha;          // [cells] Laplace coefficient

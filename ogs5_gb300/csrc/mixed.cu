@@ -428,23 +428,28 @@ __global__ void __launch_bounds__(kThreads) k_mp_restart(MixedArgs a)
 // ------------------------------------------------------------------
 // FP32 CG iteration (Chronopoulos-Gear)
 // ------------------------------------------------------------------
-// r.u, w.u, r.r of the product: block partials; one block of k_mp_dots
-// adds them (fixed order) and its thread 0 does the scalar work of the
-// iteration, so the update kernel streams after reading alpha and beta
+// r.u, w.u, r.r of the product: block partials, added by the update
+// kernel's blocks
 __device__ __forceinline__ void mp_sum_products(const float (&v)[3], KState* st)
 {
     write_partials<3, float>(v, st->cg_ps);
 }
 
 // V scalars: beta = gamma / gamma_prev ; eta = delta - beta^2 eta_prev ;
-// alpha = gamma / eta ; the replacement test
-__global__ void __launch_bounds__(kThreads) k_mp_dots(MixedArgs a)
+// alpha = gamma / eta ; the replacement test.  Called by warp 0 of every
+// update block: one warp adds the product partials in FP64 (the same fixed
+// order in every block, so all blocks hold bitwise the same scalars), lane
+// 0 does the scalar work and, when `record`, writes the iteration's state.
+// Lane 0 returns stop (non-finite or a replacement is due), alpha, beta.
+__device__ __forceinline__ void mp_iteration_scalars(const MixedArgs& a, bool record, int& stop, double& alpha_out,
+                                                     double& beta_out)
+
 {
     KState* st = a.st;
-    if (st->done || st->replace) return;
-    // thread 0 loads the state it needs (both parity slots) before the
-    // partial sums, so the loads overlap instead of following each other
-    int it = 0, base = 0, max_iter = 0, ibs[2] = {0, 0};
+    // lane 0 loads the state it needs (both parity slots, and the flags that
+    // end the iteration) before the partial sums, so the loads overlap
+    // instead of following each other
+    int it = 0, base = 0, max_iter = 0, ibs[2] = {0, 0}, ended = 0;
     double gh[2] = {0.0, 0.0}, eh[2] = {0.0, 0.0}, rbs[2] = {0.0, 0.0};
     double rmax_prev = 0.0, scale = 1.0, bnorm = 1.0, tol = 0.0, dl = 0.0, eu = 0.0;
     if (threadIdx.x == 0)
@@ -456,24 +461,29 @@ __global__ void __launch_bounds__(kThreads) k_mp_dots(MixedArgs a)
         ibs[0] = st->itbest[0]; ibs[1] = st->itbest[1];
         rmax_prev = st->rmax; scale = st->scale; bnorm = st->bnorm; tol = st->tol; dl = st->delta;
         eu = st->est_unit;
+        ended = st->done | st->replace;
     }
     double g[3];
-    reduce_partials<3>(st->cg_ps, st->nb_spmv, g);
-    if (threadIdx.x != 0) return;
+    if (!reduce_partials_warp<3>(st->cg_ps, a.nb_spmv, g) || threadIdx.x != 0) return;
+    if (ended)
+    {
+        stop = 1;  // solve over or replacement pending: the product did not run
+        return;
+    }
     const int pp = (it - 1) & 1;                 // parity slot of the previous iteration
     const double gamma = g[0], delta = g[1], rn = sqrt(g[2]);
     const bool first = it == 1;                  // no search direction yet: beta = 0
     const bool fresh = it == base + 1;           // first iteration after a (re)start
     const double rmax = fresh ? rn : rmax_prev;
-    const double beta = first ? 0.0 : gamma / gh[pp];
-    const double eta = first ? delta : delta - beta * beta * eh[pp];
+    const double beta = first ? 0.0 : gamma / (pp ? gh[1] : gh[0]);
+    const double eta = first ? delta : delta - beta * beta * (pp ? eh[1] : eh[0]);
     const double alpha = gamma / eta;
     const double est = a.scaled ? rn * eu : rn / scale / bnorm;  // estimate of |r64| / |b|
     const bool nonfinite = !isfinite(rn) || !isfinite(alpha);
     // plateau: no new smallest |r32| in the cycle for max(64, half the
     // cycle) iterations
-    const double rb_prev = fresh ? rn : rbs[pp];
-    const int ib_prev = fresh ? it : ibs[pp];
+    const double rb_prev = fresh ? rn : (pp ? rbs[1] : rbs[0]);
+    const int ib_prev = fresh ? it : (pp ? ibs[1] : ibs[0]);
     const bool better = rn < rb_prev;
     const double rb = better ? rn : rb_prev;
     const int ib = better ? it : ib_prev;
@@ -481,14 +491,16 @@ __global__ void __launch_bounds__(kThreads) k_mp_dots(MixedArgs a)
     // right after a replacement r32 is the true residual (checked in FP64 by
     // k_mp_residual), so a fresh iteration never asks for another one
     const bool repl = !nonfinite && !fresh && (est < tol || rn < dl * rmax || it > max_iter || stalled);
+    stop = nonfinite || repl;
+    alpha_out = alpha;
+    beta_out = beta;
+    if (!record) return;
     if (it & 1) { st->rbest[1] = rb; st->itbest[1] = ib; }
     else { st->rbest[0] = rb; st->itbest[0] = ib; }
     if (fresh) st->rmax = rn;
     st->gam_hist[it & 1] = gamma;
     st->eta_hist[it & 1] = eta;
     st->first = 0;  // read by the replacement kernels only
-    st->mp_alpha = alpha;
-    st->mp_beta = beta;
     if (nonfinite) { st->status = OGS_NONFINITE; st->done = 1; }
     else if (repl)
     {
@@ -803,49 +815,69 @@ __device__ __forceinline__ void mp_update_one(float u, float w, float pp, float 
     un = r * d;
 }
 
-// V: p, s, x32, r32 (and u32 = M^-1 r32 in the preconditioned form) with
-// the alpha and beta of k_mp_dots
+// V: p, s, x32, r32 (and u32 = M^-1 r32 in the preconditioned form).  The
+// block's first vector loads are issued before warp 0 forms alpha and beta
+// from the product partials, so they overlap the reduction.
+template <bool SCALED>
+__device__ __forceinline__ void mp_load4(const MixedArgs& a, int i, bool in, float4& u, float4& w, float4& p, float4& s,
+                                         float4& x, float4& r, float4& d)
+{
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    w = in ? ((const float4*)a.w32)[i] : z4;
+    p = in ? ((const float4*)a.p32)[i] : z4;
+    s = in ? ((const float4*)a.s32)[i] : z4;
+    x = in ? ((const float4*)a.x32)[i] : z4;
+    r = in ? ((const float4*)a.r32)[i] : z4;
+    if constexpr (SCALED)
+    {
+        u = r;
+        d = z4;
+    }
+    else
+    {
+        u = in ? ((const float4*)a.u32)[i] : z4;
+        d = in ? ((const float4*)a.d32)[i] : z4;
+    }
+}
+
 template <bool SCALED>
 __global__ void __launch_bounds__(kThreads) k_mp_update(MixedArgs a)
 {
-    KState* st = a.st;
-    const int done = st->done, repl = st->replace;
-    const double alpha = st->mp_alpha, beta = st->mp_beta;
-    if (done || repl) return;
-    const float fb = (float)beta, fa = (float)alpha;
     // 16-byte accesses over the first 4 * (n / 4) rows (the FP32 vectors
     // are 256-byte aligned), kU4 of them per array and thread in flight;
-    // the last n % 4 rows one by one.  Scaled form: u is r itself.
+    // the last n % 4 rows one by one.  Scaled form: u is r itself.  The
+    // first loads go out before the state is read (they are in bounds and
+    // unused when the iteration has ended).
     const int n = a.n, n4 = n >> 2, stride = gridDim.x * blockDim.x;
-    const float4 *w4 = (const float4*)a.w32, *d4 = (const float4*)a.d32;
-    const float4* u4 = (const float4*)(SCALED ? a.r32 : a.u32);
-    float4 *p4 = (float4*)a.p32, *s4 = (float4*)a.s32, *x4 = (float4*)a.x32, *r4 = (float4*)a.r32;
-    float4* uo4 = (float4*)a.u32;
-    for (int base = blockIdx.x * blockDim.x + threadIdx.x; base < n4; base += kU4 * stride)
-    {
-        float4 uv[kU4], wv[kU4], pv[kU4], sv[kU4], xv[kU4], rv[kU4], dv[kU4];
-        const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 uv[kU4], wv[kU4], pv[kU4], sv[kU4], xv[kU4], rv[kU4], dv[kU4];
+    int base = blockIdx.x * blockDim.x + threadIdx.x;
 #pragma unroll
-        for (int k = 0; k < kU4; k++)
+    for (int k = 0; k < kU4; k++)
+        mp_load4<SCALED>(a, base + k * stride, base + k * stride < n4, uv[k], wv[k], pv[k], sv[k], xv[k], rv[k], dv[k]);
+    __shared__ double s_ab[2];
+    __shared__ int s_stop;
+    if (threadIdx.x < 32)
+    {
+        int stop = 0;
+        double al = 0.0, be = 0.0;
+        mp_iteration_scalars(a, blockIdx.x == 0, stop, al, be);
+        if (threadIdx.x == 0)
         {
-            const int i = base + k * stride;
-            const bool in = i < n4;
-            wv[k] = in ? w4[i] : z4;
-            pv[k] = in ? p4[i] : z4;
-            sv[k] = in ? s4[i] : z4;
-            xv[k] = in ? x4[i] : z4;
-            rv[k] = in ? r4[i] : z4;
-            if constexpr (SCALED)
-            {
-                uv[k] = rv[k];
-                dv[k] = z4;
-            }
-            else
-            {
-                uv[k] = in ? u4[i] : z4;
-                dv[k] = in ? d4[i] : z4;
-            }
+            s_ab[0] = al;
+            s_ab[1] = be;
+            s_stop = stop;
         }
+    }
+    __syncthreads();
+    if (s_stop) return;
+    const float fa = (float)s_ab[0], fb = (float)s_ab[1];
+    float4* p4 = (float4*)a.p32;
+    float4* s4 = (float4*)a.s32;
+    float4* x4 = (float4*)a.x32;
+    float4* r4 = (float4*)a.r32;
+    float4* uo4 = (float4*)a.u32;
+    while (base < n4)
+    {
 #pragma unroll
         for (int k = 0; k < kU4; k++)
         {
@@ -864,6 +896,12 @@ __global__ void __launch_bounds__(kThreads) k_mp_update(MixedArgs a)
                 if constexpr (!SCALED) uo4[i] = u;
             }
         }
+        base += kU4 * stride;
+        if (base >= n4) break;
+#pragma unroll
+        for (int k = 0; k < kU4; k++)
+            mp_load4<SCALED>(a, base + k * stride, base + k * stride < n4, uv[k], wv[k], pv[k], sv[k], xv[k], rv[k],
+                             dv[k]);
     }
     for (int i = 4 * n4 + blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
     {
@@ -1202,7 +1240,6 @@ void launch_mp_iteration(const MixedArgs& a, cudaStream_t s, cudaEvent_t eb, cud
         default: k_mp_spmv<0><<<gs, kThreads, 0, s>>>(a); break;   // SELL-32 FP32
     }
     if (ee) cudaEventRecordWithFlags(ee, s, cudaEventRecordExternal);
-    k_mp_dots<<<1, kThreads, 0, s>>>(a);
     if (a.scaled)
         k_mp_update<true><<<red_grid(a.n), kThreads, 0, s>>>(a);
     else
