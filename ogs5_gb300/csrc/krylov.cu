@@ -198,7 +198,7 @@ __global__ void __launch_bounds__(kThreads) k_cg_update(SolveArgs a)
     if (st->done) return;
     const int it = st->iter;
     double ps[1];
-    reduce_partials<1>(st->cg_ps, st->nb_spmv, ps);
+    reduce_partials_bcast<1>(st->cg_ps, st->nb_spmv, ps);
     const double alpha = cg_rz_prev(st, it) / ps[0];
     const int n = a.A.n;
     double v[2] = {0.0, 0.0};
@@ -245,7 +245,7 @@ __global__ void __launch_bounds__(kThreads) k_cg_p(SolveArgs a)
     if (st->done) return;
     const int it = st->iter;
     double rr_rz[2];
-    reduce_partials<2>(st->cg_upd[it & 1], st->nb_upd, rr_rz);
+    reduce_partials_bcast<2>(st->cg_upd[it & 1], st->nb_upd, rr_rz);
     const double rz_prev = cg_rz_prev(st, it);
     const double error = sqrt(rr_rz[0]) / st->bnorm;
     int stop = -1;

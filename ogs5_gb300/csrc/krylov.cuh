@@ -180,7 +180,7 @@ __device__ __forceinline__ bool grid_sum(const T* vin, double* out, double* part
 // Ticket-free grid sums for the CG kernels.  A producer kernel only writes
 // one partial per block and value (write_partials); every block of the
 // consumer kernel adds the partials itself, in the same fixed order
-// (reduce_partials), so all blocks hold bitwise the same total without a
+// (reduce_partials_warp / _bcast), so all blocks hold bitwise the same total without a
 // last-block step or atomics.  Partial buffers are double-buffered by
 // iteration parity where a kernel reads last iteration's sums.
 // ------------------------------------------------------------------
@@ -201,6 +201,21 @@ __device__ __forceinline__ bool reduce_partials_warp(const double* part, int nb,
     }
     warp_allsum<NV, double>(out);
     return true;
+}
+
+// reduce_partials_warp for a whole block: warp 0 adds, the totals reach
+// every thread through shared memory
+template <int NV>
+__device__ __forceinline__ void reduce_partials_bcast(const double* part, int nb, double* out)
+{
+    __shared__ double sm[NV];
+    double v[NV];
+    if (reduce_partials_warp<NV>(part, nb, v) && threadIdx.x == 0)
+#pragma unroll
+        for (int k = 0; k < NV; k++) sm[k] = v[k];
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < NV; k++) out[k] = sm[k];
 }
 
 template <int NV, typename T>
@@ -227,33 +242,6 @@ __device__ __forceinline__ void write_partials(const T* vin, double* part)
 }
 
 // out[k] = sum of part[k * kMaxBlocks + 0 .. nb-1], identical in every thread
-template <int NV>
-__device__ __forceinline__ void reduce_partials(const double* part, int nb, double* out)
-{
-    __shared__ double sm[NV][kThreads / 32];
-    double v[NV];
-#pragma unroll
-    for (int k = 0; k < NV; k++)
-    {
-        double s = 0.0;
-        for (int q = threadIdx.x; q < nb; q += blockDim.x) s += __ldcg(part + k * kMaxBlocks + q);
-        v[k] = s;
-    }
-    warp_allsum<NV, double>(v);
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (lane == 0)
-#pragma unroll
-        for (int k = 0; k < NV; k++) sm[k][wid] = v[k];
-    __syncthreads();
-#pragma unroll
-    for (int k = 0; k < NV; k++)
-    {
-        double s = 0.0;
-        for (int q = 0; q < (int)(blockDim.x >> 5); q++) s += sm[k][q];
-        out[k] = s;
-    }
-    __syncthreads();
-}
 
 // cp.async.bulk.prefetch.L2 of [p, p + bytes), widened to 16-byte
 // boundaries (the instruction's alignment rule) and clipped to [lo, hi)

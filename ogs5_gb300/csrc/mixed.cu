@@ -1009,7 +1009,7 @@ __global__ void __launch_bounds__(kThreads) k_mp_persist(MixedArgs a, int iters)
         write_partials<3, float>(v, st->cg_ps);
         if (!mp_grid_barrier(st)) break;
         double g[3];
-        reduce_partials<3>(st->cg_ps, gridDim.x, g);
+        reduce_partials_bcast<3>(st->cg_ps, gridDim.x, g);
         // V: the scalars of k_mp_update from this block's copies
         const double gamma = g[0], delta = g[1], rn = sqrt(g[2]);
         const bool first = it == 1;
