@@ -1084,7 +1084,6 @@ static ogs_status begin_fp32_refined(ogs_system* s, KState* h)
     a.val32 = s->val32;
     for (int d = 0; d < 16 && d < (int)m->host_up_off.size(); d++) a.off[d] = m->host_up_off[d];
     a.d32 = s->d32; a.x = s->x; a.b = s->b; a.r64 = s->r;
-    a.dinv64 = s->dinv;
     // stored FP32 operators iterate on the Jacobi-scaled system; the cell
     // operator and the persistent kernel use the preconditioned form
     a.scaled = s->fmt != 2 && c.schedule == OGS_SCHEDULE_GRAPH;

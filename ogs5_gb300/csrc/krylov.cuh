@@ -266,9 +266,8 @@ struct MixedArgs
     int n_up;
     int off[16];              // up_off by value (diagonal-offset kernels)
     const float* val32;       // SELL-32 FP32 values
-    const float* d32;         // Jacobi inverse, FP32 (unscaled form)
-    const double* dinv64;     // Jacobi inverse, FP64
-    int scaled;               // 1: CG on D^-1/2 A D^-1/2 (the iterate u is r itself, no d32)
+    const float* d32;         // Jacobi inverse (preconditioned form) or the scale 1 / sqrt(a_ii), FP32
+    int scaled;               // 1: CG on D^-1/2 A D^-1/2 (the iterate u is r itself)
     double* x;                // FP64 solution
     const double* b;
     double* r64;

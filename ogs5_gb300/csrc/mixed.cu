@@ -23,6 +23,7 @@
 // r32 = S r64 scaled to unit norm; u = M^-1 r of the form above becomes r
 // itself, so an iteration reads neither u nor d (the same iterates in
 // exact arithmetic: S^-1 p, S^-1 x are the preconditioned directions).
+// S is kept in FP32 (d32) and used as rounded everywhere.
 // The cell-coefficient operator and the persistent kernel keep the
 // preconditioned form.
 //
@@ -200,22 +201,28 @@ __device__ __forceinline__ double jacobi_scale(double dinv)
     return dinv > 0.0 ? sqrt(dinv) : 1.0;
 }
 
-// U[d][i] = (float) A[i][i + off_d] (times s_i s_j when scaled);
-// d32 = (float) (1 / a_ii)
+// d32: the FP32 Jacobi inverse (preconditioned form) or the FP32 scale
+// s_i (scaled form; the operator, the restart and the accumulation all use
+// these rounded values, so the transformation is exactly S A S for them)
+__global__ void k_mp_scale(MixedArgs a, const double* __restrict__ dinv64, float* d32)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x)
+        d32[i] = (float)(a.scaled ? jacobi_scale(dinv64[i]) : dinv64[i]);
+}
+
+// U[d][i] = (float) A[i][i + off_d] (times s_i s_j when scaled)
 __global__ void k_mp_convert(MixedArgs a, const int32_t* __restrict__ row_len,
-                             const int8_t* __restrict__ slot_up, float* U, float* val32,
-                             const double* __restrict__ dinv64, float* d32)
+                             const int8_t* __restrict__ slot_up, float* U, float* val32, const float* __restrict__ d32)
 {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x)
     {
-        d32[i] = (float)dinv64[i];
-        const double si = a.scaled ? jacobi_scale(dinv64[i]) : 1.0;
+        const double si = a.scaled ? (double)d32[i] : 1.0;
         const int beg = a.A.slice_ptr[i >> 5] + (i & 31);
         const int len = row_len[i];
         for (int j = 0; j < len; j++)
         {
             const int k = beg + (j << 5);
-            const double v = a.scaled ? a.A.val[k] * si * jacobi_scale(dinv64[a.A.col[k]]) : a.A.val[k];
+            const double v = a.scaled ? a.A.val[k] * si * (double)d32[a.A.col[k]] : a.A.val[k];
             if (a.fmt == 0)
             {
                 const int d = slot_up[k];
@@ -311,7 +318,7 @@ __global__ void __launch_bounds__(kThreads) k_mp_accumulate(MixedArgs a)
     const double inv = 1.0 / st->scale;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x)
     {
-        const double si = a.scaled ? jacobi_scale(a.dinv64[i]) : 1.0;  // x = S x_scaled
+        const double si = a.scaled ? (double)a.d32[i] : 1.0;  // x = S x_scaled
         a.x[i] += (double)a.x32[i] * inv * si;
         a.x32[i] = 0.f;
     }
@@ -348,7 +355,7 @@ __global__ void __launch_bounds__(kThreads) k_mp_residual(MixedArgs a)
         v[0] += r * r;
         if (a.scaled)
         {
-            const double q = r * jacobi_scale(a.dinv64[row]);
+            const double q = r * (double)a.d32[row];
             v[1] += q * q;
         }
     }
@@ -396,7 +403,7 @@ __global__ void __launch_bounds__(kThreads) k_mp_restart(MixedArgs a)
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x)
     {
         if (a.scaled)
-            a.r32[i] = (float)(a.r64[i] * jacobi_scale(a.dinv64[i]) * sc);
+            a.r32[i] = (float)(a.r64[i] * (double)a.d32[i] * sc);
         else
         {
             const float r = (float)(a.r64[i] * sc);
@@ -1100,7 +1107,8 @@ int vec_grid(int n);
 void launch_mp_convert(const MixedArgs& a, const int32_t* row_len, const int8_t* slot_up, float* U,
                        float* val32, const double* dinv64, float* d32, cudaStream_t s)
 {
-    k_mp_convert<<<vec_grid(a.n), kThreads, 0, s>>>(a, row_len, slot_up, U, val32, dinv64, d32);
+    k_mp_scale<<<vec_grid(a.n), kThreads, 0, s>>>(a, dinv64, d32);
+    k_mp_convert<<<vec_grid(a.n), kThreads, 0, s>>>(a, row_len, slot_up, U, val32, d32);
 }
 
 int red_grid(int n);
