@@ -375,6 +375,18 @@ __device__ __forceinline__ void flow_combine(const AsmArgs& a, int64_t e, const 
     double relax0 = a.p.nls_relaxation;
     if (relax0 < DBL_MIN) relax0 = 1.0;
     const double relax1 = 1.0 - relax0;
+    // the element matrices are symmetric: each distinct entry of the LHS
+    // and of the RHS operator is formed once (the same expressions as per
+    // (i, j), so the values are the same bit for bit)
+    constexpr int NL = NN * (NN + 1) / 2;
+    double Sl[NL], Tl[NL];
+#pragma unroll
+    for (int l = 0; l < NL; l++)
+    {
+        const double m = Ml[l], lp = Ll[l];
+        Sl[l] = m * dt_inverse + lp * relax0;
+        Tl[l] = m * dt_inverse - lp * relax1;
+    }
     double S[NN * NN], r[NN];
 #pragma unroll
     for (int i = 0; i < NN; i++) r[i] = 0.0;
@@ -384,9 +396,8 @@ __device__ __forceinline__ void flow_combine(const AsmArgs& a, int64_t e, const 
         for (int j = 0; j < NN; j++)
         {
             const int l = i >= j ? i * (i + 1) / 2 + j : j * (j + 1) / 2 + i;
-            const double m = Ml[l], lp = Ll[l];
-            S[i * NN + j] = m * dt_inverse + lp * relax0;
-            r[i] += (m * dt_inverse - lp * relax1) * U[j];
+            S[i * NN + j] = Sl[l];
+            r[i] += Tl[l] * U[j];
         }
     if ((a.p.pcs_type == OGS_PCS_LIQUID_FLOW || a.p.pcs_type == OGS_PCS_RICHARDS_FLOW) && a.p.gravity_on)
 #pragma unroll
@@ -475,12 +486,26 @@ __global__ void __launch_bounds__(128) k_flow_affine(AsmArgs a)
         const double mat = flow_mat(a.p, __ldg(a.elem_k + e));
         double iJ[DIM * DIM], det;
         if (!jacobian<NN, DIM>(X, Y, Z, sdNc, iJ, det)) { flag_bad(a.bad_elem, e); continue; }
+        // axis-aligned boxes: the off-diagonal entries of J^-1, hence of C,
+        // are exactly 0, and the sums over the DIM diagonal terms equal the
+        // full sums bit for bit (the other terms add +-0)
+        bool box = true;
+#pragma unroll
+        for (int p = 0; p < DIM; p++)
+#pragma unroll
+            for (int q = 0; q < DIM; q++)
+                if (p != q && iJ[p * DIM + q] != 0.0) box = false;
         double C[DIM * DIM];
 #pragma unroll
         for (int p = 0; p < DIM; p++)
 #pragma unroll
             for (int q = 0; q < DIM; q++)
             {
+                if (box && p != q)
+                {
+                    C[p * DIM + q] = 0.0;
+                    continue;
+                }
                 double s = 0.0;
 #pragma unroll
                 for (int k = 0; k < DIM; k++) s += iJ[k * DIM + p] * iJ[k * DIM + q];
@@ -488,18 +513,36 @@ __global__ void __launch_bounds__(128) k_flow_affine(AsmArgs a)
             }
         double Ml[NN * (NN + 1) / 2], Ll[NN * (NN + 1) / 2], grav[NN];
         const double md = cm * det;
+        if (box)
+        {
 #pragma unroll
-        for (int i = 0; i < NN; i++)
+            for (int i = 0; i < NN; i++)
 #pragma unroll
-            for (int j = 0; j <= i; j++)
-            {
-                const int l = i * (i + 1) / 2 + j;
-                double s = 0.0;
+                for (int j = 0; j <= i; j++)
+                {
+                    const int l = i * (i + 1) / 2 + j;
+                    double s = 0.0;
 #pragma unroll
-                for (int pq = 0; pq < DIM * DIM; pq++) s += C[pq] * sQ[(pq * NN + i) * NN + j];
-                Ll[l] = s;
-                Ml[l] = md * sM0[i * NN + j];
-            }
+                    for (int p = 0; p < DIM; p++) s += C[p * DIM + p] * sQ[((p * DIM + p) * NN + i) * NN + j];
+                    Ll[l] = s;
+                    Ml[l] = md * sM0[i * NN + j];
+                }
+        }
+        else
+        {
+#pragma unroll
+            for (int i = 0; i < NN; i++)
+#pragma unroll
+                for (int j = 0; j <= i; j++)
+                {
+                    const int l = i * (i + 1) / 2 + j;
+                    double s = 0.0;
+#pragma unroll
+                    for (int pq = 0; pq < DIM * DIM; pq++) s += C[pq] * sQ[(pq * NN + i) * NN + j];
+                    Ll[l] = s;
+                    Ml[l] = md * sM0[i * NN + j];
+                }
+        }
         if (a.p.mass_lumping) lump_mass<ET, NN>(X, Y, Z, cm, Ml);
 #pragma unroll
         for (int i = 0; i < NN; i++) grav[i] = 0.0;
