@@ -944,6 +944,20 @@ __device__ __forceinline__ double rich_mass_coef(const ogs_assembly_params& p, c
     return val;
 }
 
+// element geometry constant over the Gauss points (see k_richards)
+template <int ET>
+__device__ __forceinline__ bool const_geometry(const double* X, const double* Y, const double* Z)
+{
+    if (ET == OGS_ELEM_TET4) return true;
+    const bool rect = (X[0] == X[3] && X[1] == X[2] && Y[0] == Y[1] && Y[2] == Y[3]) ||
+                      (X[0] == X[1] && X[2] == X[3] && Y[0] == Y[3] && Y[1] == Y[2]);
+    if (ET == OGS_ELEM_QUAD4) return rect;
+    bool box = rect && Z[0] == Z[1] && Z[0] == Z[2] && Z[0] == Z[3] && Z[4] == Z[5] && Z[4] == Z[6] && Z[4] == Z[7];
+#pragma unroll
+    for (int k = 0; k < 4; k++) box = box && X[k + 4] == X[k] && Y[k + 4] == Y[k];
+    return box;
+}
+
 template <int ET, int NGP>
 __global__ void __launch_bounds__(128) k_richards(AsmArgs a)
 {
@@ -968,13 +982,30 @@ __global__ void __launch_bounds__(128) k_richards(AsmArgs a)
         for (int l = 0; l < NN * (NN + 1) / 2; l++) Ml[l] = Ll[l] = 0.0;
 #pragma unroll
         for (int i = 0; i < NN; i++) grav[i] = 0.0;
-        bool ok = true;
+        // geometry constant over the Gauss points: linear tets (constant shape
+        // gradients), and hexes / quads that are axis-aligned boxes (exact
+        // coordinate equalities; J is then diagonal, its off-diagonal sums
+        // cancel exactly): J^-1 and |J| from the first Gauss point
+        const bool cgeo = const_geometry<ET>(X, Y, Z);
+        double iJ[DIM * DIM], det = 0.0, dNg[DIM * NN];
+        bool ok = !cgeo || jacobian<NN, DIM>(X, Y, Z, sdN, iJ, det);
+        if (ok && cgeo && ET == OGS_ELEM_TET4) grad_global<NN, DIM>(iJ, sdN, dNg);
 #pragma unroll 1
-        for (int gp = 0; gp < NGP; gp++)
+        for (int gp = 0; gp < NGP && ok; gp++)
         {
-            double iJ[DIM * DIM], det, dNg[DIM * NN];
-            if (!jacobian<NN, DIM>(X, Y, Z, sdN + gp * NN * DIM, iJ, det)) { ok = false; break; }
-            grad_global<NN, DIM>(iJ, sdN + gp * NN * DIM, dNg);
+            const double* dNr = sdN + gp * NN * DIM;
+            if (!cgeo)
+            {
+                if (!jacobian<NN, DIM>(X, Y, Z, dNr, iJ, det)) { ok = false; break; }
+                grad_global<NN, DIM>(iJ, dNr, dNg);
+            }
+            else if (ET != OGS_ELEM_TET4)
+            {
+#pragma unroll
+                for (int k = 0; k < DIM; k++)
+#pragma unroll
+                    for (int i = 0; i < NN; i++) dNg[k * NN + i] = iJ[k * DIM + k] * dNr[k * NN + i];
+            }
             const double* w = sw + gp * 3;
             const double fkt = ET == OGS_ELEM_HEX8 ? det * w[0] * w[1] * w[2]
                              : ET == OGS_ELEM_QUAD4 ? det * w[0] * w[1] : det * w[0];
@@ -996,18 +1027,22 @@ __global__ void __launch_bounds__(128) k_richards(AsmArgs a)
                 if (PG < 0.0) mc += p.porosity * -rich_dsdpc(a.r, Sw);
             }
             const double mf = mc * fkt * 1.0;
+            const double cl = fkt * mat;
 #pragma unroll
             for (int i = 0; i < NN; i++)
+            {
+                const double mi = mf * sf[i];
 #pragma unroll
                 for (int j = 0; j <= i; j++)
                 {
                     const int l = i * (i + 1) / 2 + j;
-                    Ml[l] += mf * sf[i] * sf[j];
-                    double s = Ll[l];
+                    Ml[l] += mi * sf[j];
+                    double g = 0.0;
 #pragma unroll
-                    for (int k = 0; k < DIM; k++) s += fkt * dNg[k * NN + i] * mat * dNg[k * NN + j];
-                    Ll[l] = s;
+                    for (int k = 0; k < DIM; k++) g += dNg[k * NN + i] * dNg[k * NN + j];
+                    Ll[l] += cl * g;
                 }
+            }
             if (p.gravity_on)
             {
                 // Assemble_Gravity (:5859-6000): rho g, or 1 in the head form
