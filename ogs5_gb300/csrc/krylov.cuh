@@ -44,7 +44,6 @@ struct KState
     // grid barrier of the persistent FP32 CG kernel (reset with the header)
     unsigned int bar_count, bar_gen;
     int bar_err, pad5;
-    unsigned int mp_ticket, pad6;  // spare
     double est_unit;             // |r64| / |b| estimate = est_unit * |r32| (set at each replacement)
     unsigned int ticket[8];
     double part[8][2 * kMaxBlocks];
