@@ -782,21 +782,35 @@ __global__ void __launch_bounds__(128) k_mt_tet_affine(AsmArgs a)
             const double wd = det * w;
 #pragma unroll
             for (int i = 0; i < NN; i++)
+            {
+                const double wn = wd * sN[gp * NN + i];
 #pragma unroll
-                for (int j = 0; j < NN; j++) A[i * NN + j] += wd * sN[gp * NN + i] * vd[j];
+                for (int j = 0; j < NN; j++) A[i * NN + j] += wn * vd[j];
+            }
         }
+        // L = |J| G^T Ds G (G the constant gradients): T = Ds G once, then
+        // the symmetric product, one entry per pair
+        double T[DIM * NN];
+#pragma unroll
+        for (int k = 0; k < DIM; k++)
+#pragma unroll
+            for (int j = 0; j < NN; j++)
+            {
+                double t = 0.0;
+#pragma unroll
+                for (int l = 0; l < DIM; l++) t += Ds[k * DIM + l] * dNg[l * NN + j];
+                T[k * NN + j] = t;
+            }
         double L[NN * NN], Ml[NN * (NN + 1) / 2], St[NN * (NN + 1) / 2];
 #pragma unroll
         for (int i = 0; i < NN; i++)
 #pragma unroll
-            for (int j = 0; j < NN; j++)
+            for (int j = 0; j <= i; j++)
             {
                 double s = 0.0;
 #pragma unroll
-                for (int k = 0; k < DIM; k++)
-#pragma unroll
-                    for (int l = 0; l < DIM; l++) s += dNg[k * NN + i] * Ds[k * DIM + l] * dNg[l * NN + j];
-                L[i * NN + j] = det * s;
+                for (int k = 0; k < DIM; k++) s += dNg[k * NN + i] * T[k * NN + j];
+                L[i * NN + j] = L[j * NN + i] = det * s;
             }
 #pragma unroll
         for (int i = 0; i < NN; i++)
