@@ -54,10 +54,13 @@ __device__ __forceinline__ bool jacobian(const double* X, const double* Y,
         }
         det = J[0] * J[3] - J[1] * J[2];
         if (fabs(det) < DBL_EPSILON) return false;
-        iJ[0] = J[3] / det;
-        iJ[1] = -J[1] / det;
-        iJ[2] = -J[2] / det;
-        iJ[3] = J[0] / det;
+        // one FP64 division (the cofactors times 1/det; the reference divides
+        // each, the results differ by rounding only)
+        const double id = 1.0 / det;
+        iJ[0] = J[3] * id;
+        iJ[1] = -J[1] * id;
+        iJ[2] = -J[2] * id;
+        iJ[3] = J[0] * id;
     }
     else
     {
@@ -77,15 +80,16 @@ __device__ __forceinline__ bool jacobian(const double* X, const double* Y,
         det = J[0] * (J[4] * J[8] - J[7] * J[5]) + J[6] * (J[1] * J[5] - J[4] * J[2]) +
               J[3] * (J[2] * J[7] - J[8] * J[1]);
         if (fabs(det) < DBL_EPSILON) return false;
-        iJ[0] = (J[4] * J[8] - J[7] * J[5]) / det;
-        iJ[1] = (J[2] * J[7] - J[1] * J[8]) / det;
-        iJ[2] = (J[1] * J[5] - J[2] * J[4]) / det;
-        iJ[3] = (J[5] * J[6] - J[8] * J[3]) / det;
-        iJ[4] = (J[0] * J[8] - J[6] * J[2]) / det;
-        iJ[5] = (J[2] * J[3] - J[5] * J[0]) / det;
-        iJ[6] = (J[3] * J[7] - J[6] * J[4]) / det;
-        iJ[7] = (J[1] * J[6] - J[7] * J[0]) / det;
-        iJ[8] = (J[0] * J[4] - J[3] * J[1]) / det;
+        const double id = 1.0 / det;
+        iJ[0] = (J[4] * J[8] - J[7] * J[5]) * id;
+        iJ[1] = (J[2] * J[7] - J[1] * J[8]) * id;
+        iJ[2] = (J[1] * J[5] - J[2] * J[4]) * id;
+        iJ[3] = (J[5] * J[6] - J[8] * J[3]) * id;
+        iJ[4] = (J[0] * J[8] - J[6] * J[2]) * id;
+        iJ[5] = (J[2] * J[3] - J[5] * J[0]) * id;
+        iJ[6] = (J[3] * J[7] - J[6] * J[4]) * id;
+        iJ[7] = (J[1] * J[6] - J[7] * J[0]) * id;
+        iJ[8] = (J[0] * J[4] - J[3] * J[1]) * id;
     }
     det = fabs(det);
     return true;
@@ -119,15 +123,17 @@ __device__ __forceinline__ void dispersion_raw(const ogs_assembly_params& p, con
     for (int i = 0; i < DIM * DIM; i++) D[i] = 0.0;
     if (fabs(vg) > DBL_EPSILON)
     {
+        // one division per point: (alpha_L - alpha_T) / |q| times q_i q_j
+        // (the reference divides each entry; the results differ by rounding
+        // only), the symmetric entries formed once
         const double al = p.alpha_l, at = p.alpha_t;
+        const double c = (al - at) / vg;
 #pragma unroll
         for (int i = 0; i < DIM; i++)
 #pragma unroll
-            for (int j = 0; j < DIM; j++)
-                D[i * DIM + j] = ((al - at) * (v[i] * v[j])) / vg;
+            for (int j = 0; j < i; j++) D[i * DIM + j] = D[j * DIM + i] = c * (v[i] * v[j]);
 #pragma unroll
-        for (int i = 0; i < DIM; i++)
-            D[i * DIM + i] = (at * vg) + (al - at) * (v[i] * v[i]) / vg + dm;
+        for (int i = 0; i < DIM; i++) D[i * DIM + i] = (at * vg) + c * (v[i] * v[i]) + dm;
     }
     else
     {
