@@ -892,17 +892,20 @@ __device__ __forceinline__ double mrange(double a, double b, double c)
 // Genuchten) and 6 (Brooks-Corey) (rf_mmp_new.cpp:5243-5328)
 __device__ __forceinline__ double rich_saturation(const ogs_richards_params& r, double pc)
 {
+    // divisions by parameters as products with their reciprocals (loop
+    // invariants of the Gauss-point loop; rounding-level differences)
+    const double ipb = 1.0 / r.pb;
     double se;
     if (r.capillary_model == 4)
     {
         if (pc < 0.0) pc = 0.0;
-        se = pow(pc / r.pb, 1.0 / (1.0 - r.m)) + 1.0;
+        se = pow(pc * ipb, 1.0 / (1.0 - r.m)) + 1.0;
         se = pow(se, -r.m);
     }
     else
     {
         if (pc < r.pb) pc = r.pb;
-        se = pow(pc / r.pb, -r.m);
+        se = pow(pc * ipb, -r.m);
     }
     const double sl = se * (r.slm - r.slr) + r.slr;
     return mrange(r.slr + DBL_EPSILON, sl, r.slm - DBL_EPSILON);
@@ -912,21 +915,23 @@ __device__ __forceinline__ double rich_saturation(const ogs_richards_params& r, 
 // below by -1/DBL_EPSILON (rf_mmp_new.cpp:5425-5520)
 __device__ __forceinline__ double rich_dsdpc(const ogs_richards_params& r, double sl)
 {
-    double dpds;
+    // dS/dpc = 1 / (dpc/dS) formed as one quotient; divisions by
+    // parameters as products with their reciprocals
+    const double isr = 1.0 / (r.slm - r.slr);
+    double dsdp;
     if (r.capillary_model == 4)
     {
         sl = mrange(r.slr + DBL_EPSILON, sl, r.slm - DBL_EPSILON);
-        const double v1 = pow((sl - r.slr) / (r.slm - r.slr), -1.0 / r.m);
+        const double v1 = pow((sl - r.slr) * isr, -1.0 / r.m);
         const double v2 = pow(v1 - 1.0, -r.m);
-        dpds = (r.pb * (r.m - 1.0) * v1 * v2) / (r.m * (sl - r.slr));
+        dsdp = (r.m * (sl - r.slr)) / (r.pb * (r.m - 1.0) * v1 * v2);
     }
     else
     {
         sl = mrange(r.slr + DBL_EPSILON, sl, r.slm);
-        const double v1 = pow((sl - r.slr) / (r.slm - r.slr), -1.0 / r.m);
-        dpds = (r.pb * v1) / (r.m * (r.slr - sl));
+        const double v1 = pow((sl - r.slr) * isr, -1.0 / r.m);
+        dsdp = (r.m * (r.slr - sl)) / (r.pb * v1);
     }
-    double dsdp = 1.0 / dpds;
     const double lim = (-1.0) / DBL_EPSILON;
     if (dsdp < lim) dsdp = lim;
     return dsdp;
@@ -937,10 +942,13 @@ __device__ __forceinline__ double rich_dsdpc(const ogs_richards_params& r, doubl
 __device__ __forceinline__ double rich_krel(const ogs_richards_params& r, double sl)
 {
     sl = mrange(r.kr_slr, sl, r.kr_slm);
-    const double se = (sl - r.kr_slr) / (r.kr_slm - r.kr_slr);
+    const double se = (sl - r.kr_slr) * (1.0 / (r.kr_slm - r.kr_slr));
     double kr;
     if (r.permeability_model == 4)
-        kr = sqrt(se) * pow(1.0 - pow(1.0 - pow(se, 1.0 / r.kr_m), r.kr_m), 2);
+    {
+        const double b = 1.0 - pow(1.0 - pow(se, 1.0 / r.kr_m), r.kr_m);
+        kr = sqrt(se) * (b * b);
+    }
     else
         kr = pow(se, 3.0 + 2.0 / r.kr_m);
     if (kr < r.kr_min) kr = r.kr_min;
@@ -1037,7 +1045,7 @@ __global__ void __launch_bounds__(128) k_richards(AsmArgs a)
             // * kr(Sw) / mu) * fac_perm (1); CalCoefMass (:1721-1770) reuses
             // S(-PG), the same call, when unsaturated
             const double Sw = rich_saturation(a.r, -PG);
-            const double mat = ke * (p.time_unit_factor * rich_krel(a.r, Sw) / p.viscosity) * 1.0;
+            const double mat = ke * (p.time_unit_factor * rich_krel(a.r, Sw) * (1.0 / p.viscosity)) * 1.0;
             double mc = 0.0;
             if (!p.steady)
             {
