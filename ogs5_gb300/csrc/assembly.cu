@@ -650,12 +650,14 @@ __global__ void __launch_bounds__(128) k_mt_general(AsmArgs a)
         int nd[NN];
         double X[NN], Y[NN], Z[NN], U[NN];
         gather<NN>(a, e, nd, X, Y, Z, U);
-        double Ml[NN * (NN + 1) / 2], St[NN * (NN + 1) / 2], L[NN * NN], A[NN * NN];
+        // Ls: the symmetric dispersion term, lower triangle (expanded for
+        // the combine)
+        double Ml[NN * (NN + 1) / 2], St[NN * (NN + 1) / 2], Ls[NN * (NN + 1) / 2], A[NN * NN];
         double Mx[SUPG ? NN * NN : 1];
 #pragma unroll
-        for (int l = 0; l < NN * (NN + 1) / 2; l++) Ml[l] = St[l] = 0.0;
+        for (int l = 0; l < NN * (NN + 1) / 2; l++) Ml[l] = St[l] = Ls[l] = 0.0;
 #pragma unroll
-        for (int k = 0; k < NN * NN; k++) L[k] = A[k] = 0.0;
+        for (int k = 0; k < NN * NN; k++) A[k] = 0.0;
 #pragma unroll
         for (int k = 0; k < (SUPG ? NN * NN : 1); k++) Mx[k] = 0.0;
         const double Lsupg = SUPG ? supg_length<ET>(X, Y, Z, p.supg_length) : 0.0;
@@ -678,31 +680,43 @@ __global__ void __launch_bounds__(128) k_mt_general(AsmArgs a)
             const double fs = fkt * cs;
             const double vt[3] = {1.0 * p.time_unit_factor * v[0], 1.0 * p.time_unit_factor * v[1],
                                   1.0 * p.time_unit_factor * v[2]};
+            // the Gauss-point sums with their factors hoisted: T = D grad N
+            // once, the symmetric dispersion term over distinct pairs,
+            // vd_j = v . grad N_j once (rounding-level differences from the
+            // per-entry products)
+            double T[DIM * NN], vd[NN];
+#pragma unroll
+            for (int j = 0; j < NN; j++)
+            {
+                double q = 0.0;
+#pragma unroll
+                for (int k = 0; k < DIM; k++)
+                {
+                    double t = 0.0;
+#pragma unroll
+                    for (int l2 = 0; l2 < DIM; l2++) t += D[DIM * k + l2] * dNg[l2 * NN + j];
+                    T[k * NN + j] = t;
+                    q += vt[k] * dNg[k * NN + j];
+                }
+                vd[j] = q;
+            }
 #pragma unroll
             for (int i = 0; i < NN; i++)
             {
+                const double mi = mf * sf[i], si = fs * sf[i], ai = fkt * sf[i];
 #pragma unroll
                 for (int j = 0; j <= i; j++)
                 {
                     const int l = i * (i + 1) / 2 + j;
-                    Ml[l] += mf * sf[i] * sf[j];
-                    St[l] += fs * sf[i] * sf[j];
+                    Ml[l] += mi * sf[j];
+                    St[l] += si * sf[j];
+                    double g = 0.0;
+#pragma unroll
+                    for (int k = 0; k < DIM; k++) g += dNg[k * NN + i] * T[k * NN + j];
+                    Ls[l] += fkt * g;
                 }
 #pragma unroll
-                for (int j = 0; j < NN; j++)
-                {
-                    double s = L[i * NN + j], t = A[i * NN + j];
-#pragma unroll
-                    for (int k = 0; k < DIM; k++)
-                    {
-#pragma unroll
-                        for (int l2 = 0; l2 < DIM; l2++)
-                            s += fkt * dNg[k * NN + i] * D[DIM * k + l2] * dNg[l2 * NN + j];
-                        t += fkt * sf[i] * vt[k] * dNg[k * NN + j];
-                    }
-                    L[i * NN + j] = s;
-                    A[i * NN + j] = t;
-                }
+                for (int j = 0; j < NN; j++) A[i * NN + j] += ai * vd[j];
             }
             if constexpr (SUPG)
             {
@@ -730,6 +744,11 @@ __global__ void __launch_bounds__(128) k_mt_general(AsmArgs a)
             }
         }
         if (!ok) { flag_bad(a.bad_elem, e); continue; }
+        double L[NN * NN];
+#pragma unroll
+        for (int i = 0; i < NN; i++)
+#pragma unroll
+            for (int j = 0; j < NN; j++) L[i * NN + j] = Ls[i >= j ? i * (i + 1) / 2 + j : j * (j + 1) / 2 + i];
         if (p.mass_lumping)
         {
             // CalcLumpedMass has no SUPG term
