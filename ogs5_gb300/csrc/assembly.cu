@@ -445,18 +445,22 @@ __global__ void __launch_bounds__(128) k_flow_general(AsmArgs a)
                              : ET == OGS_ELEM_QUAD4 ? det * w[0] * w[1] : det * w[0];
             const double* sf = sN + gp * NN;
             const double mf = cm * fkt * 1.0;
+            const double cl = fkt * mat;  // the Gauss-point factors hoisted
 #pragma unroll
             for (int i = 0; i < NN; i++)
+            {
+                const double mi = mf * sf[i];
 #pragma unroll
                 for (int j = 0; j <= i; j++)
                 {
                     const int l = i * (i + 1) / 2 + j;
-                    Ml[l] += mf * sf[i] * sf[j];
-                    double s = Ll[l];
+                    Ml[l] += mi * sf[j];
+                    double g = 0.0;
 #pragma unroll
-                    for (int k = 0; k < DIM; k++) s += fkt * dNg[k * NN + i] * mat * dNg[k * NN + j];
-                    Ll[l] = s;
+                    for (int k = 0; k < DIM; k++) g += dNg[k * NN + i] * dNg[k * NN + j];
+                    Ll[l] += cl * g;
                 }
+            }
             if (a.p.pcs_type == OGS_PCS_LIQUID_FLOW && a.p.gravity_on)
             {
                 const double rho = a.p.gravity < DBL_EPSILON ? 1.0 : a.p.density * a.p.gravity;
