@@ -31,6 +31,7 @@ import json
 import os
 import statistics
 import subprocess
+import tempfile
 import sys
 import time
 
@@ -75,10 +76,11 @@ class ClockSampler:
     def __init__(self, dev=0):
         self.dev = dev
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks.csv")
+        # raw samples in a temporary file; the summary goes into the JSON line
+        fd, self.path = tempfile.mkstemp(prefix="ogs_clocks_", suffix=".csv")
+        os.close(fd)
 
     def __enter__(self):
-        os.makedirs(os.path.dirname(self.path), exist_ok=True)
         try:
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.dev}", f"--query-gpu={self.Q}",
