@@ -68,6 +68,48 @@ def test_assembly_groundwater_flow(gpu, oracle, kind, distorted, ngauss):
     assert_vector_close(b, ob)
 
 
+def sheared(m):
+    """The mesh under one linear map of its coordinates: every element stays
+    affine (a parallelepiped / parallelogram) but none is an axis-aligned box,
+    so the affine kernels take their full-tensor branch."""
+    import copy
+    s = copy.copy(m)
+    x, y = m.x.astype(float), m.y.astype(float)
+    z = m.z.astype(float) if m.dim == 3 else np.zeros_like(x)
+    s.x = x + 0.31 * y + 0.17 * z
+    s.y = 0.93 * y + 0.22 * z - 0.12 * x
+    if m.dim == 3:
+        s.z = 1.07 * z + 0.05 * x
+    return s
+
+
+@pytest.mark.parametrize("kind", ["quad", "hex", "tet"])
+@pytest.mark.parametrize("pcs", ["gwf", "liquid", "transport"])
+def test_assembly_sheared_affine(gpu, oracle, kind, pcs):
+    """Affine, non-box elements through the affine kernels: entries within
+    1e-12 of the oracle for each process."""
+    m = sheared(small_mesh(kind))
+    rng = np.random.default_rng(21)
+    u0 = rng.uniform(0, 10, m.n_nodes)
+    if pcs == "transport":
+        ngp = {"quad": 9, "hex": 27, "tet": 5}[kind]
+        gpv = rng.normal(0, 1e-5, (m.n_elements, ngp, 3))
+        if m.dim == 2:
+            gpv[:, :, 2] = 0.0
+        p = gpu.make_params(gpu.MASS_TRANSPORT, dt=3600.0, theta=0.6, porosity=0.3,
+                            alpha_l=1.0, alpha_t=0.1, diffusion=1e-9, decay=1e-7, retardation=1.5)
+        _, _, (rp, col, val, b), (oval, ob) = run_assembly(gpu, oracle, m, p, None, u0, gpv)
+    elif pcs == "liquid":
+        p = gpu.make_params(gpu.LIQUID_FLOW, dt=100.0, storage=1e-9, porosity=0.3, drho_dp=4.5e-10,
+                            viscosity=1e-3, density=1000.0, gravity=9.81, gravity_on=1)
+        _, _, (rp, col, val, b), (oval, ob) = run_assembly(gpu, oracle, m, p, k_field(m, 4) * 1e-7, u0)
+    else:
+        p = gpu.make_params(gpu.GROUNDWATER_FLOW, dt=3600.0, storage=1e-4, mass_lumping=1)
+        _, _, (rp, col, val, b), (oval, ob) = run_assembly(gpu, oracle, m, p, k_field(m, 5), u0)
+    assert_matrix_close(rp, val, oval)
+    assert_vector_close(b, ob)
+
+
 @pytest.mark.parametrize("kind", ["quad", "hex", "tet"])
 def test_assembly_groundwater_relaxation_and_steady(gpu, oracle, kind):
     m = small_mesh(kind)
