@@ -19,6 +19,8 @@ def _mesh(kind):
         return M.structured_quad(10, 14, 0.2, 0.1)
     if kind == "hex":
         return distort(M.structured_hex(4, 3, 8, 0.5, 0.5, 0.25), 0.1, seed=3)
+    if kind == "hex_box":  # axis-aligned boxes: the constant-geometry path
+        return M.structured_hex(4, 3, 8, 0.5, 0.5, 0.25)
     return M.structured_tet(3, 3, 5, 0.5, 0.5, 0.3)
 
 
@@ -43,7 +45,7 @@ def _pressure(m, seed):
     return RHO_G * (0.4 * top - h) * 4.0 + rng.normal(0.0, 500.0, m.n_nodes)
 
 
-@pytest.mark.parametrize("kind", ["quad", "hex", "tet"])
+@pytest.mark.parametrize("kind", ["quad", "hex", "hex_box", "tet"])
 @pytest.mark.parametrize("opts", [(4, 0, 0), (4, 1, 1), (6, 1, 0), (6, 0, 1)])
 def test_richards_assembly_matches_oracle(gpu, oracle, kind, opts):
     model, gravity, lumping = opts
