@@ -120,9 +120,11 @@ typedef struct
 typedef struct
 {
     int32_t pcs_type;          /* ogs_pcs_type                                 */
-    int32_t steady;            /* TimType::STEADY: no mass matrix
-                                  (fem_ele_std.cpp:8549); for flow the same
-                                  as storage 0                                 */
+    int32_t steady;            /* TimType::STEADY.  MASS_TRANSPORT: no mass
+                                  matrix (fem_ele_std.cpp:8549).  Flow
+                                  processes ignore it: AssembleParabolicEquation
+                                  (:7702) keeps M/dt, so a steady flow deck is
+                                  one with storage 0                           */
     double dt;                 /* pcs->Tim->time_step_length                   */
     double theta;              /* m_num->ls_theta, MT time weighting           */
     double nls_relaxation;     /* m_num->nls_relaxation, flow LHS weight;

@@ -314,10 +314,11 @@ __device__ __forceinline__ void lump_mass(const double* X, const double* Y, cons
         for (int j = 0; j <= i; j++) Ml[i * (i + 1) / 2 + j] = i == j ? f : 0.0;
 }
 
-// CalCoefMass for GWF (StorageFunction) and LIQUID_FLOW (Ss + n drho/dp)
+// CalCoefMass for GWF (StorageFunction) and LIQUID_FLOW (Ss + n drho/dp).
+// AssembleParabolicEquation (fem_ele_std.cpp:7702-8126) has no steady branch:
+// a STEADY flow process keeps M/dt, so p.steady is not read here.
 __device__ __forceinline__ double flow_mass_coef(const ogs_assembly_params& p)
 {
-    if (p.steady) return 0.0;
     if (p.pcs_type == OGS_PCS_LIQUID_FLOW) return p.storage + p.porosity * p.drho_dp;
     return p.storage;
 }
@@ -1069,8 +1070,7 @@ __global__ void __launch_bounds__(128) k_richards(AsmArgs a)
             // S(-PG), the same call, when unsaturated
             const double Sw = rich_saturation(a.r, -PG);
             const double mat = ke * (p.time_unit_factor * rich_krel(a.r, Sw) * (1.0 / p.viscosity)) * 1.0;
-            double mc = 0.0;
-            if (!p.steady)
+            double mc;
             {
                 const double Sm = PG < 0.0 ? Sw : 1.0;
                 mc = p.storage * Sm;
@@ -1111,7 +1111,7 @@ __global__ void __launch_bounds__(128) k_richards(AsmArgs a)
             double PG = 0.0;
 #pragma unroll
             for (int i = 0; i < NN; i++) PG += U1[i] * (1.0 / NN);
-            lump_mass<ET, NN>(X, Y, Z, p.steady ? 0.0 : rich_mass_coef(p, a.r, PG), Ml);
+            lump_mass<ET, NN>(X, Y, Z, rich_mass_coef(p, a.r, PG), Ml);
         }
         flow_combine<NN>(a, e, nd, U, Ml, Ll, grav);
     }

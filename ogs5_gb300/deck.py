@@ -29,12 +29,14 @@ def write_msh(mesh: M.Mesh, path: str) -> None:
 def write_gli(path: str, points, polylines=None, surfaces=None) -> None:
     """points: [(x, y, z) or (x, y, z, name)]; polylines: {name: ([point
     indices], epsilon or None)}; surfaces: {name: [polyline names]}.  Point
-    ids are zero-based."""
+    ids are zero-based.  A point name is followed by a space: the reference's
+    readPoints registers a name only up to the next blank
+    (FileIO/OGSIOVer4.cpp:92-97)."""
     with open(path, "w") as f:
         f.write("#POINTS\n")
         for i, p in enumerate(points):
             f.write("%d %.17g %.17g %.17g" % (i, p[0], p[1], p[2]))
-            f.write(" $NAME %s\n" % p[3] if len(p) > 3 else "\n")
+            f.write(" $NAME %s \n" % p[3] if len(p) > 3 else "\n")
         for name, (ids, eps) in (polylines or {}).items():
             f.write("#POLYLINE\n $NAME\n  %s\n" % name)
             if eps is not None:

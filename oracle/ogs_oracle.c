@@ -567,7 +567,9 @@ int orc_element_matrices(int etype, int ngauss, int dim, const double* X,
         c_mass = p->porosity * p->saturation * p->retardation;
         c_stor = p->porosity * p->saturation * p->decay * p->retardation;
     }
-    if (p->steady) c_mass = 0.0;
+    /* only the transport assembly drops the mass matrix of a STEADY process
+     * (fem_ele_std.cpp:8549); AssembleParabolicEquation has no such branch */
+    if (p->steady && p->pcs_type == OGS_PCS_MASS_TRANSPORT) c_mass = 0.0;
 
     double X3[8], Y3[8], Z3[8];
     for (int i = 0; i < nn; i++)
@@ -985,7 +987,7 @@ int orc_element_matrices_richards(int etype, int ngauss, int dim, const double* 
         const double* sf = N + gp * nn;
         for (int i = 0; i < nn; i++) PG += u1[i] * sf[i]; /* interpolate(NodalVal1) */
         const double mat = orc_rich_lap_coef(p, r, k_e, PG);
-        const double mf = (p->steady ? 0.0 : orc_rich_mass_coef(p, r, PG)) * fkt * 1.0;
+        const double mf = orc_rich_mass_coef(p, r, PG) * fkt * 1.0;
         for (int i = 0; i < nn; i++)
             for (int j = 0; j <= i; j++) m->mass[i * nn + j] += mf * sf[i] * sf[j];
         for (int i = 0; i < nn; i++)
@@ -1011,7 +1013,7 @@ int orc_element_matrices_richards(int etype, int ngauss, int dim, const double* 
     {
         double PG = 0.0, factor;
         for (int i = 0; i < nn; i++) PG += u1[i] * (1.0 / nn);
-        factor = p->steady ? 0.0 : orc_rich_mass_coef(p, r, PG);
+        factor = orc_rich_mass_coef(p, r, PG);
         factor *= 1.0;
         factor *= orc_element_volume(etype, X3, Y3, Z3) / (double)nn;
         for (int i = 0; i < nn * nn; i++) m->mass[i] = 0.0;

@@ -36,7 +36,7 @@ GWF, LIQUID, MT = 0, 1, 2
 
 def build(ref: str | None = None) -> None:
     """Runs oracle/Makefile (C restatement; reference harness when present)."""
-    args = ["make", "-s", "-C", HERE]
+    args = ["make", "-s", "-j", str(min(16, os.cpu_count() or 1)), "-C", HERE]
     if ref:
         args.append(f"REF={ref}")
     subprocess.run(args, check=True)

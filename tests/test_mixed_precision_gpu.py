@@ -15,7 +15,10 @@ MIXED_RTOL = 1e-8
 
 
 def _deck(gpu, m, ek, left=10.0, right=0.0, steady=False):
-    p = gpu.make_params(gpu.GROUNDWATER_FLOW, dt=3600.0, storage=1e-4, steady=1 if steady else 0)
+    # a steady flow system has no storage (the flow assembly keeps M/dt
+    # whatever the time type)
+    p = gpu.make_params(gpu.GROUNDWATER_FLOW, dt=3600.0, storage=0.0 if steady else 1e-4,
+                        steady=1 if steady else 0)
     gm = gpu.GpuMesh(m)
     eqs = gpu.LinearEQS(gm)
     eqs.Initialize()
@@ -214,7 +217,8 @@ def test_cell_coefficient_operator(gpu, case):
                             viscosity=1e-3, density=1000.0, gravity=9.81, gravity_on=1)
         ek = ek * 1e-7
     else:
-        p = gpu.make_params(gpu.GROUNDWATER_FLOW, dt=3600.0, storage=1e-4, steady=1 if case == "steady" else 0)
+        p = gpu.make_params(gpu.GROUNDWATER_FLOW, dt=3600.0, storage=0.0 if case == "steady" else 1e-4,
+                            steady=1 if case == "steady" else 0)
     mode = gpu.DIRICHLET_ROW_ONLY if case == "row_only" else gpu.DIRICHLET_SYMMETRIC
     eqs, x0 = _hex_system(gpu, m, ek, p, mode, repeat=2 if case == "twice" else 1)
     st = _solve_pair(gpu, eqs, x0)
