@@ -432,19 +432,21 @@ ogs_status ogs_gpu_profile(ogs_system* sys, int32_t enable, ogs_profile* out);
 
 /* Jacobi-preconditioned CG that allocates no device memory.  It has no
  * counterpart in the reference.  It is for callers that cannot call
- * cudaMalloc -- a process whose HBM is owned by a caching allocator or
- * memory pool (a solve server, a PyTorch process), or host code running
- * while a stream is captured in global mode.  The caller owns every array
- * (device memory): the CSR matrix (row_ptr n+1, col and val row_ptr[n]
- * entries), b (n) and x (n, initial guess in, solution out).  The Krylov
- * vectors, scalars and reduction partials live in a static device array of
- * OGS_NOALLOC_MAX_ROWS rows (16 MiB, held by every GPU that loads the
- * library until exit); larger systems are rejected with OGS_BAD_ARG.  The
- * first call on a device looks up the array's address and must come before
- * any stream capture.  All calls share the array: calls whose work overlaps
- * on the GPU race and must be serialised by the caller.  Iteration and
- * stopping rule are those of Linear_EQS::CG for a fresh system (tol relative
- * to |b|, at most max_iter iterations).  stream: a cudaStream_t or NULL. */
+ * cudaMalloc: a process whose HBM is already owned by a caching allocator or
+ * memory pool (a solve server, a PyTorch process), where every buffer a
+ * solver allocates fails or fragments the pool.  The caller owns every
+ * array (device memory): the CSR matrix (row_ptr n+1, col and val
+ * row_ptr[n] entries), b (n) and x (n, initial guess in, solution out).  The
+ * Krylov vectors, scalars and reduction partials live in a static device
+ * array of OGS_NOALLOC_MAX_ROWS rows (16 MiB, held by every GPU that loads
+ * the library until exit); larger systems are rejected with OGS_BAD_ARG.
+ * The first call on a device looks up the array's address (do it before any
+ * stream capture); cudaDeviceReset after it is not supported.  The call
+ * reads the solver state back and synchronises its stream every 16
+ * iterations.  All calls share the array: calls whose work overlaps on the
+ * GPU race and must be serialised by the caller.  Iteration and stopping
+ * rule are those of Linear_EQS::CG for a fresh system (tol relative to |b|,
+ * at most max_iter iterations).  stream: a cudaStream_t or NULL. */
 #define OGS_NOALLOC_MAX_ROWS 524288
 ogs_status ogs_gpu_csr_cg_noalloc(int64_t n, const int32_t* row_ptr,
                                   const int32_t* col, const double* val,

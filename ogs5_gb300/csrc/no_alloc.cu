@@ -2,11 +2,11 @@
 //
 // Some callers cannot call cudaMalloc: a process whose device memory is
 // owned by a caching allocator or memory pool that has already reserved
-// the HBM (a solve server, a PyTorch process), or host code that runs while
-// a stream is captured in global mode, where cudaMalloc is an error.  For
-// them ogs_gpu_csr_cg_noalloc solves A x = b on a CSR matrix they own, with
-// the Krylov vectors (r, p, s and the Jacobi inverse), the solver scalars
-// and the reduction partials in the file-scope array below.
+// the HBM (a solve server, a PyTorch process) gets an out-of-memory error,
+// or an allocation that fragments the pool, for every buffer a solver asks
+// for.  For them ogs_gpu_csr_cg_noalloc solves A x = b on a CSR matrix they
+// own, with the Krylov vectors (r, p, s and the Jacobi inverse), the solver
+// scalars and the reduction partials in the file-scope array below.
 //
 //  * The array holds OGS_NOALLOC_MAX_ROWS rows worth of vectors (4 x 8 B per
 //    row, 16 MiB, plus 256 KiB of reduction partials); every GPU that loads
@@ -14,7 +14,9 @@
 //  * Host code cannot use the array's name as a device address, so the
 //    first call on each device (with that device current) looks the address
 //    up with cudaGetSymbolAddress and caches it.  Make that first call
-//    before any stream capture.
+//    before any stream capture.  The cached address is not looked up again:
+//    cudaDeviceReset after the first call on a device is not supported (the
+//    module may be loaded again at another address).
 //  * All calls share the array and it keeps the last call's contents: each
 //    call clears the counters and flags that must start at zero.  Calls
 //    whose work overlaps on the GPU (different streams, or threads) race on
@@ -282,7 +284,7 @@ extern "C" ogs_status ogs_gpu_csr_cg_noalloc(int64_t n, const int32_t* row_ptr, 
     {
         OGS_CUDA_TRY(cudaMemcpyAsync(&h, a.st, sizeof h, cudaMemcpyDeviceToHost, s));
         OGS_CUDA_TRY(cudaStreamSynchronize(s));
-        if (h.done || done_iters > max_iter + kChunk) break;
+        if (h.done || (int64_t)done_iters > (int64_t)max_iter + kChunk) break;
         for (int k = 0; k < kChunk; k++)
         {
             k_na_spmv<<<g, kThreads, 0, s>>>(a);

@@ -1,9 +1,12 @@
 """ogs_gpu_csr_cg_noalloc: the CG entry point for callers that cannot
-allocate device memory (their HBM belongs to a caching allocator or memory
-pool, or they run while a stream is captured in global mode).  It must give
-the same heads as the regular solver (ogs_gpu_solve, same tolerance as the
-other solver parity tests: 1e-10 relative) on two calls in a row, since all
-calls share one static scratch array that keeps the previous contents.
+allocate device memory (their HBM already belongs to a caching allocator or
+memory pool, where each solver buffer would fail or fragment the pool).  It
+must give the same heads as the regular solver (ogs_gpu_solve, same
+tolerance as the other solver parity tests: 1e-10 relative) on two calls in
+a row, since all calls share one static scratch array that keeps the
+previous contents; a following call on a smaller, different system must not
+see the larger system's leftovers; and a call must leave the device's free
+memory unchanged.
 
 This file is collected last on purpose: if it fails, a run that stops at the
 first failure has already run every other test."""
@@ -46,12 +49,45 @@ def test_noalloc_cg_matches_regular_solver_twice(gpu):
     b_d = torch.tensor(b, device="cuda")
     for call in range(2):
         x_d = torch.tensor(x0, device="cuda")
+        torch.cuda.synchronize()
+        free_before = torch.cuda.mem_get_info()[0]
         st = gpu.csr_cg_noalloc(rp_d, col_d, val_d, b_d, x_d, max_iter=5000, tol=1e-12)
         torch.cuda.synchronize()
+        if call == 1:
+            # nothing allocated (the first call may load this library's
+            # kernels, which the driver does lazily)
+            assert torch.cuda.mem_get_info()[0] == free_before
         assert st["status"] == gpu.OK, (call, st)
         assert st["rel_residual"] < 1e-12
         assert abs(st["iterations"] - it_ref) <= 2, (call, st["iterations"], it_ref)
         assert rel_max_err(x_d.cpu().numpy(), x_ref) < SOLUTION_RTOL, call
+    # a smaller, different system after the larger one: the shared scratch
+    # still holds the larger system's vectors past the new system's rows
+    m2 = M.structured_quad(60, 45)
+    ek2 = fields.lognormal_k(m2.shape, np.log(1e-4), 0.5, 4.0, seed=3)
+    gm2 = gpu.GpuMesh(m2)
+    eqs2 = gpu.LinearEQS(gm2)
+    eqs2.Initialize()
+    eqs2.GlobalAssembly(gpu.make_params(gpu.GROUNDWATER_FLOW, dt=100.0, storage=1e-3), ek2,
+                        np.zeros(m2.n_nodes))
+    lf2, rf2 = m2.face_nodes(1, 0), m2.face_nodes(1, 1)
+    eqs2.SetKnownX(np.concatenate([lf2, rf2]), np.concatenate([np.full(len(lf2), 3.0), np.full(len(rf2), 1.0)]),
+                   gpu.DIRICHLET_SYMMETRIC)
+    rp2, col2, val2 = eqs2.get_csr()
+    b2 = eqs2.get_rhs()
+    x02 = np.zeros(m2.n_nodes)
+    x02[lf2], x02[rf2] = 3.0, 1.0
+    eqs2.ConfigNumerics(gpu.LS_CG, gpu.PRECOND_JACOBI, 5000, 1e-12, check_norm_rhs=False)
+    x_ref2 = x02.copy()
+    eqs2.Solver(x_ref2)
+    x2_d = torch.tensor(x02, device="cuda")
+    st2 = gpu.csr_cg_noalloc(torch.tensor(rp2.astype(np.int32), device="cuda"),
+                             torch.tensor(col2.astype(np.int32), device="cuda"),
+                             torch.tensor(val2, device="cuda"), torch.tensor(b2, device="cuda"), x2_d,
+                             max_iter=5000, tol=1e-12)
+    torch.cuda.synchronize()
+    assert st2["status"] == gpu.OK, st2
+    assert rel_max_err(x2_d.cpu().numpy(), x_ref2) < SOLUTION_RTOL
 
 
 def test_noalloc_rejects_oversized_and_host_arrays(gpu):
