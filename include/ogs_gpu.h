@@ -411,6 +411,19 @@ int32_t ogs_gpu_mesh_gauss_points(const ogs_mesh* mesh);
  * last reset (instrumentation for benchmarks). */
 int64_t ogs_gpu_kernel_launches(int32_t reset);
 
+/* Self-test of the bounded waits of the two cooperative persistent kernels
+ * (no counterpart in the reference).  Launches `grid` blocks (0: two per
+ * SM, the most allowed) that each pass one grid barrier of the persistent
+ * FP32 CG kernel (which = 0) or of the Monte-Carlo batch kernel (which = 1),
+ * the wait limited to `spin_limit` polls of the barrier word (0: the
+ * kernel's own limit, about a second).  withhold != 0: block 0 leaves
+ * without arriving, so the other blocks wait on a word nothing sets until
+ * the limit and give up.  *passed: the blocks that passed.  Returns OGS_OK
+ * when every arriving block passed, OGS_CUDA_ERROR with "barrier timeout"
+ * in ogs_gpu_last_error when a wait gave up (the context stays usable). */
+ogs_status ogs_gpu_selftest_barrier(int32_t which, int32_t grid, int32_t spin_limit, int32_t withhold,
+                                    int32_t* passed);
+
 /* Device time of the SpMV kernel of every Krylov iteration, measured with
  * CUDA events recorded around it inside the captured iteration graphs
  * (instrumentation, no counterpart in the reference). */

@@ -52,6 +52,7 @@ EXPORTS = [
     "ogs_gpu_server_progress", "ogs_gpu_server_result", "ogs_gpu_server_info", "ogs_gpu_server_reserve",
     "ogs_gpu_cache_reset", "ogs_gpu_assemble_richards", "ogs_gpu_richards_step",
     "ogs_deck_read", "ogs_deck_destroy", "ogs_deck_mesh", "ogs_deck_geo_nodes", "ogs_deck_dirichlet",
+    "ogs_gpu_selftest_barrier",
 ]
 REQUEST_FLOW, REQUEST_TRANSPORT = 0, 1
 RICHARDS_FLOW = 3
@@ -281,6 +282,8 @@ def lib():
             getattr(L, name).restype = st
         L.ogs_gpu_kernel_launches.argtypes = [C.c_int32]
         L.ogs_gpu_kernel_launches.restype = C.c_int64
+        L.ogs_gpu_selftest_barrier.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_int32)]
+        L.ogs_gpu_selftest_barrier.restype = st
         for name in ("ogs_gpu_mesh_create", "ogs_gpu_mesh_destroy", "ogs_gpu_mesh_info",
                      "ogs_gpu_system_create", "ogs_gpu_system_destroy", "ogs_gpu_configure",
                      "ogs_gpu_initialize", "ogs_gpu_assemble", "ogs_gpu_set_dirichlet",
@@ -316,6 +319,16 @@ def _f64(a):
     if a is None or hasattr(a, "data_ptr"):
         return a
     return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def selftest_barrier(which: int, grid: int = 0, spin_limit: int = 0, withhold: bool = False) -> dict:
+    """ogs_gpu_selftest_barrier: one grid barrier of the persistent FP32 CG
+    kernel (which 0) or of the batch kernel (1), optionally with block 0
+    withholding its arrival; returns status, blocks passed and the error
+    text."""
+    n = C.c_int32(0)
+    status = lib().ogs_gpu_selftest_barrier(which, grid, spin_limit, 1 if withhold else 0, C.byref(n))
+    return {"status": status, "passed": n.value, "error": lib().ogs_gpu_last_error().decode()}
 
 
 def kernel_launches(reset: bool = False) -> int:

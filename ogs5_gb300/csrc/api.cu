@@ -39,6 +39,9 @@ void launch_ilu_factor(const IluView& f, const double* val, const int32_t* csr2s
 int vec_grid(int n);
 int red_grid(int n);
 int mp_spmv_grid(int n);
+cudaError_t launch_mp_barrier_selftest(KState* st, int grid, int withhold, unsigned limit, int* go, cudaStream_t s);
+size_t batch_ctl_bytes();
+cudaError_t launch_batch_barrier_selftest(void* ctl, unsigned limit, int grid, int withhold, int* go, cudaStream_t s);
 
 // ------------------------------------------------------------------
 // small kernels
@@ -1729,3 +1732,64 @@ ogs_status system_enqueue_velocity(ogs_system* s, const ogs_assembly_params* p, 
 ogs_status system_element_status(const ogs_system* s) { return element_flag_status(s); }
 
 }  // namespace ogs
+
+// ------------------------------------------------------------------
+// self-test of the bounded waits of the cooperative persistent kernels
+// ------------------------------------------------------------------
+extern "C" ogs_status ogs_gpu_selftest_barrier(int32_t which, int32_t grid, int32_t spin_limit, int32_t withhold,
+                                               int32_t* passed)
+{
+    if ((which != 0 && which != 1) || grid < 0 || spin_limit < 0 || !passed)
+    {
+        set_error("selftest_barrier: bad arguments");
+        return OGS_BAD_ARG;
+    }
+    int dev = 0, sms = 0, coop = 0;
+    OGS_CUDA_TRY(cudaGetDevice(&dev));
+    OGS_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    OGS_CUDA_TRY(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+    if (!coop)
+    {
+        set_error("selftest_barrier: the device cannot launch cooperative kernels");
+        return OGS_CUDA_ERROR;
+    }
+    // two blocks per SM stay co-resident for both kernels (256 threads, few
+    // registers); the cooperative launch checks it
+    const int g = grid > 0 ? grid : 2 * sms;
+    if (g > 2 * sms)
+    {
+        set_error("selftest_barrier: grid %d exceeds two blocks per SM", g);
+        return OGS_BAD_ARG;
+    }
+    const size_t ctl_bytes = which == 0 ? sizeof(KState) : batch_ctl_bytes();
+    void* ctl = nullptr;
+    int* go = nullptr;
+    OGS_CUDA_TRY(cudaMalloc(&ctl, ctl_bytes));
+    cudaError_t e = cudaMalloc(&go, sizeof(int) * g);
+    if (e == cudaSuccess) e = cudaMemset(ctl, 0, ctl_bytes);
+    if (e == cudaSuccess) e = cudaMemset(go, 0, sizeof(int) * g);
+    if (e == cudaSuccess)
+        e = which == 0 ? launch_mp_barrier_selftest((KState*)ctl, g, withhold ? 1 : 0,
+                                                    spin_limit ? (unsigned)spin_limit : (1u << 24), go, 0)
+                       : launch_batch_barrier_selftest(ctl, (unsigned)spin_limit, g, withhold ? 1 : 0, go, 0);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    std::vector<int> h(g, 0);
+    if (e == cudaSuccess) e = cudaMemcpy(h.data(), go, sizeof(int) * g, cudaMemcpyDeviceToHost);
+    cudaFree(go);
+    cudaFree(ctl);
+    if (e != cudaSuccess)
+    {
+        set_error("selftest_barrier: %s", cudaGetErrorString(e));
+        return OGS_CUDA_ERROR;
+    }
+    int n = 0;
+    for (int v : h) n += v;
+    *passed = n;
+    count_launches(1);
+    if (n < g - (withhold ? 1 : 0))
+    {
+        set_error("selftest_barrier: barrier timeout (%d of %d arriving blocks passed)", n, g - (withhold ? 1 : 0));
+        return OGS_CUDA_ERROR;
+    }
+    return OGS_OK;
+}

@@ -85,6 +85,7 @@ struct BCtl
     int step, max_steps;
     int n_act, n_act_tiles;
     unsigned long long t0;  // %globaltimer at the start of the launch (ns)
+    unsigned spin_limit;    // polls before a wait gives up (0: kSpinLimit)
 };
 
 struct BatchArgs
@@ -161,9 +162,10 @@ __device__ bool grid_barrier(BCtl* c, F on_last)
             else
             {
                 unsigned spins = 0;
+                const unsigned limit = c->spin_limit ? c->spin_limit : kSpinLimit;
                 while (ld_acquire_u32(&c->bar_gen) == gen)
                 {
-                    if (++spins > kSpinLimit)
+                    if (++spins > limit)
                     {
                         atomicExch(&c->err, 1);
                         go = 0;
@@ -671,6 +673,37 @@ __global__ void __launch_bounds__(NT, NT == 256 ? 3 : 1) k_batch(BatchArgs a)
         for (int t = blockIdx.x; t < nat; t += gridDim.x) phase_b<NT>(a, active_tile(a, n_act, t));
         if (!grid_barrier(c, [&] { end_of_step(a); })) return;
     }
+}
+
+// Self-test of the bounded wait: every block passes one barrier of the
+// batch kernel; with `withhold`, block 0 leaves without arriving, so the
+// others wait on a generation word nothing bumps and give up after
+// c->spin_limit polls.  go[b]: whether block b passed.
+__global__ void k_batch_barrier_selftest(BCtl* c, int withhold, int* go)
+{
+    if (withhold && blockIdx.x == 0)
+    {
+        if (threadIdx.x == 0) go[0] = 0;
+        return;
+    }
+    const bool ok = grid_barrier(c, [] {});
+    if (threadIdx.x == 0) go[blockIdx.x] = ok ? 1 : 0;
+}
+
+// the control block of the self-test (zeroed, then the spin limit set) and
+// its launch
+size_t batch_ctl_bytes() { return sizeof(BCtl); }
+
+cudaError_t launch_batch_barrier_selftest(void* ctl, unsigned limit, int grid, int withhold, int* go, cudaStream_t s)
+{
+    BCtl h;
+    std::memset(&h, 0, sizeof h);
+    h.spin_limit = limit;
+    cudaError_t e = cudaMemcpyAsync(ctl, &h, sizeof h, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return e;
+    BCtl* c = (BCtl*)ctl;
+    void* args[] = {&c, &withhold, &go};
+    return cudaLaunchCooperativeKernel((const void*)k_batch_barrier_selftest, dim3(grid), dim3(256), args, 0, s);
 }
 
 }  // namespace ogs

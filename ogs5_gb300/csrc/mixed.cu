@@ -948,8 +948,9 @@ __device__ __forceinline__ void st_release(unsigned* p, unsigned v)
     asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-// false in every thread of the block once any block gave up waiting
-__device__ bool mp_grid_barrier(KState* st)
+// false in every thread of the block once any block gave up waiting (after
+// `limit` polls of the generation word)
+__device__ bool mp_grid_barrier(KState* st, unsigned limit = kBarSpinLimit)
 {
     __shared__ int s_go;
     __syncthreads();
@@ -969,7 +970,7 @@ __device__ bool mp_grid_barrier(KState* st)
             unsigned spins = 0;
             while (ld_acquire(&st->bar_gen) == gen)
             {
-                if (++spins > kBarSpinLimit || *(volatile int*)&st->bar_err)
+                if (++spins > limit || *(volatile int*)&st->bar_err)
                 {
                     atomicExch(&st->bar_err, 1);
                     go = 0;
@@ -1222,6 +1223,27 @@ cudaError_t launch_mp_persist(const MixedArgs& a, int grid, int iters, cudaStrea
         case -1: return cudaLaunchKernelEx(&lc, k_mp_persist<-1>, a, iters);
         default: return cudaLaunchKernelEx(&lc, k_mp_persist<0>, a, iters);
     }
+}
+
+// Self-test of the bounded wait: every block passes one barrier of the
+// persistent FP32 kernel; with `withhold`, block 0 leaves without arriving,
+// so the others wait on a generation word nothing bumps and give up after
+// `limit` polls.  go[b]: whether block b passed.
+__global__ void k_mp_barrier_selftest(KState* st, int withhold, unsigned limit, int* go)
+{
+    if (withhold && blockIdx.x == 0)
+    {
+        if (threadIdx.x == 0) go[0] = 0;
+        return;
+    }
+    const bool ok = mp_grid_barrier(st, limit);
+    if (threadIdx.x == 0) go[blockIdx.x] = ok ? 1 : 0;
+}
+
+cudaError_t launch_mp_barrier_selftest(KState* st, int grid, int withhold, unsigned limit, int* go, cudaStream_t s)
+{
+    void* args[] = {&st, &withhold, &limit, &go};
+    return cudaLaunchCooperativeKernel((const void*)k_mp_barrier_selftest, dim3(grid), dim3(kThreads), args, 0, s);
 }
 
 void launch_mp_iteration(const MixedArgs& a, cudaStream_t s, cudaEvent_t eb, cudaEvent_t ee)
