@@ -579,7 +579,7 @@ SERVE_WARM_SLOTS = 4      # slots per class created before the timed run
 # requests: p50 267 ms against 508 ms for arrival order with 128 in flight,
 # the same throughput)
 SERVE_MAX_ACTIVE = 16
-SERVE_FLAGS = 3           # capi.SERVER_PRIORITY | capi.SERVER_SJF
+SERVE_FLAGS = 7           # capi.SERVER_PRIORITY | capi.SERVER_SJF | capi.SERVER_BATCH
 SERVE_WORKLOAD = ("Poisson arrivals 200/s of flow (steady GWF, heads 10/0 m on the x faces) and transport "
                   "(one MASS_TRANSPORT step, flux from a linear head field) requests on quad, hex and "
                   "hex-split-tet meshes, 1e4-2e6 DOF log-uniform (5 size classes per type), log-normal K "
@@ -634,6 +634,19 @@ def serve_class_setup(capi, m, kind):
     return lf, np.ones(len(lf)), capi.DIRICHLET_ROW_ONLY, p, capi.make_params(capi.GROUNDWATER_FLOW), head
 
 
+def _serve_breakdown(reqs, res):
+    """Per mesh type and request kind: requests, mean solver iterations and
+    the summed per-request solve time (overlapping requests each count)."""
+    out = {}
+    for r, x in zip(reqs, res):
+        g = out.setdefault(f"{r['key'][0]}-{'flow' if r['kind'] == 0 else 'mt'}", [0, 0, 0.0])
+        g[0] += 1
+        g[1] += x["iterations"]
+        g[2] += x["solve_ms"]
+    return {k: {"requests": n, "mean_iterations": round(it / n, 1), "sum_solve_ms": round(ms, 1)}
+            for k, (n, it, ms) in sorted(out.items())}
+
+
 def serve_leg(capi, torch, n_req=SERVE_REQUESTS, flags=None, max_active=None, plain=True):
     t_setup = time.perf_counter()
     dofs, meshes = serve_meshes()
@@ -653,13 +666,15 @@ def serve_leg(capi, torch, n_req=SERVE_REQUESTS, flags=None, max_active=None, pl
             cls[(key, kind)] = srv.add_class(gms[key], kind, p, rows, vals, mode, cfg, flow_params=fp,
                                              flow_head=head)
     outs = [torch.zeros(meshes[r["key"]].n_nodes, dtype=torch.float64, device="cuda") for r in reqs]
-    # warm-up: SERVE_WARM_SLOTS concurrent requests of every class, so each
-    # class starts with that many slots whose buffers and graphs exist
+    # warm-up: SERVE_WARM_SLOTS slots reserved for every class and as many
+    # requests of it served, so each class starts with slots whose buffers
+    # and graphs exist
     warm_out = []
     for (key, kind), cid in cls.items():
         k = next((r["k"] for r in reqs if r["key"] == key), None)
         if k is None:
             continue
+        srv.reserve(cid, SERVE_WARM_SLOTS)
         for _ in range(SERVE_WARM_SLOTS):
             warm_out.append(torch.zeros(meshes[key].n_nodes, dtype=torch.float64, device="cuda"))
             srv.submit(cid, k, 1e-6, warm_out[-1])
@@ -691,16 +706,59 @@ def serve_leg(capi, torch, n_req=SERVE_REQUESTS, flags=None, max_active=None, pl
               "p99_latency_ms": round(float(np.percentile(lat, 99)), 3),
               "ok": ok, "failed": fails, "slots": info["slots"], "hbm_bytes_used": info["bytes_used"]}
     policy = {"max_active": max_active, "priority_streams": bool(flags & capi.SERVER_PRIORITY),
-              "admission": "smallest class first" if flags & capi.SERVER_SJF else "arrival order"}
+              "admission": "smallest class first" if flags & capi.SERVER_SJF else "arrival order",
+              "dynamic_batching": bool(flags & capi.SERVER_BATCH),
+              "fp32_internal_tol": "a tenth of the request's tolerance"}
+    served["batched"] = info["batched"]
+    served["by_kind"] = _serve_breakdown(reqs, res)
+    srv.close()
     if not plain:
-        srv.close()
         return {"requests": n_req, "served": served, "policy": policy}
-    # plain FP64 path: the same requests one after another through the
-    # blocking single-system API (FP64 CG / BiCGStab + Jacobi), queued in
-    # arrival order behind one another
+    # plain FP64 path: the same arrivals replayed in real time through a
+    # server that admits one request at a time (FIFO, no batching) on the
+    # FP64 single-system solvers (CG / BiCGStab + Jacobi)
+    srv64 = capi.Server(max_active=1, flags=0)
+    cls64 = {}
+    for key, m in meshes.items():
+        for kind in (0, 1):
+            rows, vals, mode, p, fp, head = serve_class_setup(capi, m, kind)
+            cfg = (capi.solver_config(capi.LS_CG, capi.PRECOND_JACOBI, 20000) if kind == 0 else
+                   capi.solver_config(capi.LS_BICGSTAB, capi.PRECOND_JACOBI, 5000))
+            cls64[(key, kind)] = srv64.add_class(gms[key], kind, p, rows, vals, mode, cfg, flow_params=fp,
+                                                 flow_head=head)
+    outs64 = [torch.zeros(meshes[r["key"]].n_nodes, dtype=torch.float64, device="cuda") for r in reqs]
+    warm64 = []
+    for (key, kind), cid in cls64.items():  # one warm slot per class
+        k = next((r["k"] for r in reqs if r["key"] == key), None)
+        if k is not None:
+            warm64.append(torch.zeros(meshes[key].n_nodes, dtype=torch.float64, device="cuda"))
+            srv64.submit(cid, k, 1e-6, warm64[-1])
+            srv64.drain()
+    torch.cuda.synchronize()
+    ids64 = []
+    t0 = time.perf_counter()
+    for q, r in enumerate(reqs):
+        while time.perf_counter() - t0 < r["t"]:
+            srv64.progress()
+        ids64.append(srv64.submit(cls64[(r["key"], r["kind"])], r["k"], r["tol"], outs64[q]))
+        srv64.progress()
+    srv64.drain()
+    makespan64 = time.perf_counter() - t0
+    res64 = [srv64.result(i) for i in ids64]
+    lat64 = [x["latency_ms"] for x in res64]
+    srv64.close()
+    fp64 = {"value": round(n_req / makespan64, 3), "unit": "solves/s",
+            "p50_latency_ms": round(float(np.percentile(lat64, 50)), 3),
+            "p99_latency_ms": round(float(np.percentile(lat64, 99)), 3),
+            "ok": sum(1 for x in res64 if x["status"] == capi.OK),
+            "by_kind": _serve_breakdown(reqs, res64),
+            "how": "same arrivals replayed in real time, one request at a time (FIFO), FP64 CG / BiCGStab + "
+                   "Jacobi on the single-system solvers"}
+    # accuracy: every served result against an FP64 solve of its system to
+    # 1e-13 (converged), and against the FP64 path's result at its tolerance
     eqs_by = {}
-    svc = []
-    err = {1e-6: 0.0, 1e-10: 0.0}
+    err_conv = {1e-6: 0.0, 1e-10: 0.0}
+    err_path = {1e-6: 0.0, 1e-10: 0.0}
     worst = []
     for q, r in enumerate(reqs):
         key, kind = r["key"], r["kind"]
@@ -710,51 +768,37 @@ def serve_leg(capi, torch, n_req=SERVE_REQUESTS, flags=None, max_active=None, pl
             rows, vals, mode, p, fp, head = serve_class_setup(capi, m, kind)
             x0 = np.zeros(m.n_nodes)
             x0[rows] = vals
-            eqs_by[(key, kind)] = (e, rows, vals, mode, p, fp,
-                                   None if head is None else torch.tensor(head, device="cuda"),
+            eqs_by[(key, kind)] = (e, mode, p, fp, None if head is None else torch.tensor(head, device="cuda"),
                                    torch.tensor(x0, device="cuda"), torch.tensor(rows, device="cuda"),
                                    torch.tensor(vals, device="cuda"))
-        e, rows, vals, mode, p, fp, head, x0, rows_d, vals_d = eqs_by[(key, kind)]
-        torch.cuda.synchronize()
-        ts = time.perf_counter()
+        e, mode, p, fp, head, x0, rows_d, vals_d = eqs_by[(key, kind)]
+        e.Initialize()
         if kind == 0:
-            e.ConfigNumerics(capi.LS_CG, capi.PRECOND_JACOBI, 20000, r["tol"], check_norm_rhs=False)
-            e.Initialize()
+            e.ConfigNumerics(capi.LS_CG, capi.PRECOND_JACOBI, 40000, 1e-13, check_norm_rhs=False)
             e.GlobalAssembly(p, r["k"], x0)
         else:
-            e.ConfigNumerics(capi.LS_BICGSTAB, capi.PRECOND_JACOBI, 5000, r["tol"], check_norm_rhs=False)
+            e.ConfigNumerics(capi.LS_BICGSTAB, capi.PRECOND_JACOBI, 10000, 1e-13, check_norm_rhs=False)
             qbuf = torch.empty((m.n_elements, gms[key].n_gauss, 3), dtype=torch.float64, device="cuda")
             e.gp_velocity(fp, r["k"], head, qbuf)
-            e.Initialize()
             e.GlobalAssembly(p, None, x0, qbuf)
         e.SetKnownX(rows_d, vals_d, mode)
         x = x0.clone()
-        e.Solver(x)
-        torch.cuda.synchronize()
-        svc.append(time.perf_counter() - ts)
-        ref = x
-        eq = float((outs[q] - ref).abs().max() / ref.abs().max())
+        e.Solver(x, allow_fail=True)
+        scale = float(x.abs().max())
+        ec = float((outs[q] - x).abs().max()) / scale
+        ep = float((outs[q] - outs64[q]).abs().max()) / scale
         if res[q]["status"] == capi.OK:
-            err[r["tol"]] = max(err[r["tol"]], eq)
-        worst.append((eq, f"{r['key'][0]}{r['key'][1]}-{'flow' if r['kind'] == 0 else 'mt'}-{r['tol']:g}",
-                      res[q]["status"], res[q]["iterations"], e.stats()["iterations"]))
-    done = 0.0
-    lat64 = []
-    for r, sv in zip(reqs, svc):
-        start = max(done, r["t"])
-        done = start + sv
-        lat64.append((done - r["t"]) * 1e3)
-    fp64 = {"value": round(n_req / done, 3), "unit": "solves/s",
-            "p50_latency_ms": round(float(np.percentile(lat64, 50)), 3),
-            "p99_latency_ms": round(float(np.percentile(lat64, 99)), 3),
-            "busy_s": round(sum(svc), 3),
-            "how": "same requests, blocking single-system API one after another (FP64 CG / BiCGStab + "
-                   "Jacobi), FIFO queue behind the measured service times"}
-    srv.close()
+            err_conv[r["tol"]] = max(err_conv[r["tol"]], ec)
+            err_path[r["tol"]] = max(err_path[r["tol"]], ep)
+        worst.append((ec, f"{r['key'][0]}{r['key'][1]}-{'flow' if r['kind'] == 0 else 'mt'}-{r['tol']:g}",
+                      res[q]["status"], res[q]["iterations"], res[q]["batch_size"]))
     return {"workload": SERVE_WORKLOAD, "requests": n_req, "rate_per_s": SERVE_RATE,
             "classes": len(cls), "served": served, "policy": policy, "fp64_path": fp64,
             "speedup_vs_fp64_path": round(served["value"] / fp64["value"], 3),
-            "max_rel_err_vs_fp64": {"tol_1e-6": err[1e-6], "tol_1e-10": err[1e-10]},
+            "max_rel_err_vs_fp64_converged": {"tol_1e-6": err_conv[1e-6], "tol_1e-10": err_conv[1e-10]},
+            "max_rel_err_vs_fp64_path": {"tol_1e-6": err_path[1e-6], "tol_1e-10": err_path[1e-10]},
+            "error_how": "served heads against an FP64 solve of the same system to |r|/|b| < 1e-13 "
+                         "(converged), and against the FP64 path's heads at the request's tolerance",
             "worst": sorted(worst, reverse=True)[:8],
             "served_value": served["value"]}
 

@@ -579,7 +579,11 @@ typedef struct
     const int64_t* bc_rows;     /* Dirichlet rows and values (host), copied    */
     const double* bc_values;
     int64_t n_bc;
-    ogs_solver_config solver;   /* tol is replaced by each request's tol       */
+    ogs_solver_config solver;   /* tol is replaced by each request's tol (a
+                                   tenth of it in FP32-inner mode: two solves
+                                   stopped at |r|/|b| < tol differ by up to
+                                   cond(A) tol, the tighter stop keeps served
+                                   heads within the FP64 path's accuracy)    */
 } ogs_server_class;
 
 typedef struct
@@ -592,6 +596,9 @@ typedef struct
     double latency_ms;          /* submit -> completion seen by the server     */
     double queue_ms;            /* submit -> admission                         */
     double solve_ms;            /* device time of the solve                    */
+    int32_t batch_size;         /* requests of the batch launch that served it
+                                   (0: served alone on a slot)                 */
+    int32_t pad0;
 } ogs_server_result;
 
 typedef struct
@@ -599,15 +606,22 @@ typedef struct
     int32_t slots, running, queued, pad0;
     int64_t completed;
     int64_t bytes_used, bytes_budget;
+    int64_t batched;            /* requests served by batch launches           */
 } ogs_server_info;
 
 /* Scheduling policy bits of ogs_gpu_server_create. */
 enum
 {
     OGS_SERVER_PRIORITY = 1,  /* smaller classes get higher CUDA stream priorities */
-    OGS_SERVER_SJF = 2        /* admit the queued request of the smallest class
+    OGS_SERVER_SJF = 2,       /* admit the queued request of the smallest class
                                  first (arrival order among equals); default:
                                  arrival order                                 */
+    OGS_SERVER_BATCH = 4      /* dynamic batching: two or more queued requests
+                                 of one steady hex-lattice flow class (heads on
+                                 the two x faces, FP32-inner CG) with the same
+                                 tolerance are solved together by one
+                                 Monte-Carlo batch launch (ogs_gpu_batch_*),
+                                 which progress runs to completion           */
 };
 
 /* hbm_budget_bytes <= 0: 80% of the free device memory at creation.
@@ -619,13 +633,15 @@ ogs_status ogs_gpu_server_add_class(ogs_server* srv, const ogs_server_class* cls
 /* Creates idle slots of a class up to n_slots in total (within the budget),
  * so that the first requests do not pay for allocation and graph capture. */
 ogs_status ogs_gpu_server_reserve(ogs_server* srv, int32_t class_id, int32_t n_slots);
-/* Queues a request.  elem_k: device array (n_elements) that stays valid
- * until the request is done; out: n_nodes doubles (device or pinned host),
- * written when the request is done. */
+/* Queues a request.  elem_k: device array (n_elements), complete when this
+ * is called (the server's streams do not wait on the caller's), that stays
+ * valid until the request is done; out: n_nodes doubles (device or pinned
+ * host), written when the request is done. */
 ogs_status ogs_gpu_server_submit(ogs_server* srv, int32_t class_id, const double* elem_k, double tol,
                                  double* out, int64_t* request_id);
-/* One scheduling round (never blocks on the GPU): polls running requests,
- * retires finished ones, admits queued ones. */
+/* One scheduling round: polls running requests, retires finished ones,
+ * admits queued ones.  Blocks on the GPU only for a batch launch
+ * (OGS_SERVER_BATCH). */
 ogs_status ogs_gpu_server_progress(ogs_server* srv, int32_t* n_running, int32_t* n_queued);
 ogs_status ogs_gpu_server_result(const ogs_server* srv, int64_t request_id, ogs_server_result* r);
 ogs_status ogs_gpu_server_info(const ogs_server* srv, ogs_server_info* info);

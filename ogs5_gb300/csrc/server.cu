@@ -24,6 +24,17 @@
 // request runs exactly the kernels, launch shapes and order of the
 // single-system API on a system of its own, so its result does not depend on
 // what else is in flight.
+//
+// Dynamic batching (OGS_SERVER_BATCH): steady flow classes on a regular hex
+// lattice with heads given on the two x faces are the Monte-Carlo batch's
+// problem (batch.cu).  When two or more queued requests of such a class
+// with the same tolerance wait at admission, up to kMaxServerBatch of them
+// are assembled and solved together by one persistent batch launch (the
+// batch object of that class, size and tolerance is kept for reuse).
+//
+// FP32-inner requests are solved to a tenth of their tolerance: two solves
+// stopped at |r|/|b| < tol differ by up to cond(A) tol, and the tighter
+// internal stop keeps a served result within the FP64 path's accuracy.
 #include <algorithm>
 #include <chrono>
 #include <cstring>
@@ -34,6 +45,8 @@
 #include "common.cuh"
 
 namespace ogs {
+constexpr double kServedTolFactor = 0.1;  // internal stop of FP32-inner requests, times the tolerance
+constexpr int kMaxServerBatch = 32;       // requests per batch launch at most
 cudaStream_t system_stream(ogs_system* s);
 int64_t system_rows(const ogs_system* s);
 size_t system_bytes(const ogs_mesh* m, bool fp32);
@@ -62,6 +75,23 @@ struct SrvClass
     size_t bytes = 0;          // device bytes of one slot
     int64_t n = 0, ngp = 0, ne = 0;
     int priority = 0;          // CUDA stream priority of its slots
+    // the Monte-Carlo batch's problem (steady flow on a hex lattice, heads on
+    // the two x faces): lattice, cells, spacing and face heads
+    bool batchable = false;
+    int gx = 0, gy = 0, gz = 0;
+    int64_t cells = 0;
+    double hx = 0.0, hy = 0.0, hz = 0.0, h_left = 0.0, h_right = 0.0;
+};
+
+// a batch object kept for reuse: class, size, tolerance
+struct SrvBatch
+{
+    int cls = -1, count = 0;
+    double tol = 0.0;
+    ogs_batch* b = nullptr;
+    double* k_all = nullptr;   // gathered conductivities, device
+    double* heads = nullptr;   // heads of all realisations, device
+    size_t bytes = 0;
 };
 
 struct SrvSlot
@@ -84,6 +114,7 @@ struct SrvReq
     int slot = -1;
     ogs_status status = OGS_OK;
     ogs_solve_stats st{};
+    int batch_size = 0;        // requests of the batch launch that served it (0: a slot)
     Clock::time_point t_submit, t_admit, t_done;
 };
 
@@ -96,11 +127,14 @@ struct ogs_server
     int flags = 0;             // OGS_SERVER_* policy bits
     std::vector<SrvClass> classes;
     std::vector<SrvSlot> slots;
+    std::vector<SrvBatch> batches;
     std::vector<SrvReq> reqs;
     std::deque<int64_t> queue;
     std::vector<int64_t> running;
     int64_t tick = 0;
     int64_t completed = 0;
+    int64_t batched = 0;       // requests served by batch launches
+    cudaStream_t batch_stream = nullptr;  // every batch object's copies and launches
 };
 
 namespace {
@@ -117,12 +151,13 @@ void release_slot(ogs_server* S, size_t k)
         if (S->reqs[id].slot > (int)k) S->reqs[id].slot -= 1;
 }
 
-// a slot of class c: idle one, or a new one within the budget
+// a slot of class c, while fewer than max_active requests run: an idle
+// one, or a new one within the budget
 int acquire_slot(ogs_server* S, int c)
 {
+    if ((int)S->running.size() >= S->max_active) return -1;
     for (size_t k = 0; k < S->slots.size(); k++)
         if (!S->slots[k].busy && S->slots[k].cls == c) return (int)k;
-    if ((int)S->running.size() >= S->max_active) return -1;
     const SrvClass& C = S->classes[c];
     while (S->used + C.bytes > S->budget)
     {
@@ -173,7 +208,7 @@ ogs_status start(ogs_server* S, int64_t id, int k)
     const SrvClass& C = S->classes[R.cls];
     ogs_system* s = sl.sys;
     cudaStream_t st = system_stream(s);
-    system_reset_request(s, R.tol);
+    system_reset_request(s, C.c.solver.precision != OGS_PRECISION_FP64 ? R.tol * kServedTolFactor : R.tol);
     OGS_CUDA_TRY(cudaMemcpyAsync(R.out, C.x0, C.n * sizeof(double), cudaMemcpyDefault, st));
     ogs_status e;
     if (C.c.kind == OGS_REQUEST_TRANSPORT)
@@ -218,6 +253,158 @@ double ms_between(Clock::time_point a, Clock::time_point b)
     return std::chrono::duration<double, std::milli>(b - a).count();
 }
 
+// Is the class the Monte-Carlo batch's problem?  Steady GROUNDWATER_FLOW
+// (no storage) solved by FP32-inner CG + Jacobi on a regular hex lattice,
+// symmetric Dirichlet on exactly the nodes of the x = 0 and x = max faces
+// with one head per face.
+void detect_batchable(SrvClass& C, const ogs_mesh* m)
+{
+    const ogs_server_class& c = C.c;
+    C.batchable = false;
+    if (c.kind != OGS_REQUEST_FLOW || c.params.pcs_type != OGS_PCS_GROUNDWATER_FLOW || c.params.storage != 0.0 ||
+        c.solver.precision != OGS_PRECISION_FP32_REFINED || c.solver.method != OGS_LS_CG ||
+        c.solver.precond != OGS_PRECOND_JACOBI || c.bc_mode != OGS_DIRICHLET_SYMMETRIC || !m->grid ||
+        m->gx < 3 || m->gy < 3 || m->gz < 3)
+        return;
+    const int64_t face = (int64_t)m->gy * m->gz;
+    if ((int64_t)C.bc_rows.size() != 2 * face) return;
+    std::vector<unsigned char> seen((size_t)C.n, 0);
+    double hl = 0.0, hr = 0.0;
+    bool have_l = false, have_r = false;
+    for (size_t q = 0; q < C.bc_rows.size(); q++)
+    {
+        const int64_t r = C.bc_rows[q];
+        if (r < 0 || r >= C.n || seen[r]) return;
+        seen[r] = 1;
+        const int64_t ix = r % m->gx;
+        if (ix != 0 && ix != m->gx - 1) return;
+        double& h = ix == 0 ? hl : hr;
+        bool& have = ix == 0 ? have_l : have_r;
+        if (have && h != C.bc_vals[q]) return;
+        h = C.bc_vals[q];
+        have = true;
+    }
+    if (!have_l || !have_r) return;
+    C.gx = m->gx; C.gy = m->gy; C.gz = m->gz;
+    C.cells = (int64_t)(m->gx - 1) * (m->gy - 1) * (m->gz - 1);
+    C.hx = m->ghx; C.hy = m->ghy; C.hz = m->ghz;
+    C.h_left = hl;
+    C.h_right = hr;
+    C.batchable = true;
+}
+
+void release_batch(SrvBatch& B)
+{
+    if (B.b) ogs_gpu_batch_destroy(B.b);
+    cudaFree(B.k_all);
+    cudaFree(B.heads);
+    B = SrvBatch();
+}
+
+// the batch object of (class, count, tol): kept one, or a new one within the
+// budget (idle slots released, least recently used first, to make room).
+// Returns -1 when it does not fit.
+int acquire_batch(ogs_server* S, int c, int count, double tol, const std::vector<int64_t>& ids)
+{
+    for (size_t k = 0; k < S->batches.size(); k++)
+    {
+        const SrvBatch& B = S->batches[k];
+        if (B.cls == c && B.count == count && B.tol == tol) return (int)k;
+    }
+    const SrvClass& C = S->classes[c];
+    const size_t rows = (size_t)C.n * count, elems = (size_t)C.cells * count;
+    const size_t bytes = rows * (14 * 8 + 3 * 8 + 21 * 4 + 8) + 2 * elems * 8;
+    while (S->used + bytes > S->budget)
+    {
+        int lru = -1;
+        for (size_t k = 0; k < S->slots.size(); k++)
+            if (!S->slots[k].busy && (lru < 0 || S->slots[k].last_used < S->slots[lru].last_used)) lru = (int)k;
+        if (lru < 0) return -1;
+        release_slot(S, lru);
+    }
+    ogs_batch_config cfg;
+    std::memset(&cfg, 0, sizeof cfg);
+    cfg.hx = C.hx; cfg.hy = C.hy; cfg.hz = C.hz;
+    cfg.time_unit_factor = C.c.params.time_unit_factor;
+    cfg.tol = tol * kServedTolFactor;
+    cfg.inner_tol = C.c.solver.inner_tol;
+    cfg.max_iter = C.c.solver.max_iter;
+    std::vector<ogs_batch_realisation> reals(count);
+    for (int r = 0; r < count; r++)
+    {
+        std::memset(&reals[r], 0, sizeof reals[r]);
+        reals[r].nx = C.gx; reals[r].ny = C.gy; reals[r].nz = C.gz;
+        reals[r].elem_k = S->reqs[ids[r]].elem_k;
+        reals[r].h_left = C.h_left;
+        reals[r].h_right = C.h_right;
+    }
+    SrvBatch B;
+    B.cls = c;
+    B.count = count;
+    B.tol = tol;
+    B.bytes = bytes;
+    if (!S->batch_stream)
+    {
+        int least = 0, greatest = 0;
+        cudaDeviceGetStreamPriorityRange(&least, &greatest);
+        if (cudaStreamCreateWithPriority(&S->batch_stream, cudaStreamNonBlocking, greatest) != cudaSuccess)
+        {
+            cudaGetLastError();
+            S->batch_stream = nullptr;
+            return -1;
+        }
+    }
+    if (ogs_gpu_batch_create(&cfg, reals.data(), count, S->batch_stream, &B.b) != OGS_OK) return -1;
+    if (cudaMalloc(&B.k_all, elems * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&B.heads, rows * sizeof(double)) != cudaSuccess)
+    {
+        cudaGetLastError();
+        release_batch(B);
+        return -1;
+    }
+    S->used += bytes;
+    S->batches.push_back(B);
+    return (int)S->batches.size() - 1;
+}
+
+// one batch launch for the requests ids (same class and tolerance): their
+// conductivities gathered, assembly and solve, heads scattered to their
+// outputs, every copy on the server's batch stream (the batch object's
+// own), so the gather is complete before the batch reads it and the
+// scatter before the next batch overwrites its heads.  Blocks until done.
+ogs_status run_batch(ogs_server* S, int k, const std::vector<int64_t>& ids)
+{
+    SrvBatch& B = S->batches[k];
+    const SrvClass& C = S->classes[B.cls];
+    cudaStream_t st = S->batch_stream;
+    for (size_t r = 0; r < ids.size(); r++)
+        OGS_CUDA_TRY(cudaMemcpyAsync(B.k_all + r * C.cells, S->reqs[ids[r]].elem_k, C.cells * sizeof(double),
+                                     cudaMemcpyDefault, st));
+    ogs_status e = ogs_gpu_batch_set_k(B.b, B.k_all);
+    if (e) return e;
+    std::vector<ogs_batch_stats> bs(ids.size());
+    const ogs_status sst = ogs_gpu_batch_solve(B.b, bs.data());
+    if (sst != OGS_OK && sst != OGS_NOT_CONVERGED && sst != OGS_NONFINITE && sst != OGS_BREAKDOWN) return sst;
+    if ((e = ogs_gpu_batch_get_heads(B.b, B.heads))) return e;
+    for (size_t r = 0; r < ids.size(); r++)
+        OGS_CUDA_TRY(cudaMemcpyAsync(S->reqs[ids[r]].out, B.heads + r * C.n, C.n * sizeof(double),
+                                     cudaMemcpyDefault, st));
+    OGS_CUDA_TRY(cudaStreamSynchronize(st));
+    for (size_t r = 0; r < ids.size(); r++)
+    {
+        SrvReq& R = S->reqs[ids[r]];
+        std::memset(&R.st, 0, sizeof R.st);
+        R.st.iterations = bs[r].iterations;
+        R.st.status = bs[r].status;
+        R.st.refinements = bs[r].refinements;
+        R.st.rel_residual = bs[r].rel_residual;
+        R.st.solve_ms = bs[r].finish_ms;
+        R.st.fp32_operator = 0;
+        R.status = (ogs_status)bs[r].status;
+    }
+    return OGS_OK;
+}
+
 }  // namespace
 
 extern "C" ogs_status ogs_gpu_server_create(int64_t hbm_budget_bytes, int32_t max_active, int32_t flags,
@@ -248,6 +435,8 @@ extern "C" ogs_status ogs_gpu_server_destroy(ogs_server* S)
         cudaFree(sl.q);
         if (sl.stream) cudaStreamDestroy(sl.stream);
     }
+    for (SrvBatch& B : S->batches) release_batch(B);
+    if (S->batch_stream) cudaStreamDestroy(S->batch_stream);
     for (SrvClass& C : S->classes)
     {
         cudaFree(C.x0);
@@ -298,6 +487,7 @@ extern "C" ogs_status ogs_gpu_server_add_class(ogs_server* S, const ogs_server_c
         OGS_CUDA_TRY(cudaStreamSynchronize(cudaStreamLegacy));
     }
     C.bytes = system_bytes(c->mesh, c->solver.precision != OGS_PRECISION_FP64);
+    detect_batchable(C, c->mesh);
     if (c->kind == OGS_REQUEST_TRANSPORT) C.bytes += (size_t)C.ne * C.ngp * 3 * sizeof(double);
     C.c.bc_rows = nullptr;
     C.c.bc_values = nullptr;
@@ -392,6 +582,45 @@ extern "C" ogs_status ogs_gpu_server_progress(ogs_server* S, int32_t* n_running,
                 if (S->classes[S->reqs[S->queue[q]].cls].n < S->classes[S->reqs[S->queue[pick]].cls].n) pick = q;
         const int64_t id = S->queue[pick];
         SrvReq& R = S->reqs[id];
+        if ((S->flags & OGS_SERVER_BATCH) && S->classes[R.cls].batchable)
+        {
+            // same class and tolerance, in queue order from the picked one
+            std::vector<size_t> at;
+            for (size_t q = pick; q < S->queue.size() && (int)at.size() < kMaxServerBatch; q++)
+            {
+                const SrvReq& O = S->reqs[S->queue[q]];
+                if (O.cls == R.cls && O.tol == R.tol) at.push_back(q);
+            }
+            if (at.size() >= 2)
+            {
+                std::vector<int64_t> ids;
+                for (size_t q : at) ids.push_back(S->queue[q]);
+                const int bk = acquire_batch(S, R.cls, (int)ids.size(), R.tol, ids);
+                if (bk >= 0)
+                {
+                    for (size_t j = at.size(); j-- > 0;) S->queue.erase(S->queue.begin() + at[j]);
+                    const Clock::time_point ta = Clock::now();
+                    for (int64_t q : ids)
+                    {
+                        S->reqs[q].state = 1;
+                        S->reqs[q].t_admit = ta;
+                    }
+                    const ogs_status bst = run_batch(S, bk, ids);
+                    const Clock::time_point td = Clock::now();
+                    for (int64_t q : ids)
+                    {
+                        SrvReq& Q = S->reqs[q];
+                        if (bst) Q.status = bst;
+                        Q.state = 2;
+                        Q.t_done = td;
+                        Q.batch_size = (int)ids.size();
+                    }
+                    S->completed += (int64_t)ids.size();
+                    S->batched += (int64_t)ids.size();
+                    continue;
+                }
+            }
+        }
         const int k = acquire_slot(S, R.cls);
         if (k == -2) return OGS_OOM;
         if (k < 0) break;
@@ -436,8 +665,9 @@ extern "C" ogs_status ogs_gpu_server_result(const ogs_server* S, int64_t request
         r->refinements = R.st.refinements;
         r->rel_residual = R.st.rel_residual;
         r->latency_ms = ms_between(R.t_submit, R.t_done);
-        r->queue_ms = R.slot >= 0 ? ms_between(R.t_submit, R.t_admit) : r->latency_ms;
+        r->queue_ms = R.slot >= 0 || R.batch_size ? ms_between(R.t_submit, R.t_admit) : r->latency_ms;
         r->solve_ms = R.st.solve_ms;
+        r->batch_size = R.batch_size;
     }
     return OGS_OK;
 }
@@ -450,6 +680,7 @@ extern "C" ogs_status ogs_gpu_server_info(const ogs_server* S, ogs_server_info* 
     info->running = (int32_t)S->running.size();
     info->queued = (int32_t)S->queue.size();
     info->completed = S->completed;
+    info->batched = S->batched;
     info->bytes_used = (int64_t)S->used;
     info->bytes_budget = (int64_t)S->budget;
     return OGS_OK;

@@ -9,7 +9,8 @@ INFRASTRUCTURE ONLY: a calibration run where the reference's sources exist
 Deck: hex 128 x 128 x 64 cells (1,081,665 nodes), ln K Gaussian random
 field (mean ln 1e-5, variance 1, correlation length 8 cells, the bench's
 seed) as a #MEDIUM_PROPERTIES_DISTRIBUTED element file, Ss 1e-4, dt 3600 s,
-heads 10 / 0 m on the x faces (two GLI surfaces), initial heads 0.
+heads 10 / 0 m on the x faces (two GLI surfaces), initial heads 0 except
+10 m on the x = 0 face.
 Phases come from the reference's own stdout markers, read line by line as
 they are printed ("Assembling equation system...", "Calling linear
 solver...", FEM/rf_pcs.cpp:4818,4826) and the solver's iteration report.
@@ -58,6 +59,14 @@ def write_deck(dirpath, build, steps):
                 surfaces={"LEFT_FACE": ["LEFT"], "RIGHT_FACE": ["RIGHT"]})
     D.write_bc(path + ".bc", [("GROUNDWATER_FLOW", "HEAD", "SURFACE", "LEFT_FACE", 10.0),
                               ("GROUNDWATER_FLOW", "HEAD", "SURFACE", "RIGHT_FACE", 0.0)])
+    # initial heads carry the Dirichlet values (with heads 0 on the x = 0
+    # face the SP build's BiCGStab breaks down at its second iteration,
+    # equation_class.cpp:1343-1348)
+    with open(path + ".ic", "w") as f:
+        f.write("#INITIAL_CONDITION\n $PCS_TYPE\n  GROUNDWATER_FLOW\n $PRIMARY_VARIABLE\n  HEAD\n"
+                " $GEO_TYPE\n  DOMAIN\n $DIS_TYPE\n  CONSTANT 0\n"
+                "#INITIAL_CONDITION\n $PCS_TYPE\n  GROUNDWATER_FLOW\n $PRIMARY_VARIABLE\n  HEAD\n"
+                " $GEO_TYPE\n  SURFACE LEFT_FACE\n $DIS_TYPE\n  CONSTANT 10\n#STOP\n")
     with open(path + ".out", "w") as f:
         f.write("#STOP\n")
     return path
@@ -129,10 +138,12 @@ def main():
     ap.add_argument("--steps", type=int, default=1)
     ap.add_argument("--out", default=None)
     ap.add_argument("--no-port", action="store_true")
+    ap.add_argument("--builds", default="sp,fem")
     args = ap.parse_args()
     res = {"host": os.uname().machine, "cores_used": 1}
     tmp = tempfile.mkdtemp(prefix="ogs_time_")
-    for build, binary in (("sp", os.path.join(HERE, "_ref", "ogs_sp")), ("fem", os.path.join(HERE, "_ref", "ogs_fem"))):
+    for build in args.builds.split(","):
+        binary = os.path.join(HERE, "_ref", "ogs_" + build)
         path = write_deck(os.path.join(tmp, build), build, args.steps)
         res["reference_" + build] = run_reference(binary, path)
         print(build, json.dumps(res["reference_" + build])[:600], flush=True)
