@@ -29,6 +29,7 @@ from __future__ import annotations
 import argparse
 import json
 import os
+import platform
 import statistics
 import subprocess
 import tempfile
@@ -48,11 +49,6 @@ TOL = 1e-10
 SEED = 2
 WORKLOAD = ("transient GROUNDWATER_FLOW hex 128x128x64, lnK GRF var 1 ell 8, 20 steps dt 3600, "
             "CG+Jacobi 1e-10")
-# Jacobi-CG iterations per step of this deck (FP64 path over the 20 steps:
-# 6295 iterations, measured on the GPU; the parity tests hold the GPU count
-# within two iterations of the oracle's Linear_EQS::CG)
-CG_ITERS_PER_STEP = 315
-
 
 def make_deck(nx=NX, ny=NY, nz=NZ):
     from ogs5_gb300 import fields
@@ -204,33 +200,42 @@ def time_path(eqs, capi, p, deck, k_steps, warm, torch, stream, mixed, keep=Fals
             "launches": launches, "prof": prof}
 
 
-def cpu_baseline_sample():
-    """Oracle (C restatement) on a bounded sample of the workload: the full
-    assembly of one 16-cell x-slab plus 40 CG iterations on a system with the
-    full pattern.  Returns (seconds per element, seconds per CG iteration)."""
-    import copy
+class PortDeck:
+    """The deck on the oracle's C restatement (the reference's algorithm,
+    one thread): full element assembly (CFiniteElementStd::Assembly through
+    GlobalAssembly), symmetric Dirichlet elimination and Linear_EQS::CG with
+    Jacobi to 1e-10 -- one implicit-Euler step exactly as the GPU path takes
+    it.  Built once per process (mesh, conductivities, sparsity pattern)."""
 
-    from oracle import oracle as O
-    O.build("/nonexistent")
-    m, ek, rows, vals, h0 = make_deck()
-    slab = m.conn.reshape(NZ, NY, NX, 8)[:, :, :16, :].reshape(-1, 8)
-    ms = copy.copy(m)
-    ms.conn = np.ascontiguousarray(slab)
-    op = O.make_params(pcs_type=0, dt=DT, storage=SS)
-    rp, col = O.build_pattern(m.n_nodes, m.conn)
-    eks = ek.reshape(NZ, NY, NX)[:, :, :16].ravel().copy()
+    def __init__(self, dims=(NX, NY, NZ)):
+        from oracle import oracle as O
+        O.build("/nonexistent")  # the prebuilt restatement only
+        self.O = O
+        self.m, self.ek, self.rows, self.vals, self.h0 = make_deck(*dims)
+        self.rp, self.col = O.build_pattern(self.m.n_nodes, self.m.conn)
+        self.p = O.make_params(pcs_type=0, dt=DT, storage=SS)
+        self.b_norm = None
+
+    def step(self, u):
+        """One step from heads u: (new heads, CG iterations, assembly s, CG s)."""
+        O = self.O
+        t0 = time.perf_counter()
+        val, b = O.assemble(self.m, self.rp, self.col, self.p, elem_k=self.ek, u0=u)
+        O.dirichlet(self.rp, self.col, val, b, self.rows, self.vals, symmetric=True)
+        t1 = time.perf_counter()
+        x, info = O.solve(self.rp, self.col, val, b, u.copy(), method=5, precond=1, max_iter=20000, tol=TOL,
+                          b_norm=self.b_norm)
+        self.b_norm = info["b_norm"]  # Linear_EQS keeps |b| of the previous step for CheckNormRHS
+        return x, info["iterations"], t1 - t0, time.perf_counter() - t1
+
+
+def cpu_baseline_step():
+    """One full step of the deck on one core (the oracle port): no sample,
+    no extrapolation.  Returns (seconds, CG iterations, assembly s, CG s)."""
+    d = PortDeck()
     t0 = time.perf_counter()
-    O.assemble(ms, rp, col, op, elem_k=eks, u0=h0)
-    t_asm = (time.perf_counter() - t0) / len(slab)
-    # the cost of a CG iteration depends on the pattern, not on the values
-    val = np.full(len(col), 1e-3)
-    diag = np.nonzero(col == np.repeat(np.arange(m.n_nodes), np.diff(rp)))[0]
-    val[diag] = 1.0
-    b = np.ones(m.n_nodes)
-    t0 = time.perf_counter()
-    O.solve(rp, col, val, b, np.zeros(m.n_nodes), method=5, precond=1, max_iter=40, tol=1e-300)
-    t_it = (time.perf_counter() - t0) / 40
-    return t_asm, t_it
+    _, its, t_asm, t_cg = d.step(d.h0.copy())
+    return time.perf_counter() - t0, its, t_asm, t_cg
 
 
 # ------------------------------------------------------------------
@@ -897,6 +902,8 @@ def main():
         dist.barrier()
 
     N, nnz = gm.n_rows, gm.nnz
+    cfg = deck_config(world)
+    assert (cfg["nodes"], cfg["elements"], cfg["nnz"]) == (N, m.n_elements, nnz)
     hbm, peak_kind = peaks()
     pr = mix["prof"]
     t_spmv = pr["spmv_ms"] / max(1, pr["spmv_launches"])
@@ -920,9 +927,7 @@ def main():
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 inner CG, f64 residual/solution/convergence",
         "data": "synthetic (seeded GRF conductivity, generated mesh)",
-        "config": {"workload": WORKLOAD, "nodes": N, "elements": m.n_elements, "nnz": nnz,
-                   "l2": "inputs larger than L2 (FP64 matrix 343 MB re-assembled every step), no flush",
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "config": cfg,
         "p50_step_ms": round(float(np.percentile(mix["per"], 50)), 3),
         "p99_step_ms": round(float(np.percentile(mix["per"], 99)), 3),
         "max_rel_err_vs_fp64": err,
@@ -956,53 +961,182 @@ def main():
         out["batch"] = batch_leg(capi, torch, n_real=args.batch_reals, n_hi=args.batch_max_n,
                                  tol=args.batch_tol)
     if rank == 0 and not args.no_cpu_baseline:
-        t_asm, t_it = cpu_baseline_sample()
-        est = m.n_elements * t_asm + (f64["iters"] / k_steps) * t_it
-        out["cpu_baseline"] = {"value": round(1.0 / est, 6), "unit": "solves/s", "cores": 1,
-                               "kind": "port",
-                               "sample": (f"oracle C port, 1 thread: assembly of a 16-cell x-slab "
-                                          f"({t_asm*1e6:.2f} us/element) + 40 CG iterations on the full "
-                                          f"pattern ({t_it*1e3:.1f} ms/iter), extrapolated to "
-                                          f"{m.n_elements} elements + {f64['iters'] / k_steps:.0f} "
-                                          f"iterations/step")}
+        t_step, its, t_asm, t_cg = cpu_baseline_step()
+        out["cpu_baseline"] = {"value": round(1.0 / t_step, 6), "unit": "solves/s", "cores": 1, "kind": "port",
+                               "sample": (f"one full step of the deck (the first, from the initial heads) on one "
+                                          f"core by the oracle C port: assembly of {m.n_elements} hexes + "
+                                          f"Dirichlet {t_asm:.2f} s, CG + Jacobi to {TOL:g} {its} iterations "
+                                          f"{t_cg:.2f} s")}
         if "richards" in out:
             rr = out["richards"]
-            rr["cpu_baseline"] = richards_cpu_sample(rr["picard_iterations"], rr["linear_iterations"], t_it)
+            rr["cpu_baseline"] = richards_cpu_sample(rr["picard_iterations"], rr["linear_iterations"],
+                                                     t_cg / max(1, its))
     if rank == 0:
         print(json.dumps(out))
 
 
+def hex_pattern_nnz(nx, ny, nz):
+    """Stored entries of the 27-point pattern of an nx x ny x nz hex lattice:
+    per axis, (n + 1) nodes couple to 3 each except the 2 end nodes."""
+    return (3 * nx + 1) * (3 * ny + 1) * (3 * nz + 1)
+
+
+def deck_config(world=1):
+    """The workload's `config`, the same dict in both arms."""
+    return {"workload": WORKLOAD, "nodes": (NX + 1) * (NY + 1) * (NZ + 1), "elements": NX * NY * NZ,
+            "nnz": hex_pattern_nnz(NX, NY, NZ),
+            "l2": "inputs larger than L2 (FP64 matrix 343 MB re-assembled every step), no flush",
+            "parallelism": "replicas" if world > 1 else "single GPU"}
+
+
+def _split(total, workers):
+    q, r = divmod(total, workers)
+    return [q + (1 if i < r else 0) for i in range(workers)]
+
+
+def _reference_binary():
+    """The reference's own executable (oracle/_ref/ogs_sp, built from its
+    sources) when it exists and was built for this host's architecture."""
+    path = os.path.join(ROOT, "oracle", "_ref", "ogs_sp")
+    if not os.access(path, os.X_OK):
+        return None
+    try:
+        with open(path, "rb") as f:
+            head = f.read(20)
+    except OSError:
+        return None
+    machine = {62: "x86_64", 183: "aarch64"}.get(int.from_bytes(head[18:20], "little"))
+    return path if head[:4] == b"\x7fELF" and machine == platform.machine() else None
+
+
+def _port_worker(widx, n_warm, n_timed, barrier, q, dims):
+    """One process of the reference arm on the port: setup, its warm-up
+    steps, then its share of the timed steps (from the initial heads)."""
+    try:
+        d = PortDeck(dims)
+        barrier.wait(timeout=1800)
+        u = d.h0.copy()
+        for _ in range(n_warm):
+            u = d.step(u)[0]
+        barrier.wait(timeout=1800)
+        d.b_norm = None
+        u = d.h0.copy()
+        its = []
+        t0 = time.perf_counter()
+        for _ in range(n_timed):
+            u, it, _, _ = d.step(u)
+            its.append(it)
+        q.put((widx, t0, time.perf_counter(), its, None))
+    except BaseException as e:  # report, and release the others from the barrier
+        try:
+            barrier.abort()
+        except Exception:
+            pass
+        q.put((widx, 0.0, 0.0, [], repr(e)))
+
+
+def _run_port(workers, warm, timed, dims=(NX, NY, NZ)):
+    import multiprocessing as mp
+    import queue as Q
+    ctx = mp.get_context("spawn")
+    barrier = ctx.Barrier(workers)
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_port_worker, args=(i, warm[i], timed[i], barrier, q, dims))
+             for i in range(workers)]
+    for pr in procs:
+        pr.start()
+    res = []
+    try:
+        for _ in procs:
+            res.append(q.get(timeout=3600))
+    except Q.Empty:
+        res.append((-1, 0.0, 0.0, [], "a worker did not report"))
+    for pr in procs:
+        pr.join(timeout=60)
+        if pr.is_alive():
+            pr.kill()
+    errs = [r[4] for r in res if r[4]]
+    if errs:
+        raise RuntimeError("reference arm worker failed: " + errs[0])
+    wall = max(r[2] for r in res) - min(r[1] for r in res)
+    its = [it for r in res for it in r[3]]
+    return wall, its
+
+
+def _run_binary(binary, workers, warm, timed):
+    """The reference executable, one process per worker on its own copy of
+    the deck running its warm-up + timed steps; the timed span of a worker
+    runs from the assembly of its first timed step to the acceptance of its
+    last (the reference's own stdout markers)."""
+    import shutil
+    from concurrent.futures import ThreadPoolExecutor
+
+    from oracle import time_reference as TR
+    tmp = tempfile.mkdtemp(prefix="ogs_ref_arm_")
+
+    def one(i):
+        path = TR.write_deck(os.path.join(tmp, f"w{i}"), "sp", warm[i] + timed[i])
+        t_launch = time.perf_counter()
+        r = TR.run_reference(binary, path)
+        a = [t for k, t in r["marks"] if k == "assemble"]
+        acc = [t for k, t in r["marks"] if k == "accepted"]
+        if r["rc"] != 0 or len(a) < warm[i] + timed[i] or len(acc) < warm[i] + timed[i]:
+            raise RuntimeError(f"reference run {i}: rc {r['rc']}, {len(a)} assemblies, {len(acc)} accepted steps")
+        return t_launch + a[warm[i]], t_launch + acc[warm[i] + timed[i] - 1], len(r["iterations"])
+
+    try:
+        with ThreadPoolExecutor(workers) as ex:
+            res = list(ex.map(one, range(workers)))
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    return max(r[1] for r in res) - min(r[0] for r in res), [r[2] for r in res]
+
+
 def reference_arm(args, rank):
-    """CPU implementation of the path (the oracle; the reference's own build
-    needs its cmake-generated sources) on all host cores: one process per
-    core, each timing a bounded sample of one step."""
+    """The path on the host's cores without the GPU: the K timed steps
+    (after W warm-up steps) shared among one single-threaded process per
+    core, each step a full step of the deck (assembly of every hex,
+    Dirichlet, CG + Jacobi to 1e-10).  Runs the reference's own executable
+    where its build for this host exists, else the oracle's C restatement
+    of the same algorithm."""
     if rank != 0:
         return
-    import multiprocessing as mp
+    k_steps, warm_steps = max(1, args.steps), max(3, args.warmup)
     cores = os.cpu_count() or 1
-    t0 = time.perf_counter()
-    ctx = mp.get_context("spawn")
-    with ctx.Pool(cores) as pool:
-        res = pool.map(_ref_worker, range(cores))
-    wall = time.perf_counter() - t0
-    t_asm = statistics.median(r[0] for r in res)
-    t_it = statistics.median(r[1] for r in res)
-    est = NX * NY * NZ * t_asm + CG_ITERS_PER_STEP * t_it
-    value = cores / est
-    print(json.dumps({
-        "metric": "solves/s", "value": round(value, 6), "unit": "solves/s", "n_gpus": 0,
-        "steps": args.steps, "warmup": args.warmup, "impl": "reference",
-        "higher_is_better": True, "dtype": "f64", "config": {"workload": WORKLOAD},
-        "cpu_baseline": {"value": round(value, 6), "unit": "solves/s", "cores": cores, "kind": "port",
-                         "sample": (f"{cores} concurrent processes, each: assembly of a 16-cell x-slab "
-                                    f"+ 40 CG iterations on the full pattern, extrapolated to one step "
-                                    f"({CG_ITERS_PER_STEP} CG iterations); wall {wall:.1f} s")},
-        "e2e": {"value": round(value, 6), "unit": "solves/s", "h2d_bytes_per_step": 0,
-                "d2h_bytes_per_step": 0}}))
-
-
-def _ref_worker(i):
-    return cpu_baseline_sample()
+    workers = min(cores, k_steps)
+    warm, timed = _split(warm_steps, workers), _split(k_steps, workers)
+    binary = _reference_binary()
+    if binary:
+        wall, its = _run_binary(binary, workers, warm, timed)
+        kind = "reference"
+        what = (f"the reference OGS-5 (SP build: Linear_EQS, its own main), built from its sources by "
+                f"oracle/refbuild.mk, one process per core on its own copy of the deck")
+    else:
+        wall, its = _run_port(workers, warm, timed)
+        kind = "port"
+        what = ("the oracle's C restatement of the reference's assembly, Dirichlet elimination and "
+                "Linear_EQS::CG + Jacobi, one process per core; the reference's own executable is not used "
+                "here: its sources are not on this host and its build from them is for another "
+                "architecture")
+    value = k_steps / wall
+    out = {"metric": "solves/s", "value": round(value, 6), "unit": "solves/s", "n_gpus": 0,
+           "steps": k_steps, "warmup": warm_steps, "ms_per_step": round(1e3 * wall / k_steps, 1),
+           "impl": "reference", "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f64", "data": "synthetic (seeded GRF conductivity, generated mesh)",
+           "config": deck_config(int(os.environ.get("WORLD_SIZE", "1"))),
+           "cpu_baseline": {"value": round(value, 6), "unit": "solves/s", "cores": workers, "kind": kind,
+                            "sample": (f"{what}: {k_steps} full steps of the deck from the initial heads "
+                                       f"(shares {timed}) after {warm_steps} warm-up steps, wall {wall:.1f} s "
+                                       f"between barriers on {platform.machine()}")},
+           "e2e": {"value": round(value, 6), "unit": "solves/s", "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": 0}}
+    if kind == "port":
+        out["cpu_baseline"]["cg_iterations_per_step"] = round(float(np.mean(its)), 1)
+    cal = os.path.join(ROOT, "oracle", "reference_timing.json")
+    if os.path.exists(cal):
+        with open(cal) as f:
+            out["calibration"] = json.load(f).get("summary")
+    print(json.dumps(out))
 
 
 if __name__ == "__main__":

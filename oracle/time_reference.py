@@ -30,6 +30,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
+if sys.path and os.path.abspath(sys.path[0]) == HERE:
+    sys.path.pop(0)  # run as a script: oracle/oracle.py must not shadow the oracle package
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
 
@@ -142,7 +144,7 @@ def main():
     args = ap.parse_args()
     res = {"host": os.uname().machine, "cores_used": 1}
     tmp = tempfile.mkdtemp(prefix="ogs_time_")
-    for build in args.builds.split(","):
+    for build in [b for b in args.builds.split(",") if b]:
         binary = os.path.join(HERE, "_ref", "ogs_" + build)
         path = write_deck(os.path.join(tmp, build), build, args.steps)
         res["reference_" + build] = run_reference(binary, path)
@@ -150,9 +152,52 @@ def main():
     if not args.no_port:
         res["port"] = time_port()
         print("port", res["port"], flush=True)
+    res["summary"] = summarise(res)
     if args.out:
         with open(args.out, "w") as f:
             json.dump(res, f, indent=1)
+
+
+def _steps(r):
+    """Per step of a reference run: assembly, linear solve and the rest of
+    the step (Cal_Velocity, output), seconds, from the stdout markers."""
+    out, mk = [], r.get("marks", [])
+    starts = [i for i, (k, _) in enumerate(mk) if k == "assemble"]
+    for q, i in enumerate(starts):
+        end = starts[q + 1] if q + 1 < len(starts) else len(mk)
+        t = {k: v for k, v in mk[i:end]}
+        if "solve" in t and "accepted" in t:
+            after = t.get("velocity", t["accepted"])
+            out.append({"assembly_s": round(t["solve"] - t["assemble"], 2),
+                        "solve_s": round(after - t["solve"], 2),
+                        "rest_s": round(t["accepted"] - after, 2)})
+    return out
+
+
+def summarise(res):
+    """Assembly + linear solve of a step, reference builds against the
+    oracle's C restatement on the same host."""
+    s = {"host": res["host"], "deck": "hex 128 x 128 x 64, 1,081,665 nodes, 1,048,576 hexes, CG + Jacobi 1e-10"}
+    for key in ("reference_sp", "reference_fem"):
+        if key in res:
+            st = _steps(res[key])
+            its = res[key].get("iterations", [])
+            s[key] = {"setup_s": round(res[key].get("setup_s", 0.0), 1), "steps": st,
+                      "linear_iterations": its[:len(st)]}
+    if "port" in res:
+        p = res["port"]
+        s["port"] = {"assembly_s": round(p["assembly_s"], 2), "solve_s": round(p["cg_s"], 2),
+                     "linear_iterations": p["cg_iterations"]}
+        if "reference_sp" in s and s["reference_sp"]["steps"]:
+            f = s["reference_sp"]["steps"][0]
+            ip = max(1, p["cg_iterations"])
+            ir = max(1, (s["reference_sp"]["linear_iterations"] or [ip])[0])
+            s["reference_sp_over_port"] = {
+                "assembly": round(f["assembly_s"] / p["assembly_s"], 2),
+                "time_per_cg_iteration": round((f["solve_s"] / ir) / (p["cg_s"] / ip), 2),
+                "first_step_assembly_plus_solve": round((f["assembly_s"] + f["solve_s"]) /
+                                                        (p["assembly_s"] + p["cg_s"]), 2)}
+    return s
 
 
 if __name__ == "__main__":

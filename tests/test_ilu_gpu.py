@@ -69,7 +69,7 @@ def test_bicgstab_ilu0_transport(gpu, oracle, kind):
     xj = x0.copy()
     itj = eqs.Solver(xj)
     assert it < itj
-    assert rel_max_err(xj, xo) < 1e-9
+    assert rel_max_err(xj, xo) < SOLUTION_RTOL
 
 
 @pytest.mark.parametrize("kind", ["quad", "hex", "tet"])

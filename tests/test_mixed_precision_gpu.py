@@ -59,8 +59,9 @@ def test_fp32_refined_matches_fp64(gpu, kind):
     assert st["status"] == gpu.OK and st["rel_residual"] < 1e-10
     assert st["refinements"] >= 2
     assert rel_max_err(x32, x64) < MIXED_RTOL
-    # residual replacement keeps the Krylov space: iterations near the FP64 count
-    assert it32 <= 1.6 * it64 + 20
+    # residual replacement keeps the Krylov space: iterations near the FP64
+    # count (measured 1.10 x on hex and 1.12 x on tet)
+    assert it32 <= 1.2 * it64 + 5
 
 
 def test_fp32_refined_config1_quads(gpu):

@@ -1,17 +1,18 @@
 """RICHARDS_FLOW on the GPU (ogs_gpu_assemble_richards, ogs_gpu_richards_step)
 against the oracle: the assembled system at a partly unsaturated iterate
 within 1e-12 per entry, and a Picard time step with the same number of
-iterations and the same heads (1e-9 relative, the linear solves stopping at
-1e-12)."""
+iterations and the same heads (1e-10 relative, the linear solves stopping at
+1e-13)."""
 import numpy as np
 import pytest
 
 from ogs5_gb300 import mesh as M
-from tests.helpers import assert_matrix_close, assert_vector_close, distort, rel_max_err
+from tests.helpers import SOLUTION_RTOL, assert_matrix_close, assert_vector_close, distort, rel_max_err
 
 pytestmark = pytest.mark.gpu
 
 RHO_G = 1000.0 * 9.81
+LINEAR_TOL = 1e-13  # linear solves inside the Picard loops, GPU and oracle
 
 
 def _mesh(kind):
@@ -84,17 +85,17 @@ def test_richards_picard_step_matches_oracle(gpu, oracle, kind, method):
     rows = np.concatenate([top, bottom])
     vals = np.concatenate([np.zeros(len(top)), np.full(len(bottom), -1.0e4)])
     eqs = gpu.LinearEQS(gpu.GpuMesh(m))
-    eqs.ConfigNumerics(gpu.LS_CG, gpu.PRECOND_JACOBI, 5000, 1e-12, check_norm_rhs=False)
+    eqs.ConfigNumerics(gpu.LS_CG, gpu.PRECOND_JACOBI, 5000, LINEAR_TOL, check_norm_rhs=False)
     it = p_old.copy()
     st = eqs.RichardsStep(gp, gr, ek, p_old, it, rows, vals, gpu.DIRICHLET_SYMMETRIC, error_method=method,
                           max_iterations=30, tolerance=1e-3 if method == 4 else 1.0)
     orp, ocol = oracle.build_pattern(m.n_nodes, m.conn)
     oit, info = oracle.richards_picard(m, orp, ocol, op, orr, ek, p_old, p_old, rows, vals, True,
                                        error_method=method, tolerance=1e-3 if method == 4 else 1.0,
-                                       max_iterations=30, method=5, precond=1, tol=1e-12)
+                                       max_iterations=30, method=5, precond=1, tol=LINEAR_TOL)
     assert st["converged"] and info["converged"]
     assert st["iterations"] == info["iterations"] and st["iterations"] >= 3
-    assert rel_max_err(it, oit) < 1e-9
+    assert rel_max_err(it, oit) < SOLUTION_RTOL
     # the wetting front: pressures rose from the dry state, top held at 0
     assert np.all(it[top] == 0.0) and it.max() <= 1e-6 and np.mean(it) > -1.0e4
 
@@ -112,7 +113,7 @@ def test_richards_relaxation_and_stagnation(gpu, oracle):
     vals = np.zeros(len(top))
     orp, ocol = oracle.build_pattern(m.n_nodes, m.conn)
     eqs = gpu.LinearEQS(gpu.GpuMesh(m))
-    eqs.ConfigNumerics(gpu.LS_CG, gpu.PRECOND_JACOBI, 5000, 1e-12, check_norm_rhs=False)
+    eqs.ConfigNumerics(gpu.LS_CG, gpu.PRECOND_JACOBI, 5000, LINEAR_TOL, check_norm_rhs=False)
     for dt, dry, ok in ((10.0, -5.0e3, True), (60.0, -2.0e4, False)):
         gp, op = _params(gpu, oracle, dt=dt, gravity=9.81, gravity_on=1, nls_relaxation=0.5)
         p_old = np.full(m.n_nodes, dry)
@@ -120,12 +121,12 @@ def test_richards_relaxation_and_stagnation(gpu, oracle):
         st = eqs.RichardsStep(gp, gr, ek, p_old, it, top, vals, gpu.DIRICHLET_SYMMETRIC, error_method=2,
                               max_iterations=40, tolerance=1.0, allow_fail=True)
         oit, info = oracle.richards_picard(m, orp, ocol, op, orr, ek, p_old, p_old, top, vals, True, error_method=2,
-                                           tolerance=1.0, max_iterations=40, tol=1e-12)
+                                           tolerance=1.0, max_iterations=40, tol=LINEAR_TOL)
         assert st["iterations"] == info["iterations"]
         assert st["converged"] == info["converged"] == ok and st["diverged"] == info["diverged"] == (not ok)
         assert st["status"] == (gpu.OK if ok else gpu.NOT_CONVERGED)
         if ok:
-            assert rel_max_err(it, oit) < 1e-9
+            assert rel_max_err(it, oit) < SOLUTION_RTOL
 
 
 def test_richards_rejects_bad_input(gpu):
