@@ -584,7 +584,8 @@ SERVE_WARM_SLOTS = 4      # slots per class created before the timed run
 # requests: p50 267 ms against 508 ms for arrival order with 128 in flight,
 # the same throughput)
 SERVE_MAX_ACTIVE = 16
-SERVE_FLAGS = 7           # capi.SERVER_PRIORITY | capi.SERVER_SJF | capi.SERVER_BATCH
+# capi.SERVER_PRIORITY | SERVER_SJF | SERVER_BATCH | SERVER_PRECISION_FALLBACK
+SERVE_FLAGS = 15
 SERVE_WORKLOAD = ("Poisson arrivals 200/s of flow (steady GWF, heads 10/0 m on the x faces) and transport "
                   "(one MASS_TRANSPORT step, flux from a linear head field) requests on quad, hex and "
                   "hex-split-tet meshes, 1e4-2e6 DOF log-uniform (5 size classes per type), log-normal K "
@@ -713,8 +714,10 @@ def serve_leg(capi, torch, n_req=SERVE_REQUESTS, flags=None, max_active=None, pl
     policy = {"max_active": max_active, "priority_streams": bool(flags & capi.SERVER_PRIORITY),
               "admission": "smallest class first" if flags & capi.SERVER_SJF else "arrival order",
               "dynamic_batching": bool(flags & capi.SERVER_BATCH),
+              "fp64_after_fp32_fallback": bool(flags & capi.SERVER_PRECISION_FALLBACK),
               "fp32_internal_tol": "a tenth of the request's tolerance"}
     served["batched"] = info["batched"]
+    served["fp64_classes"] = info["fp64_classes"]
     served["by_kind"] = _serve_breakdown(reqs, res)
     srv.close()
     if not plain:

@@ -598,12 +598,16 @@ typedef struct
     double solve_ms;            /* device time of the solve                    */
     int32_t batch_size;         /* requests of the batch launch that served it
                                    (0: served alone on a slot)                 */
+    int32_t precision;          /* OGS_PRECISION_* the request was solved in   */
+    int32_t fp64_fallback;      /* FP32-inner solve finished in FP64 CG        */
     int32_t pad0;
 } ogs_server_result;
 
 typedef struct
 {
-    int32_t slots, running, queued, pad0;
+    int32_t slots, running, queued;
+    int32_t fp64_classes;       /* FP32 classes served in FP64 after a fallback
+                                   (OGS_SERVER_PRECISION_FALLBACK)             */
     int64_t completed;
     int64_t bytes_used, bytes_budget;
     int64_t batched;            /* requests served by batch launches           */
@@ -616,6 +620,10 @@ enum
     OGS_SERVER_SJF = 2,       /* admit the queued request of the smallest class
                                  first (arrival order among equals); default:
                                  arrival order                                 */
+    OGS_SERVER_PRECISION_FALLBACK = 8, /* a class whose FP32-inner solve finished
+                                 in FP64 CG (the FP32 cycles stopped gaining,
+                                 ogs_solve_stats.fp64_fallback) is served in
+                                 FP64 from its next request on              */
     OGS_SERVER_BATCH = 4      /* dynamic batching: two or more queued requests
                                  of one steady hex-lattice flow class (heads on
                                  the two x faces, FP32-inner CG) with the same

@@ -57,7 +57,7 @@ EXPORTS = [
 REQUEST_FLOW, REQUEST_TRANSPORT = 0, 1
 RICHARDS_FLOW = 3
 LMAX, ENORM, EVNORM, ERNORM = 1, 2, 3, 4
-SERVER_PRIORITY, SERVER_SJF, SERVER_BATCH = 1, 2, 4
+SERVER_PRIORITY, SERVER_SJF, SERVER_BATCH, SERVER_PRECISION_FALLBACK = 1, 2, 4, 8
 NOALLOC_MAX_ROWS = 524288
 
 
@@ -139,11 +139,11 @@ class ServerResult(C.Structure):
     _fields_ = [("state", C.c_int32), ("status", C.c_int32), ("iterations", C.c_int32),
                 ("refinements", C.c_int32), ("rel_residual", C.c_double), ("latency_ms", C.c_double),
                 ("queue_ms", C.c_double), ("solve_ms", C.c_double), ("batch_size", C.c_int32),
-                ("pad0", C.c_int32)]
+                ("precision", C.c_int32), ("fp64_fallback", C.c_int32), ("pad0", C.c_int32)]
 
 
 class ServerInfo(C.Structure):
-    _fields_ = [("slots", C.c_int32), ("running", C.c_int32), ("queued", C.c_int32), ("pad0", C.c_int32),
+    _fields_ = [("slots", C.c_int32), ("running", C.c_int32), ("queued", C.c_int32), ("fp64_classes", C.c_int32),
                 ("completed", C.c_int64), ("bytes_used", C.c_int64), ("bytes_budget", C.c_int64),
                 ("batched", C.c_int64)]
 
@@ -688,13 +688,15 @@ class Server:
             self._refs.pop(rid, None)
         return {"state": r.state, "status": r.status, "iterations": r.iterations,
                 "refinements": r.refinements, "rel_residual": r.rel_residual, "latency_ms": r.latency_ms,
-                "queue_ms": r.queue_ms, "solve_ms": r.solve_ms, "batch_size": r.batch_size}
+                "queue_ms": r.queue_ms, "solve_ms": r.solve_ms, "batch_size": r.batch_size,
+                "precision": r.precision, "fp64_fallback": r.fp64_fallback}
 
     def info(self) -> dict:
         i = ServerInfo()
         _check(lib().ogs_gpu_server_info(self.h, C.byref(i)))
         return {"slots": i.slots, "running": i.running, "queued": i.queued, "completed": i.completed,
-                "bytes_used": i.bytes_used, "bytes_budget": i.bytes_budget, "batched": i.batched}
+                "bytes_used": i.bytes_used, "bytes_budget": i.bytes_budget, "batched": i.batched,
+                "fp64_classes": i.fp64_classes}
 
 
 class Deck:

@@ -75,6 +75,7 @@ struct SrvClass
     size_t bytes = 0;          // device bytes of one slot
     int64_t n = 0, ngp = 0, ne = 0;
     int priority = 0;          // CUDA stream priority of its slots
+    bool fp64_only = false;    // an FP32-inner solve of the class fell back to FP64
     // the Monte-Carlo batch's problem (steady flow on a hex lattice, heads on
     // the two x faces): lattice, cells, spacing and face heads
     bool batchable = false;
@@ -100,6 +101,7 @@ struct SrvSlot
     ogs_system* sys = nullptr;
     double* q = nullptr;       // transport: Gauss-point flux
     cudaStream_t stream = nullptr;  // owned by the server, priority by class size
+    int precision = -1;        // OGS_PRECISION_* its system is configured for
     bool busy = false;
     int64_t last_used = 0;
 };
@@ -115,6 +117,7 @@ struct SrvReq
     ogs_status status = OGS_OK;
     ogs_solve_stats st{};
     int batch_size = 0;        // requests of the batch launch that served it (0: a slot)
+    int precision = -1;        // OGS_PRECISION_* it was solved in
     Clock::time_point t_submit, t_admit, t_done;
 };
 
@@ -151,6 +154,18 @@ void release_slot(ogs_server* S, size_t k)
         if (S->reqs[id].slot > (int)k) S->reqs[id].slot -= 1;
 }
 
+// the solver configuration of a class's slots: the class's own, or FP64 CG
+// of the same method once an FP32-inner solve of the class fell back
+ogs_status configure_slot(SrvSlot& sl, const SrvClass& C)
+{
+    ogs_solver_config cfg = C.c.solver;
+    if (C.fp64_only) cfg.precision = OGS_PRECISION_FP64;
+    if (sl.precision == cfg.precision) return OGS_OK;
+    const ogs_status st = ogs_gpu_configure(sl.sys, &cfg);
+    if (st == OGS_OK) sl.precision = cfg.precision;
+    return st;
+}
+
 // a slot of class c, while fewer than max_active requests run: an idle
 // one, or a new one within the budget
 int acquire_slot(ogs_server* S, int c)
@@ -180,7 +195,7 @@ int acquire_slot(ogs_server* S, int c)
         cudaStreamDestroy(sl.stream);
         return -2;
     }
-    if (ogs_gpu_configure(sl.sys, &C.c.solver) ||
+    if (configure_slot(sl, C) ||
         system_upload_dirichlet(sl.sys, C.bc_rows.data(), C.bc_vals.data(), (int64_t)C.bc_rows.size(),
                                 C.c.bc_mode))
     {
@@ -208,9 +223,13 @@ ogs_status start(ogs_server* S, int64_t id, int k)
     const SrvClass& C = S->classes[R.cls];
     ogs_system* s = sl.sys;
     cudaStream_t st = system_stream(s);
+    ogs_status e = configure_slot(sl, C);
+    if (e) return e;
+    R.precision = sl.precision;
+    // FP32 classes stop at a tenth of the tolerance, also when served in FP64
+    // after a fallback, so their heads stay as close to the converged ones
     system_reset_request(s, C.c.solver.precision != OGS_PRECISION_FP64 ? R.tol * kServedTolFactor : R.tol);
     OGS_CUDA_TRY(cudaMemcpyAsync(R.out, C.x0, C.n * sizeof(double), cudaMemcpyDefault, st));
-    ogs_status e;
     if (C.c.kind == OGS_REQUEST_TRANSPORT)
     {
         if ((e = system_enqueue_velocity(s, &C.c.flow_params, R.elem_k, C.u_flow, sl.q))) return e;
@@ -401,6 +420,7 @@ ogs_status run_batch(ogs_server* S, int k, const std::vector<int64_t>& ids)
         R.st.solve_ms = bs[r].finish_ms;
         R.st.fp32_operator = 0;
         R.status = (ogs_status)bs[r].status;
+        R.precision = OGS_PRECISION_FP32_REFINED;
     }
     return OGS_OK;
 }
@@ -567,6 +587,8 @@ extern "C" ogs_status ogs_gpu_server_progress(ogs_server* S, int32_t* n_running,
         }
         R.t_done = Clock::now();
         R.state = 2;
+        if ((S->flags & OGS_SERVER_PRECISION_FALLBACK) && R.st.fp64_fallback)
+            S->classes[R.cls].fp64_only = true;
         sl.busy = false;
         sl.last_used = S->tick;
         S->completed += 1;
@@ -582,7 +604,7 @@ extern "C" ogs_status ogs_gpu_server_progress(ogs_server* S, int32_t* n_running,
                 if (S->classes[S->reqs[S->queue[q]].cls].n < S->classes[S->reqs[S->queue[pick]].cls].n) pick = q;
         const int64_t id = S->queue[pick];
         SrvReq& R = S->reqs[id];
-        if ((S->flags & OGS_SERVER_BATCH) && S->classes[R.cls].batchable)
+        if ((S->flags & OGS_SERVER_BATCH) && S->classes[R.cls].batchable && !S->classes[R.cls].fp64_only)
         {
             // same class and tolerance, in queue order from the picked one
             std::vector<size_t> at;
@@ -668,6 +690,8 @@ extern "C" ogs_status ogs_gpu_server_result(const ogs_server* S, int64_t request
         r->queue_ms = R.slot >= 0 || R.batch_size ? ms_between(R.t_submit, R.t_admit) : r->latency_ms;
         r->solve_ms = R.st.solve_ms;
         r->batch_size = R.batch_size;
+        r->precision = R.precision;
+        r->fp64_fallback = R.st.fp64_fallback;
     }
     return OGS_OK;
 }
@@ -681,6 +705,7 @@ extern "C" ogs_status ogs_gpu_server_info(const ogs_server* S, ogs_server_info* 
     info->queued = (int32_t)S->queue.size();
     info->completed = S->completed;
     info->batched = S->batched;
+    for (const SrvClass& C : S->classes) info->fp64_classes += C.fp64_only ? 1 : 0;
     info->bytes_used = (int64_t)S->used;
     info->bytes_budget = (int64_t)S->budget;
     return OGS_OK;

@@ -217,3 +217,42 @@ def test_server_admission_respects_budget_and_max_active(gpu):
     assert srv2.result(rid)["state"] == 0  # nothing fits a 1-byte budget: stays queued
     srv2.close()
     del one
+
+
+@pytest.mark.parametrize("policy", [True, False])
+def test_server_serves_a_stalling_class_in_fp64(gpu, policy):
+    """Steady heterogeneous 375 x 375 quads, where the FP32 recurrence stalls
+    and the solve finishes in FP64 CG: with OGS_SERVER_PRECISION_FALLBACK the
+    class's next request is solved in FP64 from the start; without it, in
+    the FP32-inner mode again.  Heads within 1e-8 of an FP64 solve to 1e-13
+    either way."""
+    torch = pytest.importorskip("torch")
+    m = M.structured_quad(375, 375)
+    gm = gpu.GpuMesh(m)
+    lf, rf = m.face_nodes(0, 0), m.face_nodes(0, 1)
+    rows = np.concatenate([lf, rf])
+    vals = np.concatenate([np.full(len(lf), 10.0), np.zeros(len(rf))])
+    p = gpu.make_params(gpu.GROUNDWATER_FLOW, steady=1)
+    cfg = gpu.solver_config(gpu.LS_CG, gpu.PRECOND_JACOBI, 20000, precision=gpu.PRECISION_FP32_REFINED)
+    srv = gpu.Server(max_active=4, flags=gpu.SERVER_PRECISION_FALLBACK if policy else 0)
+    cid = srv.add_class(gm, gpu.REQUEST_FLOW, p, rows, vals, gpu.DIRICHLET_SYMMETRIC, cfg)
+    ks = [torch.tensor(fields.lognormal_k(m.shape, np.log(1e-5), 1.0, 8.0, seed=3 + q), device="cuda")
+          for q in range(2)]
+    outs = [torch.zeros(m.n_nodes, dtype=torch.float64, device="cuda") for _ in range(2)]
+    res = []
+    for q in range(2):
+        rid = srv.submit(cid, ks[q], 1e-10, outs[q])
+        srv.drain()
+        res.append(srv.result(rid))
+    assert all(r["status"] == gpu.OK for r in res)
+    assert res[0]["precision"] == gpu.PRECISION_FP32_REFINED and res[0]["fp64_fallback"] == 1
+    if policy:
+        assert res[1]["precision"] == gpu.PRECISION_FP64 and res[1]["fp64_fallback"] == 0
+        assert srv.info()["fp64_classes"] == 1
+    else:
+        assert res[1]["precision"] == gpu.PRECISION_FP32_REFINED
+        assert srv.info()["fp64_classes"] == 0
+    for q in range(2):
+        x = _fp64_converged(gpu, gm, m, p, ks[q], rows, vals)
+        assert rel_max_err(outs[q].cpu().numpy(), x) < 1e-8
+    srv.close()
