@@ -101,21 +101,27 @@ __global__ void k_dirichlet_symmetric(const int32_t* __restrict__ slice_ptr,
                                       const int32_t* __restrict__ row_len, const int32_t* __restrict__ col,
                                       const int32_t* __restrict__ diag_pos, double* val, double* b,
                                       const unsigned char* __restrict__ flag,
-                                      const double* __restrict__ valn, const double* __restrict__ valf, int n)
+                                      const double* __restrict__ valn, const double* __restrict__ valf,
+                                      const int32_t* __restrict__ rows, int n)
 {
     // MXRandbed (matrix_routines.cpp:2314-2520): lift column into b, zero
     // row and column, keep the diagonal (a zero diagonal -> DBL_EPSILON).
     // A row given twice is lifted with its first value (the column is zero
     // afterwards) and keeps its last value on the diagonal, as the
-    // sequential SetKnownX loop leaves it.
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    // sequential SetKnownX loop leaves it.  rows: the Dirichlet rows and the
+    // rows with a Dirichlet column, in row order (every other row is left as
+    // it is); one thread per row, the column loads of a group of entries
+    // issued together before the flags.
+    constexpr int G = 16;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x)
     {
+        const int i = rows[q];
+        const SellRow R(slice_ptr, row_len, i);
         if (flag[i])
         {
             const int dp = diag_pos[i];
             double d = dp >= 0 ? val[dp] : 0.0;
             if (fabs(d) < DBL_MIN) d = DBL_EPSILON;
-            const SellRow R(slice_ptr, row_len, i);
             for (int j = 0; j < R.len; j++) val[R.slot(j)] = 0.0;
             if (dp >= 0) val[dp] = d;
             b[i] = valn[i] * d;
@@ -123,16 +129,22 @@ __global__ void k_dirichlet_symmetric(const int32_t* __restrict__ slice_ptr,
         else
         {
             double bi = b[i];
-            const SellRow R(slice_ptr, row_len, i);
-            for (int j = 0; j < R.len; j++)
+            for (int j0 = 0; j0 < R.len; j0 += G)
             {
-                const int k = R.slot(j);
-                const int c = col[k];
-                if (flag[c])
-                {
-                    bi -= val[k] * valf[c];
-                    val[k] = 0.0;
-                }
+                int c[G];
+#pragma unroll
+                for (int t = 0; t < G; t++) c[t] = j0 + t < R.len ? col[R.slot(j0 + t)] : -1;
+                bool f[G];
+#pragma unroll
+                for (int t = 0; t < G; t++) f[t] = c[t] >= 0 && flag[c[t]];
+#pragma unroll
+                for (int t = 0; t < G; t++)
+                    if (f[t])
+                    {
+                        const int k = R.slot(j0 + t);
+                        bi -= val[k] * valf[c[t]];
+                        val[k] = 0.0;
+                    }
             }
             b[i] = bi;
         }
@@ -154,6 +166,19 @@ __global__ void k_mark_rows(unsigned char* flag, double* valn, double* valf, con
         flag[rows[q]] = 1;
         valn[rows[q]] = vals[q];
         valf[rows[q]] = vfirst[q];
+    }
+}
+
+// the rows a symmetric Dirichlet set touches: its own rows and, the
+// pattern being structurally symmetric, the columns of their rows
+__global__ void k_mark_touched(const int32_t* __restrict__ slice_ptr, const int32_t* __restrict__ row_len,
+                               const int32_t* __restrict__ col, const int32_t* __restrict__ rows, int nbc,
+                               unsigned char* touch)
+{
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nbc; q += gridDim.x * blockDim.x)
+    {
+        const SellRow R(slice_ptr, row_len, rows[q]);
+        for (int j = 0; j < R.len; j++) touch[col[R.slot(j)]] = 1;
     }
 }
 
@@ -223,13 +248,22 @@ struct ogs_system
     ogs_solver_config cfg{};
     bool configured = false;
     double bnorm_prev = 1.0;  // Linear_EQS ctor: bNorm = 1.0
+    bool val_zero = true;     // val holds zeros only (Initialize, nothing added since)
     // Dirichlet
     int nbc = 0;
     int bc_mode = OGS_DIRICHLET_ROW_ONLY;
+    // the set on the device, as uploaded (rows, values, first values): an
+    // identical upload leaves the device arrays as they are
+    std::vector<int32_t> bc_host_rows;
+    std::vector<double> bc_host_vals, bc_host_vfirst;
+    bool bc_host_valid = false;
     int32_t* bc_rows = nullptr;
     double* bc_vals = nullptr;
     int bc_cap = 0;
     unsigned char* bc_flag = nullptr;
+    int32_t* bc_touch = nullptr;   // symmetric sets: the rows the elimination changes
+    unsigned char* bc_mask = nullptr;
+    int ntouch = 0;
     double* bc_valn = nullptr;
     double* bc_valf = nullptr;
     double* bc_vfirst = nullptr;
@@ -412,6 +446,8 @@ extern "C" ogs_status ogs_gpu_system_destroy(ogs_system* s)
     cudaFree(s->d_bad);
     cudaFree(s->bc_rows);
     cudaFree(s->bc_flag);
+    cudaFree(s->bc_touch);
+    cudaFree(s->bc_mask);
     if (s->h_st) cudaFreeHost(s->h_st);
     if (s->h_bad) cudaFreeHost(s->h_bad);
     for (int i = 0; i < ogs_system::kChunk; i++)
@@ -542,6 +578,7 @@ extern "C" ogs_status ogs_gpu_initialize(ogs_system* s)
     if (!s) { set_error("initialize: NULL system"); return OGS_BAD_ARG; }
     OGS_CUDA_TRY(cudaMemsetAsync(s->val, 0, s->m->sell_nnz * sizeof(double), s->stream));
     OGS_CUDA_TRY(cudaMemsetAsync(s->b, 0, (size_t)s->n * sizeof(double), s->stream));
+    s->val_zero = true;
     return mf_reset(s);
 }
 
@@ -593,6 +630,7 @@ static ogs_status enqueue_element_kernel(ogs_system* s, const ogs_assembly_param
     if ((st = stage_in(s, gpv, (size_t)m->n_elem * m->ngp * 3, &s->gpv, &a.gpv))) return st;
     if ((st = stage_in(s, u1, m->n_nodes, &s->u1, &a.u1))) return st;
     if (rp) a.r = *rp;
+    a.val_store = kind == 0 && a.val == s->val && s->val_zero ? 1 : 0;
     k_set_int<<<1, 1, 0, s->stream>>>(s->d_bad, kNoBadElement);
     OGS_LAUNCH_CHECK();
     if (!launch_assembly(m, a, m->affine, kind, s->stream))
@@ -601,6 +639,7 @@ static ogs_status enqueue_element_kernel(ogs_system* s, const ogs_assembly_param
         return OGS_BAD_ARG;
     }
     OGS_LAUNCH_CHECK();
+    if (kind != 2 && a.val == s->val) s->val_zero = false;  // the velocity kernel writes q only
     // the cell-coefficient form holds for flow without mass lumping
     if (kind == 0 && s->mf_state == 1)
     {
@@ -679,6 +718,7 @@ extern "C" ogs_status ogs_gpu_assemble(ogs_system* s, const ogs_assembly_params*
     if ((st = stage_in(s, u0, m->n_nodes, &s->u0, &du))) return st;
     k_mt_from_operators<<<vec_grid(s->n), 256, 0, s->stream>>>(m->slice_ptr, m->row_len, m->sell_col, s->op_mass,
                                                              s->op_k, du, 1.0 / p->dt, p->theta, s->val, s->b, s->n);
+    s->val_zero = false;
     OGS_LAUNCH_CHECK();
     OGS_CUDA_TRY(cudaStreamSynchronize(s->stream));
     return OGS_OK;
@@ -961,6 +1001,13 @@ static ogs_status dirichlet_upload(ogs_system* s, const int64_t* rows, const dou
         vh.swap(vu);
         n_rows = (int64_t)r32.size();
     }
+    auto same_bits = [](const std::vector<double>& x, const std::vector<double>& y) {
+        return x.size() == y.size() && (x.empty() || std::memcmp(x.data(), y.data(), x.size() * sizeof(double)) == 0);
+    };
+    if (s->bc_host_valid && s->bc_mode == mode && s->bc_host_rows == r32 && same_bits(s->bc_host_vals, vh) &&
+        same_bits(s->bc_host_vfirst, vfirst))
+        return OGS_OK;
+    s->bc_host_valid = false;
     if (n_rows > s->bc_cap)
     {
         cudaFree(s->bc_rows);
@@ -989,9 +1036,33 @@ static ogs_status dirichlet_upload(ogs_system* s, const int64_t* rows, const dou
         k_mark_rows<<<g, 256, 0, s->stream>>>(s->bc_flag, s->bc_valn, s->bc_valf, s->bc_rows, s->bc_vals,
                                               s->bc_vfirst, s->nbc);
         OGS_LAUNCH_CHECK();
+        // the touched rows, through a byte mask, listed in row order (warps
+        // on neighbouring rows share the SELL segments of their entries)
+        ogs_mesh* m = s->m;
+        if (!s->bc_touch) OGS_CUDA_TRY(cudaMalloc(&s->bc_touch, std::max(1, s->n) * sizeof(int32_t)));
+        if (!s->bc_mask) OGS_CUDA_TRY(cudaMalloc(&s->bc_mask, std::max(1, s->n)));
+        OGS_CUDA_TRY(cudaMemsetAsync(s->bc_mask, 0, s->n, s->stream));
+        k_mark_touched<<<g, 256, 0, s->stream>>>(m->slice_ptr, m->row_len, m->sell_col, s->bc_rows, s->nbc,
+                                                 s->bc_mask);
+        OGS_LAUNCH_CHECK();
+        std::vector<unsigned char> hm((size_t)s->n);
+        OGS_CUDA_TRY(cudaMemcpyAsync(hm.data(), s->bc_mask, s->n, cudaMemcpyDeviceToHost, s->stream));
+        OGS_CUDA_TRY(cudaStreamSynchronize(s->stream));
+        std::vector<int32_t> list;
+        for (int i = 0; i < s->n; i++)
+            if (hm[i]) list.push_back(i);
+        s->ntouch = (int)list.size();
+        if (!list.empty())
+            OGS_CUDA_TRY(cudaMemcpyAsync(s->bc_touch, list.data(), list.size() * sizeof(int32_t),
+                                         cudaMemcpyHostToDevice, s->stream));
+        OGS_CUDA_TRY(cudaStreamSynchronize(s->stream));  // list is a host array
     }
     // the host staging vectors must outlive the copies above
     OGS_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    s->bc_host_rows = r32;
+    s->bc_host_vals = vh;
+    s->bc_host_vfirst = vfirst;
+    s->bc_host_valid = true;
     return OGS_OK;
 }
 
@@ -1000,6 +1071,7 @@ static ogs_status dirichlet_upload(ogs_system* s, const int64_t* rows, const dou
 static ogs_status dirichlet_apply(ogs_system* s)
 {
     if (!s->nbc) return OGS_OK;
+    s->val_zero = false;
     ogs_mesh* m = s->m;
     if (s->bc_mode == OGS_DIRICHLET_ROW_ONLY)
     {
@@ -1010,9 +1082,11 @@ static ogs_status dirichlet_apply(ogs_system* s)
     }
     else
     {
-        k_dirichlet_symmetric<<<vec_grid(s->n), 256, 0, s->stream>>>(m->slice_ptr, m->row_len, m->sell_col,
-                                                                      m->diag_pos, s->val, s->b, s->bc_flag,
-                                                                      s->bc_valn, s->bc_valf, s->n);
+        k_dirichlet_symmetric<<<std::max(1, (s->ntouch + 127) / 128), 128, 0, s->stream>>>(
+                                                                           m->slice_ptr, m->row_len, m->sell_col,
+                                                                           m->diag_pos, s->val, s->b, s->bc_flag,
+                                                                           s->bc_valn, s->bc_valf, s->bc_touch,
+                                                                           s->ntouch);
         OGS_LAUNCH_CHECK();
     }
     return OGS_OK;

@@ -579,6 +579,194 @@ __global__ void __launch_bounds__(128) k_flow_affine(AsmArgs a)
 }
 
 // ------------------------------------------------------------------
+// flow on a regular lattice of axis-aligned boxes, one thread per row
+// ------------------------------------------------------------------
+// Every cell of the lattice has the same Jacobian, so its element matrices
+// are mat_c L_box + M_box with L_box, M_box common to all cells, and on a
+// box an entry L_box[a][b] depends only on which coordinates of corners a
+// and b agree (the pattern: bit 0 x, 1 y, 2 z).  Row i of the assembled
+// system, at the column j = i + (dx, dy, dz), is therefore
+//   A_ij = cnt_ij M_pat / dt + relax0 L_pat S_ij,  S_ij = sum of mat_c
+// over the cells holding both nodes, and b_i = sum_j (cnt_ij M_pat / dt -
+// relax1 L_pat S_ij) u0_j (+ the gravity term of LIQUID_FLOW): the same
+// element matrices as k_flow_affine (whose per-element Gauss sums, FP64
+// atomics and scatter this replaces), added in another order.  The tables
+// come from element 0 through the element kernel's own formulas.
+struct LatticeArgs
+{
+    const int32_t* slice_ptr;
+    int nx, ny, nz;
+    int64_t n;
+};
+
+__host__ __device__ constexpr int kCornerX(int k) { return (k == 1 || k == 2 || k == 5 || k == 6) ? 1 : 0; }
+__host__ __device__ constexpr int kCornerY(int k) { return (k == 2 || k == 3 || k == 6 || k == 7) ? 1 : 0; }
+__host__ __device__ constexpr int kCornerZ(int k) { return k >= 4 ? 1 : 0; }
+
+// PLAIN: relax0 = 1 (no NLS relaxation), so b takes the mass term only
+template <bool PLAIN>
+__global__ void __launch_bounds__(256, 2) k_flow_lattice(AsmArgs a, LatticeArgs g)
+{
+    // sL: L_pat; sMC[pat][c] = c M_pat / dt for c shared cells (the product
+    // formed once here, looked up per entry); sG: gravity per corner
+    __shared__ double sL[8], sMC[8][9], sG[8];
+    __shared__ int s_ok;
+    if (threadIdx.x == 0)
+    {
+        int nd[8];
+        double X[8], Y[8], Z[8], U[8];
+        gather<8>(a, 0, nd, X, Y, Z, U);
+        const double* Q = a.aff;
+        const double* M0 = a.aff + 9 * 64;
+        const double* dNc = a.aff + 9 * 64 + 64;
+        double iJ[9], det;
+        const bool ok = jacobian<8, 3>(X, Y, Z, dNc, iJ, det);
+        s_ok = ok ? 1 : 0;
+        if (!ok)
+            flag_bad(a.bad_elem, 0);  // every cell has this Jacobian: element 0 is the first singular one
+        else
+        {
+            double c[3];
+            for (int q = 0; q < 3; q++)
+            {
+                double t = 0.0;
+                for (int k = 0; k < 3; k++) t += iJ[k * 3 + q] * iJ[k * 3 + q];
+                c[q] = det * t;
+            }
+            const double cm = flow_mass_coef(a.p), dt_inverse = 1.0 / a.p.dt;
+            const double lumped = element_volume<OGS_ELEM_HEX8>(X, Y, Z) / 8.0;
+            for (int pat = 0; pat < 8; pat++)
+            {
+                // corner b with this pattern against corner 0 = (0, 0, 0)
+                int b = 0;
+                for (int k = 0; k < 8; k++)
+                    if ((kCornerX(k) == 0) == ((pat & 1) != 0) && (kCornerY(k) == 0) == ((pat & 2) != 0) &&
+                        (kCornerZ(k) == 0) == ((pat & 4) != 0))
+                        b = k;
+                double l = 0.0;
+                for (int q = 0; q < 3; q++) l += c[q] * Q[((q * 3 + q) * 8 + 0) * 8 + b];
+                sL[pat] = l;
+                const double m = a.p.mass_lumping ? (pat == 7 ? cm * 1.0 * lumped : 0.0) : cm * det * M0[b];
+                const double mdt = m * dt_inverse;
+                for (int n = 0; n <= 8; n++) sMC[pat][n] = (double)n * mdt;
+            }
+            const bool grav = a.p.pcs_type == OGS_PCS_LIQUID_FLOW && a.p.gravity_on;
+            const double rho = a.p.gravity < DBL_EPSILON ? 1.0 : a.p.density * a.p.gravity;
+            for (int k = 0; k < 8; k++)
+            {
+                double t = 0.0;
+                for (int q = 0; q < 3; q++) t += iJ[2 * 3 + q] * dNc[q * 8 + k];
+                sG[k] = grav ? -(det * rho * 8.0) * t : 0.0;
+            }
+        }
+    }
+    __syncthreads();
+    if (!s_ok) return;
+    double relax0 = a.p.nls_relaxation;
+    if (relax0 < DBL_MIN) relax0 = 1.0;
+    const double relax1 = 1.0 - relax0;
+    const bool grav = a.p.pcs_type == OGS_PCS_LIQUID_FLOW && a.p.gravity_on;
+    // GROUNDWATER_FLOW with time_unit_factor 1: mat = k * 1.0 * 1.0 = k
+    const bool unit_mat = a.p.pcs_type == OGS_PCS_GROUNDWATER_FLOW && a.p.time_unit_factor == 1.0;
+    const int nx = g.nx, ny = g.ny, nz = g.nz, ncx = nx - 1, ncy = ny - 1, ncz = nz - 1;
+    const int64_t nxy = (int64_t)nx * ny;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < g.n; i += (int64_t)gridDim.x * blockDim.x)
+    {
+        const int iz = (int)(i / nxy), rem = (int)(i - iz * nxy), iy = rem / nx, ix = rem - iy * nx;
+        // the eight cells around the node, (ix - 1 + ex, iy - 1 + ey, iz - 1 + ez)
+        double mc[2][2][2];
+        int pc[2][2][2];
+        double gb = 0.0;
+#pragma unroll
+        for (int ez = 0; ez < 2; ez++)
+#pragma unroll
+            for (int ey = 0; ey < 2; ey++)
+#pragma unroll
+                for (int ex = 0; ex < 2; ex++)
+                {
+                    const int cx = ix - 1 + ex, cy = iy - 1 + ey, cz = iz - 1 + ez;
+                    const bool in = cx >= 0 && cx < ncx && cy >= 0 && cy < ncy && cz >= 0 && cz < ncz;
+                    const double k = in ? __ldg(a.elem_k + cx + (int64_t)ncx * (cy + (int64_t)ncy * cz)) : 0.0;
+                    const double m = unit_mat ? k : flow_mat(a.p, k);
+                    mc[ez][ey][ex] = m;
+                    pc[ez][ey][ex] = in ? 1 : 0;
+                    // the node is the cell's corner (1 - ex, 1 - ey, 1 - ez)
+                    if (grav) gb += m * sG[(1 - ez) * 4 + ((1 - ey) ? ((1 - ex) ? 2 : 3) : ((1 - ex) ? 1 : 0))];
+                }
+        // sums over the cells shared with the neighbour at offset d: per axis
+        // index 0 (d = -1: the lower cell), 1 (d = 0: both), 2 (d = +1)
+        double sx[2][2][3], sy[2][3][3], S[3][3][3];
+        int cx_[2][2][3], cy_[2][3][3], C[3][3][3];
+#pragma unroll
+        for (int ez = 0; ez < 2; ez++)
+#pragma unroll
+            for (int ey = 0; ey < 2; ey++)
+            {
+                sx[ez][ey][0] = mc[ez][ey][0];
+                sx[ez][ey][2] = mc[ez][ey][1];
+                sx[ez][ey][1] = mc[ez][ey][0] + mc[ez][ey][1];
+                cx_[ez][ey][0] = pc[ez][ey][0];
+                cx_[ez][ey][2] = pc[ez][ey][1];
+                cx_[ez][ey][1] = pc[ez][ey][0] + pc[ez][ey][1];
+            }
+#pragma unroll
+        for (int ez = 0; ez < 2; ez++)
+#pragma unroll
+            for (int kx = 0; kx < 3; kx++)
+            {
+                sy[ez][0][kx] = sx[ez][0][kx];
+                sy[ez][2][kx] = sx[ez][1][kx];
+                sy[ez][1][kx] = sx[ez][0][kx] + sx[ez][1][kx];
+                cy_[ez][0][kx] = cx_[ez][0][kx];
+                cy_[ez][2][kx] = cx_[ez][1][kx];
+                cy_[ez][1][kx] = cx_[ez][0][kx] + cx_[ez][1][kx];
+            }
+#pragma unroll
+        for (int ky = 0; ky < 3; ky++)
+#pragma unroll
+            for (int kx = 0; kx < 3; kx++)
+            {
+                S[0][ky][kx] = sy[0][ky][kx];
+                S[2][ky][kx] = sy[1][ky][kx];
+                S[1][ky][kx] = sy[0][ky][kx] + sy[1][ky][kx];
+                C[0][ky][kx] = cy_[0][ky][kx];
+                C[2][ky][kx] = cy_[1][ky][kx];
+                C[1][ky][kx] = cy_[0][ky][kx] + cy_[1][ky][kx];
+            }
+        // the row's stored entries in column order: (dz, dy, dx) lexicographic
+        const int64_t s0 = __ldg(g.slice_ptr + (i >> 5)) + (i & 31);
+        double* __restrict__ v = a.val + s0;
+        double bi = gb;
+        int rank = 0;
+#pragma unroll
+        for (int dz = -1; dz <= 1; dz++)
+#pragma unroll
+            for (int dy = -1; dy <= 1; dy++)
+#pragma unroll
+                for (int dx = -1; dx <= 1; dx++)
+                {
+                    const int jx = ix + dx, jy = iy + dy, jz = iz + dz;
+                    if (jx < 0 || jx >= nx || jy < 0 || jy >= ny || jz < 0 || jz >= nz) continue;
+                    const int pat = (dx == 0 ? 1 : 0) | (dy == 0 ? 2 : 0) | (dz == 0 ? 4 : 0);
+                    const double mt = sMC[pat][C[dz + 1][dy + 1][dx + 1]];
+                    const double lt = sL[pat] * S[dz + 1][dy + 1][dx + 1];
+                    const double u = a.u0 ? __ldg(a.u0 + i + dx + nx * (dy + (int64_t)ny * dz)) : 0.0;
+                    const double e = PLAIN ? mt + lt : mt + lt * relax0;
+                    if (a.val_store)
+                        v[(int64_t)rank * kSlice] = e;
+                    else
+                        v[(int64_t)rank * kSlice] += e;
+                    if constexpr (PLAIN)
+                        bi += mt * u;
+                    else
+                        bi += (mt - lt * relax1) * u;
+                    rank++;
+                }
+        a.b[i] += bi;
+    }
+}
+
+// ------------------------------------------------------------------
 // MASS_TRANSPORT
 // ------------------------------------------------------------------
 // STORE: the kernel may be the one that fills the stored operators (the SUPG
@@ -1189,11 +1377,28 @@ void launch_flow_cell_coef(const AsmArgs& a, double* coef, cudaStream_t s)
 }
 
 // dispatch on (element type, Gauss points); returns false for an
-// unsupported combination
+// unsupported combination.  Flow on a regular hex lattice takes the row
+// kernel (not for the split assembly of memory_type, which needs the terms
+// apart)
 bool launch_assembly(const ogs_mesh* m, const AsmArgs& a, bool affine, int kind,
                      cudaStream_t s)
 {
     const int et = m->elem_type, ngp = m->ngp;
+    if (kind == 0 && et == OGS_ELEM_HEX8 && m->grid && affine && !a.val2 &&
+        (a.p.pcs_type == OGS_PCS_GROUNDWATER_FLOW || a.p.pcs_type == OGS_PCS_LIQUID_FLOW))
+    {
+        LatticeArgs g;
+        g.slice_ptr = m->slice_ptr;
+        g.nx = m->gx; g.ny = m->gy; g.nz = m->gz;
+        g.n = m->n_nodes;
+        double relax0 = a.p.nls_relaxation;
+        if (relax0 < DBL_MIN) relax0 = 1.0;
+        if (relax0 == 1.0)
+            k_flow_lattice<true><<<grid_for(g.n, 256), 256, 0, s>>>(a, g);
+        else
+            k_flow_lattice<false><<<grid_for(g.n, 256), 256, 0, s>>>(a, g);
+        return true;
+    }
 #define OGS_DISPATCH(ET_, NGP_)                                      \
     if (et == ET_ && ngp == NGP_)                                    \
     {                                                                \

@@ -114,6 +114,8 @@ struct AsmArgs
     ogs_assembly_params p;
     const double* u1;   // RICHARDS_FLOW: the Picard iterate (coefficients)
     ogs_richards_params r;
+    int val_store;      // val is all zeros (Initialize, nothing added since):
+                        // a row kernel may store instead of add
 };
 
 }  // namespace ogs

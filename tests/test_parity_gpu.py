@@ -285,6 +285,49 @@ def test_dirichlet(gpu, oracle, symmetric):
     assert_vector_close(b2, ob)
 
 
+@pytest.mark.parametrize("kind", ["hex", "tet"])
+def test_dirichlet_sets_in_sequence(gpu, oracle, kind):
+    """One system re-assembled and given Dirichlet sets in turn: the same set
+    again (kept on the device), a different set (rows and values), the first
+    set again; every time the matrix and b of the oracle's elimination."""
+    m = M.structured_hex(9, 6, 5) if kind == "hex" else M.structured_tet(6, 5, 4)
+    ek = k_field(m, 5)
+    p = gpu.make_params(gpu.GROUNDWATER_FLOW, dt=3600.0, storage=1e-4)
+    u0 = np.random.default_rng(2).uniform(0, 1, m.n_nodes)
+    lf, rf, bf = m.face_nodes(0, 0), m.face_nodes(0, 1), m.face_nodes(2, 0)
+    set_a = (np.concatenate([lf, rf]), np.concatenate([np.full(len(lf), 10.0), np.zeros(len(rf))]))
+    set_b = (np.concatenate([lf, bf]), np.concatenate([np.full(len(lf), 4.0), np.linspace(1, 2, len(bf))]))
+    set_c = (set_a[0], np.concatenate([np.full(len(lf), 9.0), np.zeros(len(rf))]))
+    eqs = gpu.LinearEQS(gpu.GpuMesh(m))
+    orp, ocol = oracle.build_pattern(m.n_nodes, m.conn)
+    for rows, vals in (set_a, set_a, set_b, set_c, set_a):
+        eqs.Initialize()
+        eqs.GlobalAssembly(p, ek, u0)
+        eqs.SetKnownX(rows, vals, gpu.DIRICHLET_SYMMETRIC)
+        oval, ob = oracle.assemble(m, orp, ocol, oracle_params(oracle, p), elem_k=ek, u0=u0)
+        oracle.dirichlet(orp, ocol, oval, ob, rows, vals, symmetric=True)
+        assert_matrix_close(orp, eqs.get_values(), oval)
+        assert_vector_close(eqs.get_rhs(), ob)
+
+
+def test_lattice_assembly_adds_to_what_is_there(gpu, oracle):
+    """On a hex lattice the flow assembly runs row by row and stores right
+    after Initialize; a second GlobalAssembly adds to the first (A and b
+    twice the oracle's), as the element kernels do."""
+    m = M.structured_hex(9, 7, 5)
+    ek = k_field(m, 3)
+    p = gpu.make_params(gpu.GROUNDWATER_FLOW, dt=3600.0, storage=1e-4)
+    u0 = np.random.default_rng(5).uniform(0, 1, m.n_nodes)
+    eqs = gpu.LinearEQS(gpu.GpuMesh(m))
+    eqs.Initialize()
+    eqs.GlobalAssembly(p, ek, u0)
+    eqs.GlobalAssembly(p, ek, u0)
+    orp, ocol = oracle.build_pattern(m.n_nodes, m.conn)
+    oval, ob = oracle.assemble(m, orp, ocol, oracle_params(oracle, p), elem_k=ek, u0=u0)
+    assert_matrix_close(orp, eqs.get_values(), 2.0 * oval)
+    assert_vector_close(eqs.get_rhs(), 2.0 * ob)
+
+
 def test_spmv(gpu, oracle):
     m = M.structured_tet(5, 4, 3)
     ek = k_field(m, 6)
