@@ -33,7 +33,6 @@ void launch_flow_cell_coef(const AsmArgs& a, double* coef, cudaStream_t s);
 cudaError_t launch_mp_persist(const MixedArgs& a, int grid, int iters, cudaStream_t s);
 int kernels_per_iteration(int kind, int precond);
 int krylov_init_launches(int kind, int precond);
-bool ilu_cluster_ok();
 void launch_ilu_factor(const IluView& f, const double* val, const int32_t* csr2sell, int64_t nnz,
                        const KState* st, cudaStream_t s);
 int vec_grid(int n);
@@ -236,6 +235,10 @@ struct ogs_system
     double *op_mass = nullptr, *op_k = nullptr;
     bool op_valid = false;
     int* d_ilu_bad = nullptr;
+    int* ilu_flags = nullptr;                // [3][n] rows published per launch (ILU kernels)
+    unsigned long long* ilu_ticket = nullptr;  // [3] block tickets of the ILU kernels
+    int32_t *ilu_pl_row = nullptr, *ilu_pl_col = nullptr, *ilu_pu_row = nullptr, *ilu_pu_col = nullptr;
+    double *ilu_pl_val = nullptr, *ilu_pu_val = nullptr, *ilu_pu_diag = nullptr;  // packed sweep rows
     double *ek = nullptr, *u0 = nullptr, *gpv = nullptr, *qbuf = nullptr, *vec_in = nullptr,
            *vec_out = nullptr, *u1 = nullptr;
     // RICHARDS_FLOW Picard step: iterate, solution, old level, reductions
@@ -340,11 +343,21 @@ SolveArgs make_solve_args(ogs_system* s)
     a.ilu.diag = m->csr_diag;
     a.ilu.lu = s->lu;
     a.ilu.lrows = m->lvl_rows;
-    a.ilu.lptr = m->lvl_ptr;
     a.ilu.urows = m->ulvl_rows;
+    a.ilu.n = s->n;
+    a.ilu.n_lpos = m->n_lpos;
+    a.ilu.n_upos = m->n_upos;
+    a.ilu.flags = s->ilu_flags;
+    a.ilu.ticket = s->ilu_ticket;
+    a.ilu.lptr = m->lvl_ptr;
     a.ilu.uptr = m->ulvl_ptr;
     a.ilu.n_lev = m->n_lvl;
     a.ilu.n_ulev = m->n_ulvl;
+    a.ilu.kl = m->ilu_kl;
+    a.ilu.ku = m->ilu_ku;
+    a.ilu.pl_row = s->ilu_pl_row; a.ilu.pl_col = s->ilu_pl_col; a.ilu.pl_val = s->ilu_pl_val;
+    a.ilu.pu_row = s->ilu_pu_row; a.ilu.pu_col = s->ilu_pu_col; a.ilu.pu_val = s->ilu_pu_val;
+    a.ilu.pu_diag = s->ilu_pu_diag;
     a.ilu.bad = s->d_ilu_bad;
     return a;
 }
@@ -442,6 +455,15 @@ extern "C" ogs_status ogs_gpu_system_destroy(ogs_system* s)
     cudaFree(s->d_check);
     if (s->h_check) cudaFreeHost(s->h_check);
     cudaFree(s->d_ilu_bad);
+    cudaFree(s->ilu_flags);
+    cudaFree(s->ilu_ticket);
+    cudaFree(s->ilu_pl_row);
+    cudaFree(s->ilu_pl_col);
+    cudaFree(s->ilu_pl_val);
+    cudaFree(s->ilu_pu_row);
+    cudaFree(s->ilu_pu_col);
+    cudaFree(s->ilu_pu_val);
+    cudaFree(s->ilu_pu_diag);
     cudaFree(s->st);
     cudaFree(s->d_bad);
     cudaFree(s->bc_rows);
@@ -1265,15 +1287,28 @@ static ogs_status begin_fp32_refined(ogs_system* s, KState* h)
 static ogs_status ilu_factor(ogs_system* s)
 {
     ogs_mesh* m = s->m;
-    if (!ilu_cluster_ok())
-    {
-        set_error("solve: ILU(0) needs an 8-CTA thread-block cluster of 1024 threads, not available on this device");
-        return OGS_CUDA_ERROR;
-    }
     if (!s->lu)
     {
         OGS_CUDA_TRY(cudaMalloc(&s->lu, std::max<int64_t>(1, m->nnz) * sizeof(double)));
         OGS_CUDA_TRY(cudaMalloc(&s->d_ilu_bad, sizeof(int)));
+        // publication flags start below every launch number, tickets at 0
+        OGS_CUDA_TRY(cudaMalloc(&s->ilu_flags, 3 * (size_t)std::max(1, s->n) * sizeof(int)));
+        OGS_CUDA_TRY(cudaMalloc(&s->ilu_ticket, 3 * sizeof(unsigned long long)));
+        OGS_CUDA_TRY(cudaMemsetAsync(s->ilu_flags, 0, 3 * (size_t)std::max(1, s->n) * sizeof(int), s->stream));
+        OGS_CUDA_TRY(cudaMemsetAsync(s->ilu_ticket, 0, 3 * sizeof(unsigned long long), s->stream));
+        // the sweeps' packed rows (rows of at most 16 L / U entries)
+        if (std::max(m->ilu_kl, m->ilu_ku) <= 16)
+        {
+            const size_t nl = std::max(1, m->n_lpos), nu = std::max(1, m->n_upos);
+            const size_t kl = std::max(1, m->ilu_kl), ku = std::max(1, m->ilu_ku);
+            OGS_CUDA_TRY(cudaMalloc(&s->ilu_pl_row, nl * sizeof(int32_t)));
+            OGS_CUDA_TRY(cudaMalloc(&s->ilu_pl_col, kl * nl * sizeof(int32_t)));
+            OGS_CUDA_TRY(cudaMalloc(&s->ilu_pl_val, kl * nl * sizeof(double)));
+            OGS_CUDA_TRY(cudaMalloc(&s->ilu_pu_row, nu * sizeof(int32_t)));
+            OGS_CUDA_TRY(cudaMalloc(&s->ilu_pu_col, ku * nu * sizeof(int32_t)));
+            OGS_CUDA_TRY(cudaMalloc(&s->ilu_pu_val, ku * nu * sizeof(double)));
+            OGS_CUDA_TRY(cudaMalloc(&s->ilu_pu_diag, nu * sizeof(double)));
+        }
         drop_graphs(s);  // captured sweeps hold the factor pointer
     }
     const int big = 0x7fffffff;
@@ -1284,6 +1319,11 @@ static ogs_status ilu_factor(ogs_system* s)
     count_launches(1);
     OGS_CUDA_TRY(cudaMemcpyAsync(s->h_bad, s->d_ilu_bad, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
     OGS_CUDA_TRY(cudaStreamSynchronize(s->stream));
+    if (*s->h_bad == -1)
+    {
+        set_error("solve: ILU(0) factorisation: a wait for a row gave up");
+        return OGS_CUDA_ERROR;
+    }
     if (*s->h_bad != big)
     {
         set_error("solve: ILU(0) zero pivot in row %d", *s->h_bad);
@@ -1578,6 +1618,18 @@ static ogs_status solve_end(ogs_system* s, ogs_solve_stats* stats)
 {
     SolveTask& T = s->task;
     const KState* h = s->h_st;
+    if (s->cfg.precond == OGS_PRECOND_ILU0 && s->d_ilu_bad && T.status == OGS_OK)
+    {
+        // an ILU sweep that gave up waiting for a row marked -1
+        int bad = 0;
+        if (cudaMemcpy(&bad, s->d_ilu_bad, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+            T.status = OGS_CUDA_ERROR;
+        else if (bad == -1)
+        {
+            set_error("solve: an ILU(0) sweep gave up waiting for a row");
+            T.status = OGS_CUDA_ERROR;
+        }
+    }
     if (stats)
     {
         std::memset(stats, 0, sizeof *stats);

@@ -156,13 +156,16 @@ struct ogs_mesh
     int32_t* diag_pos = nullptr;   // [n_nodes] SELL slot of the diagonal
     int32_t* slot_t = nullptr;     // [nn*nn][n_elem] SELL slot of (i, j)
     // ILU(0): CSR diagonal positions and the dependency levels of the
-    // forward (lower) and backward (upper) sweeps in natural row order
+    // forward (lower) and backward (upper) sweeps in natural row order;
+    // the rows by level, each level padded with -1 to a multiple of 32
     int32_t* csr_diag = nullptr;   // [n_nodes]
-    int32_t* lvl_rows = nullptr;   // [n_nodes] rows by forward level
-    int32_t* lvl_ptr = nullptr;    // [n_lvl + 1]
-    int32_t* ulvl_rows = nullptr;  // [n_nodes] rows by backward level
+    int32_t* lvl_rows = nullptr;   // [n_lpos] rows by forward level
+    int32_t* lvl_ptr = nullptr;    // [n_lvl + 1] first position of a level
+    int32_t* ulvl_rows = nullptr;  // [n_upos] rows by backward level
     int32_t* ulvl_ptr = nullptr;   // [n_ulvl + 1]
     int n_lvl = 0, n_ulvl = 0;
+    int n_lpos = 0, n_upos = 0;
+    int ilu_kl = 0, ilu_ku = 0;    // most entries left / right of the diagonal in a row
     // diagonal-offset form of the pattern (structured grids): the distinct
     // column offsets (col - row), sorted, and per SELL slot the index of
     // its offset (-1 for padding); n_off == 0 when there are too many

@@ -13,25 +13,39 @@
 // grouped into levels (rows of a level are independent; computed once per
 // mesh on the host).  A structured grid in natural order has
 // nx + ny + nz levels (Kuhn tets) or about nx + 2 ny + 4 nz (27-point
-// hexes): hundreds of levels of a few thousand rows each -- far too
-// little work per level for the whole GPU, and far too many levels for
-// one launch each.  One thread-block cluster (8 CTAs x 1024 threads) walks
-// all levels in a single launch and separates levels with the hardware
-// cluster barrier (barrier.cluster arrive.release / wait.acquire): no
-// spin-waits, no grid-wide synchronisation, no launch per level.  Values
-// written by other CTAs of the cluster are read with L2 (.cg) loads.
-#include <cooperative_groups.h>
-
+// hexes): hundreds of levels of a few thousand rows each.  The whole GPU
+// walks them in one launch per sweep without grid-wide barriers: the rows
+// lie in level order (each level padded to whole warps); a persistent grid
+// of blocks takes consecutive ranges of them from a ticket counter; one
+// thread per row polls the flags of the rows its row reads (relaxed loads,
+// backing off), takes one acquire fence, computes, and publishes its value
+// with a release store of its flag (the launch number).  A block waits only
+// on ranges taken earlier, by blocks that are resident and do not wait on
+// later ranges, so the sweep cannot deadlock; a warp holds one level, so no
+// lane waits on a lane of its warp.  Every wait polls at most kIluSpin
+// times and then records -1 in f.bad and goes on (the host reports the
+// solve as failed).  That is the factorisation's kernel (the most FP64
+// work per row, which needs the whole GPU's FP64 units).
+//
+// The sweeps do little work per row, so a level costs what its dependent
+// loads cost.  After each factorisation the rows' L and U entries are
+// packed by sweep position (k_ilu_pack); one thread-block cluster (16 CTAs
+// where the device allows, else 8) walks the levels, the threads of a level
+// holding their rows' packed entries in registers: a level is one
+// dependent L2 round trip (the neighbours' results) between two halves of
+// the cluster barrier, and the next level's entries are loaded while the
+// barrier completes.
 #include <algorithm>
 
 #include "krylov.cuh"
 
-namespace cg = cooperative_groups;
-
 namespace ogs {
 
-constexpr int kIluCtas = 8;       // portable cluster size
-constexpr int kIluThreads = 1024;
+constexpr int kIluBlock = 128;          // rows (positions) per ticket and block
+constexpr int kIluBlocksPerSm = 4;      // persistent grid
+constexpr unsigned kIluSpin = 1u << 18;  // polls of one wait before it gives up
+constexpr int kIluRowMax = 32;          // factorisation: rows held in a local array
+constexpr int kIluUMax = 16;            // U entries of a pivot row loaded per batch
 
 // lu = A on the CSR pattern (values live in SELL-32 order)
 __global__ void k_ilu_copy(const double* __restrict__ val, const int32_t* __restrict__ csr2sell,
@@ -41,76 +55,325 @@ __global__ void k_ilu_copy(const double* __restrict__ val, const int32_t* __rest
         lu[k] = val[csr2sell[k]];
 }
 
+__device__ __forceinline__ int ld_relaxed_s32(const int* p)
+{
+    int v;
+    asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release_s32(int* p, int v)
+{
+    asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// until row j is published by this launch (relaxed polls with a growing
+// pause, bounded; once any wait of the launch has given up, f.bad is -1
+// and the others stop waiting too).  The caller takes the acquire fence
+// after all its waits.
+__device__ __forceinline__ void ilu_wait(const int* flags, int j, int launch, int* bad)
+{
+    if (ld_relaxed_s32(flags + j) >= launch) return;
+    unsigned spins = 0, pause = 32;
+    while (ld_relaxed_s32(flags + j) < launch)
+    {
+        if (++spins > kIluSpin || ((spins & 255) == 0 && *(volatile int*)bad == -1))
+        {
+            atomicMin(bad, -1);
+            return;
+        }
+        __nanosleep(pause);
+        pause = min(pause * 2, 512u);
+    }
+}
+
+__device__ __forceinline__ void fence_acquire() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
+
+// one row of MODE 0 / 1 / 2 (below)
+template <int MODE>
+__device__ __forceinline__ void ilu_row(const IluView& f, const double* __restrict__ in, double* out, int* flags,
+                                        int i, int launch, double (*s_a)[kIluBlock], int (*s_cj)[kIluBlock])
+{
+    const int rb = __ldg(f.row_ptr + i), re = __ldg(f.row_ptr + i + 1);
+    const int d = __ldg(f.diag + i);
+    if (d < 0)
+    {
+        // a node in no element has no diagonal: a zero pivot
+        if (MODE == 0) atomicMin(f.bad, i);
+        st_release_s32(flags + i, launch);
+        return;
+    }
+    // the rows this row reads: its columns before (MODE 0, 1) or after
+    // (MODE 2) the diagonal
+    const int w0 = MODE == 2 ? d + 1 : rb, w1 = MODE == 2 ? re : d;
+    for (int k = w0; k < w1; k++) ilu_wait(flags, __ldg(f.col + k), launch, f.bad);
+    fence_acquire();
+    if (MODE == 0 && re - rb <= kIluRowMax && f.ku <= kIluUMax)
+    {
+        // row i -= l_ik row k for every k < i of the pattern, in column
+        // order; products and differences rounded separately (no FMA), like
+        // the sequential elimination.  Row i stays in shared memory for the
+        // whole elimination (a column per thread); row k's U part is loaded
+        // into registers in one batch, the next k's batch issued before this
+        // one is used.
+        const int len = re - rb, nlow = d - rb, t = threadIdx.x;
+        for (int q = 0; q < len; q++)
+        {
+            s_cj[q][t] = __ldg(f.col + rb + q);
+            s_a[q][t] = __ldcg(f.lu + rb + q);
+        }
+        int uc[kIluUMax], nc[kIluUMax];
+        double uv[kIluUMax], nv[kIluUMax], piv = 0.0, npiv = 0.0;
+        auto fetch = [&](int kk, int* c, double* v, double& pv) {
+            const int k = s_cj[kk][t];
+            const int dk = __ldg(f.diag + k), ke = __ldg(f.row_ptr + k + 1);
+            pv = __ldcg(f.lu + dk);
+#pragma unroll
+            for (int q = 0; q < kIluUMax; q++)
+            {
+                const bool in = dk + 1 + q < ke;
+                c[q] = in ? __ldg(f.col + dk + 1 + q) : 0x7fffffff;
+                v[q] = in ? __ldcg(f.lu + dk + 1 + q) : 0.0;
+            }
+        };
+        if (nlow > 0) fetch(0, uc, uv, piv);
+        for (int kk = 0; kk < nlow; kk++)
+        {
+            if (kk + 1 < nlow) fetch(kk + 1, nc, nv, npiv);
+            if (piv == 0.0) atomicMin(f.bad, s_cj[kk][t]);
+            const double lik = s_a[kk][t] / piv;
+            s_a[kk][t] = lik;
+            int p = kk + 1;
+#pragma unroll
+            for (int q = 0; q < kIluUMax; q++)
+            {
+                const int j = uc[q];
+                while (p < len && s_cj[p][t] < j) p++;
+                if (p < len && s_cj[p][t] == j) s_a[p][t] = __dsub_rn(s_a[p][t], __dmul_rn(lik, uv[q]));
+            }
+#pragma unroll
+            for (int q = 0; q < kIluUMax; q++)
+            {
+                uc[q] = nc[q];
+                uv[q] = nv[q];
+            }
+            piv = npiv;
+        }
+        for (int q = 0; q < len; q++) __stcg(f.lu + rb + q, s_a[q][t]);
+        if (s_a[nlow][t] == 0.0) atomicMin(f.bad, i);
+    }
+    else if (MODE == 0)
+    {
+        // rows longer than the local array: the same elimination in place
+        for (int kk = rb; kk < d; kk++)
+        {
+            const int k = __ldg(f.col + kk);
+            const int dk = __ldg(f.diag + k), ke = __ldg(f.row_ptr + k + 1);
+            const double piv = __ldcg(f.lu + dk);
+            if (piv == 0.0) atomicMin(f.bad, k);
+            const double lik = __ldcg(f.lu + kk) / piv;
+            __stcg(f.lu + kk, lik);
+            int p = kk + 1;
+            for (int q = dk + 1; q < ke; q++)
+            {
+                const int j = __ldg(f.col + q);
+                while (p < re && __ldg(f.col + p) < j) p++;
+                if (p < re && __ldg(f.col + p) == j)
+                    __stcg(f.lu + p, __dsub_rn(__ldcg(f.lu + p), __dmul_rn(lik, __ldcg(f.lu + q))));
+            }
+        }
+        if (__ldcg(f.lu + d) == 0.0) atomicMin(f.bad, i);
+    }
+    else if (MODE == 1)
+    {
+        double s = in[i];
+        for (int k = rb; k < d; k++)
+            s = __dsub_rn(s, __dmul_rn(__ldg(f.lu + k), __ldcg(out + __ldg(f.col + k))));
+        __stcg(out + i, s);
+    }
+    else
+    {
+        double s = __ldcg(out + i);
+        for (int k = d + 1; k < re; k++)
+            s = __dsub_rn(s, __dmul_rn(__ldg(f.lu + k), __ldcg(out + __ldg(f.col + k))));
+        __stcg(out + i, s / __ldg(f.lu + d));
+    }
+    st_release_s32(flags + i, launch);
+}
+
 // MODE 0: factorisation (IKJ, rows in forward levels)
 // MODE 1: forward sweep  out_i = in_i - sum_{k<i} L_ik out_k
 // MODE 2: backward sweep out_i = (out_i - sum_{j>i} U_ij out_j) / U_ii
-// The sweeps return at once when the solve has finished (uniform over the
-// cluster: st->done is not written while this kernel runs).
+// Persistent blocks take tickets until this launch's are used up: a launch
+// hands out nblk + gridDim.x tickets (nblk ranges of kIluBlock positions,
+// then one closing ticket per block), so the launch number follows from
+// any ticket.  The sweeps return at once when the solve has finished
+// (uniform over the grid: st->done is not written while this kernel runs,
+// so either every block takes its tickets or none does).
 template <int MODE>
-__global__ void __cluster_dims__(kIluCtas, 1, 1) __launch_bounds__(kIluThreads)
-    k_ilu_levels(IluView f, const double* __restrict__ in, double* out, const KState* st)
+__global__ void __launch_bounds__(kIluBlock) k_ilu_flow(IluView f, const double* __restrict__ in, double* out,
+                                                       const KState* st)
 {
     if (MODE != 0 && st->done) return;
-    cg::cluster_group cluster = cg::this_cluster();
-    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-    const int nt = gridDim.x * blockDim.x;
+    const int npos = MODE == 2 ? f.n_upos : f.n_lpos;
+    const unsigned long long nblk = (unsigned long long)((npos + kIluBlock - 1) / kIluBlock);
+    const unsigned long long per = nblk + gridDim.x;
     const int32_t* rows = MODE == 2 ? f.urows : f.lrows;
+    int* flags = f.flags + (size_t)MODE * f.n;
+    __shared__ unsigned long long s_ticket;
+    // the factorisation's rows, a column per thread
+    __shared__ double s_a[MODE == 0 ? kIluRowMax : 1][kIluBlock];
+    __shared__ int s_cj[MODE == 0 ? kIluRowMax : 1][kIluBlock];
+    for (;;)
+    {
+        __syncthreads();
+        if (threadIdx.x == 0) s_ticket = atomicAdd(f.ticket + MODE, 1ull);
+        __syncthreads();
+        const unsigned long long t = s_ticket;
+        const unsigned long long blk = t % per;
+        if (blk >= nblk) return;  // this block's closing ticket
+        const int launch = (int)(t / per) + 1;
+        const int pos = (int)blk * kIluBlock + threadIdx.x;
+        if (pos < npos)
+        {
+            const int i = __ldg(rows + pos);
+            if (i >= 0) ilu_row<MODE>(f, in, out, flags, i, launch, s_a, s_cj);  // i < 0: padding of a level
+        }
+    }
+}
+
+// after a factorisation: the sweeps' rows packed by position (rows without
+// a diagonal as -1: the factorisation has reported them)
+__global__ void k_ilu_pack(IluView f)
+{
+    const int stride = gridDim.x * blockDim.x;
+    for (int pos = blockIdx.x * blockDim.x + threadIdx.x; pos < f.n_lpos; pos += stride)
+    {
+        int i = __ldg(f.lrows + pos);
+        const int d = i >= 0 ? __ldg(f.diag + i) : -1;
+        if (d < 0) i = -1;
+        const int rb = i >= 0 ? __ldg(f.row_ptr + i) : 0;
+        f.pl_row[pos] = i;
+        for (int k = 0; k < f.kl; k++)
+        {
+            const bool in = i >= 0 && rb + k < d;
+            f.pl_col[(size_t)k * f.n_lpos + pos] = in ? __ldg(f.col + rb + k) : -1;
+            f.pl_val[(size_t)k * f.n_lpos + pos] = in ? f.lu[rb + k] : 0.0;
+        }
+    }
+    for (int pos = blockIdx.x * blockDim.x + threadIdx.x; pos < f.n_upos; pos += stride)
+    {
+        int i = __ldg(f.urows + pos);
+        const int d = i >= 0 ? __ldg(f.diag + i) : -1;
+        if (d < 0) i = -1;
+        const int re = i >= 0 ? __ldg(f.row_ptr + i + 1) : 0;
+        f.pu_row[pos] = i;
+        f.pu_diag[pos] = i >= 0 ? f.lu[d] : 1.0;
+        for (int k = 0; k < f.ku; k++)
+        {
+            const bool in = i >= 0 && d + 1 + k < re;
+            f.pu_col[(size_t)k * f.n_upos + pos] = in ? __ldg(f.col + d + 1 + k) : -1;
+            f.pu_val[(size_t)k * f.n_upos + pos] = in ? f.lu[d + 1 + k] : 0.0;
+        }
+    }
+}
+
+// One packed row: index, entries, start value (forward: in_i, backward:
+// the forward result out_i), diagonal (backward)
+template <int K>
+struct PackedRow
+{
+    int i;
+    int c[K];
+    double v[K];
+    double s0, dg;
+};
+
+template <int MODE, int K>
+__device__ __forceinline__ void ilu_fetch(const IluView& f, const double* __restrict__ in, const double* out,
+                                          int pos, int npos, PackedRow<K>& R)
+{
+    const int32_t* prow = MODE == 2 ? f.pu_row : f.pl_row;
+    const int32_t* pcol = MODE == 2 ? f.pu_col : f.pl_col;
+    const double* pval = MODE == 2 ? f.pu_val : f.pl_val;
+    const int kmax = MODE == 2 ? f.ku : f.kl;
+    R.i = pos >= 0 ? __ldg(prow + pos) : -1;
+#pragma unroll
+    for (int k = 0; k < K; k++)
+    {
+        const bool in_k = R.i >= 0 && k < kmax;
+        R.c[k] = in_k ? __ldg(pcol + (size_t)k * npos + pos) : -1;
+        R.v[k] = in_k ? __ldg(pval + (size_t)k * npos + pos) : 0.0;
+    }
+    R.s0 = R.i >= 0 ? (MODE == 1 ? in[R.i] : __ldcg(out + R.i)) : 0.0;
+    R.dg = R.i >= 0 && MODE == 2 ? __ldg(f.pu_diag + pos) : 1.0;
+}
+
+// the row's result: s0 - sum_k v_k out_{c_k} in column order, products and
+// differences rounded separately (no FMA), then over the diagonal (MODE 2)
+template <int MODE, int K>
+__device__ __forceinline__ void ilu_solve_row(const PackedRow<K>& R, double* out)
+{
+    if (R.i < 0) return;
+    double x[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) x[k] = R.c[k] >= 0 ? __ldcg(out + R.c[k]) : 0.0;
+    double s = R.s0;
+#pragma unroll
+    for (int k = 0; k < K; k++)
+        if (R.c[k] >= 0) s = __dsub_rn(s, __dmul_rn(R.v[k], x[k]));
+    if (MODE == 2) s = s / R.dg;
+    __stcg(out + R.i, s);
+}
+
+// the two halves of the cluster barrier (.aligned: the warp reconverges
+// first, after the divergent row work)
+__device__ __forceinline__ void cluster_arrive_release()
+{
+    __syncwarp();
+    asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void cluster_wait_acquire()
+{
+    __syncwarp();
+    asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+// MODE 1: forward sweep, MODE 2: backward sweep over the packed rows; the
+// grid is one cluster.  A thread's first row of the next level is fetched
+// between the arrive and the wait of the barrier that ends this level.
+template <int MODE, int K, int NT>
+__global__ void __launch_bounds__(NT, 1) k_ilu_sweep(IluView f, const double* __restrict__ in, double* out,
+                                                    const KState* st)
+{
+    if (st->done) return;
+    const int tid = blockIdx.x * NT + threadIdx.x, nt = gridDim.x * NT;
     const int32_t* ptr = MODE == 2 ? f.uptr : f.lptr;
     const int nl = MODE == 2 ? f.n_ulev : f.n_lev;
+    const int npos = MODE == 2 ? f.n_upos : f.n_lpos;
+    PackedRow<K> R;
+    {
+        const int b = __ldg(ptr), e = __ldg(ptr + 1);
+        ilu_fetch<MODE, K>(f, in, out, b + tid < e ? b + tid : -1, npos, R);
+    }
     for (int l = 0; l < nl; l++)
     {
         const int b = __ldg(ptr + l), e = __ldg(ptr + l + 1);
-        for (int t = b + tid; t < e; t += nt)
+        ilu_solve_row<MODE, K>(R, out);
+        // a level wider than the cluster: its further rows fetched here
+        for (int pos = b + tid + nt; pos < e; pos += nt)
         {
-            const int i = __ldg(rows + t);
-            const int rb = __ldg(f.row_ptr + i), re = __ldg(f.row_ptr + i + 1);
-            const int d = __ldg(f.diag + i);
-            if (d < 0)
-            {
-                // a node in no element has no diagonal: a zero pivot
-                if (MODE == 0) atomicMin(f.bad, i);
-                continue;
-            }
-            if (MODE == 0)
-            {
-                // row i -= l_ik row k for every k < i of the pattern, in
-                // column order; products and differences rounded
-                // separately (no FMA), like the sequential elimination
-                for (int kk = rb; kk < d; kk++)
-                {
-                    const int k = __ldg(f.col + kk);
-                    const int dk = __ldg(f.diag + k), ke = __ldg(f.row_ptr + k + 1);
-                    const double piv = __ldcg(f.lu + dk);
-                    if (piv == 0.0) atomicMin(f.bad, k);
-                    const double lik = __ldcg(f.lu + kk) / piv;
-                    __stcg(f.lu + kk, lik);
-                    int p = kk + 1;
-                    for (int q = dk + 1; q < ke; q++)
-                    {
-                        const int j = __ldg(f.col + q);
-                        while (p < re && __ldg(f.col + p) < j) p++;
-                        if (p < re && __ldg(f.col + p) == j)
-                            __stcg(f.lu + p, __dsub_rn(__ldcg(f.lu + p), __dmul_rn(lik, __ldcg(f.lu + q))));
-                    }
-                }
-                if (__ldcg(f.lu + d) == 0.0) atomicMin(f.bad, i);
-            }
-            else if (MODE == 1)
-            {
-                double s = in[i];
-                for (int k = rb; k < d; k++)
-                    s = __dsub_rn(s, __dmul_rn(__ldg(f.lu + k), __ldcg(out + __ldg(f.col + k))));
-                __stcg(out + i, s);
-            }
-            else
-            {
-                double s = __ldcg(out + i);
-                for (int k = d + 1; k < re; k++)
-                    s = __dsub_rn(s, __dmul_rn(__ldg(f.lu + k), __ldcg(out + __ldg(f.col + k))));
-                __stcg(out + i, s / __ldg(f.lu + d));
-            }
+            PackedRow<K> T;
+            ilu_fetch<MODE, K>(f, in, out, pos, npos, T);
+            ilu_solve_row<MODE, K>(T, out);
         }
-        cluster.sync();
+        cluster_arrive_release();
+        if (l + 1 < nl)
+        {
+            const int b1 = e, e1 = __ldg(ptr + l + 2);
+            ilu_fetch<MODE, K>(f, in, out, b1 + tid < e1 ? b1 + tid : -1, npos, R);
+        }
+        cluster_wait_acquire();
     }
 }
 
@@ -152,29 +415,19 @@ __global__ void __launch_bounds__(kThreads) k_cg_init_z(SolveArgs a)
 // ------------------------------------------------------------------
 // host side
 // ------------------------------------------------------------------
-bool ilu_cluster_ok()
+// the persistent grid (the same for every launch of a system: tickets per
+// launch depend on it)
+static int ilu_grid(int npos)
 {
-    static int ok = -1;
-    if (ok < 0)
+    static int sms = 0;
+    if (!sms)
     {
-        cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3(kIluCtas);
-        cfg.blockDim = dim3(kIluThreads);
-        cudaLaunchAttribute attr;
-        attr.id = cudaLaunchAttributeClusterDimension;
-        attr.val.clusterDim.x = kIluCtas;
-        attr.val.clusterDim.y = 1;
-        attr.val.clusterDim.z = 1;
-        cfg.attrs = &attr;
-        cfg.numAttrs = 1;
-        int n0 = 0, n1 = 0, n2 = 0;
-        const bool q = cudaOccupancyMaxActiveClusters(&n0, k_ilu_levels<0>, &cfg) == cudaSuccess &&
-                       cudaOccupancyMaxActiveClusters(&n1, k_ilu_levels<1>, &cfg) == cudaSuccess &&
-                       cudaOccupancyMaxActiveClusters(&n2, k_ilu_levels<2>, &cfg) == cudaSuccess;
-        if (!q) cudaGetLastError();
-        ok = q && n0 > 0 && n1 > 0 && n2 > 0;
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 152;
     }
-    return ok == 1;
+    return std::max(1, std::min((npos + kIluBlock - 1) / kIluBlock, sms * kIluBlocksPerSm));
 }
 
 void launch_ilu_factor(const IluView& f, const double* val, const int32_t* csr2sell, int64_t nnz,
@@ -182,14 +435,94 @@ void launch_ilu_factor(const IluView& f, const double* val, const int32_t* csr2s
 {
     const int g = (int)std::max<int64_t>(1, std::min<int64_t>((nnz + 255) / 256, 4096));
     k_ilu_copy<<<g, 256, 0, s>>>(val, csr2sell, f.lu, nnz);
-    k_ilu_levels<0><<<kIluCtas, kIluThreads, 0, s>>>(f, nullptr, nullptr, st);
+    k_ilu_flow<0><<<ilu_grid(f.n_lpos), kIluBlock, 0, s>>>(f, nullptr, nullptr, st);
+    if (f.pl_row) k_ilu_pack<<<ilu_grid(std::max(f.n_lpos, f.n_upos)), kIluBlock, 0, s>>>(f);
+}
+
+// the cluster sweeps: rows of at most 8 (tets, quads) or 16 (hexes) L / U
+// entries, a 16-CTA cluster where the device takes one, else 8
+template <int MODE, int K, int NT>
+static cudaError_t launch_sweep(const IluView& f, const double* in, double* out, const KState* st, int ctas,
+                                cudaStream_t s)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(ctas);
+    cfg.blockDim = dim3(NT);
+    cfg.stream = s;
+    cudaLaunchAttribute attr;
+    attr.id = cudaLaunchAttributeClusterDimension;
+    attr.val.clusterDim.x = ctas;
+    attr.val.clusterDim.y = 1;
+    attr.val.clusterDim.z = 1;
+    cfg.attrs = &attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_ilu_sweep<MODE, K, NT>, f, in, out, st);
+}
+
+template <int K, int NT>
+static int sweep_ctas()
+{
+    static int ctas = -1;
+    if (ctas < 0)
+    {
+        ctas = 0;
+        const int want[2] = {16, 8};
+        for (int c : want)
+        {
+            if (c > 8)
+            {
+                if (cudaFuncSetAttribute(k_ilu_sweep<1, K, NT>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+                        cudaSuccess ||
+                    cudaFuncSetAttribute(k_ilu_sweep<2, K, NT>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+                        cudaSuccess)
+                {
+                    cudaGetLastError();
+                    continue;
+                }
+            }
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(c);
+            cfg.blockDim = dim3(NT);
+            cudaLaunchAttribute attr;
+            attr.id = cudaLaunchAttributeClusterDimension;
+            attr.val.clusterDim.x = c;
+            attr.val.clusterDim.y = 1;
+            attr.val.clusterDim.z = 1;
+            cfg.attrs = &attr;
+            cfg.numAttrs = 1;
+            int n1 = 0, n2 = 0;
+            if (cudaOccupancyMaxActiveClusters(&n1, k_ilu_sweep<1, K, NT>, &cfg) == cudaSuccess &&
+                cudaOccupancyMaxActiveClusters(&n2, k_ilu_sweep<2, K, NT>, &cfg) == cudaSuccess && n1 > 0 && n2 > 0)
+            {
+                ctas = c;
+                break;
+            }
+            cudaGetLastError();
+        }
+    }
+    return ctas;
 }
 
 // out = (LU)^-1 in
 void launch_ilu_apply(const IluView& f, const double* in, double* out, const KState* st, cudaStream_t s)
 {
-    k_ilu_levels<1><<<kIluCtas, kIluThreads, 0, s>>>(f, in, out, st);
-    k_ilu_levels<2><<<kIluCtas, kIluThreads, 0, s>>>(f, nullptr, out, st);
+    const int k = std::max(f.kl, f.ku);
+    if (f.pl_row && k <= 8 && sweep_ctas<8, 1024>() > 0)
+    {
+        const int c = sweep_ctas<8, 1024>();
+        launch_sweep<1, 8, 1024>(f, in, out, st, c, s);
+        launch_sweep<2, 8, 1024>(f, nullptr, out, st, c, s);
+        return;
+    }
+    if (f.pl_row && k <= 16 && sweep_ctas<16, 512>() > 0)
+    {
+        const int c = sweep_ctas<16, 512>();
+        launch_sweep<1, 16, 512>(f, in, out, st, c, s);
+        launch_sweep<2, 16, 512>(f, nullptr, out, st, c, s);
+        return;
+    }
+    k_ilu_flow<1><<<ilu_grid(f.n_lpos), kIluBlock, 0, s>>>(f, in, out, st);
+    k_ilu_flow<2><<<ilu_grid(f.n_upos), kIluBlock, 0, s>>>(f, nullptr, out, st);
 }
 
 void launch_cg_dots_z(const SolveArgs& a, int grid, cudaStream_t s)

@@ -81,12 +81,24 @@ struct IluView
     const int32_t* col;
     const int32_t* diag;      // CSR position of the diagonal
     double* lu;
-    const int32_t* lrows;     // rows ordered by forward level
+    const int32_t* lrows;     // rows by forward level, levels padded to 32 with -1
+    const int32_t* urows;     // rows by backward level, the same
+    int n, n_lpos, n_upos;
+    int* flags;               // [3][n]: launch number with which a row was published
+                              // (factorisation, forward, backward sweep)
+    unsigned long long* ticket;  // [3] block tickets handed out so far, per kernel
+    int* bad;                 // smallest row with a zero pivot (factorisation);
+                              // -1: a sweep gave up waiting
+    // the sweeps' rows packed by position (level order, padded levels):
+    // level starts, the row (-1: padding or no diagonal), and the row's L
+    // (forward) or U (backward) entries as columns / values [k][pos]
+    // (column -1 past the row's entries), the diagonal for the backward sweep
     const int32_t* lptr;      // [n_lev + 1]
-    const int32_t* urows;     // rows ordered by backward level
     const int32_t* uptr;      // [n_ulev + 1]
     int n_lev, n_ulev;
-    int* bad;                 // smallest row with a zero pivot (factorisation)
+    int kl, ku;               // entries per row in the packed arrays
+    int32_t *pl_row, *pl_col, *pu_row, *pu_col;
+    double *pl_val, *pu_val, *pu_diag;
 };
 
 struct SolveArgs

@@ -288,11 +288,14 @@ static void sweep_levels(int64_t N, const std::vector<int32_t>& row_ptr, const s
         lev[r] = l;
         nl = std::max(nl, l + 1);
     }
+    // rows by level, every level padded with -1 to a whole number of warps
+    // (32 positions): a warp of the sweep kernels then holds rows of one
+    // level only, which never wait on each other
     ptr.assign((size_t)nl + 1, 0);
     for (int64_t r = 0; r < N; r++) ptr[lev[r] + 1]++;
-    for (int32_t l = 0; l < nl; l++) ptr[l + 1] += ptr[l];
+    for (int32_t l = 0; l < nl; l++) ptr[l + 1] = ptr[l] + ((ptr[l + 1] + 31) & ~31);
     std::vector<int32_t> fill(ptr.begin(), ptr.end() - 1);
-    rows.resize(N);
+    rows.assign((size_t)ptr[nl], -1);
     for (int64_t r = 0; r < N; r++) rows[fill[lev[r]]++] = (int32_t)r;
 }
 
@@ -458,6 +461,14 @@ extern "C" ogs_status ogs_gpu_mesh_create(const ogs_mesh_desc* d, ogs_mesh** out
     sweep_levels(N, row_ptr, col, false, ulvl_rows, ulvl_ptr);
     m->n_lvl = (int)lvl_ptr.size() - 1;
     m->n_ulvl = (int)ulvl_ptr.size() - 1;
+    m->n_lpos = lvl_ptr.back();
+    m->n_upos = ulvl_ptr.back();
+    for (int64_t r = 0; r < N; r++)
+        if (diag[r] >= 0)
+        {
+            m->ilu_kl = std::max(m->ilu_kl, diag[r] - row_ptr[r]);
+            m->ilu_ku = std::max(m->ilu_ku, row_ptr[r + 1] - diag[r] - 1);
+        }
     // SELL-32 layout of the pattern
     const int n_slices = (int)((N + kSlice - 1) / kSlice);
     std::vector<int32_t> slice_ptr(n_slices + 1, 0);
