@@ -41,21 +41,22 @@
 //             surface when it is within the search length of the bounding
 //             box (AABB::containsPoint, GEO/AxisAlignedBoundingBox.cpp:73-90)
 //             and in one triangle by MathLib::isPointInTriangle
-//             (MathLib/AnalyticalGeometry.cpp:180-221); the search length is
+//             (MathLib/AnalyticalGeometry.cpp:180-221) among the triangles
+//             of the surface grid's cell that holds the node -- a node
+//             outside the grid (the bounding box grown by 1e-6 relative at
+//             its upper corner) belongs to no triangle (GEOLIB::SurfaceGrid,
+//             GEO/SurfaceGrid.cpp:29-240, 367-395); the search length is
 //             the BC's $EPSILON or 0.375 * h_min / 2 (msh_mesh.cpp:944-946,
 //             1917-1928), h_min the mesh's minimum edge length.
-// Deliberate differences: the SurfaceGrid box that also bounds the surface
-// search (GEO/SurfaceGrid.cpp:29-60) is not restated, nor is the merging of
-// coordinate-equal geometry points; nodes outside a surface's bounding box
-// by less than the search length, and decks with repeated point
-// coordinates, can differ.  Mesh nodes either on a geometry or at least one
-// minimum edge length away from it, as in structured decks, get the same
-// sets.
+// Deliberate difference: the merging of coordinate-equal geometry points is
+// not restated; decks with repeated point coordinates can differ.
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
+#include <limits>
 #include <map>
 #include <sstream>
 #include <string>
@@ -484,6 +485,109 @@ void ear_clip(const std::vector<double>& u, const std::vector<double>& v, std::v
     tris.insert(tris.end(), idx.begin(), idx.end());
 }
 
+// The grid of a surface's triangles that bounds its node search: the
+// bounding box with its upper corner moved out by 1e-6 relative (a flat
+// axis widened by 1e-3 of the largest extent), cut into cells so that
+// about five triangles fall into one; a triangle is listed in every cell of
+// the index box of its corners.  Cell indices are the truncated offsets;
+// a negative offset truncates toward zero on the reference's x86 build
+// (offsets in (-1, 0) give cell 0, lower ones no cell), which cell_of
+// reproduces on every host.
+struct SurfaceCells
+{
+    double lo[3], hi[3], inv[3];
+    size_t n[3] = {1, 1, 1};
+    std::vector<std::vector<int>> tri;  // per cell: first corners' offsets in the triangle list
+
+    bool axis(int k, double p, size_t& i) const
+    {
+        const double t = std::trunc((p - lo[k]) * inv[k]);
+        if (!(t > -1.0) || t >= (double)n[k]) return false;
+        i = (size_t)(t < 0.0 ? 0.0 : t);
+        return true;
+    }
+    bool cell_of(const double* p, size_t& c) const
+    {
+        size_t i, j, k;
+        if (!axis(0, p[0], i) || !axis(1, p[1], j) || !axis(2, p[2], k)) return false;
+        c = i + n[0] * (j + n[1] * k);
+        return true;
+    }
+};
+
+SurfaceCells surface_cells(const double* lo, const double* hi, const std::vector<double>& P,
+                           const std::vector<int>& tris)
+{
+    SurfaceCells g;
+    double dl[3];
+    const double eps = std::numeric_limits<double>::epsilon();
+    for (int k = 0; k < 3; k++)
+    {
+        g.lo[k] = lo[k];
+        g.hi[k] = hi[k] + std::fabs(hi[k]) * 1e-6;
+        if (std::fabs(g.hi[k]) < eps) g.hi[k] = (g.hi[k] - g.lo[k]) * (1.0 + 1e-6);
+        dl[k] = g.hi[k] - g.lo[k];
+    }
+    for (int k = 0; k < 3; k++)
+        if (dl[k] < eps)
+        {
+            const double m = std::max(dl[(k + 1) % 3], dl[(k + 2) % 3]);
+            g.lo[k] -= m * 0.5e-3;
+            g.hi[k] += m * 0.5e-3;
+            dl[k] = g.hi[k] - g.lo[k];
+        }
+    const double nt = (double)(tris.size() / 3), per = 5.0;
+    const bool f0 = std::fabs(dl[0]) < eps, f1 = std::fabs(dl[1]) < eps, f2 = std::fabs(dl[2]) < eps;
+    auto up = [](double v) { return (size_t)std::ceil(v); };
+    if (f0 || f1 || f2)
+    {
+        if (f1 && f2) g.n[0] = up(nt / per);
+        else if (f0 && f2) g.n[1] = up(nt / per);
+        else if (f0 && f1) g.n[2] = up(nt / per);
+        else if (f1)
+        {
+            g.n[0] = up(std::sqrt(nt * dl[0] / (per * dl[2])));
+            g.n[2] = up(g.n[0] * dl[2] / dl[0]);
+        }
+        else if (f2)
+        {
+            g.n[0] = up(std::sqrt(nt * dl[0] / (per * dl[1])));
+            g.n[1] = up(g.n[0] * dl[1] / dl[0]);
+        }
+        else
+        {
+            g.n[1] = up(std::sqrt(nt / per * dl[1] / dl[2]));
+            g.n[2] = up(nt * dl[2] / (per * dl[1]));
+        }
+    }
+    else
+    {
+        g.n[0] = up(std::pow(nt * dl[0] * dl[0] / (per * dl[1] * dl[2]), 1.0 / 3.0));
+        g.n[1] = up(g.n[0] * std::min(dl[1] / dl[0], 100.0));
+        g.n[2] = up(g.n[0] * std::min(dl[2] / dl[0], 100.0));
+    }
+    for (int k = 0; k < 3; k++) g.inv[k] = 1.0 / (dl[k] / (double)g.n[k]);
+    g.tri.assign(g.n[0] * g.n[1] * g.n[2], {});
+    for (size_t t = 0; t < tris.size(); t += 3)
+    {
+        // the corners' cells (a corner is inside the grid by construction)
+        size_t mn[3] = {SIZE_MAX, SIZE_MAX, SIZE_MAX}, mx[3] = {0, 0, 0};
+        for (int v = 0; v < 3; v++)
+            for (int k = 0; k < 3; k++)
+            {
+                size_t i = 0;
+                if (!g.axis(k, P[3 * tris[t + v] + k], i)) i = 0;
+                mn[k] = std::min(mn[k], i);
+                mx[k] = std::max(mx[k], i);
+            }
+        for (size_t i = mn[0]; i <= mx[0]; i++)
+            for (size_t j = mn[1]; j <= mx[1]; j++)
+                for (size_t k = mn[2]; k <= mx[2]; k++)
+                    g.tri[i + g.n[0] * (j + g.n[1] * k)].push_back((int)t);
+    }
+    return g;
+}
+
 ogs_status nodes_on_surface(const ogs_deck* d, const Surface& S, double eps, std::vector<int64_t>& out)
 {
     auto it = d->polylines.find(S.ply);
@@ -532,6 +636,7 @@ ogs_status nodes_on_surface(const ogs_deck* d, const Surface& S, double eps, std
     }
     std::vector<int> tris;
     ear_clip(pu, pv, tris);
+    const SurfaceCells grid = surface_cells(lo, hi, P, tris);
     for (size_t j = 0; j < d->x.size(); j++)
     {
         const double p[3] = {d->x[j], d->y[j], d->z[j]};
@@ -539,8 +644,9 @@ ogs_status nodes_on_surface(const ogs_deck* d, const Surface& S, double eps, std
         for (int q = 0; q < 3; q++)
             in_bv = in_bv && ((lo[q] <= p[q] && p[q] <= hi[q]) || std::fabs(lo[q] - p[q]) < eps ||
                               std::fabs(p[q] - hi[q]) < eps);
-        if (!in_bv) continue;
-        for (size_t t = 0; t < tris.size(); t += 3)
+        size_t cell = 0;
+        if (!in_bv || !grid.cell_of(p, cell)) continue;
+        for (int t : grid.tri[cell])
             if (in_triangle(p, &P[3 * tris[t]], &P[3 * tris[t + 1]], &P[3 * tris[t + 2]], eps))
             {
                 out.push_back((int64_t)j);

@@ -34,7 +34,7 @@ DECK = os.path.join(HERE, "deck")
 NODE_SETS = os.path.join(HERE, "deck_node_sets.npz")
 
 POLYLINE_RADII = (0.01, 0.2, 0.6)
-SURFACE_EPS = (None, 0.05)  # None: 0.375 * h_min / 2
+SURFACE_EPS = (None, 0.05, 0.2, 0.6)  # None: 0.375 * h_min / 2; 0.2 and 0.6 reach past the mesh spacing
 
 
 def jittered_tet_deck():
