@@ -424,6 +424,15 @@ int64_t ogs_gpu_kernel_launches(int32_t reset);
 ogs_status ogs_gpu_selftest_barrier(int32_t which, int32_t grid, int32_t spin_limit, int32_t withhold,
                                     int32_t* passed);
 
+/* Bounds checks of the debug build (compiled with -DOGS_BOUNDS_CHECK): the
+ * first out-of-range index any kernel met since the previous call (the
+ * access was skipped), as its site (1 element-assembly slot, 2 element
+ * node, 3 lattice slot, 4 lattice node, 5 FP64 product column, 6 FP32
+ * product column, 7 Dirichlet column/row, 8 Dirichlet slot, 9 ILU column)
+ * and index; site 0: none; site -1: a build without the checks.  Waits for
+ * the device.  (Instrumentation, no counterpart in the reference.) */
+ogs_status ogs_gpu_debug_oob(int64_t* site, int64_t* index);
+
 /* Device time of the SpMV kernel of every Krylov iteration, measured with
  * CUDA events recorded around it inside the captured iteration graphs
  * (instrumentation, no counterpart in the reference). */

@@ -4,6 +4,8 @@ Each .cu file under csrc/ is compiled in parallel with
 ``nvcc -gencode arch=compute_103a,code=sm_103a -lineinfo -O3``; the objects
 are linked into ``ogs5_gb300/_build/libogs_gpu.so`` with the static CUDA
 runtime.  Rebuilds only what changed (mtime of sources and headers).
+``build(debug=True)`` makes the bounds-checked variant (-DOGS_BOUNDS_CHECK)
+in ``ogs5_gb300/_build/debug/libogs_gpu_debug.so``.
 """
 from __future__ import annotations
 
@@ -36,12 +38,17 @@ def _headers() -> list[str]:
             + glob.glob(os.path.join(ROOT, "include", "*.h")))
 
 
-def _compile(src: str) -> tuple[str, str]:
-    obj = os.path.join(BUILD, os.path.splitext(os.path.basename(src))[0] + ".o")
+DEBUG_BUILD = os.path.join(BUILD, "debug")
+DEBUG_LIB = os.path.join(DEBUG_BUILD, "libogs_gpu_debug.so")
+
+
+def _compile(src: str, debug: bool = False) -> tuple[str, str]:
+    out_dir = DEBUG_BUILD if debug else BUILD
+    obj = os.path.join(out_dir, os.path.splitext(os.path.basename(src))[0] + ".o")
     newest_dep = max([os.path.getmtime(src)] + [os.path.getmtime(h) for h in _headers()])
     if os.path.exists(obj) and os.path.getmtime(obj) >= newest_dep:
         return obj, ""
-    cmd = [_nvcc(), *ARCH, *NVCC_FLAGS, "-c", src, "-o", obj]
+    cmd = [_nvcc(), *ARCH, *NVCC_FLAGS, *(["-DOGS_BOUNDS_CHECK"] if debug else []), "-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     with open(obj + ".log", "w") as f:
         f.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)
@@ -50,21 +57,23 @@ def _compile(src: str) -> tuple[str, str]:
     return obj, r.stderr
 
 
-def build(verbose: bool = False) -> str:
-    """Compiles and links; returns the path of libogs_gpu.so."""
-    os.makedirs(BUILD, exist_ok=True)
+def build(verbose: bool = False, debug: bool = False) -> str:
+    """Compiles and links; returns the path of the library (the bounds-checked
+    variant with debug)."""
+    out_dir, lib = (DEBUG_BUILD, DEBUG_LIB) if debug else (BUILD, LIB)
+    os.makedirs(out_dir, exist_ok=True)
     srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
     with cf.ThreadPoolExecutor(max_workers=min(16, len(srcs))) as ex:
-        objs = [o for o, _ in ex.map(_compile, srcs)]
-    if not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(o) for o in objs):
-        cmd = [_nvcc(), *ARCH, "-shared", "-o", LIB + ".tmp", *objs, "-cudart", "static"]
+        objs = [o for o, _ in ex.map(lambda f: _compile(f, debug), srcs)]
+    if not os.path.exists(lib) or os.path.getmtime(lib) < max(os.path.getmtime(o) for o in objs):
+        cmd = [_nvcc(), *ARCH, "-shared", "-o", lib + ".tmp", *objs, "-cudart", "static"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n" + r.stderr[-4000:])
-        os.replace(LIB + ".tmp", LIB)
+        os.replace(lib + ".tmp", lib)
     if verbose:
-        print(LIB)
-    return LIB
+        print(lib)
+    return lib
 
 
 if __name__ == "__main__":

@@ -52,7 +52,7 @@ EXPORTS = [
     "ogs_gpu_server_progress", "ogs_gpu_server_result", "ogs_gpu_server_info", "ogs_gpu_server_reserve",
     "ogs_gpu_cache_reset", "ogs_gpu_assemble_richards", "ogs_gpu_richards_step",
     "ogs_deck_read", "ogs_deck_destroy", "ogs_deck_mesh", "ogs_deck_geo_nodes", "ogs_deck_dirichlet",
-    "ogs_gpu_selftest_barrier",
+    "ogs_gpu_selftest_barrier", "ogs_gpu_debug_oob",
 ]
 REQUEST_FLOW, REQUEST_TRANSPORT = 0, 1
 RICHARDS_FLOW = 3
@@ -196,7 +196,9 @@ _LIB = None
 
 
 def library_path() -> str:
-    return _build.LIB
+    """The library to load: OGS_GPU_LIB when set (e.g. the bounds-checked
+    build), else the in-tree build."""
+    return os.environ.get("OGS_GPU_LIB") or _build.LIB
 
 
 def lib():
@@ -292,8 +294,18 @@ def lib():
                      "ogs_gpu_solve", "ogs_gpu_gp_velocity", "ogs_gpu_get_csr", "ogs_gpu_get_rhs",
                      "ogs_gpu_get_x", "ogs_gpu_spmv", "ogs_gpu_get_ilu0"):
             getattr(L, name).restype = st
+        L.ogs_gpu_debug_oob.argtypes = [C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+        L.ogs_gpu_debug_oob.restype = st
         _LIB = L
     return _LIB
+
+
+def debug_oob():
+    """(site, index) of the first out-of-range index met since the last
+    call (debug build); (0, 0) none, (-1, 0) a build without the checks."""
+    site, index = C.c_int64(), C.c_int64()
+    _check(lib().ogs_gpu_debug_oob(C.byref(site), C.byref(index)))
+    return site.value, index.value
 
 
 def _check(status: int, allow=()):

@@ -101,7 +101,7 @@ __global__ void k_dirichlet_symmetric(const int32_t* __restrict__ slice_ptr,
                                       const int32_t* __restrict__ diag_pos, double* val, double* b,
                                       const unsigned char* __restrict__ flag,
                                       const double* __restrict__ valn, const double* __restrict__ valf,
-                                      const int32_t* __restrict__ rows, int n)
+                                      const int32_t* __restrict__ rows, int n, int nrows)
 {
     // MXRandbed (matrix_routines.cpp:2314-2520): lift column into b, zero
     // row and column, keep the diagonal (a zero diagonal -> DBL_EPSILON).
@@ -115,6 +115,7 @@ __global__ void k_dirichlet_symmetric(const int32_t* __restrict__ slice_ptr,
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x)
     {
         const int i = rows[q];
+        if (!OGS_IN(i, nrows, kOobDirCol)) continue;
         const SellRow R(slice_ptr, row_len, i);
         if (flag[i])
         {
@@ -135,7 +136,7 @@ __global__ void k_dirichlet_symmetric(const int32_t* __restrict__ slice_ptr,
                 for (int t = 0; t < G; t++) c[t] = j0 + t < R.len ? col[R.slot(j0 + t)] : -1;
                 bool f[G];
 #pragma unroll
-                for (int t = 0; t < G; t++) f[t] = c[t] >= 0 && flag[c[t]];
+                for (int t = 0; t < G; t++) f[t] = c[t] >= 0 && OGS_IN(c[t], nrows, kOobDirCol) && flag[c[t]];
 #pragma unroll
                 for (int t = 0; t < G; t++)
                     if (f[t])
@@ -653,6 +654,8 @@ static ogs_status enqueue_element_kernel(ogs_system* s, const ogs_assembly_param
     if ((st = stage_in(s, u1, m->n_nodes, &s->u1, &a.u1))) return st;
     if (rp) a.r = *rp;
     a.val_store = kind == 0 && a.val == s->val && s->val_zero ? 1 : 0;
+    a.nslots = m->sell_nnz;
+    a.nrows = m->n_nodes;
     k_set_int<<<1, 1, 0, s->stream>>>(s->d_bad, kNoBadElement);
     OGS_LAUNCH_CHECK();
     if (!launch_assembly(m, a, m->affine, kind, s->stream))
@@ -1108,7 +1111,7 @@ static ogs_status dirichlet_apply(ogs_system* s)
                                                                            m->slice_ptr, m->row_len, m->sell_col,
                                                                            m->diag_pos, s->val, s->b, s->bc_flag,
                                                                            s->bc_valn, s->bc_valf, s->bc_touch,
-                                                                           s->ntouch);
+                                                                           s->ntouch, s->n);
         OGS_LAUNCH_CHECK();
     }
     return OGS_OK;
@@ -1917,5 +1920,38 @@ extern "C" ogs_status ogs_gpu_selftest_barrier(int32_t which, int32_t grid, int3
         set_error("selftest_barrier: barrier timeout (%d of %d arriving blocks passed)", n, g - (withhold ? 1 : 0));
         return OGS_CUDA_ERROR;
     }
+    return OGS_OK;
+}
+
+// ------------------------------------------------------------------
+// bounds checks of the debug build
+// ------------------------------------------------------------------
+unsigned long long ogs_oob_assembly();
+unsigned long long ogs_oob_krylov();
+unsigned long long ogs_oob_mixed();
+unsigned long long ogs_oob_ilu();
+
+extern "C" ogs_status ogs_gpu_debug_oob(int64_t* site, int64_t* index)
+{
+    if (!site || !index) { set_error("debug_oob: NULL argument"); return OGS_BAD_ARG; }
+#ifdef OGS_BOUNDS_CHECK
+    OGS_CUDA_TRY(cudaDeviceSynchronize());
+    unsigned long long w = ogs::oob_take();
+    for (unsigned long long v : {ogs_oob_assembly(), ogs_oob_krylov(), ogs_oob_mixed(), ogs_oob_ilu()})
+        w = std::min(w, v);
+    if (w == ~0ull)
+    {
+        *site = 0;
+        *index = 0;
+    }
+    else
+    {
+        *site = (int64_t)(w >> 40);
+        *index = (int64_t)(w & 0xffffffffffull);
+    }
+#else
+    *site = -1;  // not a bounds-checked build
+    *index = 0;
+#endif
     return OGS_OK;
 }

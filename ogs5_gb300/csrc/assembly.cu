@@ -340,7 +340,11 @@ __device__ __forceinline__ void gather(const AsmArgs& a, int64_t e, int* nd, dou
 {
     const int64_t E = a.E;
 #pragma unroll
-    for (int i = 0; i < NN; i++) nd[i] = __ldg(a.conn_t + (int64_t)i * E + e);
+    for (int i = 0; i < NN; i++)
+    {
+        nd[i] = __ldg(a.conn_t + (int64_t)i * E + e);
+        if (!OGS_IN(nd[i], a.nrows, kOobAsmNode)) nd[i] = 0;
+    }
 #pragma unroll
     for (int i = 0; i < NN; i++)
     {
@@ -363,7 +367,7 @@ __device__ __forceinline__ void scatter(const AsmArgs& a, int64_t e, const int* 
         for (int j = 0; j < NN; j++)
         {
             const int32_t k = __ldg(a.slot_t + (int64_t)(i * NN + j) * E + e);
-            atomicAdd(a.val + k, S[i * NN + j]);
+            if (OGS_IN(k, a.nslots, kOobAsmSlot)) atomicAdd(a.val + k, S[i * NN + j]);
         }
         atomicAdd(a.b + nd[i], r[i]);
     }
@@ -750,12 +754,16 @@ __global__ void __launch_bounds__(256, 2) k_flow_lattice(AsmArgs a, LatticeArgs 
                     const int pat = (dx == 0 ? 1 : 0) | (dy == 0 ? 2 : 0) | (dz == 0 ? 4 : 0);
                     const double mt = sMC[pat][C[dz + 1][dy + 1][dx + 1]];
                     const double lt = sL[pat] * S[dz + 1][dy + 1][dx + 1];
-                    const double u = a.u0 ? __ldg(a.u0 + i + dx + nx * (dy + (int64_t)ny * dz)) : 0.0;
+                    const int64_t j = i + dx + nx * (dy + (int64_t)ny * dz);
+                    const double u = a.u0 && OGS_IN(j, g.n, kOobLatNode) ? __ldg(a.u0 + j) : 0.0;
                     const double e = PLAIN ? mt + lt : mt + lt * relax0;
-                    if (a.val_store)
-                        v[(int64_t)rank * kSlice] = e;
-                    else
-                        v[(int64_t)rank * kSlice] += e;
+                    if (OGS_IN(s0 + (int64_t)rank * kSlice, a.nslots, kOobLatSlot))
+                    {
+                        if (a.val_store)
+                            v[(int64_t)rank * kSlice] = e;
+                        else
+                            v[(int64_t)rank * kSlice] += e;
+                    }
                     if constexpr (PLAIN)
                         bi += mt * u;
                     else
@@ -1420,3 +1428,5 @@ bool launch_assembly(const ogs_mesh* m, const AsmArgs& a, bool affine, int kind,
 }
 
 }  // namespace ogs
+
+unsigned long long ogs_oob_assembly() { return ogs::oob_take(); }

@@ -18,6 +18,47 @@ const char* last_error();
 // Count of this library's kernel launches (ogs_gpu_kernel_launches).
 void count_launches(int64_t n);
 
+// Bounds checks of the debug build (-DOGS_BOUNDS_CHECK): OGS_IN(i, n, site)
+// is true when 0 <= i < n; otherwise it records (site, i) in this file's
+// device word (the smallest site first) and is false, and the caller skips
+// the access.  Without the macro it is true and costs nothing.  The sites:
+enum OobSite
+{
+    kOobAsmSlot = 1,     // element assembly: SELL slot of an (i, j) pair
+    kOobAsmNode = 2,     // element assembly: node of an element
+    kOobLatSlot = 3,     // lattice assembly: SELL slot of a row entry
+    kOobLatNode = 4,     // lattice assembly: neighbour node / cell
+    kOobSpmvCol = 5,     // FP64 SELL product: column
+    kOobMixedCol = 6,    // FP32 SELL product: column
+    kOobDirCol = 7,      // Dirichlet elimination: column / row
+    kOobDirSlot = 8,     // Dirichlet elimination: slot
+    kOobIluCol = 9,      // ILU(0) sweeps and factorisation: column
+};
+#ifdef OGS_BOUNDS_CHECK
+static __device__ unsigned long long g_oob = ~0ull;
+__device__ __forceinline__ bool oob_ok(long long i, long long n, int site)
+{
+    if (i >= 0 && i < n) return true;
+    atomicMin(&g_oob, ((unsigned long long)site << 40) | ((unsigned long long)i & 0xffffffffffull));
+    return false;
+}
+#define OGS_IN(i, n, site) ::ogs::oob_ok((long long)(i), (long long)(n), (site))
+// this file's word, then reset
+static inline unsigned long long oob_take()
+{
+    unsigned long long v = ~0ull, r = ~0ull;
+    if (cudaMemcpyFromSymbol(&v, g_oob, sizeof v) != cudaSuccess || cudaMemcpyToSymbol(g_oob, &r, sizeof r) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return ~0ull;
+    }
+    return v;
+}
+#else
+#define OGS_IN(i, n, site) true
+static inline unsigned long long oob_take() { return ~0ull; }
+#endif
+
 #define OGS_CUDA_TRY(expr)                                                  \
     do                                                                      \
     {                                                                       \
@@ -116,6 +157,7 @@ struct AsmArgs
     ogs_richards_params r;
     int val_store;      // val is all zeros (Initialize, nothing added since):
                         // a row kernel may store instead of add
+    int64_t nslots, nrows;  // SELL slots and rows (the debug build's bounds)
 };
 
 }  // namespace ogs

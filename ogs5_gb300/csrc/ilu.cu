@@ -106,7 +106,11 @@ __device__ __forceinline__ void ilu_row(const IluView& f, const double* __restri
     // the rows this row reads: its columns before (MODE 0, 1) or after
     // (MODE 2) the diagonal
     const int w0 = MODE == 2 ? d + 1 : rb, w1 = MODE == 2 ? re : d;
-    for (int k = w0; k < w1; k++) ilu_wait(flags, __ldg(f.col + k), launch, f.bad);
+    for (int k = w0; k < w1; k++)
+    {
+        const int c = __ldg(f.col + k);
+        if (OGS_IN(c, f.n, kOobIluCol)) ilu_wait(flags, c, launch, f.bad);
+    }
     fence_acquire();
     if (MODE == 0 && re - rb <= kIluRowMax && f.ku <= kIluUMax)
     {
@@ -312,12 +316,12 @@ __device__ __forceinline__ void ilu_fetch(const IluView& f, const double* __rest
 // the row's result: s0 - sum_k v_k out_{c_k} in column order, products and
 // differences rounded separately (no FMA), then over the diagonal (MODE 2)
 template <int MODE, int K>
-__device__ __forceinline__ void ilu_solve_row(const PackedRow<K>& R, double* out)
+__device__ __forceinline__ void ilu_solve_row(const IluView& f, const PackedRow<K>& R, double* out)
 {
     if (R.i < 0) return;
     double x[K];
 #pragma unroll
-    for (int k = 0; k < K; k++) x[k] = R.c[k] >= 0 ? __ldcg(out + R.c[k]) : 0.0;
+    for (int k = 0; k < K; k++) x[k] = R.c[k] >= 0 && OGS_IN(R.c[k], f.n, kOobIluCol) ? __ldcg(out + R.c[k]) : 0.0;
     double s = R.s0;
 #pragma unroll
     for (int k = 0; k < K; k++)
@@ -359,13 +363,13 @@ __global__ void __launch_bounds__(NT, 1) k_ilu_sweep(IluView f, const double* __
     for (int l = 0; l < nl; l++)
     {
         const int b = __ldg(ptr + l), e = __ldg(ptr + l + 1);
-        ilu_solve_row<MODE, K>(R, out);
+        ilu_solve_row<MODE, K>(f, R, out);
         // a level wider than the cluster: its further rows fetched here
         for (int pos = b + tid + nt; pos < e; pos += nt)
         {
             PackedRow<K> T;
             ilu_fetch<MODE, K>(f, in, out, pos, npos, T);
-            ilu_solve_row<MODE, K>(T, out);
+            ilu_solve_row<MODE, K>(f, T, out);
         }
         cluster_arrive_release();
         if (l + 1 < nl)
@@ -536,3 +540,5 @@ void launch_cg_init_z(const SolveArgs& a, int grid, cudaStream_t s)
 }
 
 }  // namespace ogs
+
+unsigned long long ogs_oob_ilu() { return ogs::oob_take(); }

@@ -55,7 +55,8 @@ __device__ __forceinline__ double sell_row(const SellView<T>& A, const double* _
     for (int j = 0; j < w; j++)
     {
         const int k = beg + (j << 5);
-        acc += (double)__ldcs(A.val + k) * __ldg(x + __ldcs(A.col + k));
+        const int c = __ldcs(A.col + k);
+        if (OGS_IN(c, A.n, kOobSpmvCol)) acc += (double)__ldcs(A.val + k) * __ldg(x + c);
     }
     return acc;
 }
@@ -520,3 +521,5 @@ void launch_bicgstab_finish(const SolveArgs& a, cudaStream_t s)
 }
 
 }  // namespace ogs
+
+unsigned long long ogs_oob_krylov() { return ogs::oob_take(); }

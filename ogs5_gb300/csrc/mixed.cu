@@ -107,7 +107,8 @@ __device__ __forceinline__ float sell32_row(const MixedArgs& a, const float* x, 
     for (int j = 0; j < w; j++)
     {
         const int k = beg + (j << 5);
-        acc += __ldg(a.val32 + k) * ldx<X_NC>(x, __ldg(a.A.col + k));
+        const int c = __ldg(a.A.col + k);
+        if (OGS_IN(c, a.n, kOobMixedCol)) acc += __ldg(a.val32 + k) * ldx<X_NC>(x, c);
     }
     return acc;
 }
@@ -1277,3 +1278,5 @@ void launch_mp_iteration(const MixedArgs& a, cudaStream_t s, cudaEvent_t eb, cud
 }
 
 }  // namespace ogs
+
+unsigned long long ogs_oob_mixed() { return ogs::oob_take(); }
