@@ -223,12 +223,14 @@ __global__ void k_mp_convert(MixedArgs a, const int32_t* __restrict__ row_len,
         for (int j = 0; j < len; j++)
         {
             const int k = beg + (j << 5);
+            // the diagonal-offset form stores the upper half only: the lower
+            // entries' FP64 products (GB300's scarce FP64) and scale loads
+            // are skipped
+            const int d = a.fmt == 0 ? (int)slot_up[k] : 0;
+            if (d < 0) continue;
             const double v = a.scaled ? a.A.val[k] * si * (double)d32[a.A.col[k]] : a.A.val[k];
             if (a.fmt == 0)
-            {
-                const int d = slot_up[k];
-                if (d >= 0) U[(size_t)d * a.ustride + i] = (float)v;
-            }
+                U[(size_t)d * a.ustride + i] = (float)v;
             else
                 val32[k] = (float)v;
         }
