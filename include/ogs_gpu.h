@@ -420,7 +420,12 @@ int64_t ogs_gpu_kernel_launches(int32_t reset);
  * without arriving, so the other blocks wait on a word nothing sets until
  * the limit and give up.  *passed: the blocks that passed.  Returns OGS_OK
  * when every arriving block passed, OGS_CUDA_ERROR with "barrier timeout"
- * in ogs_gpu_last_error when a wait gave up (the context stays usable). */
+ * in ogs_gpu_last_error when a wait gave up (the context stays usable).
+ * which = 2: the row waits of the ILU(0) kernels, on a forward sweep over a
+ * 64-row lower bidiagonal factor (grid ignored); withhold != 0 leaves row 0
+ * unpublished, so every later row's wait runs out; *passed: the rows with
+ * their exact value; OGS_CUDA_ERROR with "ILU row wait timeout" when a wait
+ * gave up. */
 ogs_status ogs_gpu_selftest_barrier(int32_t which, int32_t grid, int32_t spin_limit, int32_t withhold,
                                     int32_t* passed);
 

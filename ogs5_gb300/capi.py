@@ -338,8 +338,8 @@ def _f64(a):
 def selftest_barrier(which: int, grid: int = 0, spin_limit: int = 0, withhold: bool = False) -> dict:
     """ogs_gpu_selftest_barrier: one grid barrier of the persistent FP32 CG
     kernel (which 0) or of the batch kernel (1), optionally with block 0
-    withholding its arrival; returns status, blocks passed and the error
-    text."""
+    withholding its arrival, or the ILU(0) row waits (2) with row 0 left
+    unpublished; returns status, blocks (rows) passed and the error text."""
     n = C.c_int32(0)
     status = lib().ogs_gpu_selftest_barrier(which, grid, spin_limit, 1 if withhold else 0, C.byref(n))
     return {"status": status, "passed": n.value, "error": lib().ogs_gpu_last_error().decode()}

@@ -39,6 +39,7 @@ int vec_grid(int n);
 int red_grid(int n);
 int mp_spmv_grid(int n);
 cudaError_t launch_mp_barrier_selftest(KState* st, int grid, int withhold, unsigned limit, int* go, cudaStream_t s);
+cudaError_t ilu_wait_selftest(int withhold, unsigned limit, int* gave_up, int* rows_ok, cudaStream_t s);
 size_t batch_ctl_bytes();
 cudaError_t launch_batch_barrier_selftest(void* ctl, unsigned limit, int grid, int withhold, int* go, cudaStream_t s);
 
@@ -1868,10 +1869,29 @@ ogs_status system_element_status(const ogs_system* s) { return element_flag_stat
 extern "C" ogs_status ogs_gpu_selftest_barrier(int32_t which, int32_t grid, int32_t spin_limit, int32_t withhold,
                                                int32_t* passed)
 {
-    if ((which != 0 && which != 1) || grid < 0 || spin_limit < 0 || !passed)
+    if (which < 0 || which > 2 || grid < 0 || spin_limit < 0 || !passed)
     {
         set_error("selftest_barrier: bad arguments");
         return OGS_BAD_ARG;
+    }
+    if (which == 2)
+    {
+        int gave_up = 0, ok = 0;
+        const cudaError_t e = ilu_wait_selftest(withhold ? 1 : 0, spin_limit ? (unsigned)spin_limit : 0u, &gave_up, &ok,
+                                                nullptr);
+        if (e != cudaSuccess)
+        {
+            set_error("selftest_barrier: %s", cudaGetErrorString(e));
+            return OGS_CUDA_ERROR;
+        }
+        *passed = ok;
+        count_launches(1);
+        if (gave_up)
+        {
+            set_error("selftest_barrier: ILU row wait timeout (%d of 64 rows exact)", ok);
+            return OGS_CUDA_ERROR;
+        }
+        return OGS_OK;
     }
     int dev = 0, sms = 0, coop = 0;
     OGS_CUDA_TRY(cudaGetDevice(&dev));

@@ -36,6 +36,8 @@
 // the cluster barrier, and the next level's entries are loaded while the
 // barrier completes.
 #include <algorithm>
+#include <cstring>
+#include <vector>
 
 #include "krylov.cuh"
 
@@ -71,13 +73,13 @@ __device__ __forceinline__ void st_release_s32(int* p, int v)
 // pause, bounded; once any wait of the launch has given up, f.bad is -1
 // and the others stop waiting too).  The caller takes the acquire fence
 // after all its waits.
-__device__ __forceinline__ void ilu_wait(const int* flags, int j, int launch, int* bad)
+__device__ __forceinline__ void ilu_wait(const int* flags, int j, int launch, int* bad, unsigned limit)
 {
     if (ld_relaxed_s32(flags + j) >= launch) return;
     unsigned spins = 0, pause = 32;
     while (ld_relaxed_s32(flags + j) < launch)
     {
-        if (++spins > kIluSpin || ((spins & 255) == 0 && *(volatile int*)bad == -1))
+        if (++spins > limit || ((spins & 255) == 0 && *(volatile int*)bad == -1))
         {
             atomicMin(bad, -1);
             return;
@@ -109,7 +111,7 @@ __device__ __forceinline__ void ilu_row(const IluView& f, const double* __restri
     for (int k = w0; k < w1; k++)
     {
         const int c = __ldg(f.col + k);
-        if (OGS_IN(c, f.n, kOobIluCol)) ilu_wait(flags, c, launch, f.bad);
+        if (OGS_IN(c, f.n, kOobIluCol)) ilu_wait(flags, c, launch, f.bad, f.spin ? f.spin : kIluSpin);
     }
     fence_acquire();
     if (MODE == 0 && re - rb <= kIluRowMax && f.ku <= kIluUMax)
@@ -527,6 +529,91 @@ void launch_ilu_apply(const IluView& f, const double* in, double* out, const KSt
     }
     k_ilu_flow<1><<<ilu_grid(f.n_lpos), kIluBlock, 0, s>>>(f, in, out, st);
     k_ilu_flow<2><<<ilu_grid(f.n_upos), kIluBlock, 0, s>>>(f, nullptr, out, st);
+}
+
+// Self-test of the bounded row waits: a forward sweep over a 64-row lower
+// bidiagonal L (row i reads row i - 1; one row per level, each level padded
+// to a warp).  withhold: row 0 is left out of the level list, so nothing
+// publishes it and every later row's wait runs out (f.bad = -1).  Returns
+// through *gave_up whether a wait gave up and through *rows_ok how many
+// rows hold the chain's exact value.
+cudaError_t ilu_wait_selftest(int withhold, unsigned limit, int* gave_up, int* rows_ok, cudaStream_t s)
+{
+    constexpr int n = 64, npos = n * 32;
+    std::vector<int32_t> rp(n + 1), col, dg(n), rows(npos, -1);
+    std::vector<double> lu;
+    for (int i = 0; i < n; i++)
+    {
+        rp[i] = (int32_t)col.size();
+        if (i > 0)
+        {
+            col.push_back(i - 1);
+            lu.push_back(0.5);
+        }
+        dg[i] = (int32_t)col.size();
+        col.push_back(i);
+        lu.push_back(1.0);
+        rows[32 * i] = withhold && i == 0 ? -1 : i;
+    }
+    rp[n] = (int32_t)col.size();
+    const int nnz = (int)col.size();
+    char* buf = nullptr;
+    const size_t bytes = 4096 + sizeof(int32_t) * (n + 1 + nnz + n + npos + 3 * n + 1) + sizeof(double) * (nnz + 2 * n) +
+                         sizeof(unsigned long long) * 3 + sizeof(KState);
+    cudaError_t e = cudaMalloc(&buf, bytes);
+    if (e != cudaSuccess) return e;
+    e = cudaMemsetAsync(buf, 0, bytes, s);
+    size_t off = 0;
+    auto take = [&](size_t b) { char* p = buf + off; off = (off + b + 255) & ~size_t(255); return p; };
+    int32_t* d_rp = (int32_t*)take(sizeof(int32_t) * (n + 1));
+    int32_t* d_col = (int32_t*)take(sizeof(int32_t) * nnz);
+    int32_t* d_dg = (int32_t*)take(sizeof(int32_t) * n);
+    int32_t* d_rows = (int32_t*)take(sizeof(int32_t) * npos);
+    int* d_flags = (int*)take(sizeof(int) * 3 * n);
+    int* d_bad = (int*)take(sizeof(int));
+    double* d_lu = (double*)take(sizeof(double) * nnz);
+    double* d_in = (double*)take(sizeof(double) * n);
+    double* d_out = (double*)take(sizeof(double) * n);
+    unsigned long long* d_ticket = (unsigned long long*)take(sizeof(unsigned long long) * 3);
+    KState* d_st = (KState*)take(sizeof(KState));
+    std::vector<double> ones(n, 1.0);
+    const int big = 0x7fffffff;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_rp, rp.data(), sizeof(int32_t) * (n + 1), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_col, col.data(), sizeof(int32_t) * nnz, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_dg, dg.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_rows, rows.data(), sizeof(int32_t) * npos, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_lu, lu.data(), sizeof(double) * nnz, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_in, ones.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_bad, &big, sizeof(int), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+    {
+        IluView f;
+        std::memset(&f, 0, sizeof f);
+        f.row_ptr = d_rp; f.col = d_col; f.diag = d_dg; f.lu = d_lu;
+        f.lrows = d_rows; f.urows = d_rows;
+        f.n = n; f.n_lpos = npos; f.n_upos = npos;
+        f.flags = d_flags; f.ticket = d_ticket; f.bad = d_bad; f.spin = limit;
+        k_ilu_flow<1><<<ilu_grid(npos), kIluBlock, 0, s>>>(f, d_in, d_out, d_st);
+        e = cudaGetLastError();
+    }
+    int bad = 0;
+    std::vector<double> out(n);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out.data(), d_out, sizeof(double) * n, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(buf);
+    if (e != cudaSuccess) return e;
+    // exact chain: x_0 = 1, x_i = 1 - x_{i-1} / 2 (products and differences rounded as the kernel does)
+    int ok = 0;
+    double x = 0.0;
+    for (int i = 0; i < n; i++)
+    {
+        x = i == 0 ? 1.0 : 1.0 - 0.5 * x;
+        ok += out[i] == x ? 1 : 0;
+    }
+    *gave_up = bad == -1 ? 1 : 0;
+    *rows_ok = ok;
+    return cudaSuccess;
 }
 
 void launch_cg_dots_z(const SolveArgs& a, int grid, cudaStream_t s)

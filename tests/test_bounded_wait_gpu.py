@@ -2,8 +2,10 @@
 (the persistent FP32 CG kernel and the Monte-Carlo batch kernel) end in an
 error status instead of hanging: one block withholds its arrival, so the
 others wait on a barrier word that nothing sets until their poll limit runs
-out.  The failure is made on purpose only through that withheld arrival;
-the context stays usable afterwards (a regular solve follows)."""
+out.  The same for the row waits of the ILU(0) kernels: a row left out of
+the sweep is never published, so the rows after it give up.  The failure is
+made on purpose only through that withheld arrival or row; the context stays
+usable afterwards (a regular solve follows)."""
 import numpy as np
 import pytest
 
@@ -45,5 +47,32 @@ def test_withheld_arrival_times_out_with_an_error(gpu, which):
 
 
 def test_selftest_rejects_bad_arguments(gpu):
-    assert gpu.selftest_barrier(2)["status"] == gpu.BAD_ARG
+    assert gpu.selftest_barrier(3)["status"] == gpu.BAD_ARG
     assert gpu.selftest_barrier(0, grid=100000)["status"] == gpu.BAD_ARG
+
+
+def test_ilu_row_waits_pass_when_every_row_is_published(gpu):
+    r = gpu.selftest_barrier(2, spin_limit=SHORT_LIMIT)
+    assert r["status"] == gpu.OK, r
+    assert r["passed"] == 64  # every row of the chain exact
+
+
+def test_ilu_unpublished_row_times_out_with_an_error(gpu):
+    r = gpu.selftest_barrier(2, spin_limit=SHORT_LIMIT, withhold=True)
+    assert r["status"] == gpu.CUDA_ERROR, r
+    assert "ILU row wait timeout" in r["error"]
+    assert r["passed"] < 64
+    # the context is still usable: the sweep passes again, and an ILU solve runs
+    assert gpu.selftest_barrier(2, spin_limit=SHORT_LIMIT)["status"] == gpu.OK
+    m = M.structured_tet(6, 5, 4)
+    ek = np.repeat(fields.lognormal_k((6, 5, 4), np.log(1e-5), 1.0, 3.0, seed=2), 6)
+    eqs = gpu.LinearEQS(gpu.GpuMesh(m))
+    eqs.ConfigNumerics(gpu.LS_BICGSTAB, gpu.PRECOND_ILU0, 2000, 1e-10)
+    eqs.Initialize()
+    eqs.GlobalAssembly(gpu.make_params(gpu.GROUNDWATER_FLOW, dt=3600.0, storage=1e-4), ek, np.zeros(m.n_nodes))
+    lf = m.face_nodes(0, 0)
+    eqs.SetKnownX(lf, np.ones(len(lf)), gpu.DIRICHLET_ROW_ONLY)
+    x = np.zeros(m.n_nodes)
+    x[lf] = 1.0
+    eqs.Solver(x)
+    assert eqs.stats()["status"] == gpu.OK
