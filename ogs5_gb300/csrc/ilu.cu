@@ -274,7 +274,7 @@ __global__ void k_ilu_pack(IluView f)
         if (d < 0) i = -1;
         const int re = i >= 0 ? __ldg(f.row_ptr + i + 1) : 0;
         f.pu_row[pos] = i;
-        f.pu_diag[pos] = i >= 0 ? f.lu[d] : 1.0;
+        f.pu_diag[pos] = i >= 0 ? 1.0 / f.lu[d] : 1.0;  // the sweep multiplies by it
         for (int k = 0; k < f.ku; k++)
         {
             const bool in = i >= 0 && d + 1 + k < re;
@@ -285,7 +285,7 @@ __global__ void k_ilu_pack(IluView f)
 }
 
 // One packed row: index, entries, start value (forward: in_i, backward:
-// the forward result out_i), diagonal (backward)
+// the forward result out_i), reciprocal of the diagonal (backward)
 template <int K>
 struct PackedRow
 {
@@ -315,8 +315,11 @@ __device__ __forceinline__ void ilu_fetch(const IluView& f, const double* __rest
     R.dg = R.i >= 0 && MODE == 2 ? __ldg(f.pu_diag + pos) : 1.0;
 }
 
-// the row's result: s0 - sum_k v_k out_{c_k} in column order, products and
-// differences rounded separately (no FMA), then over the diagonal (MODE 2)
+// the row's result: s0 - sum_k v_k out_{c_k} in column order (one FMA per
+// entry: the cluster's 16 SMs retire FP64 at 1/64 of the FP32 rate, and a
+// level's FP64 work is on its critical path), then times the reciprocal of
+// the diagonal (MODE 2; formed once per factorisation, no division in the
+// level)
 template <int MODE, int K>
 __device__ __forceinline__ void ilu_solve_row(const IluView& f, const PackedRow<K>& R, double* out)
 {
@@ -327,9 +330,36 @@ __device__ __forceinline__ void ilu_solve_row(const IluView& f, const PackedRow<
     double s = R.s0;
 #pragma unroll
     for (int k = 0; k < K; k++)
-        if (R.c[k] >= 0) s = __dsub_rn(s, __dmul_rn(R.v[k], x[k]));
-    if (MODE == 2) s = s / R.dg;
+        if (R.c[k] >= 0) s = __fma_rn(-R.v[k], x[k], s);
+    if (MODE == 2) s = s * R.dg;  // the packed reciprocal of U_ii
     __stcg(out + R.i, s);
+}
+
+// L2 prefetch of level l's packed rows (row, the K column and value arrays,
+// the diagonal): levels start on multiples of 32 positions, so every
+// segment starts and ends on a 128-byte boundary.  The cluster's CTAs share
+// the segments.
+template <int MODE>
+__device__ __forceinline__ void ilu_prefetch_level(const IluView& f, int b, int e)
+{
+    if (threadIdx.x != 0 || e <= b) return;
+    const int npos = MODE == 2 ? f.n_upos : f.n_lpos;
+    const int kmax = MODE == 2 ? f.ku : f.kl;
+    const int32_t* prow = MODE == 2 ? f.pu_row : f.pl_row;
+    const int32_t* pcol = MODE == 2 ? f.pu_col : f.pl_col;
+    const double* pval = MODE == 2 ? f.pu_val : f.pl_val;
+    const int nseg = 2 * kmax + (MODE == 2 ? 2 : 1);
+    const unsigned n4 = (unsigned)(e - b) * 4u, n8 = (unsigned)(e - b) * 8u;
+    for (int q = blockIdx.x; q < nseg; q += gridDim.x)
+    {
+        const void* p;
+        unsigned bytes;
+        if (q == 0) { p = prow + b; bytes = n4; }
+        else if (q <= kmax) { p = pcol + (size_t)(q - 1) * npos + b; bytes = n4; }
+        else if (q <= 2 * kmax) { p = pval + (size_t)(q - 1 - kmax) * npos + b; bytes = n8; }
+        else { p = f.pu_diag + b; bytes = n8; }
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+    }
 }
 
 // the two halves of the cluster barrier (.aligned: the warp reconverges
@@ -360,11 +390,13 @@ __global__ void __launch_bounds__(NT, 1) k_ilu_sweep(IluView f, const double* __
     PackedRow<K> R;
     {
         const int b = __ldg(ptr), e = __ldg(ptr + 1);
+        if (nl > 1) ilu_prefetch_level<MODE>(f, e, __ldg(ptr + 2));
         ilu_fetch<MODE, K>(f, in, out, b + tid < e ? b + tid : -1, npos, R);
     }
     for (int l = 0; l < nl; l++)
     {
         const int b = __ldg(ptr + l), e = __ldg(ptr + l + 1);
+        if (l + 2 < nl) ilu_prefetch_level<MODE>(f, __ldg(ptr + l + 2), __ldg(ptr + l + 3));
         ilu_solve_row<MODE, K>(f, R, out);
         // a level wider than the cluster: its further rows fetched here
         for (int pos = b + tid + nt; pos < e; pos += nt)

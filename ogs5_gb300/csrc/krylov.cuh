@@ -93,7 +93,8 @@ struct IluView
     // the sweeps' rows packed by position (level order, padded levels):
     // level starts, the row (-1: padding or no diagonal), and the row's L
     // (forward) or U (backward) entries as columns / values [k][pos]
-    // (column -1 past the row's entries), the diagonal for the backward sweep
+    // (column -1 past the row's entries), the reciprocal of the diagonal for
+    // the backward sweep
     const int32_t* lptr;      // [n_lev + 1]
     const int32_t* uptr;      // [n_ulev + 1]
     int n_lev, n_ulev;
