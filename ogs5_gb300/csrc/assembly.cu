@@ -1110,6 +1110,12 @@ __device__ __forceinline__ double mrange(double a, double b, double c)
 
 // CMediumProperties::SaturationCapillaryPressureFunction, models 4 (van
 // Genuchten) and 6 (Brooks-Corey) (rf_mmp_new.cpp:5243-5328)
+// x^y for x >= 0 as exp(y log x): the curves' bases are never negative, and
+// 0^y (0 for y > 0, inf for y < 0) comes out of log(0) = -inf.  Cheaper than
+// pow on GB300's FP64 unit; the result is within |y log x| ulps of pow's
+// (<= ~1e-14 relative on the curves' range)
+__device__ __forceinline__ double powp(double x, double y) { return exp(y * log(x)); }
+
 __device__ __forceinline__ double rich_saturation(const ogs_richards_params& r, double pc)
 {
     // divisions by parameters as products with their reciprocals (loop
@@ -1119,13 +1125,13 @@ __device__ __forceinline__ double rich_saturation(const ogs_richards_params& r, 
     if (r.capillary_model == 4)
     {
         if (pc < 0.0) pc = 0.0;
-        se = pow(pc * ipb, 1.0 / (1.0 - r.m)) + 1.0;
-        se = pow(se, -r.m);
+        se = powp(pc * ipb, 1.0 / (1.0 - r.m)) + 1.0;
+        se = powp(se, -r.m);
     }
     else
     {
         if (pc < r.pb) pc = r.pb;
-        se = pow(pc * ipb, -r.m);
+        se = powp(pc * ipb, -r.m);
     }
     const double sl = se * (r.slm - r.slr) + r.slr;
     return mrange(r.slr + DBL_EPSILON, sl, r.slm - DBL_EPSILON);
@@ -1142,14 +1148,14 @@ __device__ __forceinline__ double rich_dsdpc(const ogs_richards_params& r, doubl
     if (r.capillary_model == 4)
     {
         sl = mrange(r.slr + DBL_EPSILON, sl, r.slm - DBL_EPSILON);
-        const double v1 = pow((sl - r.slr) * isr, -1.0 / r.m);
-        const double v2 = pow(v1 - 1.0, -r.m);
+        const double v1 = powp((sl - r.slr) * isr, -1.0 / r.m);
+        const double v2 = powp(v1 - 1.0, -r.m);
         dsdp = (r.m * (sl - r.slr)) / (r.pb * (r.m - 1.0) * v1 * v2);
     }
     else
     {
         sl = mrange(r.slr + DBL_EPSILON, sl, r.slm);
-        const double v1 = pow((sl - r.slr) * isr, -1.0 / r.m);
+        const double v1 = powp((sl - r.slr) * isr, -1.0 / r.m);
         dsdp = (r.m * (r.slr - sl)) / (r.pb * v1);
     }
     const double lim = (-1.0) / DBL_EPSILON;
@@ -1166,11 +1172,11 @@ __device__ __forceinline__ double rich_krel(const ogs_richards_params& r, double
     double kr;
     if (r.permeability_model == 4)
     {
-        const double b = 1.0 - pow(1.0 - pow(se, 1.0 / r.kr_m), r.kr_m);
+        const double b = 1.0 - powp(1.0 - powp(se, 1.0 / r.kr_m), r.kr_m);
         kr = sqrt(se) * (b * b);
     }
     else
-        kr = pow(se, 3.0 + 2.0 / r.kr_m);
+        kr = powp(se, 3.0 + 2.0 / r.kr_m);
     if (kr < r.kr_min) kr = r.kr_min;
     return kr;
 }
