@@ -433,10 +433,18 @@ ogs_status ogs_gpu_selftest_barrier(int32_t which, int32_t grid, int32_t spin_li
  * first out-of-range index any kernel met since the previous call (the
  * access was skipped), as its site (1 element-assembly slot, 2 element
  * node, 3 lattice slot, 4 lattice node, 5 FP64 product column, 6 FP32
- * product column, 7 Dirichlet column/row, 8 Dirichlet slot, 9 ILU column)
- * and index; site 0: none; site -1: a build without the checks.  Waits for
+ * product column, 7 Dirichlet column/row, 8 Dirichlet slot, 9 ILU column,
+ * 10 FP32 lattice product window) and index; site 0: none; site -1: a build without the checks.  Waits for
  * the device.  (Instrumentation, no counterpart in the reference.) */
 ogs_status ogs_gpu_debug_oob(int64_t* site, int64_t* index);
+
+/* The FP32 product of the Jacobi-scaled operator on x (n host values), by
+ * the row kernel (y_rows) and by the four-rows-per-thread lattice kernel
+ * (y_lines), n host values each; the two are bit for bit equal.  Needs the
+ * FP32 operator of a 27-point lattice, i.e. a solve with
+ * OGS_PRECISION_FP32_REFINED on a hex lattice before; OGS_BAD_ARG
+ * otherwise.  (Instrumentation, no counterpart in the reference.) */
+ogs_status ogs_gpu_debug_fp32_product(ogs_system* sys, const float* x, float* y_rows, float* y_lines);
 
 /* Device time of the SpMV kernel of every Krylov iteration, measured with
  * CUDA events recorded around it inside the captured iteration graphs

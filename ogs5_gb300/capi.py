@@ -52,7 +52,7 @@ EXPORTS = [
     "ogs_gpu_server_progress", "ogs_gpu_server_result", "ogs_gpu_server_info", "ogs_gpu_server_reserve",
     "ogs_gpu_cache_reset", "ogs_gpu_assemble_richards", "ogs_gpu_richards_step",
     "ogs_deck_read", "ogs_deck_destroy", "ogs_deck_mesh", "ogs_deck_geo_nodes", "ogs_deck_dirichlet",
-    "ogs_gpu_selftest_barrier", "ogs_gpu_debug_oob",
+    "ogs_gpu_selftest_barrier", "ogs_gpu_debug_oob", "ogs_gpu_debug_fp32_product",
 ]
 REQUEST_FLOW, REQUEST_TRANSPORT = 0, 1
 RICHARDS_FLOW = 3
@@ -296,6 +296,8 @@ def lib():
             getattr(L, name).restype = st
         L.ogs_gpu_debug_oob.argtypes = [C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
         L.ogs_gpu_debug_oob.restype = st
+        L.ogs_gpu_debug_fp32_product.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.ogs_gpu_debug_fp32_product.restype = st
         _LIB = L
     return _LIB
 
@@ -518,6 +520,15 @@ class LinearEQS:
             out = np.zeros(self.n)
         _check(lib().ogs_gpu_spmv(self.h, _ptr(_f64(x)), _ptr(out)))
         return out
+
+    def debug_fp32_product(self, x):
+        """(y_rows, y_lines): the FP32 product of the Jacobi-scaled lattice
+        operator on x by the row kernel and by the four-rows-per-thread
+        kernel (after a FP32_REFINED solve on a hex lattice)."""
+        xs = np.ascontiguousarray(x, dtype=np.float32)
+        y_rows, y_lines = np.zeros(self.n, np.float32), np.zeros(self.n, np.float32)
+        _check(lib().ogs_gpu_debug_fp32_product(self.h, _ptr(xs), _ptr(y_rows), _ptr(y_lines)))
+        return y_rows, y_lines
 
 
 def csr_cg_noalloc(row_ptr, col, val, b, x, max_iter=1000, tol=1e-10, stream=None):

@@ -37,7 +37,8 @@ void launch_ilu_factor(const IluView& f, const double* val, const int32_t* csr2s
                        const KState* st, cudaStream_t s);
 int vec_grid(int n);
 int red_grid(int n);
-int mp_spmv_grid(int n);
+int mp_spmv_grid(const MixedArgs& a);
+void launch_mp_product_pair(const MixedArgs& a, float* y_rows, float* y_lines, cudaStream_t s);
 cudaError_t launch_mp_barrier_selftest(KState* st, int grid, int withhold, unsigned limit, int* go, cudaStream_t s);
 cudaError_t ilu_wait_selftest(int withhold, unsigned limit, int* gave_up, int* rows_ok, cudaStream_t s);
 size_t batch_ctl_bytes();
@@ -283,6 +284,9 @@ struct ogs_system
     float *x32 = nullptr, *r32 = nullptr, *p32 = nullptr, *s32 = nullptr, *d32 = nullptr, *U = nullptr,
           *val32 = nullptr, *u32 = nullptr, *w32 = nullptr;
     int fmt = -1;
+    int f32_pad = 0;       // zero pad in front of every FP32 vector and operator row (values)
+    int f32_ustride = 0;   // values per operator row of the diagonal-offset form
+    int mp_lines = 0;      // product kernel the captured iterations use (MixedArgs::lines)
     cudaGraphExec_t mp_chunk = nullptr, mp_replace = nullptr;
     int mp_replace_scaled = 0;  // form (MixedArgs::scaled) mp_replace was captured with
     // persistent FP32 CG (OGS_SCHEDULE_PERSISTENT): the arguments of the
@@ -1133,6 +1137,22 @@ extern "C" ogs_status ogs_gpu_set_dirichlet(ogs_system* s, const int64_t* rows, 
 // operator, first replacement; x64 already holds the initial guess with the
 // Dirichlet values, dinv the FP64 Jacobi inverse.  Leaves the replacement
 // graph launched; the task loop reads the header next.
+// The 14 upper offsets of a 27-point lattice numbered line by line, with
+// nx = off[3] nodes per line and nxy = off[9] per plane: 0, 1, then
+// B - 1, B, B + 1 for the line bases B = nx, nxy - nx, nxy, nxy + nx
+static bool lattice27_offsets(const std::vector<int32_t>& off)
+{
+    if (off.size() != 14) return false;
+    const int64_t nx = off[3], nxy = off[9];
+    if (nx < 3 || nxy - nx - 1 <= nx + 1) return false;
+    const int64_t base[4] = {nx, nxy - nx, nxy, nxy + nx};
+    if (off[0] != 0 || off[1] != 1) return false;
+    for (int l = 0; l < 4; l++)
+        for (int dx = -1; dx <= 1; dx++)
+            if (off[2 + 3 * l + dx + 1] != base[l] + dx) return false;
+    return true;
+}
+
 static ogs_status begin_fp32_refined(ogs_system* s, KState* h)
 {
     ogs_mesh* m = s->m;
@@ -1157,20 +1177,27 @@ static ogs_status begin_fp32_refined(ogs_system* s, KState* h)
     {
         s->fmt = want;
         auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
-        const size_t v4 = al((size_t)n * sizeof(float));
-        const size_t op = s->fmt == 0 ? (size_t)m->n_up * ((n + 31) & ~31) * sizeof(float)
+        // diagonal-offset form: zero pads of pad values in front of every
+        // operator row and FP32 vector and of pad + 64 behind, so the
+        // lattice product's windows (at most the largest offset + 4 values
+        // outside [0, n)) read zeros
+        const int pad = s->fmt == 0 ? (m->host_up_off.back() + 16 + 31) & ~31 : 0;
+        s->f32_pad = pad;
+        s->f32_ustride = s->fmt == 0 ? (pad + n + 64 + 31) & ~31 : (n + 31) & ~31;
+        const size_t v4 = al(((size_t)n + 2 * (size_t)pad + 64) * sizeof(float));
+        const size_t op = s->fmt == 0 ? (size_t)m->n_up * s->f32_ustride * sizeof(float)
                         : s->fmt == 1 ? (size_t)m->sell_nnz * sizeof(float)
                                       : al(cells * sizeof(float)) + 256 + v4 + al((size_t)n);
         s->f32_bytes = 7 * v4 + op;
         OGS_CUDA_TRY(cudaMalloc(&s->f32_block, s->f32_bytes));
         OGS_CUDA_TRY(cudaMemsetAsync(s->f32_block, 0, s->f32_bytes, s->stream));
         char* p = (char*)s->f32_block;
-        s->p32 = (float*)p; s->r32 = (float*)(p + v4); s->x32 = (float*)(p + 2 * v4);
-        s->s32 = (float*)(p + 3 * v4); s->d32 = (float*)(p + 4 * v4);
-        s->u32 = (float*)(p + 5 * v4); s->w32 = (float*)(p + 6 * v4);
+        auto vec = [&](int k) { return (float*)(p + k * v4) + pad; };
+        s->p32 = vec(0); s->r32 = vec(1); s->x32 = vec(2); s->s32 = vec(3); s->d32 = vec(4);
+        s->u32 = vec(5); s->w32 = vec(6);
         char* opb = p + 7 * v4;
         s->U = nullptr; s->val32 = nullptr;
-        if (s->fmt == 0) s->U = (float*)opb;
+        if (s->fmt == 0) s->U = (float*)opb + pad;
         else if (s->fmt == 1) s->val32 = (float*)opb;
         else
         {
@@ -1183,13 +1210,26 @@ static ogs_status begin_fp32_refined(ogs_system* s, KState* h)
     MixedArgs a;
     std::memset(&a, 0, sizeof a);
     a.A.slice_ptr = m->slice_ptr; a.A.col = m->sell_col; a.A.val = s->val; a.A.n = n;
-    a.fmt = s->fmt; a.U = s->U; a.ustride = (n + 31) & ~31; a.up_off = m->up_off; a.n_up = m->n_up;
+    a.fmt = s->fmt; a.U = s->U; a.ustride = s->f32_ustride; a.pad = s->f32_pad; a.up_off = m->up_off;
+    a.n_up = m->n_up;
     a.val32 = s->val32;
     for (int d = 0; d < 16 && d < (int)m->host_up_off.size(); d++) a.off[d] = m->host_up_off[d];
     a.d32 = s->d32; a.x = s->x; a.b = s->b; a.r64 = s->r;
     // stored FP32 operators iterate on the Jacobi-scaled system; the cell
     // operator and the persistent kernel use the preconditioned form
     a.scaled = s->fmt != 2 && c.schedule == OGS_SCHEDULE_GRAPH;
+    // the four-rows-per-thread product when the offsets are a line-by-line
+    // 27-point lattice's (OGS_FP32_PRODUCT=rows keeps the row kernel, for
+    // comparisons)
+    {
+        const char* e = std::getenv("OGS_FP32_PRODUCT");
+        a.lines = s->fmt == 0 && a.scaled && lattice27_offsets(m->host_up_off) && !(e && !std::strcmp(e, "rows"));
+        if (a.lines != s->mp_lines)
+        {
+            drop_graphs(s);  // the captured iterations hold the product kernel
+            s->mp_lines = a.lines;
+        }
+    }
     a.x32 = s->x32; a.r32 = s->r32; a.p32 = s->p32; a.s32 = s->s32; a.u32 = s->u32; a.w32 = s->w32;
     a.st = s->st; a.n = n;
     if (s->fmt == 2)
@@ -1247,7 +1287,7 @@ static ogs_status begin_fp32_refined(ogs_system* s, KState* h)
     h->scale = 1.0;
     h->ratio = 1.0;
     h->first = 1;
-    h->nb_spmv = s->fmt == 2 ? cell_spmv_grid(m->gx, m->gy, m->gz) : mp_spmv_grid(n);
+    h->nb_spmv = s->fmt == 2 ? cell_spmv_grid(m->gx, m->gy, m->gz) : mp_spmv_grid(a);
     a.nb_spmv = h->nb_spmv;
     h->nb_upd = red_grid(n);
     h->delta = c.inner_tol > 0.0 ? c.inner_tol : 1e-2;
@@ -1973,5 +2013,39 @@ extern "C" ogs_status ogs_gpu_debug_oob(int64_t* site, int64_t* index)
     *site = -1;  // not a bounds-checked build
     *index = 0;
 #endif
+    return OGS_OK;
+}
+
+extern "C" ogs_status ogs_gpu_debug_fp32_product(ogs_system* s, const float* x, float* y_rows, float* y_lines)
+{
+    if (!s || !x || !y_rows || !y_lines) { set_error("debug_fp32_product: NULL argument"); return OGS_BAD_ARG; }
+    if (s->fmt != 0 || !s->U || !lattice27_offsets(s->m->host_up_off))
+    {
+        set_error("debug_fp32_product: no FP32 operator of a 27-point lattice (solve with "
+                  "OGS_PRECISION_FP32_REFINED on a hex lattice first)");
+        return OGS_BAD_ARG;
+    }
+    MixedArgs a = s->mp_args;
+    a.lines = 1;
+    const size_t bytes = (size_t)s->n * sizeof(float);
+    float* d = nullptr;
+    OGS_CUDA_TRY(cudaMalloc(&d, 2 * bytes));
+    // r32 is the product's padded input; the next solve rebuilds it
+    cudaError_t e = cudaMemcpyAsync(s->r32, x, bytes, cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess)
+    {
+        launch_mp_product_pair(a, d, d + s->n, s->stream);
+        count_launches(1);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(y_rows, d, bytes, cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(y_lines, d + s->n, bytes, cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    cudaFree(d);
+    if (e != cudaSuccess)
+    {
+        set_error("debug_fp32_product: %s", cudaGetErrorString(e));
+        return OGS_CUDA_ERROR;
+    }
     return OGS_OK;
 }

@@ -33,6 +33,7 @@ enum OobSite
     kOobDirCol = 7,      // Dirichlet elimination: column / row
     kOobDirSlot = 8,     // Dirichlet elimination: slot
     kOobIluCol = 9,      // ILU(0) sweeps and factorisation: column
+    kOobMixedWindow = 10,  // FP32 lattice product: a 16-byte window outside its padded row / vector
 };
 #ifdef OGS_BOUNDS_CHECK
 static __device__ unsigned long long g_oob = ~0ull;

@@ -274,7 +274,10 @@ struct MixedArgs
     SellView<double> A;       // FP64 matrix
     int fmt;                  // 0: diagonal-offset upper half, 1: SELL-32 FP32
     const float* U;           // [n_up][ustride]
-    int ustride;              // n rounded up to 32 values: every U row starts on a 128-byte line
+    int ustride;              // values per U row (a multiple of 32: every row starts on a 128-byte line);
+                              // U[d] = U + d * ustride, zero pads before [0, n) and after it
+    int lines;                // 1: the 27-point lattice product of four rows per thread (k_mp_spmv_lines)
+    int pad;                  // zero values in front of each U row and FP32 vector (n + pad + 64 behind)
     const int32_t* up_off;    // [n_up]
     int n_up;
     int off[16];              // up_off by value (diagonal-offset kernels)

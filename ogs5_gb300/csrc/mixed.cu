@@ -541,6 +541,175 @@ __global__ void __launch_bounds__(kThreads, 3) k_mp_spmv(MixedArgs a)
     mp_sum_products(v, st);
 }
 
+// ------------------------------------------------------------------
+// The Jacobi-scaled 27-point lattice product, four rows per thread
+// ------------------------------------------------------------------
+// When the 13 upper offsets are those of a lattice numbered line by line
+// (1 ; nx - 1, nx, nx + 1 ; nxy - nx - 1 .. nxy - nx + 1 ; nxy - 1 ..
+// nxy + 1 ; nxy + nx - 1 .. nxy + nx + 1, nx nodes per line and nxy per
+// plane), the 27 columns of a row form nine lines of three consecutive
+// nodes, and rows 4g .. 4g + 3 need six consecutive x of each line.  A
+// thread then reads every operand as aligned 16-byte words: its own
+// operator values U[d][4g .. 4g + 3] (13 words), each line's six x (two or
+// three words) and each mirrored window U[d][4g - off_d ..] (one or two
+// words) -- 57 wide loads for four rows instead of 53 four-byte loads with
+// bounds predicates per row.  The word alignment of every window depends
+// only on nx mod 4 and nxy mod 4 (template arguments RX, RXY).  There are
+// no bounds predicates: the operator rows and the FP32 vectors carry zero
+// pads of at least nxy + nx + 16 values on both sides, so a window that
+// leaves [0, n) reads zeros where the predicated form adds 0 * 0.  The
+// terms are added in the order of dia_row<14, true, true> (unit diagonal,
+// then per offset the upper and the mirrored lower entry), so the product
+// is bit for bit that of k_mp_spmv<14, true>.
+__host__ __device__ constexpr int mod4(int v) { return ((v % 4) + 4) % 4; }
+
+// Aligned 16-byte words q[0 .. W - 1] of p from index f = 0 (mod 4).  The
+// debug build checks that they lie in [-pad, hi) of their padded row or
+// vector (and reads zeros otherwise).
+template <int W>
+__device__ __forceinline__ void words(const float* p, int f, int pad, int hi, float (&w)[4 * W])
+{
+    if (!OGS_IN(f + pad, hi + pad - 4 * W + 1, kOobMixedWindow))
+    {
+#pragma unroll
+        for (int k = 0; k < 4 * W; k++) w[k] = 0.f;
+        return;
+    }
+    const float4* q = reinterpret_cast<const float4*>(p + f);
+#pragma unroll
+    for (int k = 0; k < W; k++)
+    {
+        const float4 v = __ldg(q + k);
+        w[4 * k] = v.x; w[4 * k + 1] = v.y; w[4 * k + 2] = v.z; w[4 * k + 3] = v.w;
+    }
+}
+
+// p[start .. start + 3], start = T (mod 4), from aligned 16-byte words
+template <int T>
+__device__ __forceinline__ void window4(const float* p, int start, int pad, int hi, float (&o)[4])
+{
+    constexpr int W = T == 0 ? 1 : 2;
+    float w[4 * W];
+    words<W>(p, start - T, pad, hi, w);
+#pragma unroll
+    for (int k = 0; k < 4; k++) o[k] = w[T + k];
+}
+
+// p[start .. start + 5], start = S (mod 4)
+template <int S>
+__device__ __forceinline__ void window6(const float* p, int start, int pad, int hi, float (&o)[6])
+{
+    constexpr int W = S > 2 ? 3 : 2;
+    float w[4 * W];
+    words<W>(p, start - S, pad, hi, w);
+#pragma unroll
+    for (int k = 0; k < 6; k++) o[k] = w[S + k];
+}
+
+// offset off_d = B + DX of a line with base B: the upper entries
+// U_d[i + m] x[i + m + B + DX] (xu = x[i + B - 1 ..]) and the mirrored lower
+// entries U_d[i + m - off_d] x[i + m - off_d] (xl = x[i - B - 1 ..]); the
+// lower window starts at i - off_d = T (mod 4)
+template <int T, int DX>
+__device__ __forceinline__ void lines_entry(const MixedArgs& a, const float* Ud, int i, int lo_start,
+                                            const float (&xu)[6], const float (&xl)[6], float (&acc)[4])
+{
+    const int uhi = a.ustride - a.pad;  // a U row holds indices [-pad, ustride - pad)
+    float uo[4], ul[4];
+    words<1>(Ud, i, a.pad, uhi, uo);
+    window4<T>(Ud, lo_start, a.pad, uhi, ul);
+#pragma unroll
+    for (int m = 0; m < 4; m++)
+    {
+        acc[m] = fmaf(uo[m], xu[m + 1 + DX], acc[m]);
+        acc[m] = fmaf(ul[m], xl[m + 1 - DX], acc[m]);
+    }
+}
+
+// the line (DY, DZ) with base B = DY nx + DZ nxy, stored offsets D0 .. D0 + 2
+// (B - 1 .. B + 1), and its mirror (-DY, -DZ)
+template <int RX, int RXY, int DY, int DZ, int D0>
+__device__ __forceinline__ void lines_pair(const MixedArgs& a, const float* x, int i, int nx, int nxy,
+                                           float (&acc)[4])
+{
+    constexpr int SB = mod4(DY * RX + DZ * RXY);
+    const int B = DY * nx + DZ * nxy, xhi = a.n + a.pad + 64;
+    float xu[6], xl[6];
+    window6<mod4(SB - 1)>(x, i + B - 1, a.pad, xhi, xu);
+    window6<mod4(-SB - 1)>(x, i - B - 1, a.pad, xhi, xl);
+    const float* U0 = a.U + (size_t)D0 * a.ustride;
+    lines_entry<mod4(1 - SB), -1>(a, U0, i, i - B + 1, xu, xl, acc);
+    lines_entry<mod4(-SB), 0>(a, U0 + a.ustride, i, i - B, xu, xl, acc);
+    lines_entry<mod4(-1 - SB), 1>(a, U0 + 2 * (size_t)a.ustride, i, i - B - 1, xu, xl, acc);
+}
+
+// rows i .. i + 3 (i = 0 mod 4) of S A S x; x0 receives x[i - 1 .. i + 4]
+template <int RX, int RXY>
+__device__ __forceinline__ void lines_group(const MixedArgs& a, const float* x, int i, float (&acc)[4],
+                                            float (&x0)[6])
+{
+    const int nx = a.off[3], nxy = a.off[9];
+    window6<3>(x, i - 1, a.pad, a.n + a.pad + 64, x0);
+#pragma unroll
+    for (int m = 0; m < 4; m++) acc[m] = 0.f + x0[m + 1];
+    lines_entry<3, 1>(a, a.U + a.ustride, i, i - 1, x0, x0, acc);  // offset 1
+    lines_pair<RX, RXY, 1, 0, 2>(a, x, i, nx, nxy, acc);
+    lines_pair<RX, RXY, -1, 1, 5>(a, x, i, nx, nxy, acc);
+    lines_pair<RX, RXY, 0, 1, 8>(a, x, i, nx, nxy, acc);
+    lines_pair<RX, RXY, 1, 1, 11>(a, x, i, nx, nxy, acc);
+}
+
+// S: iter += 1 ; w32 = S A S r32 ; partials of r.r, w.r, r.r
+template <int RX, int RXY>
+__global__ void __launch_bounds__(kThreads, 2) k_mp_spmv_lines(MixedArgs a)
+{
+    KState* st = a.st;
+    if (st->done || st->replace) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) st->iter += 1;  // no block of this kernel reads iter
+    const float* x = a.r32;
+    const int ng = (a.n + 3) >> 2;
+    float v[3] = {0.f, 0.f, 0.f};
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x)
+    {
+        float acc[4], x0[6];
+        lines_group<RX, RXY>(a, x, 4 * g, acc, x0);
+        // rows n .. 4 ng - 1 come out 0 (zero operator rows, zero r pad)
+        reinterpret_cast<float4*>(a.w32)[g] = make_float4(acc[0], acc[1], acc[2], acc[3]);
+#pragma unroll
+        for (int m = 0; m < 4; m++)
+        {
+            const float r = x0[m + 1], w = acc[m];
+            v[0] += r * r;
+            v[1] += w * r;
+            v[2] += r * r;
+        }
+    }
+    mp_sum_products(v, st);
+}
+
+// Both forms of the product on a.r32 (instrumentation): y_rows by the row
+// kernel's dia_row, y_lines by lines_group, n values each
+template <int RX, int RXY>
+__global__ void k_mp_product_pair(MixedArgs a, float* y_rows, float* y_lines)
+{
+    const int ng = (a.n + 3) >> 2;
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x)
+    {
+        float acc[4], x0[6];
+        lines_group<RX, RXY>(a, a.r32, 4 * g, acc, x0);
+#pragma unroll
+        for (int m = 0; m < 4; m++)
+        {
+            const int i = 4 * g + m;
+            if (i < a.n)
+            {
+                y_lines[i] = acc[m];
+                y_rows[i] = dia_row<14, true, true>(a, a.r32, i);
+            }
+        }
+    }
+}
+
 // fmt 2 product on the lattice: blocks of 4 warps, a warp holds 32
 // consecutive x-columns of one y-line and marches up kCellZ planes in z.
 // x at ix +- 1 comes from the neighbouring lanes (loads at the warp edges
@@ -1157,13 +1326,63 @@ void launch_mp_check(const MixedArgs& a, unsigned* out, cudaStream_t s)
 
 // grids of the FP32 CG kernels (the update/p kernels add this many SpMV
 // partials, the p kernel this many update partials)
-int mp_spmv_grid(int n)
+using LinesKernel = void (*)(MixedArgs);
+using PairKernel = void (*)(MixedArgs, float*, float*);
+
+template <int RX>
+static LinesKernel lines_kernel_rx(int rxy, PairKernel* pair)
+{
+    switch (rxy)
+    {
+        case 0: *pair = k_mp_product_pair<RX, 0>; return k_mp_spmv_lines<RX, 0>;
+        case 1: *pair = k_mp_product_pair<RX, 1>; return k_mp_spmv_lines<RX, 1>;
+        case 2: *pair = k_mp_product_pair<RX, 2>; return k_mp_spmv_lines<RX, 2>;
+        default: *pair = k_mp_product_pair<RX, 3>; return k_mp_spmv_lines<RX, 3>;
+    }
+}
+
+// the instantiations for nx mod 4 and nxy mod 4 (pair: the comparison
+// kernel, may be NULL)
+static LinesKernel lines_kernel(const MixedArgs& a, PairKernel* pair = nullptr)
+{
+    PairKernel p = nullptr;
+    LinesKernel k;
+    const int rxy = a.off[9] & 3;
+    switch (a.off[3] & 3)
+    {
+        case 0: k = lines_kernel_rx<0>(rxy, &p); break;
+        case 1: k = lines_kernel_rx<1>(rxy, &p); break;
+        case 2: k = lines_kernel_rx<2>(rxy, &p); break;
+        default: k = lines_kernel_rx<3>(rxy, &p); break;
+    }
+    if (pair) *pair = p;
+    return k;
+}
+
+// both products of the lattice operator on a.r32 (a.lines set)
+void launch_mp_product_pair(const MixedArgs& a, float* y_rows, float* y_lines, cudaStream_t s)
+{
+    PairKernel pair = nullptr;
+    lines_kernel(a, &pair);
+    pair<<<vec_grid((a.n + 3) / 4), kThreads, 0, s>>>(a, y_rows, y_lines);
+}
+
+int mp_spmv_grid(const MixedArgs& a)
 {
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (a.lines)
+    {
+        // as many blocks as are resident at once, each thread a group of
+        // four rows per pass
+        int occ = 2;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, lines_kernel(a), kThreads, 0);
+        const int need = ((a.n + 3) / 4 + kThreads - 1) / kThreads;
+        return std::max(1, std::min(need, std::min(sms * std::max(1, occ), kMaxBlocks)));
+    }
     // three blocks of the register-heavy diagonal kernel are resident per SM
-    return std::max(1, std::min((n + kThreads - 1) / kThreads, std::min(sms * 3, kMaxBlocks)));
+    return std::max(1, std::min((a.n + kThreads - 1) / kThreads, std::min(sms * 3, kMaxBlocks)));
 }
 
 // FP64 residual replacement: accumulate, residual, restart
@@ -1251,12 +1470,13 @@ cudaError_t launch_mp_barrier_selftest(KState* st, int grid, int withhold, unsig
 
 void launch_mp_iteration(const MixedArgs& a, cudaStream_t s, cudaEvent_t eb, cudaEvent_t ee)
 {
-    const int gs = mp_spmv_grid(a.n);
+    const int gs = mp_spmv_grid(a);
     if (eb) cudaEventRecordWithFlags(eb, s, cudaEventRecordExternal);
     switch (a.fmt == 0 ? a.n_up : a.fmt == 2 ? -1 : 0)
     {
         case 14:  // hex, 27-point
-            if (a.scaled) k_mp_spmv<14, true><<<gs, kThreads, 0, s>>>(a);
+            if (a.lines) lines_kernel(a)<<<gs, kThreads, 0, s>>>(a);
+            else if (a.scaled) k_mp_spmv<14, true><<<gs, kThreads, 0, s>>>(a);
             else k_mp_spmv<14><<<gs, kThreads, 0, s>>>(a);
             break;
         case 8:  // Kuhn tets, 15-point

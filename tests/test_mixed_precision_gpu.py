@@ -83,6 +83,59 @@ def test_fp32_refined_rejects_bicgstab(gpu):
     assert ei.value.status == gpu.BAD_ARG
 
 
+# hex cells (x, y, z): node counts nx = x + 1 and nxy = nx (y + 1) cover
+# every nx mod 4 and every nxy mod 4 the product's window alignments depend on
+LATTICES = [(3, 4, 3), (4, 4, 3), (5, 3, 3), (6, 4, 3), (5, 4, 4), (6, 5, 2), (4, 5, 3), (3, 6, 2), (4, 2, 5),
+            (24, 20, 12)]
+
+
+@pytest.mark.parametrize("cells", LATTICES)
+def test_lattice_product_bitwise(gpu, cells):
+    """The four-rows-per-thread product of the 27-point lattice operator
+    (aligned 16-byte windows, zero pads instead of bounds predicates) gives
+    bit for bit the row kernel's values, boundary rows included."""
+    m = M.structured_hex(*cells)
+    nx, nxy = cells[0] + 1, (cells[0] + 1) * (cells[1] + 1)
+    ek = fields.lognormal_k(m.shape, np.log(1e-5), 1.0, 4.0, seed=3)
+    eqs, x0 = _deck(gpu, m, ek)
+    _both(gpu, eqs, x0)
+    rng = np.random.default_rng(nx * 7 + nxy)
+    for x in (rng.standard_normal(m.n_nodes), np.ones(m.n_nodes), -np.arange(m.n_nodes, dtype=float)):
+        y_rows, y_lines = eqs.debug_fp32_product(x)
+        assert np.abs(y_rows).max() > 0
+        # equal values; for non-zero floats that is equal bits
+        assert np.array_equal(y_rows, y_lines)
+
+
+def test_lattice_product_needs_lattice_operator(gpu):
+    m, _ = renumber(M.structured_hex(8, 6, 4), 5)  # SELL-32 FP32 operator
+    eqs, x0 = _deck(gpu, m, np.ones(m.n_elements))
+    _both(gpu, eqs, x0)
+    with pytest.raises(gpu.OgsError) as ei:
+        eqs.debug_fp32_product(np.ones(m.n_nodes))
+    assert ei.value.status == gpu.BAD_ARG
+
+
+def test_lattice_product_solve_matches_row_kernel(gpu, monkeypatch):
+    """The solve with the four-rows-per-thread product and with the row
+    kernel (OGS_FP32_PRODUCT=rows): the same products, partial sums grouped
+    differently, so heads within the solve tolerance of each other and
+    iteration counts within a few."""
+    m = M.structured_hex(30, 22, 14)
+    ek = fields.lognormal_k(m.shape, np.log(1e-5), 1.0, 4.0, seed=5)
+    eqs, x0 = _deck(gpu, m, ek)
+    x64, it64, xl, itl, st = _both(gpu, eqs, x0)
+    assert st["status"] == gpu.OK
+    monkeypatch.setenv("OGS_FP32_PRODUCT", "rows")
+    eqs.ConfigNumerics(gpu.LS_CG, gpu.PRECOND_JACOBI, 20000, 1e-10, precision=gpu.PRECISION_FP32_REFINED,
+                       check_norm_rhs=False)
+    xr = x0.copy()
+    itr = eqs.Solver(xr)
+    assert eqs.stats()["status"] == gpu.OK
+    assert rel_max_err(xl, xr) < MIXED_RTOL and rel_max_err(xl, x64) < MIXED_RTOL
+    assert abs(itl - itr) <= max(5, itr // 50)
+
+
 @pytest.mark.parametrize("mixed,schedule", [(False, 0), (True, 0), (True, 1)])
 def test_profile_counts_spmv_launches(gpu, mixed, schedule):
     """ogs_gpu_profile times one SpMV in four iterations of the graph
