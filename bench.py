@@ -943,8 +943,9 @@ def main():
         "gpu_launches": int(mix["launches"]),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                      "frac": round(achieved / hbm, 4),
-                     "traffic": measured_traffic("k_mp_spmv_fp32_diagonal_hex128x128x64.md"),
-                     "kernel": "k_mp_spmv (FP32 Jacobi-scaled upper-diagonal-offset SpMV, unit diagonal, + fused dots)",
+                     "traffic": measured_traffic("k_mp_spmv_lines_hex128x128x64.md"),
+                     "kernel": "k_mp_spmv_lines (FP32 Jacobi-scaled upper-diagonal-offset SpMV of the 27-point "
+                               "lattice, four rows per thread from 16-byte windows, unit diagonal, + fused dots)",
                      "bytes_per_launch": spmv_bytes, "launch_ms": round(t_spmv, 5),
                      "launches": pr["spmv_launches"], "peak_kind": peak_kind},
         "clocks": clk.summary(),

@@ -660,8 +660,11 @@ __device__ __forceinline__ void lines_group(const MixedArgs& a, const float* x, 
 }
 
 // S: iter += 1 ; w32 = S A S r32 ; partials of r.r, w.r, r.r
+// One block per SM (up to 255 registers: the loads of several line pairs
+// in flight at once); the grid is one block per SM, so the product's
+// partial sums are one per SM for the update kernel to add.
 template <int RX, int RXY>
-__global__ void __launch_bounds__(kThreads, 2) k_mp_spmv_lines(MixedArgs a)
+__global__ void __launch_bounds__(kThreads, 1) k_mp_spmv_lines(MixedArgs a)
 {
     KState* st = a.st;
     if (st->done || st->replace) return;
