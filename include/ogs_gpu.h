@@ -407,6 +407,13 @@ ogs_status ogs_gpu_spmv(ogs_system* sys, const double* x, double* y);
  * $ELE_GAUSS_POINTS 3 for quad/hex, 5 for tets). */
 int32_t ogs_gpu_mesh_gauss_points(const ogs_mesh* mesh);
 
+/* Tiles of 8^3 nodes the ILU(0) sweeps walk on this mesh: non-zero when the
+ * pattern is a lattice numbered line by line whose columns left of the
+ * diagonal lie at no larger x, y, z than their row (Kuhn tets, 7-point
+ * stencils); 0 when the sweeps walk dependency levels of rows.
+ * (Instrumentation, no counterpart in the reference.) */
+int32_t ogs_gpu_mesh_ilu_tiles(const ogs_mesh* mesh);
+
 /* Number of this library's kernels launched on the calling thread since the
  * last reset (instrumentation for benchmarks). */
 int64_t ogs_gpu_kernel_launches(int32_t reset);

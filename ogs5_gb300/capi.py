@@ -43,7 +43,8 @@ EXPORTS = [
     "ogs_gpu_mesh_info", "ogs_gpu_system_create", "ogs_gpu_system_destroy", "ogs_gpu_configure",
     "ogs_gpu_initialize", "ogs_gpu_assemble", "ogs_gpu_set_dirichlet", "ogs_gpu_solve",
     "ogs_gpu_gp_velocity", "ogs_gpu_get_csr", "ogs_gpu_get_rhs", "ogs_gpu_get_x",
-    "ogs_gpu_spmv", "ogs_gpu_mesh_gauss_points", "ogs_gpu_kernel_launches", "ogs_gpu_profile",
+    "ogs_gpu_spmv", "ogs_gpu_mesh_gauss_points", "ogs_gpu_mesh_ilu_tiles", "ogs_gpu_kernel_launches",
+    "ogs_gpu_profile",
     "ogs_gpu_csr_cg_noalloc", "ogs_gpu_get_ilu0",
     "ogs_gpu_batch_create", "ogs_gpu_batch_destroy", "ogs_gpu_batch_set_k", "ogs_gpu_batch_autotune",
     "ogs_gpu_batch_set_tuning", "ogs_gpu_batch_solve", "ogs_gpu_batch_get_heads", "ogs_gpu_batch_info",
@@ -231,6 +232,8 @@ def lib():
         L.ogs_gpu_spmv.argtypes = [vp, vp, vp]
         L.ogs_gpu_mesh_gauss_points.argtypes = [vp]
         L.ogs_gpu_mesh_gauss_points.restype = C.c_int32
+        L.ogs_gpu_mesh_ilu_tiles.argtypes = [vp]
+        L.ogs_gpu_mesh_ilu_tiles.restype = C.c_int32
         L.ogs_gpu_profile.argtypes = [vp, C.c_int32, C.POINTER(Profile)]
         L.ogs_gpu_profile.restype = st
         L.ogs_gpu_csr_cg_noalloc.argtypes = [C.c_int64, vp, vp, vp, vp, vp, C.c_int32, C.c_double, vp,
@@ -371,6 +374,7 @@ class GpuMesh:
         _check(lib().ogs_gpu_mesh_info(h, C.byref(n), C.byref(nnz)))
         self.n_rows, self.nnz = n.value, nnz.value
         self.n_gauss = int(lib().ogs_gpu_mesh_gauss_points(h))
+        self.ilu_tiles = int(lib().ogs_gpu_mesh_ilu_tiles(h))
 
     def close(self):
         if getattr(self, "h", None):

@@ -242,6 +242,12 @@ struct ogs_system
     unsigned long long* ilu_ticket = nullptr;  // [3] block tickets of the ILU kernels
     int32_t *ilu_pl_row = nullptr, *ilu_pl_col = nullptr, *ilu_pu_row = nullptr, *ilu_pu_col = nullptr;
     double *ilu_pl_val = nullptr, *ilu_pu_val = nullptr, *ilu_pu_diag = nullptr;  // packed sweep rows
+    // the tile sweeps' rows (lattice patterns), flags and tickets
+    bool ilu_use_tiles = false;
+    int* ilu_tile_flags = nullptr;
+    unsigned long long* ilu_tile_ticket = nullptr;
+    double *ilu_tl_val = nullptr, *ilu_tu_val = nullptr, *ilu_tu_dg = nullptr;
+    unsigned char *ilu_tl_mask = nullptr, *ilu_tu_mask = nullptr;
     double *ek = nullptr, *u0 = nullptr, *gpv = nullptr, *qbuf = nullptr, *vec_in = nullptr,
            *vec_out = nullptr, *u1 = nullptr;
     // RICHARDS_FLOW Picard step: iterate, solution, old level, reductions
@@ -334,11 +340,11 @@ ogs_status stage_in(ogs_system* s, const double* src, size_t n, double** scratch
 SolveArgs make_solve_args(ogs_system* s)
 {
     SolveArgs a;
+    std::memset(&a, 0, sizeof a);  // every field not set below is 0 (no tiles, the default spin limit)
     a.A.slice_ptr = s->m->slice_ptr;
     a.A.col = s->m->sell_col;
     a.A.val = s->val;
     a.A.n = s->n;
-    std::memset(&a.v, 0, sizeof a.v);
     a.v.x = s->x; a.v.b = s->b; a.v.r = s->r; a.v.r0 = s->r0; a.v.p = s->p; a.v.ph = s->ph;
     a.v.s = s->s; a.v.sh = s->sh; a.v.t = s->t; a.v.v = s->v; a.v.dinv = s->dinv;
     a.st = s->st;
@@ -365,6 +371,17 @@ SolveArgs make_solve_args(ogs_system* s)
     a.ilu.pu_row = s->ilu_pu_row; a.ilu.pu_col = s->ilu_pu_col; a.ilu.pu_val = s->ilu_pu_val;
     a.ilu.pu_diag = s->ilu_pu_diag;
     a.ilu.bad = s->d_ilu_bad;
+    if (s->ilu_use_tiles && s->ilu_tile_flags)
+    {
+        a.ilu.tiles = m->tiles;
+        a.ilu.lnx = m->lnx; a.ilu.lny = m->lny; a.ilu.lnz = m->lnz;
+        a.ilu.tnx = m->tnx; a.ilu.tny = m->tny; a.ilu.tnz = m->tnz;
+        a.ilu.tile_order = m->tile_order;
+        a.ilu.tile_flags = s->ilu_tile_flags;
+        a.ilu.tile_ticket = s->ilu_tile_ticket;
+        a.ilu.tl_val = s->ilu_tl_val; a.ilu.tu_val = s->ilu_tu_val; a.ilu.tu_dg = s->ilu_tu_dg;
+        a.ilu.tl_mask = s->ilu_tl_mask; a.ilu.tu_mask = s->ilu_tu_mask;
+    }
     return a;
 }
 
@@ -470,6 +487,13 @@ extern "C" ogs_status ogs_gpu_system_destroy(ogs_system* s)
     cudaFree(s->ilu_pu_col);
     cudaFree(s->ilu_pu_val);
     cudaFree(s->ilu_pu_diag);
+    cudaFree(s->ilu_tile_flags);
+    cudaFree(s->ilu_tile_ticket);
+    cudaFree(s->ilu_tl_val);
+    cudaFree(s->ilu_tu_val);
+    cudaFree(s->ilu_tu_dg);
+    cudaFree(s->ilu_tl_mask);
+    cudaFree(s->ilu_tu_mask);
     cudaFree(s->st);
     cudaFree(s->d_bad);
     cudaFree(s->bc_rows);
@@ -1354,6 +1378,30 @@ static ogs_status ilu_factor(ogs_system* s)
             OGS_CUDA_TRY(cudaMalloc(&s->ilu_pu_diag, nu * sizeof(double)));
         }
         drop_graphs(s);  // captured sweeps hold the factor pointer
+    }
+    // the tile sweeps on lattice patterns (OGS_ILU_SWEEP=levels: the level
+    // kernels, for comparisons; read at every factorisation)
+    {
+        const char* e = std::getenv("OGS_ILU_SWEEP");
+        const bool tiles = m->tiles && !(e && !std::strcmp(e, "levels"));
+        if (tiles != s->ilu_use_tiles)
+        {
+            drop_graphs(s);  // the captured iterations hold the sweep kernels
+            s->ilu_use_tiles = tiles;
+        }
+        if (tiles && !s->ilu_tile_flags)
+        {
+            const size_t rows = (size_t)m->tiles * kIluTile * kIluTile * kIluTile;
+            OGS_CUDA_TRY(cudaMalloc(&s->ilu_tile_flags, 2 * (size_t)m->tiles * sizeof(int)));
+            OGS_CUDA_TRY(cudaMalloc(&s->ilu_tile_ticket, 2 * sizeof(unsigned long long)));
+            OGS_CUDA_TRY(cudaMemsetAsync(s->ilu_tile_flags, 0, 2 * (size_t)m->tiles * sizeof(int), s->stream));
+            OGS_CUDA_TRY(cudaMemsetAsync(s->ilu_tile_ticket, 0, 2 * sizeof(unsigned long long), s->stream));
+            OGS_CUDA_TRY(cudaMalloc(&s->ilu_tl_val, 7 * rows * sizeof(double)));
+            OGS_CUDA_TRY(cudaMalloc(&s->ilu_tu_val, 7 * rows * sizeof(double)));
+            OGS_CUDA_TRY(cudaMalloc(&s->ilu_tu_dg, rows * sizeof(double)));
+            OGS_CUDA_TRY(cudaMalloc(&s->ilu_tl_mask, rows));
+            OGS_CUDA_TRY(cudaMalloc(&s->ilu_tu_mask, rows));
+        }
     }
     const int big = 0x7fffffff;
     OGS_CUDA_TRY(cudaMemcpyAsync(s->d_ilu_bad, &big, sizeof(int), cudaMemcpyHostToDevice, s->stream));

@@ -87,6 +87,7 @@ static inline unsigned long long oob_take() { return ~0ull; }
     } while (0)
 
 constexpr int kThreads = 256;
+constexpr int kIluTile = 8;  // ILU(0) tile edge (nodes per axis)
 constexpr int kMaxBlocks = 4096;  // reduction partial slots per kernel
 
 inline int nodes_per_element(int et) { return et == OGS_ELEM_HEX8 ? 8 : 4; }
@@ -209,6 +210,16 @@ struct ogs_mesh
     int n_lvl = 0, n_ulvl = 0;
     int n_lpos = 0, n_upos = 0;
     int ilu_kl = 0, ilu_ku = 0;    // most entries left / right of the diagonal in a row
+    // ILU(0) tiles: a lattice pattern numbered line by line whose columns
+    // left of the diagonal lie at no larger x, y, z than their row (and
+    // those right of it at no smaller), every entry at most one step away
+    // on each axis (Kuhn tets, 7-point stencils): lnx x lny x lnz nodes,
+    // tiles of kIluTile^3 nodes, tnx x tny x tnz of them, listed in
+    // tile_order by the sum of their tile coordinates.  tiles == 0: the
+    // pattern is not of that form.
+    int tiles = 0;
+    int lnx = 0, lny = 0, lnz = 0, tnx = 0, tny = 0, tnz = 0;
+    int32_t* tile_order = nullptr;  // [tiles]
     // diagonal-offset form of the pattern (structured grids): the distinct
     // column offsets (col - row), sorted, and per SELL slot the index of
     // its offset (-1 for padding); n_off == 0 when there are too many

@@ -416,6 +416,210 @@ __global__ void __launch_bounds__(NT, 1) k_ilu_sweep(IluView f, const double* __
 }
 
 // ------------------------------------------------------------------
+// Tiled sweeps of lattice patterns (ogs_mesh::tiles).  Row (x, y, z) of the
+// forward sweep reads only rows of [x-1, x] x [y-1, y] x [z-1, z], so the
+// lattice is cut into tiles of 8^3 rows: a tile reads only itself and the
+// up to 7 tiles before it on each axis, and the tiles go in the order of
+// the sum of their tile coordinates.  A block of 64 threads takes a tile
+// (tickets, as the level kernels take rows), loads the entries of its 512
+// rows into shared memory before it waits, waits for the neighbouring
+// tiles' flags, loads their results at its faces into a 9^3 cube in shared
+// memory, and walks its rows in 22 steps of lx + ly + lz with a block
+// barrier between steps: a thread owns the column (lx, ly) and does row lz
+// at step lx + ly + lz.  Every value a row reads is then in shared memory,
+// and a tile costs two dependent global round trips (its flags, its faces)
+// instead of one per level of rows.  The backward sweep is the mirror
+// image (tiles from the end of the list, steps reversed, faces at +1).
+// Each row's arithmetic is the level kernels' (ilu_solve_row): the start
+// value, one FMA per entry in column order, then times 1 / U_ii
+// (backward), so the results are bit for bit the same.
+//
+// Slots: forward slot s is the neighbour -(q & 1, q >> 1 & 1, q >> 2 & 1)
+// with q = 7 - s, backward slot u the neighbour (q & 1, q >> 1 & 1, q >> 2
+// & 1) with q = u + 1: both in ascending column order on a lattice with
+// nxy > nx + 1 > 2.
+constexpr int kTileT = kIluTile * kIluTile;       // threads of a tile block
+constexpr int kTileSteps = 3 * kIluTile - 2;       // steps of lx + ly + lz
+constexpr int kTileCube = (kIluTile + 1) * (kIluTile + 1) * (kIluTile + 1);
+
+__device__ __forceinline__ int tile_slot_offset(int mode, int slot)
+{
+    const int q = mode == 1 ? 7 - slot : slot + 1;
+    const int sg = mode == 1 ? -1 : 1;
+    return sg * ((q & 1) + (kIluTile + 1) * (((q >> 1) & 1) + (kIluTile + 1) * ((q >> 2) & 1)));
+}
+
+// the packed tile rows after a factorisation
+__global__ void k_ilu_pack_tiles(IluView f)
+{
+    const int64_t total = (int64_t)f.tiles * kIluTile * kTileT;
+    const int nxy = f.lnx * f.lny;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x)
+    {
+        const int t = (int)(idx % kTileT), lz = (int)((idx / kTileT) % kIluTile);
+        const int tile = (int)(idx / ((int64_t)kTileT * kIluTile));
+        const int a = tile % f.tnx, b = (tile / f.tnx) % f.tny, c = tile / (f.tnx * f.tny);
+        const int x = a * kIluTile + t % kIluTile, y = b * kIluTile + t / kIluTile, z = c * kIluTile + lz;
+        unsigned lm = 0, um = 0;
+        double lv[7], uv[7], dg = 1.0;
+#pragma unroll
+        for (int q = 0; q < 7; q++) lv[q] = uv[q] = 0.0;
+        if (x < f.lnx && y < f.lny && z < f.lnz)
+        {
+            const int i = x + f.lnx * (y + f.lny * z);
+            const int d = __ldg(f.diag + i);
+            if (d >= 0)
+            {
+                lm = um = 0x80;
+                const int rb = __ldg(f.row_ptr + i), re = __ldg(f.row_ptr + i + 1);
+                for (int k = rb; k < re; k++)
+                {
+                    if (k == d) continue;
+                    const int j = __ldg(f.col + k);
+                    const int dx = j % f.lnx - x, dy = (j / f.lnx) % f.lny - y, dz = j / nxy - z;
+                    if (k < d)
+                    {
+                        const int q = (-dx) | ((-dy) << 1) | ((-dz) << 2);  // 1 .. 7 on a checked pattern
+                        if (OGS_IN(q - 1, 7, kOobIluCol))
+                        {
+                            lv[7 - q] = f.lu[k];
+                            lm |= 1u << (7 - q);
+                        }
+                    }
+                    else
+                    {
+                        const int q = dx | (dy << 1) | (dz << 2);
+                        if (OGS_IN(q - 1, 7, kOobIluCol))
+                        {
+                            uv[q - 1] = f.lu[k];
+                            um |= 1u << (q - 1);
+                        }
+                    }
+                }
+                dg = 1.0 / f.lu[d];
+            }
+        }
+        const size_t row = ((size_t)tile * kIluTile + lz) * kTileT + t;
+        const size_t v0 = ((size_t)tile * kIluTile + lz) * 7 * kTileT + t;
+#pragma unroll
+        for (int q = 0; q < 7; q++)
+        {
+            f.tl_val[v0 + (size_t)q * kTileT] = lv[q];
+            f.tu_val[v0 + (size_t)q * kTileT] = uv[q];
+        }
+        f.tl_mask[row] = (unsigned char)lm;
+        f.tu_mask[row] = (unsigned char)um;
+        f.tu_dg[row] = dg;
+    }
+}
+
+// MODE 1: forward sweep, MODE 2: backward sweep, tile by tile
+template <int MODE>
+__global__ void __launch_bounds__(kTileT) k_ilu_tiles(IluView f, const double* __restrict__ in, double* out,
+                                                     const KState* st)
+{
+    if (st->done) return;
+    const int ntiles = f.tiles;
+    const unsigned long long per = (unsigned long long)ntiles + gridDim.x;
+    int* tflags = f.tile_flags + (MODE - 1) * ntiles;
+    const double* vals = MODE == 1 ? f.tl_val : f.tu_val;
+    const unsigned char* masks = MODE == 1 ? f.tl_mask : f.tu_mask;
+    __shared__ double s_x[kTileCube];                 // results: the tile and its faces
+    __shared__ double s_v[kIluTile][7][kTileT];       // entries of the block's rows
+    __shared__ double s_s0[kIluTile][kTileT];         // start values
+    __shared__ double s_dg[MODE == 2 ? kIluTile : 1][kTileT];
+    __shared__ unsigned char s_mk[kIluTile][kTileT];
+    __shared__ unsigned long long s_ticket;
+    const int t = threadIdx.x, lx = t % kIluTile, ly = t / kIluTile;
+    constexpr int E = kIluTile + 1;
+    for (;;)
+    {
+        __syncthreads();
+        if (t == 0) s_ticket = atomicAdd(f.tile_ticket + (MODE - 1), 1ull);
+        __syncthreads();
+        const unsigned long long tk = s_ticket;
+        const unsigned long long idx = tk % per;
+        if (idx >= (unsigned long long)ntiles) return;  // this block's closing ticket
+        const int launch = (int)(tk / per) + 1;
+        const int tile = __ldg(f.tile_order + (MODE == 1 ? (int)idx : ntiles - 1 - (int)idx));
+        const int a = tile % f.tnx, b = (tile / f.tnx) % f.tny, c = tile / (f.tnx * f.tny);
+        const int x = a * kIluTile + lx, y = b * kIluTile + ly;
+        // the rows' entries, masks and start values (final before this
+        // launch: the forward input, or the forward results for MODE 2)
+#pragma unroll
+        for (int lz = 0; lz < kIluTile; lz++)
+        {
+            const size_t row = ((size_t)tile * kIluTile + lz) * kTileT + t;
+            const size_t v0 = ((size_t)tile * kIluTile + lz) * 7 * kTileT + t;
+            const unsigned mk = OGS_IN(row, (int64_t)ntiles * kIluTile * kTileT, kOobIluCol) ? __ldg(masks + row) : 0u;
+            const int z = c * kIluTile + lz;
+            const int i = x + f.lnx * (y + f.lny * z);
+            s_mk[lz][t] = (unsigned char)mk;
+            s_s0[lz][t] = (mk & 0x80) && OGS_IN(i, f.n, kOobIluCol) ? (MODE == 1 ? in[i] : __ldcg(out + i)) : 0.0;
+            if constexpr (MODE == 2) s_dg[lz][t] = __ldg(f.tu_dg + row);
+#pragma unroll
+            for (int q = 0; q < 7; q++) s_v[lz][q][t] = __ldg(vals + v0 + (size_t)q * kTileT);
+        }
+        // the neighbouring tiles before this one in the sweep
+        if (t < 7)
+        {
+            const int q = t + 1, sg = MODE == 1 ? -1 : 1;
+            const int na = a + sg * (q & 1), nb = b + sg * ((q >> 1) & 1), nc = c + sg * ((q >> 2) & 1);
+            const int nt = na + f.tnx * (nb + f.tny * nc);
+            if (na >= 0 && na < f.tnx && nb >= 0 && nb < f.tny && nc >= 0 && nc < f.tnz &&
+                OGS_IN(nt, ntiles, kOobIluCol))
+                ilu_wait(tflags, nt, launch, f.bad, f.spin ? f.spin : kIluSpin);
+        }
+        fence_acquire();
+        __syncthreads();
+        fence_acquire();
+        // their results at this tile's faces (forward: cube index 0 on some
+        // axis, the lattice coordinate one below the tile; backward: index 8)
+        for (int h = t; h < kTileCube; h += kTileT)
+        {
+            const int cx = h % E, cy = (h / E) % E, cz = h / (E * E);
+            const int face = MODE == 1 ? 0 : kIluTile;
+            if (cx != face && cy != face && cz != face) continue;
+            const int o = MODE == 1 ? -1 : 0;
+            const int gx = a * kIluTile + cx + o, gy = b * kIluTile + cy + o, gz = c * kIluTile + cz + o;
+            const bool in_l = gx >= 0 && gx < f.lnx && gy >= 0 && gy < f.lny && gz >= 0 && gz < f.lnz;
+            const int gi = gx + f.lnx * (gy + f.lny * gz);
+            s_x[h] = in_l && OGS_IN(gi, f.n, kOobIluCol) ? __ldcg(out + gi) : 0.0;
+        }
+        __syncthreads();
+        // the tile's rows, step by step
+        const int co = MODE == 1 ? 1 : 0;  // cube index of local coordinate 0
+        for (int step = 0; step < kTileSteps; step++)
+        {
+            const int sl = MODE == 1 ? step : kTileSteps - 1 - step;
+            const int lz = sl - lx - ly;
+            if (lz >= 0 && lz < kIluTile)
+            {
+                const unsigned mk = s_mk[lz][t];
+                if (mk & 0x80)
+                {
+                    const int ci = (lx + co) + E * ((ly + co) + E * (lz + co));
+                    double s = s_s0[lz][t];
+#pragma unroll
+                    for (int q = 0; q < 7; q++)
+                        if (mk & (1u << q)) s = __fma_rn(-s_v[lz][q][t], s_x[ci + tile_slot_offset(MODE, q)], s);
+                    if (MODE == 2) s = s * s_dg[lz][t];
+                    s_x[ci] = s;
+                    const int i = x + f.lnx * (y + f.lny * (c * kIluTile + lz));
+                    if (OGS_IN(i, f.n, kOobIluCol)) __stcg(out + i, s);
+                }
+            }
+            __syncthreads();
+        }
+        // publish the tile
+        __threadfence();
+        __syncthreads();
+        if (t == 0) st_release_s32(tflags + tile, launch);
+    }
+}
+
+// ------------------------------------------------------------------
 // CG with ILU(0): the update kernel leaves r, z = M^-1 r comes from the
 // sweeps, this kernel writes the partials of r . r and r . z for k_cg_p
 // ------------------------------------------------------------------
@@ -475,6 +679,32 @@ void launch_ilu_factor(const IluView& f, const double* val, const int32_t* csr2s
     k_ilu_copy<<<g, 256, 0, s>>>(val, csr2sell, f.lu, nnz);
     k_ilu_flow<0><<<ilu_grid(f.n_lpos), kIluBlock, 0, s>>>(f, nullptr, nullptr, st);
     if (f.pl_row) k_ilu_pack<<<ilu_grid(std::max(f.n_lpos, f.n_upos)), kIluBlock, 0, s>>>(f);
+    if (f.tiles)
+    {
+        const int64_t rows = (int64_t)f.tiles * kIluTile * kTileT;
+        k_ilu_pack_tiles<<<(int)std::min<int64_t>((rows + 255) / 256, 8192), 256, 0, s>>>(f);
+    }
+}
+
+// the tile sweeps' persistent grid: as many blocks as are resident at once
+// (the same for every launch: tickets per launch depend on it)
+static int tile_grid()
+{
+    static int g = 0;
+    if (!g)
+    {
+        int dev = 0, sms = 152, o1 = 0, o2 = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o1, k_ilu_tiles<1>, kTileT, 0) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o2, k_ilu_tiles<2>, kTileT, 0) != cudaSuccess)
+        {
+            cudaGetLastError();
+            o1 = o2 = 1;
+        }
+        g = std::max(1, sms * std::max(1, std::min(o1, o2)));
+    }
+    return g;
 }
 
 // the cluster sweeps: rows of at most 8 (tets, quads) or 16 (hexes) L / U
@@ -544,6 +774,13 @@ static int sweep_ctas()
 // out = (LU)^-1 in
 void launch_ilu_apply(const IluView& f, const double* in, double* out, const KState* st, cudaStream_t s)
 {
+    if (f.tiles)
+    {
+        const int g = tile_grid();
+        k_ilu_tiles<1><<<g, kTileT, 0, s>>>(f, in, out, st);
+        k_ilu_tiles<2><<<g, kTileT, 0, s>>>(f, nullptr, out, st);
+        return;
+    }
     const int k = std::max(f.kl, f.ku);
     if (f.pl_row && k <= 8 && sweep_ctas<8, 1024>() > 0)
     {

@@ -101,6 +101,19 @@ struct IluView
     int kl, ku;               // entries per row in the packed arrays
     int32_t *pl_row, *pl_col, *pu_row, *pu_col;
     double *pl_val, *pu_val, *pu_diag;
+    // lattice tiles (ogs_mesh::tiles; 0: the level kernels sweep): per tile
+    // and its 8 z layers the 64 rows (x, y) of a layer, their entries by
+    // neighbour slot (forward: the 7 neighbours at offsets in {-1, 0}^3,
+    // backward: in {0, 1}^3, each in ascending column order) and a mask
+    // (bit s: slot s is an entry of the row; bit 7: the row exists and has
+    // a diagonal)
+    int tiles, lnx, lny, lnz, tnx, tny, tnz;
+    const int32_t* tile_order;       // [tiles] by the sum of the tile coordinates
+    int* tile_flags;                 // [2][tiles] launch number of the forward / backward publication
+    unsigned long long* tile_ticket; // [2]
+    double *tl_val, *tu_val;         // [tiles][8][7][64]
+    double* tu_dg;                   // [tiles][8][64] 1 / U_ii
+    unsigned char *tl_mask, *tu_mask;  // [tiles][8][64]
 };
 
 struct SolveArgs

@@ -271,6 +271,54 @@ extern "C" int64_t ogs_gpu_kernel_launches(int32_t reset) { return ogs::launches
 // columns below the diagonal for the forward sweep, above it for the
 // backward sweep.  Rows are returned grouped by level, ascending inside a
 // level; ptr holds the level boundaries.
+// Is the pattern that of a lattice numbered line by line (nx nodes per
+// line, nxy = nx ny per plane), every entry joining nodes at most one step
+// apart on each axis, with the columns left of the diagonal at no larger
+// x, y and z than the row?  Row 0's columns give the candidate: 0, 1, nx
+// (nx + 1), then nxy; every entry is then checked.
+static bool lattice_monotone(int64_t N, const std::vector<int32_t>& row_ptr, const std::vector<int32_t>& col,
+                             int& nx, int& ny, int& nz)
+{
+    if (N < 8) return false;
+    const int32_t* c0 = col.data() + row_ptr[0];
+    const int64_t n0 = row_ptr[1] - row_ptr[0];
+    if (n0 < 4 || c0[0] != 0 || c0[1] != 1) return false;
+    const int64_t cx = c0[2];
+    int64_t cxy = -1;
+    for (int64_t k = 0; k < n0; k++)
+        if (c0[k] != 0 && c0[k] != 1 && c0[k] != cx && c0[k] != cx + 1)
+        {
+            cxy = c0[k];
+            break;
+        }
+    if (cx < 3 || cxy < 3 * cx || cxy % cx != 0 || N % cxy != 0 || N / cxy < 2) return false;
+    const int64_t x_n = cx, y_n = cxy / cx, z_n = N / cxy;
+    std::atomic<bool> ok(true);
+    parallel_for(N, [&](int64_t lo, int64_t hi) {
+        for (int64_t r = lo; r < hi && ok.load(std::memory_order_relaxed); r++)
+        {
+            const int64_t rx = r % x_n, ry = (r / x_n) % y_n, rz = r / cxy;
+            for (int64_t k = row_ptr[r]; k < row_ptr[r + 1]; k++)
+            {
+                const int64_t j = col[k];
+                const int64_t dx = j % x_n - rx, dy = (j / x_n) % y_n - ry, dz = j / cxy - rz;
+                const bool near = dx >= -1 && dx <= 1 && dy >= -1 && dy <= 1 && dz >= -1 && dz <= 1;
+                const bool mono = j < r ? dx <= 0 && dy <= 0 && dz <= 0 : dx >= 0 && dy >= 0 && dz >= 0;
+                if (!near || !mono)
+                {
+                    ok = false;
+                    break;
+                }
+            }
+        }
+    });
+    if (!ok) return false;
+    nx = (int)x_n;
+    ny = (int)y_n;
+    nz = (int)z_n;
+    return true;
+}
+
 static void sweep_levels(int64_t N, const std::vector<int32_t>& row_ptr, const std::vector<int32_t>& col,
                          bool forward, std::vector<int32_t>& rows, std::vector<int32_t>& ptr)
 {
@@ -323,6 +371,7 @@ extern "C" ogs_status ogs_gpu_mesh_destroy(ogs_mesh* m)
     cudaFree(m->lvl_ptr);
     cudaFree(m->ulvl_rows);
     cudaFree(m->ulvl_ptr);
+    cudaFree(m->tile_order);
     delete m;
     return OGS_OK;
 }
@@ -469,6 +518,29 @@ extern "C" ogs_status ogs_gpu_mesh_create(const ogs_mesh_desc* d, ogs_mesh** out
             m->ilu_kl = std::max(m->ilu_kl, diag[r] - row_ptr[r]);
             m->ilu_ku = std::max(m->ilu_ku, row_ptr[r + 1] - diag[r] - 1);
         }
+    // ILU(0) tiles, ordered by the sum of their coordinates (the forward
+    // sweep's dependency order between tiles; the backward sweep walks the
+    // list from its end)
+    std::vector<int32_t> tile_order;
+    if (N < (int64_t(1) << 30) &&
+        lattice_monotone(N, row_ptr, col, m->lnx, m->lny, m->lnz))
+    {
+        m->tnx = (m->lnx + kIluTile - 1) / kIluTile;
+        m->tny = (m->lny + kIluTile - 1) / kIluTile;
+        m->tnz = (m->lnz + kIluTile - 1) / kIluTile;
+        const int64_t nt = (int64_t)m->tnx * m->tny * m->tnz;
+        if (nt * kIluTile * kIluTile * kIluTile < (int64_t(1) << 31))
+        {
+            m->tiles = (int)nt;
+            for (int l = 0; l <= m->tnx + m->tny + m->tnz - 3; l++)
+                for (int c = 0; c < m->tnz; c++)
+                    for (int b = 0; b < m->tny; b++)
+                    {
+                        const int a = l - b - c;
+                        if (a >= 0 && a < m->tnx) tile_order.push_back(a + m->tnx * (b + m->tny * c));
+                    }
+        }
+    }
     // SELL-32 layout of the pattern
     const int n_slices = (int)((N + kSlice - 1) / kSlice);
     std::vector<int32_t> slice_ptr(n_slices + 1, 0);
@@ -619,6 +691,7 @@ extern "C" ogs_status ogs_gpu_mesh_create(const ogs_mesh_desc* d, ogs_mesh** out
         (st = upload(&m->lvl_ptr, lvl_ptr.data(), lvl_ptr.size())) ||
         (st = upload(&m->ulvl_rows, ulvl_rows.data(), ulvl_rows.size())) ||
         (st = upload(&m->ulvl_ptr, ulvl_ptr.data(), ulvl_ptr.size())) ||
+        (m->tiles && (st = upload(&m->tile_order, tile_order.data(), tile_order.size()))) ||
         (st = upload(&m->tab, tab.data(), tab.size())) ||
         (st = upload(&m->aff, affb.data(), affb.size())))
     {
@@ -638,3 +711,5 @@ extern "C" ogs_status ogs_gpu_mesh_info(const ogs_mesh* m, int64_t* n_rows, int6
 }
 
 extern "C" int32_t ogs_gpu_mesh_gauss_points(const ogs_mesh* m) { return m ? m->ngp : 0; }
+
+extern "C" int32_t ogs_gpu_mesh_ilu_tiles(const ogs_mesh* m) { return m ? m->tiles : 0; }

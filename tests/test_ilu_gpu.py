@@ -11,7 +11,7 @@ import pytest
 
 from ogs5_gb300 import fields
 from ogs5_gb300 import mesh as M
-from tests.helpers import SOLUTION_RTOL, assert_matrix_close, rel_max_err
+from tests.helpers import SOLUTION_RTOL, assert_matrix_close, rel_max_err, renumber
 from tests.test_parity_gpu import _flow_system, k_field
 
 pytestmark = pytest.mark.gpu
@@ -142,3 +142,40 @@ def test_ilu0_rejected_in_fp32_mode(gpu):
     with pytest.raises(gpu.OgsError) as e:
         eqs.Solver(np.zeros(m.n_nodes))
     assert e.value.status == gpu.BAD_ARG
+
+
+@pytest.mark.parametrize("cells", [(8, 5, 4), (7, 8, 9), (16, 16, 8), (17, 9, 10), (3, 3, 2)])
+def test_tile_sweeps_match_level_sweeps(gpu, oracle, monkeypatch, cells):
+    """On a Kuhn-tet lattice the sweeps walk tiles of 8^3 nodes; with
+    OGS_ILU_SWEEP=levels they walk dependency levels of rows.  The same
+    system solved both ways (one assembly: the element scatter's FP64
+    atomics make two assemblies differ in the last bits): the same factors
+    and the same arithmetic per row give the same iterations and bit for bit
+    the same solution (full and partial tiles, BiCGStab and CG)."""
+    m = M.structured_tet(*cells)
+    eqs, _, x0 = _transport_system(gpu, m)
+    assert eqs.gmesh.ilu_tiles > 0
+    ek = np.repeat(fields.lognormal_k(cells, np.log(1e-5), 1.0, 3.0, seed=4), 6)
+    feqs, _, f0 = _flow_system(gpu, oracle, m, ek, symmetric=True, dt=3600.0, storage=1e-4, left=10.0, right=0.0)
+    eqs.ConfigNumerics(gpu.LS_BICGSTAB, gpu.PRECOND_ILU0, 1000, 1e-13, check_norm_rhs=False)
+    feqs.ConfigNumerics(gpu.LS_CG, gpu.PRECOND_ILU0, 3000, 1e-13)
+    out = {}
+    for mode in ("tiles", "levels", "tiles again"):
+        if mode == "levels":
+            monkeypatch.setenv("OGS_ILU_SWEEP", "levels")
+        else:
+            monkeypatch.delenv("OGS_ILU_SWEEP", raising=False)
+        x, h = x0.copy(), f0.copy()
+        out[mode] = (eqs.Solver(x), x, feqs.Solver(h), h)
+    for mode in ("levels", "tiles again"):
+        it, x, fit, h = out[mode]
+        assert it == out["tiles"][0] and fit == out["tiles"][2]
+        assert np.array_equal(x, out["tiles"][1]) and np.array_equal(h, out["tiles"][3])
+
+
+def test_ilu_tiles_only_on_monotone_lattices(gpu):
+    """Tiles for Kuhn tets in lattice order; none for 27-point hexes (a
+    column left of the diagonal at x + 1) or a renumbered tet mesh."""
+    assert gpu.GpuMesh(M.structured_tet(9, 8, 7)).ilu_tiles == 2 * 2 * 1
+    assert gpu.GpuMesh(M.structured_hex(9, 8, 7)).ilu_tiles == 0
+    assert gpu.GpuMesh(renumber(M.structured_tet(9, 8, 7), 3)[0]).ilu_tiles == 0
