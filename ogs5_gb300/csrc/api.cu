@@ -39,6 +39,7 @@ int vec_grid(int n);
 int red_grid(int n);
 int mp_spmv_grid(const MixedArgs& a);
 void launch_mp_product_pair(const MixedArgs& a, float* y_rows, float* y_lines, cudaStream_t s);
+void launch_ilu_tile_pattern(const IluView& f, cudaStream_t s);
 cudaError_t launch_mp_barrier_selftest(KState* st, int grid, int withhold, unsigned limit, int* go, cudaStream_t s);
 cudaError_t ilu_wait_selftest(int withhold, unsigned limit, int* gave_up, int* rows_ok, cudaStream_t s);
 size_t batch_ctl_bytes();
@@ -246,7 +247,8 @@ struct ogs_system
     bool ilu_use_tiles = false;
     int* ilu_tile_flags = nullptr;
     unsigned long long* ilu_tile_ticket = nullptr;
-    double *ilu_tl_val = nullptr, *ilu_tu_val = nullptr, *ilu_tu_dg = nullptr;
+    double *ilu_tl_val = nullptr, *ilu_tu_val = nullptr, *ilu_tu_dg = nullptr, *ilu_tu_piv = nullptr;
+    int32_t* ilu_t_rb = nullptr;
     unsigned char *ilu_tl_mask = nullptr, *ilu_tu_mask = nullptr;
     double *ek = nullptr, *u0 = nullptr, *gpv = nullptr, *qbuf = nullptr, *vec_in = nullptr,
            *vec_out = nullptr, *u1 = nullptr;
@@ -380,6 +382,7 @@ SolveArgs make_solve_args(ogs_system* s)
         a.ilu.tile_flags = s->ilu_tile_flags;
         a.ilu.tile_ticket = s->ilu_tile_ticket;
         a.ilu.tl_val = s->ilu_tl_val; a.ilu.tu_val = s->ilu_tu_val; a.ilu.tu_dg = s->ilu_tu_dg;
+        a.ilu.tu_piv = s->ilu_tu_piv; a.ilu.t_rb = s->ilu_t_rb;
         a.ilu.tl_mask = s->ilu_tl_mask; a.ilu.tu_mask = s->ilu_tu_mask;
     }
     return a;
@@ -492,6 +495,8 @@ extern "C" ogs_status ogs_gpu_system_destroy(ogs_system* s)
     cudaFree(s->ilu_tl_val);
     cudaFree(s->ilu_tu_val);
     cudaFree(s->ilu_tu_dg);
+    cudaFree(s->ilu_tu_piv);
+    cudaFree(s->ilu_t_rb);
     cudaFree(s->ilu_tl_mask);
     cudaFree(s->ilu_tu_mask);
     cudaFree(s->st);
@@ -1392,15 +1397,20 @@ static ogs_status ilu_factor(ogs_system* s)
         if (tiles && !s->ilu_tile_flags)
         {
             const size_t rows = (size_t)m->tiles * kIluTile * kIluTile * kIluTile;
-            OGS_CUDA_TRY(cudaMalloc(&s->ilu_tile_flags, 2 * (size_t)m->tiles * sizeof(int)));
-            OGS_CUDA_TRY(cudaMalloc(&s->ilu_tile_ticket, 2 * sizeof(unsigned long long)));
-            OGS_CUDA_TRY(cudaMemsetAsync(s->ilu_tile_flags, 0, 2 * (size_t)m->tiles * sizeof(int), s->stream));
-            OGS_CUDA_TRY(cudaMemsetAsync(s->ilu_tile_ticket, 0, 2 * sizeof(unsigned long long), s->stream));
+            OGS_CUDA_TRY(cudaMalloc(&s->ilu_tile_flags, 3 * (size_t)m->tiles * sizeof(int)));
+            OGS_CUDA_TRY(cudaMalloc(&s->ilu_tile_ticket, 3 * sizeof(unsigned long long)));
+            OGS_CUDA_TRY(cudaMemsetAsync(s->ilu_tile_flags, 0, 3 * (size_t)m->tiles * sizeof(int), s->stream));
+            OGS_CUDA_TRY(cudaMemsetAsync(s->ilu_tile_ticket, 0, 3 * sizeof(unsigned long long), s->stream));
             OGS_CUDA_TRY(cudaMalloc(&s->ilu_tl_val, 7 * rows * sizeof(double)));
             OGS_CUDA_TRY(cudaMalloc(&s->ilu_tu_val, 7 * rows * sizeof(double)));
             OGS_CUDA_TRY(cudaMalloc(&s->ilu_tu_dg, rows * sizeof(double)));
+            OGS_CUDA_TRY(cudaMalloc(&s->ilu_tu_piv, rows * sizeof(double)));
+            OGS_CUDA_TRY(cudaMalloc(&s->ilu_t_rb, rows * sizeof(int32_t)));
             OGS_CUDA_TRY(cudaMalloc(&s->ilu_tl_mask, rows));
             OGS_CUDA_TRY(cudaMalloc(&s->ilu_tu_mask, rows));
+            SolveArgs pa = make_solve_args(s);
+            launch_ilu_tile_pattern(pa.ilu, s->stream);
+            OGS_LAUNCH_CHECK();
         }
     }
     const int big = 0x7fffffff;

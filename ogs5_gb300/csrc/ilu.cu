@@ -449,8 +449,9 @@ __device__ __forceinline__ int tile_slot_offset(int mode, int slot)
     return sg * ((q & 1) + (kIluTile + 1) * (((q >> 1) & 1) + (kIluTile + 1) * ((q >> 2) & 1)));
 }
 
-// the packed tile rows after a factorisation
-__global__ void k_ilu_pack_tiles(IluView f)
+// The tile rows' pattern, once per system: the slots of each row's entries
+// (bit 7: the row lies in the lattice and has a diagonal) and its CSR start
+__global__ void k_ilu_tile_pattern(IluView f)
 {
     const int64_t total = (int64_t)f.tiles * kIluTile * kTileT;
     const int nxy = f.lnx * f.lny;
@@ -462,9 +463,7 @@ __global__ void k_ilu_pack_tiles(IluView f)
         const int a = tile % f.tnx, b = (tile / f.tnx) % f.tny, c = tile / (f.tnx * f.tny);
         const int x = a * kIluTile + t % kIluTile, y = b * kIluTile + t / kIluTile, z = c * kIluTile + lz;
         unsigned lm = 0, um = 0;
-        double lv[7], uv[7], dg = 1.0;
-#pragma unroll
-        for (int q = 0; q < 7; q++) lv[q] = uv[q] = 0.0;
+        int rb = -1;
         if (x < f.lnx && y < f.lny && z < f.lnz)
         {
             const int i = x + f.lnx * (y + f.lny * z);
@@ -472,45 +471,222 @@ __global__ void k_ilu_pack_tiles(IluView f)
             if (d >= 0)
             {
                 lm = um = 0x80;
-                const int rb = __ldg(f.row_ptr + i), re = __ldg(f.row_ptr + i + 1);
+                rb = __ldg(f.row_ptr + i);
+                const int re = __ldg(f.row_ptr + i + 1);
                 for (int k = rb; k < re; k++)
                 {
                     if (k == d) continue;
                     const int j = __ldg(f.col + k);
                     const int dx = j % f.lnx - x, dy = (j / f.lnx) % f.lny - y, dz = j / nxy - z;
-                    if (k < d)
+                    // 1 .. 7 on a checked pattern
+                    const int q = k < d ? (-dx) | ((-dy) << 1) | ((-dz) << 2) : dx | (dy << 1) | (dz << 2);
+                    if (OGS_IN(q - 1, 7, kOobIluCol))
                     {
-                        const int q = (-dx) | ((-dy) << 1) | ((-dz) << 2);  // 1 .. 7 on a checked pattern
-                        if (OGS_IN(q - 1, 7, kOobIluCol))
-                        {
-                            lv[7 - q] = f.lu[k];
-                            lm |= 1u << (7 - q);
-                        }
-                    }
-                    else
-                    {
-                        const int q = dx | (dy << 1) | (dz << 2);
-                        if (OGS_IN(q - 1, 7, kOobIluCol))
-                        {
-                            uv[q - 1] = f.lu[k];
-                            um |= 1u << (q - 1);
-                        }
+                        if (k < d) lm |= 1u << (7 - q);
+                        else um |= 1u << (q - 1);
                     }
                 }
-                dg = 1.0 / f.lu[d];
             }
         }
         const size_t row = ((size_t)tile * kIluTile + lz) * kTileT + t;
-        const size_t v0 = ((size_t)tile * kIluTile + lz) * 7 * kTileT + t;
-#pragma unroll
-        for (int q = 0; q < 7; q++)
-        {
-            f.tl_val[v0 + (size_t)q * kTileT] = lv[q];
-            f.tu_val[v0 + (size_t)q * kTileT] = uv[q];
-        }
         f.tl_mask[row] = (unsigned char)lm;
         f.tu_mask[row] = (unsigned char)um;
-        f.tu_dg[row] = dg;
+        f.t_rb[row] = rb;
+    }
+}
+
+// The entry of row i that a_ij -= l_ik u_kj updates, for row k = i + (lower
+// slot s) and j = k + (upper slot u of row k): 0 .. 6 a lower slot, 7 the
+// diagonal, 8 .. 14 an upper slot; -1 when j - i has components of both
+// signs (no entry of a monotone pattern)
+__host__ __device__ constexpr int tile_target(int s, int u)
+{
+    const int ql = 7 - s, qu = u + 1;
+    const int sx = (qu & 1) - (ql & 1), sy = ((qu >> 1) & 1) - ((ql >> 1) & 1),
+              sz = ((qu >> 2) & 1) - ((ql >> 2) & 1);
+    if (sx == 0 && sy == 0 && sz == 0) return 7;
+    if (sx <= 0 && sy <= 0 && sz <= 0) return 7 - ((-sx) | ((-sy) << 1) | ((-sz) << 2));
+    if (sx >= 0 && sy >= 0 && sz >= 0) return 8 + ((sx | (sy << 1) | (sz << 2)) - 1);
+    return -1;
+}
+
+// ILU(0) tile by tile (lattice patterns): rows of a tile eliminated in the
+// order of lx + ly + lz, each in the IKJ order of the level kernel (its
+// lower entries in column order, l_ik = a_ik / u_kk, then a_ij -= l_ik
+// u_kj over row k's upper entries, products and differences rounded
+// separately), with the pivot rows' U parts (u_kk and 7 upper values) in a
+// 9^3 cube in shared memory: this tile's rows as they are done, the faces
+// from the tiles before it.  Writes the factors in CSR order (lu) and the
+// sweeps' tile arrays.  Dynamic shared memory: kTileFactorSmem bytes.
+constexpr size_t kTileFactorSmem = sizeof(double) * (kIluTile * 15 * kTileT + kTileCube * 8) +
+                                   sizeof(int) * kIluTile * kTileT + kTileCube + 2 * kIluTile * kTileT;
+
+__global__ void __launch_bounds__(kTileT) k_ilu_factor_tiles(IluView f)
+{
+    extern __shared__ double dsm[];
+    double(*s_a)[15][kTileT] = reinterpret_cast<double(*)[15][kTileT]>(dsm);  // the rows' entries
+    double(*s_u)[8] = reinterpret_cast<double(*)[8]>(dsm + kIluTile * 15 * kTileT);  // U parts of the cube
+    int* s_rb = reinterpret_cast<int*>(dsm + kIluTile * 15 * kTileT + kTileCube * 8);
+    unsigned char* s_um = reinterpret_cast<unsigned char*>(s_rb + kIluTile * kTileT);  // cube: upper mask
+    unsigned char* s_lm = s_um + kTileCube;                                           // rows: lower mask
+    unsigned char* s_ur = s_lm + kIluTile * kTileT;                                   // rows: upper mask
+    __shared__ unsigned long long s_ticket;
+    const int ntiles = f.tiles;
+    const unsigned long long per = (unsigned long long)ntiles + gridDim.x;
+    int* tflags = f.tile_flags + 2 * ntiles;
+    const int t = threadIdx.x, lx = t % kIluTile, ly = t / kIluTile;
+    constexpr int E = kIluTile + 1;
+    const int64_t nrows = (int64_t)ntiles * kIluTile * kTileT;
+    for (;;)
+    {
+        __syncthreads();
+        if (t == 0) s_ticket = atomicAdd(f.tile_ticket + 2, 1ull);
+        __syncthreads();
+        const unsigned long long tk = s_ticket;
+        const unsigned long long idx = tk % per;
+        if (idx >= (unsigned long long)ntiles) return;  // this block's closing ticket
+        const int launch = (int)(tk / per) + 1;
+        const int tile = __ldg(f.tile_order + (int)idx);
+        const int a = tile % f.tnx, b = (tile / f.tnx) % f.tny, c = tile / (f.tnx * f.tny);
+        const int x = a * kIluTile + lx, y = b * kIluTile + ly;
+        // the rows' entries (the matrix values in lu), before the wait
+#pragma unroll
+        for (int lz = 0; lz < kIluTile; lz++)
+        {
+            const size_t row = ((size_t)tile * kIluTile + lz) * kTileT + t;
+            const bool rin = OGS_IN(row, nrows, kOobIluCol);
+            const unsigned lm = rin ? __ldg(f.tl_mask + row) : 0u, um = rin ? __ldg(f.tu_mask + row) : 0u;
+            const int rb = rin ? __ldg(f.t_rb + row) : -1;
+            s_lm[lz * kTileT + t] = (unsigned char)lm;
+            s_ur[lz * kTileT + t] = (unsigned char)um;
+            s_rb[lz * kTileT + t] = rb;
+            const int z = c * kIluTile + lz;
+            if (lm & 0x80)
+            {
+                int p = rb;
+#pragma unroll
+                for (int q = 0; q < 7; q++)
+                    if (lm & (1u << q)) s_a[lz][q][t] = __ldcg(f.lu + p++);
+                s_a[lz][7][t] = __ldcg(f.lu + p++);
+#pragma unroll
+                for (int q = 0; q < 7; q++)
+                    if (um & (1u << q)) s_a[lz][8 + q][t] = __ldcg(f.lu + p++);
+            }
+            else if (x < f.lnx && y < f.lny && z < f.lnz)
+                atomicMin(f.bad, x + f.lnx * (y + f.lny * z));  // no diagonal: a zero pivot
+        }
+        // the tiles before this one
+        if (t < 7)
+        {
+            const int q = t + 1;
+            const int na = a - (q & 1), nb = b - ((q >> 1) & 1), nc = c - ((q >> 2) & 1);
+            const int nt = na + f.tnx * (nb + f.tny * nc);
+            if (na >= 0 && nb >= 0 && nc >= 0 && OGS_IN(nt, ntiles, kOobIluCol))
+                ilu_wait(tflags, nt, launch, f.bad, f.spin ? f.spin : kIluSpin);
+            fence_acquire();  // the block barrier below passes it on to the other threads
+        }
+        __syncthreads();
+        // their rows' U parts at this tile's faces (cube index 0 on some axis)
+        for (int h = t; h < kTileCube; h += kTileT)
+        {
+            const int cx = h % E, cy = (h / E) % E, cz = h / (E * E);
+            if (cx != 0 && cy != 0 && cz != 0) continue;
+            const int gx = a * kIluTile + cx - 1, gy = b * kIluTile + cy - 1, gz = c * kIluTile + cz - 1;
+            unsigned um = 0;
+            if (gx >= 0 && gy >= 0 && gz >= 0)
+            {
+                const int tt = gx / kIluTile + f.tnx * (gy / kIluTile + f.tny * (gz / kIluTile));
+                const size_t r8 = ((size_t)tt * kIluTile + gz % kIluTile) * kTileT + gx % kIluTile +
+                                  kIluTile * (gy % kIluTile);
+                if (OGS_IN(r8, nrows, kOobIluCol))
+                {
+                    um = __ldg(f.tu_mask + r8);
+                    if (um & 0x80)
+                    {
+                        s_u[h][0] = __ldcg(f.tu_piv + r8);
+                        const size_t v0 = ((size_t)tt * kIluTile + gz % kIluTile) * 7 * kTileT + gx % kIluTile +
+                                          kIluTile * (gy % kIluTile);
+#pragma unroll
+                        for (int q = 0; q < 7; q++) s_u[h][1 + q] = __ldcg(f.tu_val + v0 + (size_t)q * kTileT);
+                    }
+                }
+            }
+            s_um[h] = (unsigned char)um;
+        }
+        __syncthreads();
+        for (int step = 0; step < kTileSteps; step++)
+        {
+            const int lz = step - lx - ly;
+            if (lz >= 0 && lz < kIluTile)
+            {
+                const unsigned lm = s_lm[lz * kTileT + t], um = s_ur[lz * kTileT + t];
+                if (lm & 0x80)
+                {
+                    const int z = c * kIluTile + lz;
+                    const int i = x + f.lnx * (y + f.lny * z);
+                    const int ci = (lx + 1) + E * ((ly + 1) + E * (lz + 1));
+                    double av[15];
+#pragma unroll
+                    for (int q = 0; q < 15; q++) av[q] = s_a[lz][q][t];
+#pragma unroll
+                    for (int sl = 0; sl < 7; sl++)
+                    {
+                        if (!(lm & (1u << sl))) continue;
+                        const int nb = ci + tile_slot_offset(1, sl);
+                        const double piv = s_u[nb][0];
+                        const unsigned kum = s_um[nb];
+                        if (piv == 0.0)
+                        {
+                            const int qq = 7 - sl;
+                            atomicMin(f.bad, i - ((qq & 1) + f.lnx * (((qq >> 1) & 1) + f.lny * ((qq >> 2) & 1))));
+                        }
+                        const double lik = av[sl] / piv;
+                        av[sl] = lik;
+#pragma unroll
+                        for (int u = 0; u < 7; u++)
+                        {
+                            const int T = tile_target(sl, u);
+                            if (T < 0 || !(kum & (1u << u))) continue;
+                            const bool present = T < 7 ? (lm >> T) & 1u : T == 7 ? 1u : (um >> (T - 8)) & 1u;
+                            if (present) av[T] = __dsub_rn(av[T], __dmul_rn(lik, s_u[nb][1 + u]));
+                        }
+                    }
+                    if (av[7] == 0.0) atomicMin(f.bad, i);
+                    // this row's U part for the rows after it
+                    s_u[ci][0] = av[7];
+#pragma unroll
+                    for (int q = 0; q < 7; q++) s_u[ci][1 + q] = av[8 + q];
+                    s_um[ci] = (unsigned char)um;
+                    // the factors: CSR order, and the sweeps' tile arrays
+                    int p = s_rb[lz * kTileT + t];
+#pragma unroll
+                    for (int q = 0; q < 7; q++)
+                        if (lm & (1u << q)) __stcg(f.lu + p++, av[q]);
+                    __stcg(f.lu + p++, av[7]);
+#pragma unroll
+                    for (int q = 0; q < 7; q++)
+                        if (um & (1u << q)) __stcg(f.lu + p++, av[8 + q]);
+                    const size_t row = ((size_t)tile * kIluTile + lz) * kTileT + t;
+                    const size_t v0 = ((size_t)tile * kIluTile + lz) * 7 * kTileT + t;
+#pragma unroll
+                    for (int q = 0; q < 7; q++)
+                    {
+                        __stcg(f.tl_val + v0 + (size_t)q * kTileT, (lm & (1u << q)) ? av[q] : 0.0);
+                        __stcg(f.tu_val + v0 + (size_t)q * kTileT, (um & (1u << q)) ? av[8 + q] : 0.0);
+                    }
+                    __stcg(f.tu_piv + row, av[7]);
+                    __stcg(f.tu_dg + row, 1.0 / av[7]);
+                }
+            }
+            __syncthreads();
+        }
+        // the block's stores are ordered before thread 0's fence by the last
+        // step's barrier (the grid-barrier pattern: one fence per block)
+        if (t == 0)
+        {
+            __threadfence();
+            st_release_s32(tflags + tile, launch);
+        }
     }
 }
 
@@ -570,10 +746,9 @@ __global__ void __launch_bounds__(kTileT) k_ilu_tiles(IluView f, const double* _
             if (na >= 0 && na < f.tnx && nb >= 0 && nb < f.tny && nc >= 0 && nc < f.tnz &&
                 OGS_IN(nt, ntiles, kOobIluCol))
                 ilu_wait(tflags, nt, launch, f.bad, f.spin ? f.spin : kIluSpin);
+            fence_acquire();  // the block barrier below passes it on to the other threads
         }
-        fence_acquire();
         __syncthreads();
-        fence_acquire();
         // their results at this tile's faces (forward: cube index 0 on some
         // axis, the lattice coordinate one below the tile; backward: index 8)
         for (int h = t; h < kTileCube; h += kTileT)
@@ -612,10 +787,13 @@ __global__ void __launch_bounds__(kTileT) k_ilu_tiles(IluView f, const double* _
             }
             __syncthreads();
         }
-        // publish the tile
-        __threadfence();
-        __syncthreads();
-        if (t == 0) st_release_s32(tflags + tile, launch);
+        // publish the tile: the block's stores are ordered before thread 0's
+        // fence by the last step's barrier (the grid-barrier pattern)
+        if (t == 0)
+        {
+            __threadfence();
+            st_release_s32(tflags + tile, launch);
+        }
     }
 }
 
@@ -672,18 +850,47 @@ static int ilu_grid(int npos)
     return std::max(1, std::min((npos + kIluBlock - 1) / kIluBlock, sms * kIluBlocksPerSm));
 }
 
+// the tile factorisation's persistent grid (dynamic shared memory opted in)
+static int tile_factor_grid()
+{
+    static int g = 0;
+    if (!g)
+    {
+        int dev = 0, sms = 152, o = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (cudaFuncSetAttribute(k_ilu_factor_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)kTileFactorSmem) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_ilu_factor_tiles, kTileT, kTileFactorSmem) !=
+                cudaSuccess)
+        {
+            cudaGetLastError();
+            o = 1;
+        }
+        g = std::max(1, sms * std::max(1, o));
+    }
+    return g;
+}
+
 void launch_ilu_factor(const IluView& f, const double* val, const int32_t* csr2sell, int64_t nnz,
                        const KState* st, cudaStream_t s)
 {
     const int g = (int)std::max<int64_t>(1, std::min<int64_t>((nnz + 255) / 256, 4096));
     k_ilu_copy<<<g, 256, 0, s>>>(val, csr2sell, f.lu, nnz);
-    k_ilu_flow<0><<<ilu_grid(f.n_lpos), kIluBlock, 0, s>>>(f, nullptr, nullptr, st);
-    if (f.pl_row) k_ilu_pack<<<ilu_grid(std::max(f.n_lpos, f.n_upos)), kIluBlock, 0, s>>>(f);
     if (f.tiles)
     {
-        const int64_t rows = (int64_t)f.tiles * kIluTile * kTileT;
-        k_ilu_pack_tiles<<<(int)std::min<int64_t>((rows + 255) / 256, 8192), 256, 0, s>>>(f);
+        k_ilu_factor_tiles<<<tile_factor_grid(), kTileT, kTileFactorSmem, s>>>(f);
+        return;
     }
+    k_ilu_flow<0><<<ilu_grid(f.n_lpos), kIluBlock, 0, s>>>(f, nullptr, nullptr, st);
+    if (f.pl_row) k_ilu_pack<<<ilu_grid(std::max(f.n_lpos, f.n_upos)), kIluBlock, 0, s>>>(f);
+}
+
+// once per system: the tile rows' slots and CSR starts
+void launch_ilu_tile_pattern(const IluView& f, cudaStream_t s)
+{
+    const int64_t rows = (int64_t)f.tiles * kIluTile * kTileT;
+    k_ilu_tile_pattern<<<(int)std::min<int64_t>((rows + 255) / 256, 8192), 256, 0, s>>>(f);
 }
 
 // the tile sweeps' persistent grid: as many blocks as are resident at once

@@ -109,10 +109,13 @@ struct IluView
     // a diagonal)
     int tiles, lnx, lny, lnz, tnx, tny, tnz;
     const int32_t* tile_order;       // [tiles] by the sum of the tile coordinates
-    int* tile_flags;                 // [2][tiles] launch number of the forward / backward publication
-    unsigned long long* tile_ticket; // [2]
+    int* tile_flags;                 // [3][tiles] launch number of the forward / backward sweep's and the
+                                     // factorisation's publication
+    unsigned long long* tile_ticket; // [3]
     double *tl_val, *tu_val;         // [tiles][8][7][64]
     double* tu_dg;                   // [tiles][8][64] 1 / U_ii
+    double* tu_piv;                  // [tiles][8][64] U_ii
+    int32_t* t_rb;                   // [tiles][8][64] CSR start of the row (-1: none)
     unsigned char *tl_mask, *tu_mask;  // [tiles][8][64]
 };
 

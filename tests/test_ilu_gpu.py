@@ -146,12 +146,13 @@ def test_ilu0_rejected_in_fp32_mode(gpu):
 
 @pytest.mark.parametrize("cells", [(8, 5, 4), (7, 8, 9), (16, 16, 8), (17, 9, 10), (3, 3, 2)])
 def test_tile_sweeps_match_level_sweeps(gpu, oracle, monkeypatch, cells):
-    """On a Kuhn-tet lattice the sweeps walk tiles of 8^3 nodes; with
-    OGS_ILU_SWEEP=levels they walk dependency levels of rows.  The same
-    system solved both ways (one assembly: the element scatter's FP64
-    atomics make two assemblies differ in the last bits): the same factors
-    and the same arithmetic per row give the same iterations and bit for bit
-    the same solution (full and partial tiles, BiCGStab and CG)."""
+    """On a Kuhn-tet lattice the factorisation and the sweeps walk tiles of
+    8^3 nodes; with OGS_ILU_SWEEP=levels they walk dependency levels of rows.
+    The same system solved both ways (one assembly: the element scatter's
+    FP64 atomics make two assemblies differ in the last bits): the same
+    arithmetic per row gives bit for bit the same factors, the same
+    iterations and the same solution (full and partial tiles, BiCGStab and
+    CG)."""
     m = M.structured_tet(*cells)
     eqs, _, x0 = _transport_system(gpu, m)
     assert eqs.gmesh.ilu_tiles > 0
@@ -166,9 +167,11 @@ def test_tile_sweeps_match_level_sweeps(gpu, oracle, monkeypatch, cells):
         else:
             monkeypatch.delenv("OGS_ILU_SWEEP", raising=False)
         x, h = x0.copy(), f0.copy()
-        out[mode] = (eqs.Solver(x), x, feqs.Solver(h), h)
+        it, fit = eqs.Solver(x), feqs.Solver(h)
+        out[mode] = (it, x, fit, h, eqs.get_ilu0(), feqs.get_ilu0())
     for mode in ("levels", "tiles again"):
-        it, x, fit, h = out[mode]
+        it, x, fit, h, lu, flu = out[mode]
+        assert np.array_equal(lu, out["tiles"][4]) and np.array_equal(flu, out["tiles"][5])
         assert it == out["tiles"][0] and fit == out["tiles"][2]
         assert np.array_equal(x, out["tiles"][1]) and np.array_equal(h, out["tiles"][3])
 
