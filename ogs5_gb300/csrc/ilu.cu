@@ -35,6 +35,14 @@
 // dependent L2 round trip (the neighbours' results) between two halves of
 // the cluster barrier, and the next level's entries are loaded while the
 // barrier completes.
+//
+// Lattice patterns whose lower columns lie at no larger x, y, z than their
+// row (Kuhn tets in lattice order: ogs_mesh::tiles) take a third form for
+// the factorisation and both sweeps: tiles of 8^3 rows in the order of the
+// sum of their tile coordinates, the rows of a tile in 22 steps of
+// lx + ly + lz from shared memory (k_ilu_factor_tiles, k_ilu_tiles below).
+// Every form does the same arithmetic per row, so all give bit for bit the
+// same factors and sweep results.
 #include <algorithm>
 #include <cstring>
 #include <vector>
