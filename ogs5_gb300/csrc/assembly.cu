@@ -991,20 +991,48 @@ __global__ void __launch_bounds__(128) k_mt_tet_affine(AsmArgs a)
         for (int k = 0; k < DIM * DIM; k++) Ds[k] = 0.0;
 #pragma unroll
         for (int k = 0; k < NN * NN; k++) A[k] = 0.0;
+        // the Gauss-point fluxes; when all five are bit for bit the same (a
+        // linear head field on an affine tet: Cal_Velocity gives one flux)
+        // the dispersion tensor and v . grad N are formed once and reused,
+        // which gives the same values as forming them per point
+        double vg[NGP][3];
+        bool same = true;
+#pragma unroll
+        for (int gp = 0; gp < NGP; gp++)
+#pragma unroll
+            for (int k = 0; k < 3; k++)
+            {
+                vg[gp][k] = __ldg(ve + gp * 3 + k);
+                same = same && __double_as_longlong(vg[gp][k]) == __double_as_longlong(vg[0][k]);
+            }
+        const double tf = 1.0 * p.time_unit_factor;
+        double D0[DIM * DIM], vd0[NN];
+        dispersion<DIM>(p, vg[0], D0);
+#pragma unroll
+        for (int j = 0; j < NN; j++)
+            vd0[j] = tf * vg[0][0] * dNg[j] + tf * vg[0][1] * dNg[NN + j] + tf * vg[0][2] * dNg[2 * NN + j];
 #pragma unroll
         for (int gp = 0; gp < NGP; gp++)
         {
             const double w = sw[gp * 3];
-            const double v[3] = {__ldg(ve + gp * 3), __ldg(ve + gp * 3 + 1), __ldg(ve + gp * 3 + 2)};
-            double D[DIM * DIM];
-            dispersion<DIM>(p, v, D);
+            const double* v = vg[gp];
+            double D[DIM * DIM], vd[NN];
+            if (gp == 0 || same)
+            {
+#pragma unroll
+                for (int k = 0; k < DIM * DIM; k++) D[k] = D0[k];
+#pragma unroll
+                for (int j = 0; j < NN; j++) vd[j] = vd0[j];
+            }
+            else
+            {
+                dispersion<DIM>(p, v, D);
+#pragma unroll
+                for (int j = 0; j < NN; j++)
+                    vd[j] = tf * v[0] * dNg[j] + tf * v[1] * dNg[NN + j] + tf * v[2] * dNg[2 * NN + j];
+            }
 #pragma unroll
             for (int k = 0; k < DIM * DIM; k++) Ds[k] += w * D[k];
-            const double tf = 1.0 * p.time_unit_factor;
-            double vd[NN];
-#pragma unroll
-            for (int j = 0; j < NN; j++)
-                vd[j] = tf * v[0] * dNg[j] + tf * v[1] * dNg[NN + j] + tf * v[2] * dNg[2 * NN + j];
             const double wd = det * w;
 #pragma unroll
             for (int i = 0; i < NN; i++)

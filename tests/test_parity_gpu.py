@@ -140,13 +140,19 @@ def test_assembly_liquid_flow_gravity(gpu, oracle, kind, distorted):
 
 @pytest.mark.parametrize("kind", ["quad", "hex", "tet"])
 @pytest.mark.parametrize("distorted", [False, True])
-def test_assembly_mass_transport(gpu, oracle, kind, distorted):
+@pytest.mark.parametrize("flux", ["per_point", "per_element"])
+def test_assembly_mass_transport(gpu, oracle, kind, distorted, flux):
+    """per_element: every Gauss point of an element carries the same flux
+    (what Cal_Velocity gives on affine tets), on every other element; the
+    tet kernel then forms the dispersion tensor once per element."""
     m = small_mesh(kind)
     if distorted:
         m = distort(m, 0.15, seed=9)
     ngp = {"quad": 9, "hex": 27, "tet": 5}[kind]
     rng = np.random.default_rng(11)
     gpv = rng.normal(0, 1e-5, (m.n_elements, ngp, 3))
+    if flux == "per_element":
+        gpv[::2] = gpv[::2, :1, :]
     if m.dim == 2:
         gpv[:, :, 2] = 0.0
     gpv[0, :, :] = 0.0  # zero-velocity branch of the dispersion tensor
