@@ -243,6 +243,7 @@ struct ogs_system
     unsigned long long* ilu_ticket = nullptr;  // [3] block tickets of the ILU kernels
     int32_t *ilu_pl_row = nullptr, *ilu_pl_col = nullptr, *ilu_pu_row = nullptr, *ilu_pu_col = nullptr;
     double *ilu_pl_val = nullptr, *ilu_pu_val = nullptr, *ilu_pu_diag = nullptr;  // packed sweep rows
+    double* ilu_rdiag = nullptr;  // [n] 1 / u_ii of the factored rows
     // the tile sweeps' rows (lattice patterns), flags and tickets
     bool ilu_use_tiles = false;
     int* ilu_tile_flags = nullptr;
@@ -373,6 +374,7 @@ SolveArgs make_solve_args(ogs_system* s)
     a.ilu.pu_row = s->ilu_pu_row; a.ilu.pu_col = s->ilu_pu_col; a.ilu.pu_val = s->ilu_pu_val;
     a.ilu.pu_diag = s->ilu_pu_diag;
     a.ilu.bad = s->d_ilu_bad;
+    a.ilu.rdiag = s->ilu_rdiag;
     if (s->ilu_use_tiles && s->ilu_tile_flags)
     {
         a.ilu.tiles = m->tiles;
@@ -490,6 +492,7 @@ extern "C" ogs_status ogs_gpu_system_destroy(ogs_system* s)
     cudaFree(s->ilu_pu_col);
     cudaFree(s->ilu_pu_val);
     cudaFree(s->ilu_pu_diag);
+    cudaFree(s->ilu_rdiag);
     cudaFree(s->ilu_tile_flags);
     cudaFree(s->ilu_tile_ticket);
     cudaFree(s->ilu_tl_val);
@@ -1364,6 +1367,7 @@ static ogs_status ilu_factor(ogs_system* s)
     {
         OGS_CUDA_TRY(cudaMalloc(&s->lu, std::max<int64_t>(1, m->nnz) * sizeof(double)));
         OGS_CUDA_TRY(cudaMalloc(&s->d_ilu_bad, sizeof(int)));
+        OGS_CUDA_TRY(cudaMalloc(&s->ilu_rdiag, std::max(1, s->n) * sizeof(double)));
         // publication flags start below every launch number, tickets at 0
         OGS_CUDA_TRY(cudaMalloc(&s->ilu_flags, 3 * (size_t)std::max(1, s->n) * sizeof(int)));
         OGS_CUDA_TRY(cudaMalloc(&s->ilu_ticket, 3 * sizeof(unsigned long long)));

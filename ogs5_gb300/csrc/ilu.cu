@@ -99,6 +99,22 @@ __device__ __forceinline__ void ilu_wait(const int* flags, int j, int launch, in
 
 __device__ __forceinline__ void fence_acquire() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
 
+// l_ik = a_ik / u_kk in the elimination, from r = 1 / u_kk (one IEEE
+// division per pivot row, done when that row is finished) by Markstein's
+// division step: q = a r, the remainder e = a - u q exact by one FMA, then
+// q + e r.  Two dependent FMAs after the product instead of a division on
+// the row's dependent chain: GB300's FP64 units make each dependent FP64
+// operation slow, and a row of the factorisation divides by up to 7 pivots
+// in sequence.  The quotient is within rounding of a / u (every form of
+// the factorisation uses this, so they agree bit for bit; the factors stay
+// within 1e-12 of the oracle's IEEE divisions).
+__device__ __forceinline__ double ilu_div(double a, double u, double r)
+{
+    const double q = __dmul_rn(a, r);
+    const double e = __fma_rn(-q, u, a);
+    return __fma_rn(e, r, q);
+}
+
 // one row of MODE 0 / 1 / 2 (below)
 template <int MODE>
 __device__ __forceinline__ void ilu_row(const IluView& f, const double* __restrict__ in, double* out, int* flags,
@@ -125,8 +141,9 @@ __device__ __forceinline__ void ilu_row(const IluView& f, const double* __restri
     if (MODE == 0 && re - rb <= kIluRowMax && f.ku <= kIluUMax)
     {
         // row i -= l_ik row k for every k < i of the pattern, in column
-        // order; products and differences rounded separately (no FMA), like
-        // the sequential elimination.  Row i stays in shared memory for the
+        // order; l_ik by ilu_div from row k's published reciprocal pivot,
+        // products and differences rounded separately (no FMA), like the
+        // sequential elimination.  Row i stays in shared memory for the
         // whole elimination (a column per thread); row k's U part is loaded
         // into registers in one batch, the next k's batch issued before this
         // one is used.
@@ -137,11 +154,12 @@ __device__ __forceinline__ void ilu_row(const IluView& f, const double* __restri
             s_a[q][t] = __ldcg(f.lu + rb + q);
         }
         int uc[kIluUMax], nc[kIluUMax];
-        double uv[kIluUMax], nv[kIluUMax], piv = 0.0, npiv = 0.0;
-        auto fetch = [&](int kk, int* c, double* v, double& pv) {
+        double uv[kIluUMax], nv[kIluUMax], piv = 0.0, npiv = 0.0, rpiv = 0.0, nrpiv = 0.0;
+        auto fetch = [&](int kk, int* c, double* v, double& pv, double& rv) {
             const int k = s_cj[kk][t];
             const int dk = __ldg(f.diag + k), ke = __ldg(f.row_ptr + k + 1);
             pv = __ldcg(f.lu + dk);
+            rv = __ldcg(f.rdiag + k);
 #pragma unroll
             for (int q = 0; q < kIluUMax; q++)
             {
@@ -150,12 +168,12 @@ __device__ __forceinline__ void ilu_row(const IluView& f, const double* __restri
                 v[q] = in ? __ldcg(f.lu + dk + 1 + q) : 0.0;
             }
         };
-        if (nlow > 0) fetch(0, uc, uv, piv);
+        if (nlow > 0) fetch(0, uc, uv, piv, rpiv);
         for (int kk = 0; kk < nlow; kk++)
         {
-            if (kk + 1 < nlow) fetch(kk + 1, nc, nv, npiv);
+            if (kk + 1 < nlow) fetch(kk + 1, nc, nv, npiv, nrpiv);
             if (piv == 0.0) atomicMin(f.bad, s_cj[kk][t]);
-            const double lik = s_a[kk][t] / piv;
+            const double lik = ilu_div(s_a[kk][t], piv, rpiv);
             s_a[kk][t] = lik;
             int p = kk + 1;
 #pragma unroll
@@ -172,9 +190,11 @@ __device__ __forceinline__ void ilu_row(const IluView& f, const double* __restri
                 uv[q] = nv[q];
             }
             piv = npiv;
+            rpiv = nrpiv;
         }
         for (int q = 0; q < len; q++) __stcg(f.lu + rb + q, s_a[q][t]);
         if (s_a[nlow][t] == 0.0) atomicMin(f.bad, i);
+        __stcg(f.rdiag + i, 1.0 / s_a[nlow][t]);
     }
     else if (MODE == 0)
     {
@@ -185,7 +205,7 @@ __device__ __forceinline__ void ilu_row(const IluView& f, const double* __restri
             const int dk = __ldg(f.diag + k), ke = __ldg(f.row_ptr + k + 1);
             const double piv = __ldcg(f.lu + dk);
             if (piv == 0.0) atomicMin(f.bad, k);
-            const double lik = __ldcg(f.lu + kk) / piv;
+            const double lik = ilu_div(__ldcg(f.lu + kk), piv, __ldcg(f.rdiag + k));
             __stcg(f.lu + kk, lik);
             int p = kk + 1;
             for (int q = dk + 1; q < ke; q++)
@@ -197,6 +217,7 @@ __device__ __forceinline__ void ilu_row(const IluView& f, const double* __restri
             }
         }
         if (__ldcg(f.lu + d) == 0.0) atomicMin(f.bad, i);
+        __stcg(f.rdiag + i, 1.0 / __ldcg(f.lu + d));
     }
     else if (MODE == 1)
     {
@@ -520,13 +541,13 @@ __host__ __device__ constexpr int tile_target(int s, int u)
 
 // ILU(0) tile by tile (lattice patterns): rows of a tile eliminated in the
 // order of lx + ly + lz, each in the IKJ order of the level kernel (its
-// lower entries in column order, l_ik = a_ik / u_kk, then a_ij -= l_ik
-// u_kj over row k's upper entries, products and differences rounded
-// separately), with the pivot rows' U parts (u_kk and 7 upper values) in a
-// 9^3 cube in shared memory: this tile's rows as they are done, the faces
-// from the tiles before it.  Writes the factors in CSR order (lu) and the
+// lower entries in column order, l_ik = a_ik / u_kk by ilu_div, then a_ij
+// -= l_ik u_kj over row k's upper entries, products and differences
+// rounded separately), with the pivot rows' U parts (u_kk, 1 / u_kk and 7
+// upper values) in a 9^3 cube in shared memory: this tile's rows as they
+// are done, the faces from the tiles before it.  Writes the factors in CSR order (lu) and the
 // sweeps' tile arrays.  Dynamic shared memory: kTileFactorSmem bytes.
-constexpr size_t kTileFactorSmem = sizeof(double) * (kIluTile * 15 * kTileT + kTileCube * 8) +
+constexpr size_t kTileFactorSmem = sizeof(double) * (kIluTile * 15 * kTileT + kTileCube * 9) +
                                    sizeof(int) * kIluTile * kTileT + kTileCube + 2 * kIluTile * kTileT;
 
 __global__ void __launch_bounds__(kTileT) k_ilu_factor_tiles(IluView f)
@@ -534,7 +555,8 @@ __global__ void __launch_bounds__(kTileT) k_ilu_factor_tiles(IluView f)
     extern __shared__ double dsm[];
     double(*s_a)[15][kTileT] = reinterpret_cast<double(*)[15][kTileT]>(dsm);  // the rows' entries
     double(*s_u)[8] = reinterpret_cast<double(*)[8]>(dsm + kIluTile * 15 * kTileT);  // U parts of the cube
-    int* s_rb = reinterpret_cast<int*>(dsm + kIluTile * 15 * kTileT + kTileCube * 8);
+    double* s_r = dsm + kIluTile * 15 * kTileT + kTileCube * 8;                          // 1 / u_kk of the cube
+    int* s_rb = reinterpret_cast<int*>(dsm + kIluTile * 15 * kTileT + kTileCube * 9);
     unsigned char* s_um = reinterpret_cast<unsigned char*>(s_rb + kIluTile * kTileT);  // cube: upper mask
     unsigned char* s_lm = s_um + kTileCube;                                           // rows: lower mask
     unsigned char* s_ur = s_lm + kIluTile * kTileT;                                   // rows: upper mask
@@ -612,6 +634,7 @@ __global__ void __launch_bounds__(kTileT) k_ilu_factor_tiles(IluView f)
                     if (um & 0x80)
                     {
                         s_u[h][0] = __ldcg(f.tu_piv + r8);
+                        s_r[h] = __ldcg(f.tu_dg + r8);
                         const size_t v0 = ((size_t)tt * kIluTile + gz % kIluTile) * 7 * kTileT + gx % kIluTile +
                                           kIluTile * (gy % kIluTile);
 #pragma unroll
@@ -648,7 +671,7 @@ __global__ void __launch_bounds__(kTileT) k_ilu_factor_tiles(IluView f)
                             const int qq = 7 - sl;
                             atomicMin(f.bad, i - ((qq & 1) + f.lnx * (((qq >> 1) & 1) + f.lny * ((qq >> 2) & 1))));
                         }
-                        const double lik = av[sl] / piv;
+                        const double lik = ilu_div(av[sl], piv, s_r[nb]);
                         av[sl] = lik;
 #pragma unroll
                         for (int u = 0; u < 7; u++)
@@ -661,7 +684,9 @@ __global__ void __launch_bounds__(kTileT) k_ilu_factor_tiles(IluView f)
                     }
                     if (av[7] == 0.0) atomicMin(f.bad, i);
                     // this row's U part for the rows after it
+                    const double rd = 1.0 / av[7];
                     s_u[ci][0] = av[7];
+                    s_r[ci] = rd;
 #pragma unroll
                     for (int q = 0; q < 7; q++) s_u[ci][1 + q] = av[8 + q];
                     s_um[ci] = (unsigned char)um;
@@ -683,7 +708,7 @@ __global__ void __launch_bounds__(kTileT) k_ilu_factor_tiles(IluView f)
                         __stcg(f.tu_val + v0 + (size_t)q * kTileT, (um & (1u << q)) ? av[8 + q] : 0.0);
                     }
                     __stcg(f.tu_piv + row, av[7]);
-                    __stcg(f.tu_dg + row, 1.0 / av[7]);
+                    __stcg(f.tu_dg + row, rd);
                 }
             }
             __syncthreads();

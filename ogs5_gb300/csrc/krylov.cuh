@@ -90,6 +90,7 @@ struct IluView
     int* bad;                 // smallest row with a zero pivot (factorisation);
                               // -1: a sweep gave up waiting
     unsigned spin;            // polls of one wait before it gives up (0: the default)
+    double* rdiag;            // [n] 1 / u_ii of each factored row (published with the row)
     // the sweeps' rows packed by position (level order, padded levels):
     // level starts, the row (-1: padding or no diagonal), and the row's L
     // (forward) or U (backward) entries as columns / values [k][pos]
