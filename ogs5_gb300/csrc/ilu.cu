@@ -81,7 +81,8 @@ __device__ __forceinline__ void st_release_s32(int* p, int v)
 // pause, bounded; once any wait of the launch has given up, f.bad is -1
 // and the others stop waiting too).  The caller takes the acquire fence
 // after all its waits.
-__device__ __forceinline__ void ilu_wait(const int* flags, int j, int launch, int* bad, unsigned limit)
+__device__ __forceinline__ void ilu_wait(const int* flags, int j, int launch, int* bad, unsigned limit,
+                                         unsigned max_pause = 512u)
 {
     if (ld_relaxed_s32(flags + j) >= launch) return;
     unsigned spins = 0, pause = 32;
@@ -93,9 +94,13 @@ __device__ __forceinline__ void ilu_wait(const int* flags, int j, int launch, in
             return;
         }
         __nanosleep(pause);
-        pause = min(pause * 2, 512u);
+        pause = min(pause * 2, max_pause);
     }
 }
+
+// the tile kernels' waits: few waiting blocks (one per SM), each on the
+// critical path of the sweep, so they poll at most 128 ns apart
+constexpr unsigned kTilePause = 128u;
 
 __device__ __forceinline__ void fence_acquire() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
 
@@ -612,7 +617,7 @@ __global__ void __launch_bounds__(kTileT) k_ilu_factor_tiles(IluView f)
             const int na = a - (q & 1), nb = b - ((q >> 1) & 1), nc = c - ((q >> 2) & 1);
             const int nt = na + f.tnx * (nb + f.tny * nc);
             if (na >= 0 && nb >= 0 && nc >= 0 && OGS_IN(nt, ntiles, kOobIluCol))
-                ilu_wait(tflags, nt, launch, f.bad, f.spin ? f.spin : kIluSpin);
+                ilu_wait(tflags, nt, launch, f.bad, f.spin ? f.spin : kIluSpin, kTilePause);
             fence_acquire();  // the block barrier below passes it on to the other threads
         }
         __syncthreads();
@@ -778,7 +783,7 @@ __global__ void __launch_bounds__(kTileT) k_ilu_tiles(IluView f, const double* _
             const int nt = na + f.tnx * (nb + f.tny * nc);
             if (na >= 0 && na < f.tnx && nb >= 0 && nb < f.tny && nc >= 0 && nc < f.tnz &&
                 OGS_IN(nt, ntiles, kOobIluCol))
-                ilu_wait(tflags, nt, launch, f.bad, f.spin ? f.spin : kIluSpin);
+                ilu_wait(tflags, nt, launch, f.bad, f.spin ? f.spin : kIluSpin, kTilePause);
             fence_acquire();  // the block barrier below passes it on to the other threads
         }
         __syncthreads();
@@ -926,8 +931,10 @@ void launch_ilu_tile_pattern(const IluView& f, cudaStream_t s)
     k_ilu_tile_pattern<<<(int)std::min<int64_t>((rows + 255) / 256, 8192), 256, 0, s>>>(f);
 }
 
-// the tile sweeps' persistent grid: as many blocks as are resident at once
-// (the same for every launch: tickets per launch depend on it)
+// the tile sweeps' persistent grid: one block per SM (a tile level of the
+// 129 x 129 x 65 lattice holds at most ~130 tiles; more blocks only add
+// blocks that wait and poll; the same for every launch: tickets per launch
+// depend on it)
 static int tile_grid()
 {
     static int g = 0;
@@ -942,7 +949,7 @@ static int tile_grid()
             cudaGetLastError();
             o1 = o2 = 1;
         }
-        g = std::max(1, sms * std::max(1, std::min(o1, o2)));
+        g = std::max(1, sms * std::max(1, std::min(std::min(o1, o2), 1)));
     }
     return g;
 }
