@@ -448,8 +448,8 @@ ogs_status ogs_gpu_debug_oob(int64_t* site, int64_t* index);
 /* The FP32 product of the Jacobi-scaled operator on x (n host values), by
  * the row kernel (y_rows) and by the four-rows-per-thread lattice kernel
  * (y_lines), n host values each; the two are bit for bit equal.  Needs the
- * FP32 operator of a 27-point lattice, i.e. a solve with
- * OGS_PRECISION_FP32_REFINED on a hex lattice before; OGS_BAD_ARG
+ * FP32 operator of a 27-point (hex) or 9-point (quad) lattice, i.e. a
+ * solve with OGS_PRECISION_FP32_REFINED on such a mesh before; OGS_BAD_ARG
  * otherwise.  (Instrumentation, no counterpart in the reference.) */
 ogs_status ogs_gpu_debug_fp32_product(ogs_system* sys, const float* x, float* y_rows, float* y_lines);
 

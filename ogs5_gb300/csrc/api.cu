@@ -1185,6 +1185,21 @@ static bool lattice27_offsets(const std::vector<int32_t>& off)
     return true;
 }
 
+// The 5 upper offsets of a 9-point plane lattice numbered line by line
+// (quads), nx = off[3] nodes per line: 0, 1, nx - 1, nx, nx + 1
+static bool lattice9_offsets(const std::vector<int32_t>& off)
+{
+    if (off.size() != 5) return false;
+    const int64_t nx = off[3];
+    return nx >= 3 && off[0] == 0 && off[1] == 1 && off[2] == nx - 1 && off[4] == nx + 1;
+}
+
+// which four-rows-per-thread product the offsets allow (MixedArgs::lines)
+static int lattice_lines(const std::vector<int32_t>& off)
+{
+    return lattice27_offsets(off) ? 1 : lattice9_offsets(off) ? 2 : 0;
+}
+
 static ogs_status begin_fp32_refined(ogs_system* s, KState* h)
 {
     ogs_mesh* m = s->m;
@@ -1255,7 +1270,7 @@ static ogs_status begin_fp32_refined(ogs_system* s, KState* h)
     // comparisons)
     {
         const char* e = std::getenv("OGS_FP32_PRODUCT");
-        a.lines = s->fmt == 0 && a.scaled && lattice27_offsets(m->host_up_off) && !(e && !std::strcmp(e, "rows"));
+        a.lines = s->fmt == 0 && a.scaled && !(e && !std::strcmp(e, "rows")) ? lattice_lines(m->host_up_off) : 0;
         if (a.lines != s->mp_lines)
         {
             drop_graphs(s);  // the captured iterations hold the product kernel
@@ -2081,14 +2096,14 @@ extern "C" ogs_status ogs_gpu_debug_oob(int64_t* site, int64_t* index)
 extern "C" ogs_status ogs_gpu_debug_fp32_product(ogs_system* s, const float* x, float* y_rows, float* y_lines)
 {
     if (!s || !x || !y_rows || !y_lines) { set_error("debug_fp32_product: NULL argument"); return OGS_BAD_ARG; }
-    if (s->fmt != 0 || !s->U || !lattice27_offsets(s->m->host_up_off))
+    if (s->fmt != 0 || !s->U || !lattice_lines(s->m->host_up_off))
     {
-        set_error("debug_fp32_product: no FP32 operator of a 27-point lattice (solve with "
-                  "OGS_PRECISION_FP32_REFINED on a hex lattice first)");
+        set_error("debug_fp32_product: no FP32 operator of a 27-point or 9-point lattice (solve with "
+                  "OGS_PRECISION_FP32_REFINED on a hex or quad lattice first)");
         return OGS_BAD_ARG;
     }
     MixedArgs a = s->mp_args;
-    a.lines = 1;
+    a.lines = lattice_lines(s->m->host_up_off);
     const size_t bytes = (size_t)s->n * sizeof(float);
     float* d = nullptr;
     OGS_CUDA_TRY(cudaMalloc(&d, 2 * bytes));

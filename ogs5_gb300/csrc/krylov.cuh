@@ -293,7 +293,8 @@ struct MixedArgs
     const float* U;           // [n_up][ustride]
     int ustride;              // values per U row (a multiple of 32: every row starts on a 128-byte line);
                               // U[d] = U + d * ustride, zero pads before [0, n) and after it
-    int lines;                // 1: the 27-point lattice product of four rows per thread (k_mp_spmv_lines)
+    int lines;                // four rows per thread (k_mp_spmv_lines): 1 the 27-point lattice, 2 the 9-point
+                              // plane lattice; 0 the row kernel
     int pad;                  // zero values in front of each U row and FP32 vector (n + pad + 64 behind)
     const int32_t* up_off;    // [n_up]
     int n_up;

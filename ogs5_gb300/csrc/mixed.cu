@@ -643,8 +643,11 @@ __device__ __forceinline__ void lines_pair(const MixedArgs& a, const float* x, i
     lines_entry<mod4(-1 - SB), 1>(a, U0 + 2 * (size_t)a.ustride, i, i - B - 1, xu, xl, acc);
 }
 
-// rows i .. i + 3 (i = 0 mod 4) of S A S x; x0 receives x[i - 1 .. i + 4]
-template <int RX, int RXY>
+// rows i .. i + 3 (i = 0 mod 4) of S A S x; x0 receives x[i - 1 .. i + 4].
+// NP line pairs: 4 for the 27-point lattice, 1 for the 9-point plane
+// lattice of quads (upper offsets 1 ; nx - 1, nx, nx + 1: the same terms in
+// the same order as dia_row<5, true, true>)
+template <int RX, int RXY, int NP>
 __device__ __forceinline__ void lines_group(const MixedArgs& a, const float* x, int i, float (&acc)[4],
                                             float (&x0)[6])
 {
@@ -654,16 +657,19 @@ __device__ __forceinline__ void lines_group(const MixedArgs& a, const float* x, 
     for (int m = 0; m < 4; m++) acc[m] = 0.f + x0[m + 1];
     lines_entry<3, 1>(a, a.U + a.ustride, i, i - 1, x0, x0, acc);  // offset 1
     lines_pair<RX, RXY, 1, 0, 2>(a, x, i, nx, nxy, acc);
-    lines_pair<RX, RXY, -1, 1, 5>(a, x, i, nx, nxy, acc);
-    lines_pair<RX, RXY, 0, 1, 8>(a, x, i, nx, nxy, acc);
-    lines_pair<RX, RXY, 1, 1, 11>(a, x, i, nx, nxy, acc);
+    if constexpr (NP == 4)
+    {
+        lines_pair<RX, RXY, -1, 1, 5>(a, x, i, nx, nxy, acc);
+        lines_pair<RX, RXY, 0, 1, 8>(a, x, i, nx, nxy, acc);
+        lines_pair<RX, RXY, 1, 1, 11>(a, x, i, nx, nxy, acc);
+    }
 }
 
 // S: iter += 1 ; w32 = S A S r32 ; partials of r.r, w.r, r.r
 // One block per SM (up to 255 registers: the loads of several line pairs
 // in flight at once); the grid is one block per SM, so the product's
 // partial sums are one per SM for the update kernel to add.
-template <int RX, int RXY>
+template <int RX, int RXY, int NP>
 __global__ void __launch_bounds__(kThreads, 1) k_mp_spmv_lines(MixedArgs a)
 {
     KState* st = a.st;
@@ -675,7 +681,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_mp_spmv_lines(MixedArgs a)
     for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x)
     {
         float acc[4], x0[6];
-        lines_group<RX, RXY>(a, x, 4 * g, acc, x0);
+        lines_group<RX, RXY, NP>(a, x, 4 * g, acc, x0);
         // rows n .. 4 ng - 1 come out 0 (zero operator rows, zero r pad)
         reinterpret_cast<float4*>(a.w32)[g] = make_float4(acc[0], acc[1], acc[2], acc[3]);
 #pragma unroll
@@ -692,14 +698,14 @@ __global__ void __launch_bounds__(kThreads, 1) k_mp_spmv_lines(MixedArgs a)
 
 // Both forms of the product on a.r32 (instrumentation): y_rows by the row
 // kernel's dia_row, y_lines by lines_group, n values each
-template <int RX, int RXY>
+template <int RX, int RXY, int NP>
 __global__ void k_mp_product_pair(MixedArgs a, float* y_rows, float* y_lines)
 {
     const int ng = (a.n + 3) >> 2;
     for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x)
     {
         float acc[4], x0[6];
-        lines_group<RX, RXY>(a, a.r32, 4 * g, acc, x0);
+        lines_group<RX, RXY, NP>(a, a.r32, 4 * g, acc, x0);
 #pragma unroll
         for (int m = 0; m < 4; m++)
         {
@@ -707,7 +713,7 @@ __global__ void k_mp_product_pair(MixedArgs a, float* y_rows, float* y_lines)
             if (i < a.n)
             {
                 y_lines[i] = acc[m];
-                y_rows[i] = dia_row<14, true, true>(a, a.r32, i);
+                y_rows[i] = dia_row<NP == 4 ? 14 : 5, true, true>(a, a.r32, i);
             }
         }
     }
@@ -1333,30 +1339,36 @@ using LinesKernel = void (*)(MixedArgs);
 using PairKernel = void (*)(MixedArgs, float*, float*);
 
 template <int RX>
-static LinesKernel lines_kernel_rx(int rxy, PairKernel* pair)
+static LinesKernel lines_kernel_rx(int rxy, int plane, PairKernel* pair)
 {
+    if (plane)
+    {
+        *pair = k_mp_product_pair<RX, 0, 1>;
+        return k_mp_spmv_lines<RX, 0, 1>;
+    }
     switch (rxy)
     {
-        case 0: *pair = k_mp_product_pair<RX, 0>; return k_mp_spmv_lines<RX, 0>;
-        case 1: *pair = k_mp_product_pair<RX, 1>; return k_mp_spmv_lines<RX, 1>;
-        case 2: *pair = k_mp_product_pair<RX, 2>; return k_mp_spmv_lines<RX, 2>;
-        default: *pair = k_mp_product_pair<RX, 3>; return k_mp_spmv_lines<RX, 3>;
+        case 0: *pair = k_mp_product_pair<RX, 0, 4>; return k_mp_spmv_lines<RX, 0, 4>;
+        case 1: *pair = k_mp_product_pair<RX, 1, 4>; return k_mp_spmv_lines<RX, 1, 4>;
+        case 2: *pair = k_mp_product_pair<RX, 2, 4>; return k_mp_spmv_lines<RX, 2, 4>;
+        default: *pair = k_mp_product_pair<RX, 3, 4>; return k_mp_spmv_lines<RX, 3, 4>;
     }
 }
 
-// the instantiations for nx mod 4 and nxy mod 4 (pair: the comparison
-// kernel, may be NULL)
+// the instantiations for nx mod 4 and nxy mod 4 (a.lines 1: the 27-point
+// lattice) or nx mod 4 (a.lines 2: the 9-point plane lattice); pair: the
+// comparison kernel, may be NULL
 static LinesKernel lines_kernel(const MixedArgs& a, PairKernel* pair = nullptr)
 {
     PairKernel p = nullptr;
     LinesKernel k;
-    const int rxy = a.off[9] & 3;
+    const int rxy = a.off[9] & 3, plane = a.lines == 2;
     switch (a.off[3] & 3)
     {
-        case 0: k = lines_kernel_rx<0>(rxy, &p); break;
-        case 1: k = lines_kernel_rx<1>(rxy, &p); break;
-        case 2: k = lines_kernel_rx<2>(rxy, &p); break;
-        default: k = lines_kernel_rx<3>(rxy, &p); break;
+        case 0: k = lines_kernel_rx<0>(rxy, plane, &p); break;
+        case 1: k = lines_kernel_rx<1>(rxy, plane, &p); break;
+        case 2: k = lines_kernel_rx<2>(rxy, plane, &p); break;
+        default: k = lines_kernel_rx<3>(rxy, plane, &p); break;
     }
     if (pair) *pair = p;
     return k;
@@ -1487,7 +1499,8 @@ void launch_mp_iteration(const MixedArgs& a, cudaStream_t s, cudaEvent_t eb, cud
             else k_mp_spmv<8><<<gs, kThreads, 0, s>>>(a);
             break;
         case 5:  // quads, 9-point
-            if (a.scaled) k_mp_spmv<5, true><<<gs, kThreads, 0, s>>>(a);
+            if (a.lines) lines_kernel(a)<<<gs, kThreads, 0, s>>>(a);
+            else if (a.scaled) k_mp_spmv<5, true><<<gs, kThreads, 0, s>>>(a);
             else k_mp_spmv<5><<<gs, kThreads, 0, s>>>(a);
             break;
         case -1:  // hex lattice, cell coefficients

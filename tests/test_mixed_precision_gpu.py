@@ -107,6 +107,22 @@ def test_lattice_product_bitwise(gpu, cells):
         assert np.array_equal(y_rows, y_lines)
 
 
+@pytest.mark.parametrize("cells", [(3, 4), (4, 3), (5, 6), (6, 2), (120, 90)])
+def test_quad_lattice_product_bitwise(gpu, cells):
+    """The same four-rows-per-thread product on the 9-point operator of a
+    quad lattice (one line pair): bit for bit the row kernel's values, for
+    every nx mod 4."""
+    m = M.structured_quad(*cells)
+    ek = fields.lognormal_k(m.shape, np.log(1e-5), 1.0, 4.0, seed=3)
+    eqs, x0 = _deck(gpu, m, ek)
+    _both(gpu, eqs, x0)
+    rng = np.random.default_rng(cells[0] * 31 + cells[1])
+    for x in (rng.standard_normal(m.n_nodes), np.ones(m.n_nodes)):
+        y_rows, y_lines = eqs.debug_fp32_product(x)
+        assert np.abs(y_rows).max() > 0
+        assert np.array_equal(y_rows, y_lines)
+
+
 def test_lattice_product_needs_lattice_operator(gpu):
     m, _ = renumber(M.structured_hex(8, 6, 4), 5)  # SELL-32 FP32 operator
     eqs, x0 = _deck(gpu, m, np.ones(m.n_elements))
