@@ -59,3 +59,17 @@ def test_calibration_summary_from_markers():
     r = s["reference_sp_over_port"]
     assert r["assembly"] == 4.0 and r["first_step_assembly_plus_solve"] == round(40 / 15, 2)
     assert r["time_per_cg_iteration"] == round((20 / 200) / (10 / 250), 2)
+
+
+def test_roofline_traffic_comes_from_the_committed_profile():
+    """The bench line's roofline traffic is read from the ncu summary of the
+    roofline kernel; every profile that names a per-launch figure keeps it
+    readable."""
+    import glob
+    import os
+    t = bench.measured_traffic("k_mp_spmv_lines_hex128x128x64.md")
+    assert isinstance(t, int) and 0.9 * 64.9e6 < t < 1.1 * 64.9e6
+    for p in glob.glob(os.path.join(bench.ROOT, "profiles", "*.md")):
+        for line in open(p):
+            if line.startswith("dram_bytes_per_launch:"):
+                assert int(line.split(":")[1]) > 0
