@@ -36,7 +36,7 @@
 // FP32 operator storage: for patterns with at most 64 distinct column
 // offsets (structured grids) the symmetric matrix is stored as the upper
 // half of its diagonal-offset form, U[d][i] = A[i][i + off_d] for off_d >= 0
-// (14 rows of 4 bytes per node for hexes: the config-2 matrix is 61 MB and
+// (14 rows of 4 bytes per node for hexes: the 129 x 129 x 65 lattice's matrix is 61 MB and
 // stays in L2 with the FP32 vectors); y_i = sum_d U[d][i] x_{i+off_d} +
 // sum_{d>0} U[d][i-off_d] x_{i-off_d}.  Other patterns use SELL-32 with
 // FP32 values.

@@ -9,8 +9,8 @@ import pytest
 from ogs5_gb300 import build as B
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-SRC = os.path.join(ROOT, "tests", "cpp", "linear_eqs_config1.cpp")
-OUT = os.path.join(ROOT, "tests", "cpp", "_build", "linear_eqs_config1")
+SRC = os.path.join(ROOT, "tests", "cpp", "linear_eqs_quad100.cpp")
+OUT = os.path.join(ROOT, "tests", "cpp", "_build", "linear_eqs_quad100")
 
 
 def _compile():
@@ -28,7 +28,7 @@ def test_cpp_mirror_compiles_and_links():
 
 
 @pytest.mark.gpu
-def test_cpp_mirror_config1_deck():
+def test_cpp_mirror_quad100_deck():
     _compile()
     r = subprocess.run([OUT], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0 and "PASS" in r.stdout, r.stdout + r.stderr

@@ -50,7 +50,7 @@ def test_reference_tet(oracle):
 
 
 def test_linear_profile_exact(oracle):
-    """Config-1 deck: h = 1 - x/100 is reproduced to rounding."""
+    """The 100 x 100 quad deck: h = 1 - x/100 is reproduced to rounding."""
     m = M.structured_quad(100, 100)
     rp, col = oracle.build_pattern(m.n_nodes, m.conn)
     assert len(col) == 301 * 301  # 90,601 stored entries

@@ -64,8 +64,8 @@ def test_fp32_refined_matches_fp64(gpu, kind):
     assert it32 <= 1.2 * it64 + 5
 
 
-def test_fp32_refined_config1_quads(gpu):
-    """Precision form of config 1 (100x100 quads, K=1e-4) to 1e-10."""
+def test_fp32_refined_quad100(gpu):
+    """The FP32-inner form on the 100 x 100 quad deck (K=1e-4) to 1e-10."""
     m = M.structured_quad(100, 100)
     ek = np.full(m.n_elements, 1e-4)
     eqs, x0 = _deck(gpu, m, ek, 1.0, 0.0, steady=True)

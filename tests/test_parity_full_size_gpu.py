@@ -37,7 +37,7 @@ def _faces(m):
     return lf, rf, rows, vals, x0
 
 
-def test_config2_hex_assembly_and_step(gpu, oracle):
+def test_hex_128x128x64_assembly_and_step(gpu, oracle):
     m = M.structured_hex(NX, NY, NZ)
     ek = fields.lognormal_k(m.shape, np.log(1e-5), 1.0, 8.0, seed=SEED)
     lf, rf, rows, vals, x0 = _faces(m)
@@ -69,7 +69,7 @@ def test_config2_hex_assembly_and_step(gpu, oracle):
     assert rel_max_err(x32, xo) < 1e-8
 
 
-def test_config3b_tet_flux_transport_assembly_and_step(gpu, oracle):
+def test_tet_128x128x64_flux_transport_assembly_and_step(gpu, oracle):
     m = M.structured_tet(NX, NY, NZ)
     ek = np.repeat(fields.lognormal_k((NX, NY, NZ), np.log(1e-5), 1.0, 8.0, seed=SEED), 6)
     lf, rf, rows, vals, x0 = _faces(m)

@@ -364,8 +364,8 @@ def _flow_system(gpu, oracle, m, ek, symmetric, dt=None, storage=0.0, left=1.0, 
     return eqs, (rp, col, val, b), x0
 
 
-def test_config1_bicgstab_jacobi_linear_profile(gpu, oracle):
-    """Config-1 deck: 100x100 quads, K=1e-4, h=1|0 on the x faces, BiCGStab+Jacobi.
+def test_quad100_bicgstab_jacobi_linear_profile(gpu, oracle):
+    """The 100 x 100 quad deck: K=1e-4, h=1|0 on the x faces, BiCGStab+Jacobi.
 
     At the deck's tolerance 1e-10 both codes stop on |r|/|b| < 1e-10 within
     two iterations of each other; their heads then differ by up to
