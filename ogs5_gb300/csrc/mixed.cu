@@ -552,8 +552,9 @@ __global__ void __launch_bounds__(kThreads, 3) k_mp_spmv(MixedArgs a)
 // thread then reads every operand as aligned 16-byte words: its own
 // operator values U[d][4g .. 4g + 3] (13 words), each line's six x (two or
 // three words) and each mirrored window U[d][4g - off_d ..] (one or two
-// words) -- 57 wide loads for four rows instead of 53 four-byte loads with
-// bounds predicates per row.  The word alignment of every window depends
+// words) -- 55 to 62 wide loads for four rows by the windows' alignments
+// (57 for nx = nxy = 1 mod 4), instead of 53 four-byte loads with bounds
+// predicates per row.  The word alignment of every window depends
 // only on nx mod 4 and nxy mod 4 (template arguments RX, RXY).  There are
 // no bounds predicates: the operator rows and the FP32 vectors carry zero
 // pads of at least nxy + nx + 16 values on both sides, so a window that
