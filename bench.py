@@ -892,12 +892,7 @@ def main():
     configure(eqs, capi, True)
     ms_e2e, per_e2e, it_e2e, heads_e2e, _ = run_steps(eqs, capi, p, ek, rows, vals, h0, k_steps, True,
                                                       torch, stream)
-    ms = mix["ms"]
-    if world > 1:
-        t = torch.tensor([ms, ms_e2e, f64["ms"]], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms, ms_e2e, f64["ms"] = float(t[0]), float(t[1]), float(t[2])
-        dist.barrier()
+    ms, ms_e2e, f64["ms"] = replica_times([mix["ms"], ms_e2e, f64["ms"]], world)
 
     N, nnz = gm.n_rows, gm.nnz
     cfg = deck_config(world)
@@ -914,9 +909,9 @@ def main():
     pr64 = f64["prof"]
     t64 = pr64["spmv_ms"] / max(1, pr64["spmv_launches"])
     b64 = nnz * 12 + N * 20
-    value = world * k_steps / (ms * 1e-3)
-    value64 = world * k_steps / (f64["ms"] * 1e-3)
-    e2e = world * k_steps / (ms_e2e * 1e-3)
+    value = job_rate(world, k_steps, ms)
+    value64 = job_rate(world, k_steps, f64["ms"])
+    e2e = job_rate(world, k_steps, ms_e2e)
     h2d = 8 * m.n_elements + 8 * N * 2 + 12 * len(rows)
     d2h = 8 * N
     out = {
@@ -977,6 +972,27 @@ def hex_pattern_nnz(nx, ny, nz):
     """Stored entries of the 27-point pattern of an nx x ny x nz hex lattice:
     per axis, (n + 1) nodes couple to 3 each except the 2 end nodes."""
     return (3 * nx + 1) * (3 * ny + 1) * (3 * nz + 1)
+
+
+def replica_times(times, world):
+    """Each timing (ms) as the maximum over the ranks, on every rank: with
+    one replica per GPU and no exchange between them, the job takes as long
+    as its slowest replica.  A barrier follows, so no rank prints before all
+    have timed."""
+    if world <= 1:
+        return list(times)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor(list(times), dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.barrier()
+    return [float(v) for v in t]
+
+
+def job_rate(world, steps, ms):
+    """Whole-job solves/s: each of the world replicas did steps solves
+    within ms milliseconds."""
+    return world * steps / (ms * 1e-3)
 
 
 def deck_config(world=1):
